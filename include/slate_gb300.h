@@ -1,0 +1,167 @@
+/* slate_gb300.h -- C ABI of the GB300 LU / Cholesky solve library.
+ *
+ * Three layers, all extern "C", plain pointers and sizes:
+ *
+ *  1. LAPACK-compatible entry points (host pointers, Fortran by-pointer
+ *     arguments, 32-bit int, 1-based ipiv), drop-ins for SLATE's lapack_api.
+ *     Exported both as slate_dgesv and slate_dgesv_ (the two manglings
+ *     SLATE's BLAS_FORTRAN_NAME can produce).
+ *  2. Device entry points (device pointers, column-major, a CUDA stream):
+ *     the Matrix::fromDevices / Target::Devices form of SLATE's drivers on a
+ *     1 x 1 grid.
+ *  3. Options and status helpers.
+ *
+ * Matrices are column-major; the tile size nb of SLATE's tile layout is an
+ * option.  ipiv on the device is stored per panel: ipiv[k*nb + j] is the pivot
+ * row of global row k*nb + j, relative to row k*nb (SLATE's Pivot(tile index,
+ * offset) flattened, include/slate/types.hh:84-117).
+ */
+#ifndef SLATE_GB300_H
+#define SLATE_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* CUDA stream, passed as an opaque pointer so this header needs no CUDA. */
+typedef void* slt_stream_t;
+
+/* Precision of the O(n^3) factorisation inside the mixed solvers. */
+enum slt_precision {
+    SLT_PREC_FP64 = 0,   /* plain FP64 factorisation (no refinement)        */
+    SLT_PREC_FP32 = 1,   /* FP32 factorisation, SLATE's gesv_mixed<double,float> */
+    SLT_PREC_TF32 = 2,   /* FP32 storage, TF32 tensor-core trailing update   */
+    SLT_PREC_BF16 = 3,   /* FP32 storage, BF16 tensor-core trailing update   */
+    SLT_PREC_FP16 = 4    /* FP32 storage, FP16 tensor-core trailing update   */
+};
+
+/* Options (SLATE Option keys, include/slate/enums.hh:453-490). */
+typedef struct slt_options {
+    int64_t nb;               /* Option::BlockSize (tile size), default 512       */
+    int64_t ib;               /* Option::InnerBlocking, default 32                */
+    int64_t lookahead;        /* Option::Lookahead, default 1                     */
+    int64_t max_iterations;   /* Option::MaxIterations, default 30                */
+    double  tolerance;        /* Option::Tolerance; <= 0: eps * sqrt(n)           */
+    int     use_fallback;     /* Option::UseFallbackSolver, default 1             */
+    double  pivot_threshold;  /* Option::PivotThreshold, default 1 (partial piv.) */
+    int     factor_precision; /* slt_precision of mixed solvers, default FP32     */
+    int     gemm_engine;      /* FP64 update engine: 0 auto, 1 SIMT, 2 DMMA       */
+} slt_options;
+
+void slt_options_default(slt_options* opts);
+
+/* Status codes returned by the device layer (0 = success). */
+const char* slt_status_string(int status);
+
+/* Library version string. */
+const char* slt_version(void);
+
+/* ------------------------------------------------------------------------- */
+/* Device entry points.  Return an slt status (0 ok); *info receives SLATE's   */
+/* info (0, or the 1-based column of a zero pivot / non-positive minor).      */
+/* All calls are complete (stream synchronised) on return.                    */
+
+/* slate::getrf, src/getrf.cc:319-356 */
+int slt_dgetrf_device(int64_t m, int64_t n, double* dA, int64_t lda, int* d_ipiv,
+                      const slt_options* opts, slt_stream_t stream, int64_t* info);
+int slt_sgetrf_device(int64_t m, int64_t n, float* dA, int64_t lda, int* d_ipiv,
+                      const slt_options* opts, slt_stream_t stream, int64_t* info);
+/* slate::getrs (NoTrans), src/getrs.cc:66-117 */
+int slt_dgetrs_device(int64_t n, int64_t nrhs, const double* dLU, int64_t lda, const int* d_ipiv,
+                      double* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream);
+int slt_sgetrs_device(int64_t n, int64_t nrhs, const float* dLU, int64_t lda, const int* d_ipiv,
+                      float* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream);
+/* slate::gesv, src/gesv.cc:85-109 */
+int slt_dgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv,
+                     double* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream,
+                     int64_t* info);
+/* slate::potrf (lower), src/potrf.cc:261-281 */
+int slt_dpotrf_device(int64_t n, double* dA, int64_t lda, const slt_options* opts,
+                      slt_stream_t stream, int64_t* info);
+int slt_spotrf_device(int64_t n, float* dA, int64_t lda, const slt_options* opts,
+                      slt_stream_t stream, int64_t* info);
+/* slate::potrs (lower), src/potrs.cc:55-78 */
+int slt_dpotrs_device(int64_t n, int64_t nrhs, const double* dL, int64_t lda, double* dB,
+                      int64_t ldb, const slt_options* opts, slt_stream_t stream);
+/* slate::posv (lower), src/posv.cc:70-94 */
+int slt_dposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, double* dB, int64_t ldb,
+                     const slt_options* opts, slt_stream_t stream, int64_t* info);
+/* slate::gesv_mixed, src/gesv_mixed.cc:105-289.  A is left unchanged unless
+ * the FP64 fallback runs (then it holds the FP64 LU factors). */
+int slt_dsgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv,
+                      const double* dB, int64_t ldb, double* dX, int64_t ldx,
+                      const slt_options* opts, slt_stream_t stream, int* iter, int64_t* info);
+/* slate::gesv_mixed_gmres, src/gesv_mixed_gmres.cc:110-410 (nrhs columns are
+ * solved as independent single-right-hand-side FGMRES-IR instances). */
+int slt_dsgesv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv,
+                            const double* dB, int64_t ldb, double* dX, int64_t ldx,
+                            const slt_options* opts, slt_stream_t stream, int* iter,
+                            int64_t* info);
+/* slate::posv_mixed, src/posv_mixed.cc:105-320 (A lower) */
+int slt_dsposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, const double* dB,
+                      int64_t ldb, double* dX, int64_t ldx, const slt_options* opts,
+                      slt_stream_t stream, int* iter, int64_t* info);
+/* slate::posv_mixed_gmres, src/posv_mixed_gmres.cc:109-436 (A lower) */
+int slt_dsposv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, const double* dB,
+                            int64_t ldb, double* dX, int64_t ldx, const slt_options* opts,
+                            slt_stream_t stream, int* iter, int64_t* info);
+
+/* Philox test-matrix generator, same values as slate::random::generate
+ * (matgen/random.cc:197-230) for the uniform distributions. */
+int slt_dgenerate_device(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
+                         double* dA, int64_t lda, slt_stream_t stream);
+
+/* Seconds spent in named phases of the last driver call on this thread
+ * (the keys of SLATE's slate::timers map, e.g. "gesv_mixed::getrf_lo");
+ * returns -1 if the key is unknown. */
+double slt_timer(const char* name);
+
+/* ------------------------------------------------------------------------- */
+/* LAPACK-compatible entry points (lapack_api/lapack_*.cc).  Host memory.     */
+/* Tile size from SLATE_LAPACK_NB (default 512), inner blocking from          */
+/* SLATE_LAPACK_IB (default 32).                                              */
+
+/* lapack_api/lapack_gesv.cc:32 */
+void slate_dgesv(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
+                 double* b, const int* ldb, int* info);
+void slate_sgesv(const int* n, const int* nrhs, float* a, const int* lda, int* ipiv,
+                 float* b, const int* ldb, int* info);
+/* lapack_api/lapack_getrf.cc */
+void slate_dgetrf(const int* m, const int* n, double* a, const int* lda, int* ipiv, int* info);
+void slate_sgetrf(const int* m, const int* n, float* a, const int* lda, int* ipiv, int* info);
+/* lapack_api/lapack_getrs.cc:29 (trans 'N' only) */
+void slate_dgetrs(const char* trans, const int* n, const int* nrhs, double* a, const int* lda,
+                  int* ipiv, double* b, const int* ldb, int* info);
+/* lapack_api/lapack_gesv_mixed.cc:24 (dsgesv signature; x receives the solution) */
+void slate_dsgesv(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
+                  double* b, const int* ldb, double* x, const int* ldx, double* work,
+                  float* swork, int* iter, int* info);
+/* lapack_api/lapack_posv.cc:32 (uplo 'L' or 'U') */
+void slate_dposv(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda,
+                 double* b, const int* ldb, int* info);
+/* lapack_api/lapack_potrf.cc:30 */
+void slate_dpotrf(const char* uplo, const int* n, double* a, const int* lda, int* info);
+
+void slate_dgesv_(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
+                  double* b, const int* ldb, int* info);
+void slate_sgesv_(const int* n, const int* nrhs, float* a, const int* lda, int* ipiv,
+                  float* b, const int* ldb, int* info);
+void slate_dgetrf_(const int* m, const int* n, double* a, const int* lda, int* ipiv, int* info);
+void slate_sgetrf_(const int* m, const int* n, float* a, const int* lda, int* ipiv, int* info);
+void slate_dgetrs_(const char* trans, const int* n, const int* nrhs, double* a, const int* lda,
+                   int* ipiv, double* b, const int* ldb, int* info);
+void slate_dsgesv_(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
+                   double* b, const int* ldb, double* x, const int* ldx, double* work,
+                   float* swork, int* iter, int* info);
+void slate_dposv_(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda,
+                  double* b, const int* ldb, int* info);
+void slate_dpotrf_(const char* uplo, const int* n, double* a, const int* lda, int* info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLATE_GB300_H */

@@ -1,0 +1,338 @@
+"""slate_gb300 -- GB300-native LU / Cholesky solve path with SLATE's API.
+
+Python mirror of SLATE's drivers for one GPU (a 1 x 1 grid with
+Target::Devices): ``getrf/getrs/gesv``, ``potrf/potrs/posv``, ``gesv_mixed``,
+``gesv_mixed_gmres``, ``posv_mixed`` and ``posv_mixed_gmres``, plus the
+LAPACK-compatible host entry points (``lapack`` namespace).  Every call goes
+through the C ABI of ``libslate_gb300.so`` (include/slate_gb300.h); there is
+no CPU or library fallback -- importing fails if the library is missing.
+
+Device arrays are torch CUDA tensors in column-major layout (``colmajor()``
+makes one); host arrays for the LAPACK entry points are Fortran-ordered numpy
+arrays.
+"""
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libslate_gb300.so")
+
+PREC_FP64, PREC_FP32, PREC_TF32, PREC_BF16, PREC_FP16 = 0, 1, 2, 3, 4
+_PREC_NAMES = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "fp16": 4}
+
+
+class SlateError(RuntimeError):
+    """A non-zero status from the library (slate::Exception analogue)."""
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("nb", ctypes.c_int64), ("ib", ctypes.c_int64), ("lookahead", ctypes.c_int64),
+                ("max_iterations", ctypes.c_int64), ("tolerance", ctypes.c_double),
+                ("use_fallback", ctypes.c_int), ("pivot_threshold", ctypes.c_double),
+                ("factor_precision", ctypes.c_int), ("gemm_engine", ctypes.c_int)]
+
+
+@dataclass
+class Options:
+    """SLATE Option keys used on this path (include/slate/enums.hh:453-490)."""
+    nb: int = 512
+    ib: int = 32
+    lookahead: int = 1
+    max_iterations: int = 30
+    tolerance: float = 0.0
+    use_fallback: bool = True
+    pivot_threshold: float = 1.0
+    factor_precision: object = "fp32"
+    gemm_engine: int = 0
+
+    def _c(self):
+        p = self.factor_precision
+        p = _PREC_NAMES[p] if isinstance(p, str) else int(p)
+        return _Options(int(self.nb), int(self.ib), int(self.lookahead), int(self.max_iterations),
+                        float(self.tolerance), int(bool(self.use_fallback)),
+                        float(self.pivot_threshold), p, int(self.gemm_engine))
+
+
+_lib = None
+
+
+def lib():
+    """Load libslate_gb300.so; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libslate_gb300.so not built: run python -m slate_gb300.build")
+        L = ctypes.CDLL(LIB_PATH)
+        i64, vp, ip, dp = ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)
+        optp = ctypes.POINTER(_Options)
+        iptr = ctypes.POINTER(ctypes.c_int)
+        sig = {
+            "slt_dgetrf_device": [i64, i64, vp, i64, ip, optp, vp, dp],
+            "slt_sgetrf_device": [i64, i64, vp, i64, ip, optp, vp, dp],
+            "slt_dgetrs_device": [i64, i64, vp, i64, ip, vp, i64, optp, vp],
+            "slt_sgetrs_device": [i64, i64, vp, i64, ip, vp, i64, optp, vp],
+            "slt_dgesv_device": [i64, i64, vp, i64, ip, vp, i64, optp, vp, dp],
+            "slt_dpotrf_device": [i64, vp, i64, optp, vp, dp],
+            "slt_spotrf_device": [i64, vp, i64, optp, vp, dp],
+            "slt_dpotrs_device": [i64, i64, vp, i64, vp, i64, optp, vp],
+            "slt_dposv_device": [i64, i64, vp, i64, vp, i64, optp, vp, dp],
+            "slt_dsgesv_device": [i64, i64, vp, i64, ip, vp, i64, vp, i64, optp, vp, iptr, dp],
+            "slt_dsgesv_gmres_device": [i64, i64, vp, i64, ip, vp, i64, vp, i64, optp, vp, iptr, dp],
+            "slt_dsposv_device": [i64, i64, vp, i64, vp, i64, vp, i64, optp, vp, iptr, dp],
+            "slt_dsposv_gmres_device": [i64, i64, vp, i64, vp, i64, vp, i64, optp, vp, iptr, dp],
+            "slt_dgenerate_device": [ctypes.c_int, i64, i64, i64, i64, i64, vp, i64, vp],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = ctypes.c_int
+        L.slt_status_string.restype = ctypes.c_char_p
+        L.slt_status_string.argtypes = [ctypes.c_int]
+        L.slt_version.restype = ctypes.c_char_p
+        L.slt_timer.restype = ctypes.c_double
+        L.slt_timer.argtypes = [ctypes.c_char_p]
+        _lib = L
+    return _lib
+
+
+def version():
+    return lib().slt_version().decode()
+
+
+def timer(name):
+    """Seconds of a named phase of the last driver call (slate::timers key)."""
+    return float(lib().slt_timer(name.encode()))
+
+
+def _check(rc):
+    if rc != 0:
+        raise SlateError("slate_gb300: %s (status %d)" % (lib().slt_status_string(rc).decode(), rc))
+
+
+# ---------------------------------------------------------------------------
+# torch device helpers
+def colmajor(x):
+    """Return a column-major (Fortran-strided) copy/view of a 2-D tensor."""
+    if x.dim() == 1:
+        x = x.reshape(-1, 1)
+    if x.stride(0) == 1 and (x.shape[1] <= 1 or x.stride(1) >= max(1, x.shape[0])):
+        return x
+    return x.t().contiguous().t()
+
+
+def _ld(x):
+    return max(1, x.stride(1) if x.shape[1] > 1 else x.shape[0])
+
+
+def _dev(x, dtype=None):
+    import torch
+    if not (isinstance(x, torch.Tensor) and x.is_cuda):
+        raise TypeError("expected a CUDA tensor")
+    if dtype is not None and x.dtype != dtype:
+        raise TypeError("expected dtype %s, got %s" % (dtype, x.dtype))
+    if x.dim() != 2 or x.stride(0) != 1:
+        raise ValueError("expected a column-major 2-D tensor (use slate_gb300.colmajor)")
+    return ctypes.c_void_p(x.data_ptr())
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _opts(opts):
+    o = opts if isinstance(opts, Options) else Options(**(opts or {}))
+    return ctypes.byref(o._c()), o
+
+
+def _ipiv_buf(n, device):
+    import torch
+    return torch.zeros(max(n, 1), dtype=torch.int32, device=device)
+
+
+# ---------------------------------------------------------------------------
+# SLATE drivers (include/slate/slate.hh:503-770)
+def getrf(A, opts=None):
+    """LU with partial pivoting in place (slate::getrf).  Returns (info, ipiv)
+    with ipiv per panel (row of panel k relative to row k*nb)."""
+    import torch
+    po, o = _opts(opts)
+    m, n = A.shape
+    ipiv = _ipiv_buf(min(m, n), A.device)
+    info = ctypes.c_int64(0)
+    f = lib().slt_dgetrf_device if A.dtype == torch.float64 else lib().slt_sgetrf_device
+    _check(f(m, n, _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), po, _stream(), ctypes.byref(info)))
+    return int(info.value), ipiv[:min(m, n)]
+
+
+def getrs(A, ipiv, B, opts=None):
+    """Solve A X = B with the factors of getrf; B is overwritten (slate::getrs)."""
+    import torch
+    po, o = _opts(opts)
+    n = A.shape[0]
+    f = lib().slt_dgetrs_device if A.dtype == torch.float64 else lib().slt_sgetrs_device
+    _check(f(n, B.shape[1], _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), _dev(B), _ld(B), po,
+             _stream()))
+
+
+def gesv(A, B, opts=None):
+    """slate::gesv: A <- LU, B <- X.  Returns (info, ipiv)."""
+    import torch
+    po, o = _opts(opts)
+    n = A.shape[0]
+    ipiv = _ipiv_buf(n, A.device)
+    info = ctypes.c_int64(0)
+    _check(lib().slt_dgesv_device(n, B.shape[1], _dev(A, torch.float64), _ld(A), ctypes.c_void_p(ipiv.data_ptr()),
+                                  _dev(B, torch.float64), _ld(B), po, _stream(), ctypes.byref(info)))
+    return int(info.value), ipiv[:n]
+
+
+def potrf(A, opts=None):
+    """Cholesky A = L L^T of the lower triangle in place (slate::potrf).  Returns info."""
+    import torch
+    po, o = _opts(opts)
+    n = A.shape[0]
+    info = ctypes.c_int64(0)
+    f = lib().slt_dpotrf_device if A.dtype == torch.float64 else lib().slt_spotrf_device
+    _check(f(n, _dev(A), _ld(A), po, _stream(), ctypes.byref(info)))
+    return int(info.value)
+
+
+def potrs(A, B, opts=None):
+    import torch
+    po, o = _opts(opts)
+    _check(lib().slt_dpotrs_device(A.shape[0], B.shape[1], _dev(A, torch.float64), _ld(A),
+                                   _dev(B, torch.float64), _ld(B), po, _stream()))
+
+
+def posv(A, B, opts=None):
+    import torch
+    po, o = _opts(opts)
+    info = ctypes.c_int64(0)
+    _check(lib().slt_dposv_device(A.shape[0], B.shape[1], _dev(A, torch.float64), _ld(A),
+                                  _dev(B, torch.float64), _ld(B), po, _stream(), ctypes.byref(info)))
+    return int(info.value)
+
+
+def _mixed(fn, chol, A, B, X, opts):
+    import torch
+    po, o = _opts(opts)
+    n = A.shape[0]
+    info = ctypes.c_int64(0)
+    it = ctypes.c_int(0)
+    args = [n, B.shape[1], _dev(A, torch.float64), _ld(A)]
+    ipiv = None
+    if not chol:
+        ipiv = _ipiv_buf(n, A.device)
+        args.append(ctypes.c_void_p(ipiv.data_ptr()))
+    args += [_dev(B, torch.float64), _ld(B), _dev(X, torch.float64), _ld(X), po, _stream(),
+             ctypes.byref(it), ctypes.byref(info)]
+    _check(fn(*args))
+    return int(info.value), int(it.value), (ipiv[:n] if ipiv is not None else None)
+
+
+def gesv_mixed(A, B, X, opts=None):
+    """slate::gesv_mixed: low-precision LU + FP64 iterative refinement.
+    Returns (info, iter, ipiv)."""
+    return _mixed(lib().slt_dsgesv_device, False, A, B, X, opts)
+
+
+def gesv_mixed_gmres(A, B, X, opts=None):
+    """slate::gesv_mixed_gmres: low-precision LU + FP64 FGMRES-IR."""
+    return _mixed(lib().slt_dsgesv_gmres_device, False, A, B, X, opts)
+
+
+def posv_mixed(A, B, X, opts=None):
+    """slate::posv_mixed (A lower).  Returns (info, iter, None)."""
+    return _mixed(lib().slt_dsposv_device, True, A, B, X, opts)
+
+
+def posv_mixed_gmres(A, B, X, opts=None):
+    return _mixed(lib().slt_dsposv_gmres_device, True, A, B, X, opts)
+
+
+def generate(dist, seed, A, ioff=0, joff=0):
+    """slate::random::generate on the device (matgen/random.cc)."""
+    _check(lib().slt_dgenerate_device(int(dist), int(seed), A.shape[0], A.shape[1], ioff, joff,
+                                      _dev(A), _ld(A), _stream()))
+
+
+def ipiv_to_lapack(ipiv, nb):
+    """Per-panel pivots -> LAPACK 1-based ipiv (lapack_api/lapack_gesv.cc:90-100)."""
+    p = np.asarray(ipiv.cpu() if hasattr(ipiv, "cpu") else ipiv, dtype=np.int64)
+    r = np.arange(p.size)
+    return (r // nb) * nb + p + 1
+
+
+# ---------------------------------------------------------------------------
+# LAPACK-compatible host entry points (lapack_api/*.cc)
+class lapack:
+    @staticmethod
+    def _ptr(a):
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    @staticmethod
+    def dgesv(a, b):
+        """slate_dgesv: returns (info, ipiv); a <- LU, b <- X (Fortran arrays)."""
+        n, nrhs = a.shape[0], b.shape[1]
+        ipiv = np.zeros(n, np.int32)
+        info = ctypes.c_int(0)
+        c = ctypes.c_int
+        lib().slate_dgesv(ctypes.byref(c(n)), ctypes.byref(c(nrhs)), lapack._ptr(a), ctypes.byref(c(n)),
+                          lapack._ptr(ipiv), lapack._ptr(b), ctypes.byref(c(n)), ctypes.byref(info))
+        return info.value, ipiv
+
+    @staticmethod
+    def dgetrf(a):
+        m, n = a.shape
+        ipiv = np.zeros(min(m, n), np.int32)
+        info = ctypes.c_int(0)
+        c = ctypes.c_int
+        lib().slate_dgetrf(ctypes.byref(c(m)), ctypes.byref(c(n)), lapack._ptr(a), ctypes.byref(c(m)),
+                           lapack._ptr(ipiv), ctypes.byref(info))
+        return info.value, ipiv
+
+    @staticmethod
+    def dgetrs(a, ipiv, b):
+        n, nrhs = a.shape[0], b.shape[1]
+        info = ctypes.c_int(0)
+        c = ctypes.c_int
+        ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+        lib().slate_dgetrs(ctypes.c_char_p(b"N"), ctypes.byref(c(n)), ctypes.byref(c(nrhs)), lapack._ptr(a),
+                           ctypes.byref(c(n)), lapack._ptr(ipiv), lapack._ptr(b), ctypes.byref(c(n)),
+                           ctypes.byref(info))
+        return info.value
+
+    @staticmethod
+    def dsgesv(a, b, x):
+        n, nrhs = a.shape[0], b.shape[1]
+        ipiv = np.zeros(n, np.int32)
+        info = ctypes.c_int(0)
+        it = ctypes.c_int(0)
+        c = ctypes.c_int
+        lib().slate_dsgesv(ctypes.byref(c(n)), ctypes.byref(c(nrhs)), lapack._ptr(a), ctypes.byref(c(n)),
+                           lapack._ptr(ipiv), lapack._ptr(b), ctypes.byref(c(n)), lapack._ptr(x),
+                           ctypes.byref(c(n)), None, None, ctypes.byref(it), ctypes.byref(info))
+        return info.value, it.value, ipiv
+
+    @staticmethod
+    def dposv(uplo, a, b):
+        n, nrhs = a.shape[0], b.shape[1]
+        info = ctypes.c_int(0)
+        c = ctypes.c_int
+        lib().slate_dposv(ctypes.c_char_p(uplo.encode()), ctypes.byref(c(n)), ctypes.byref(c(nrhs)),
+                          lapack._ptr(a), ctypes.byref(c(n)), lapack._ptr(b), ctypes.byref(c(n)),
+                          ctypes.byref(info))
+        return info.value
+
+    @staticmethod
+    def dpotrf(uplo, a):
+        n = a.shape[0]
+        info = ctypes.c_int(0)
+        c = ctypes.c_int
+        lib().slate_dpotrf(ctypes.c_char_p(uplo.encode()), ctypes.byref(c(n)), lapack._ptr(a),
+                           ctypes.byref(c(n)), ctypes.byref(info))
+        return info.value

@@ -1,0 +1,560 @@
+// capi.cc -- the public C ABI (include/slate_gb300.h).
+//
+// LAPACK-compatible host entry points mirror SLATE's lapack_api/
+// (lapack_gesv.cc, lapack_gesv_mixed.cc, lapack_getrf.cc, lapack_getrs.cc,
+// lapack_posv.cc, lapack_potrf.cc): wrap the caller's column-major arrays,
+// run the Target::Devices path on a 1 x 1 grid, and return LAPACK's 1-based
+// ipiv (lapack_api/lapack_gesv.cc:90-100).
+
+#include "drivers.h"
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+namespace slt {
+double timer_value(const char* name);
+void timers_clear();
+}
+
+extern "C" int slt_dtranspose(int64_t m, int64_t n, const double* A, int64_t lda, double* B, int64_t ldb,
+                              cudaStream_t stream);
+
+using namespace slt;
+
+namespace {
+
+slt_options resolve(const slt_options* o)
+{
+    slt_options r;
+    slt_options_default(&r);
+    if (o) r = *o;
+    if (r.nb <= 0) r.nb = 512;
+    if (r.ib <= 0) r.ib = 32;
+    if (r.max_iterations < 0) r.max_iterations = 30;
+    return r;
+}
+
+cudaStream_t as_stream(slt_stream_t s) { return static_cast<cudaStream_t>(s); }
+
+struct Status {
+    DevBuf buf;
+    FactorCtx fc;
+    int init(cudaStream_t s) {
+        int rc = buf.alloc(2 * sizeof(int), s);
+        if (rc) return rc;
+        SLT_CUDA_TRY(cudaMemsetAsync(buf.p, 0, 2 * sizeof(int), s));
+        fc.d_info = buf.as<int>();
+        fc.d_status = buf.as<int>() + 1;
+        return SLT_OK;
+    }
+};
+
+int64_t env_int(const char* name, int64_t dflt)
+{
+    const char* v = std::getenv(name);
+    if (!v) return dflt;
+    int64_t x = std::strtoll(v, nullptr, 0);
+    return x != 0 ? x : dflt;
+}
+
+slt_options lapack_opts()
+{
+    slt_options o;
+    slt_options_default(&o);
+    o.nb = env_int("SLATE_LAPACK_NB", 512);
+    o.ib = std::min<int64_t>(env_int("SLATE_LAPACK_IB", 32), o.nb);
+    return o;
+}
+
+// Host <-> device helpers for the LAPACK entry points.
+template <typename T>
+int to_device(const T* h, int64_t m, int64_t n, int64_t ld, DevBuf& d, cudaStream_t s)
+{
+    int rc = d.alloc(sizeof(T) * size_t(std::max<int64_t>(m, 1)) * size_t(std::max<int64_t>(n, 1)), s);
+    if (rc) return rc;
+    if (m > 0 && n > 0)
+        SLT_CUDA_TRY(cudaMemcpy2DAsync(d.p, size_t(m) * sizeof(T), h, size_t(ld) * sizeof(T),
+                                       size_t(m) * sizeof(T), size_t(n), cudaMemcpyHostToDevice, s));
+    return SLT_OK;
+}
+
+template <typename T>
+int to_host(const DevBuf& d, T* h, int64_t m, int64_t n, int64_t ld, cudaStream_t s)
+{
+    if (m > 0 && n > 0)
+        SLT_CUDA_TRY(cudaMemcpy2DAsync(h, size_t(ld) * sizeof(T), d.p, size_t(m) * sizeof(T),
+                                       size_t(m) * sizeof(T), size_t(n), cudaMemcpyDeviceToHost, s));
+    return SLT_OK;
+}
+
+// Per-panel relative pivots -> LAPACK 1-based global ipiv, and back.
+void ipiv_to_lapack(const std::vector<int>& rel, int64_t nb, int* ipiv, int64_t cnt)
+{
+    for (int64_t r = 0; r < cnt; ++r) ipiv[r] = int((r / nb) * nb + rel[r] + 1);
+}
+
+void ipiv_from_lapack(const int* ipiv, int64_t nb, std::vector<int>& rel, int64_t cnt)
+{
+    rel.resize(cnt);
+    for (int64_t r = 0; r < cnt; ++r) rel[r] = int(ipiv[r] - 1 - (r / nb) * nb);
+}
+
+struct LapackStream {
+    cudaStream_t s = nullptr;
+    LapackStream() { if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) s = nullptr; }
+    ~LapackStream() { if (s) cudaStreamDestroy(s); }
+};
+
+cudaStream_t lapack_stream()
+{
+    static thread_local LapackStream ls;
+    return ls.s;
+}
+
+template <typename T>
+int getrf_device_impl(int64_t m, int64_t n, T* dA, int64_t lda, int* d_ipiv, const slt_options* opts,
+                      slt_stream_t stream, int64_t* info)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    Status st;
+    int rc = st.init(s);
+    if (rc) return rc;
+    rc = getrf_dev<T>(m, n, dA, lda, d_ipiv, o, st.fc, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, info, s);
+}
+
+} // namespace
+
+extern "C" {
+
+void slt_options_default(slt_options* o)
+{
+    if (!o) return;
+    o->nb = 512;
+    o->ib = 32;
+    o->lookahead = 1;
+    o->max_iterations = 30;
+    o->tolerance = 0.0;
+    o->use_fallback = 1;
+    o->pivot_threshold = 1.0;
+    o->factor_precision = SLT_PREC_FP32;
+    o->gemm_engine = 0;
+}
+
+const char* slt_status_string(int st)
+{
+    switch (st) {
+        case SLT_OK: return "success";
+        case SLT_ERR_ARG: return "invalid argument";
+        case SLT_ERR_TIMEOUT: return "a bounded device wait timed out";
+        case SLT_ERR_NOMEM: return "device allocation failed";
+        case SLT_ERR_NOT_SUPPORTED: return "not supported on this device or configuration";
+        case SLT_ERR_NO_DEVICE: return "no CUDA device";
+        case SLT_ERR_LIMIT: return "size exceeds a fixed limit";
+        default:
+            if (st >= SLT_ERR_CUDA_BASE) return cudaGetErrorString(cudaError_t(st - SLT_ERR_CUDA_BASE));
+            return "unknown status";
+    }
+}
+
+const char* slt_version(void) { return "slate_gb300 0.1 (sm_103a)"; }
+
+double slt_timer(const char* name) { return timer_value(name); }
+
+int slt_dgetrf_device(int64_t m, int64_t n, double* dA, int64_t lda, int* d_ipiv,
+                      const slt_options* opts, slt_stream_t stream, int64_t* info)
+{ return getrf_device_impl<double>(m, n, dA, lda, d_ipiv, opts, stream, info); }
+
+int slt_sgetrf_device(int64_t m, int64_t n, float* dA, int64_t lda, int* d_ipiv,
+                      const slt_options* opts, slt_stream_t stream, int64_t* info)
+{ return getrf_device_impl<float>(m, n, dA, lda, d_ipiv, opts, stream, info); }
+
+int slt_dgetrs_device(int64_t n, int64_t nrhs, const double* dLU, int64_t lda, const int* d_ipiv,
+                      double* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    int rc = getrs_dev<double>(n, nrhs, dLU, lda, d_ipiv, o.nb, dB, ldb, s);
+    if (rc) return rc;
+    return slt_from_cuda(cudaStreamSynchronize(s));
+}
+
+int slt_sgetrs_device(int64_t n, int64_t nrhs, const float* dLU, int64_t lda, const int* d_ipiv,
+                      float* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    int rc = getrs_dev<float>(n, nrhs, dLU, lda, d_ipiv, o.nb, dB, ldb, s);
+    if (rc) return rc;
+    return slt_from_cuda(cudaStreamSynchronize(s));
+}
+
+int slt_dgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv, double* dB,
+                     int64_t ldb, const slt_options* opts, slt_stream_t stream, int64_t* info)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    TimerSet tm(s);
+    tm.start("gesv");
+    tm.start("gesv::getrf");
+    Status st;
+    int rc = st.init(s);
+    if (rc) return rc;
+    rc = getrf_dev<double>(n, n, dA, lda, d_ipiv, o, st.fc, s);
+    if (rc) return rc;
+    tm.stop("gesv::getrf");
+    rc = finish_factor(st.fc, info, s);
+    if (rc) return rc;
+    tm.start("gesv::getrs");
+    if (*info == 0) {
+        rc = getrs_dev<double>(n, nrhs, dA, lda, d_ipiv, o.nb, dB, ldb, s);
+        if (rc) return rc;
+    }
+    tm.stop("gesv::getrs");
+    tm.stop("gesv");
+    return slt_from_cuda(cudaStreamSynchronize(s));
+}
+
+int slt_dpotrf_device(int64_t n, double* dA, int64_t lda, const slt_options* opts, slt_stream_t stream,
+                      int64_t* info)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    Status st;
+    int rc = st.init(s);
+    if (rc) return rc;
+    rc = potrf_dev<double>(n, dA, lda, o, st.fc, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, info, s);
+}
+
+int slt_spotrf_device(int64_t n, float* dA, int64_t lda, const slt_options* opts, slt_stream_t stream,
+                      int64_t* info)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    Status st;
+    int rc = st.init(s);
+    if (rc) return rc;
+    rc = potrf_dev<float>(n, dA, lda, o, st.fc, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, info, s);
+}
+
+int slt_dpotrs_device(int64_t n, int64_t nrhs, const double* dL, int64_t lda, double* dB, int64_t ldb,
+                      const slt_options* opts, slt_stream_t stream)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    int rc = potrs_dev<double>(n, nrhs, dL, lda, o.nb, dB, ldb, s);
+    if (rc) return rc;
+    return slt_from_cuda(cudaStreamSynchronize(s));
+}
+
+int slt_dposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, double* dB, int64_t ldb,
+                     const slt_options* opts, slt_stream_t stream, int64_t* info)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    TimerSet tm(s);
+    tm.start("posv");
+    Status st;
+    int rc = st.init(s);
+    if (rc) return rc;
+    tm.start("posv::potrf");
+    rc = potrf_dev<double>(n, dA, lda, o, st.fc, s);
+    if (rc) return rc;
+    tm.stop("posv::potrf");
+    rc = finish_factor(st.fc, info, s);
+    if (rc) return rc;
+    tm.start("posv::potrs");
+    if (*info == 0) {
+        rc = potrs_dev<double>(n, nrhs, dA, lda, o.nb, dB, ldb, s);
+        if (rc) return rc;
+    }
+    tm.stop("posv::potrs");
+    tm.stop("posv");
+    return slt_from_cuda(cudaStreamSynchronize(s));
+}
+
+int slt_dsgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv, const double* dB,
+                      int64_t ldb, double* dX, int64_t ldx, const slt_options* opts, slt_stream_t stream,
+                      int* iter, int64_t* info)
+{
+    slt_options o = resolve(opts);
+    return gesv_mixed_dev(0, n, nrhs, dA, lda, d_ipiv, dB, ldb, dX, ldx, o, iter, info, as_stream(stream));
+}
+
+int slt_dsgesv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv,
+                            const double* dB, int64_t ldb, double* dX, int64_t ldx,
+                            const slt_options* opts, slt_stream_t stream, int* iter, int64_t* info)
+{
+    slt_options o = resolve(opts);
+    return gesv_mixed_gmres_dev(0, n, nrhs, dA, lda, d_ipiv, dB, ldb, dX, ldx, o, iter, info,
+                                as_stream(stream));
+}
+
+int slt_dsposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, const double* dB, int64_t ldb,
+                      double* dX, int64_t ldx, const slt_options* opts, slt_stream_t stream, int* iter,
+                      int64_t* info)
+{
+    slt_options o = resolve(opts);
+    return gesv_mixed_dev(1, n, nrhs, dA, lda, nullptr, dB, ldb, dX, ldx, o, iter, info, as_stream(stream));
+}
+
+int slt_dsposv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, const double* dB,
+                            int64_t ldb, double* dX, int64_t ldx, const slt_options* opts,
+                            slt_stream_t stream, int* iter, int64_t* info)
+{
+    slt_options o = resolve(opts);
+    return gesv_mixed_gmres_dev(1, n, nrhs, dA, lda, nullptr, dB, ldb, dX, ldx, o, iter, info,
+                                as_stream(stream));
+}
+
+int slt_dgenerate_device(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
+                         double* dA, int64_t lda, slt_stream_t stream)
+{
+    cudaStream_t s = as_stream(stream);
+    int rc = slt_dgenerate(dist, seed, m, n, ioff, joff, dA, lda, s);
+    if (rc) return rc;
+    return slt_from_cuda(cudaStreamSynchronize(s));
+}
+
+// ---------------------------------------------------------------------------
+// LAPACK-compatible entry points.
+
+static void lapack_gesv_impl(int n, int nrhs, double* a, int lda, int* ipiv, double* b, int ldb, int* info)
+{
+    *info = 0;
+    if (n < 0) { *info = -1; return; }
+    if (nrhs < 0) { *info = -2; return; }
+    if (lda < std::max(1, n)) { *info = -4; return; }
+    if (ldb < std::max(1, n)) { *info = -7; return; }
+    if (n == 0) return;
+    cudaStream_t s = lapack_stream();
+    slt_options o = lapack_opts();
+    DevBuf dA, dB, dP;
+    if (to_device(a, n, n, lda, dA, s) || to_device(b, n, nrhs, ldb, dB, s) ||
+        dP.alloc(sizeof(int) * size_t(n), s)) { *info = -100; return; }
+    int64_t inf = 0;
+    int rc = slt_dgesv_device(n, nrhs, dA.as<double>(), n, dP.as<int>(), dB.as<double>(), n, &o, s, &inf);
+    if (rc) { *info = -1000 + rc; return; }
+    std::vector<int> rel(n);
+    if (to_host(dA, a, n, n, lda, s) || to_host(dB, b, n, nrhs, ldb, s) ||
+        cudaMemcpyAsync(rel.data(), dP.p, sizeof(int) * size_t(n), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+    ipiv_to_lapack(rel, o.nb, ipiv, n);
+    *info = int(inf);
+}
+
+void slate_dgesv(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv, double* b,
+                 const int* ldb, int* info)
+{ lapack_gesv_impl(*n, *nrhs, a, *lda, ipiv, b, *ldb, info); }
+void slate_dgesv_(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv, double* b,
+                  const int* ldb, int* info)
+{ lapack_gesv_impl(*n, *nrhs, a, *lda, ipiv, b, *ldb, info); }
+
+static void lapack_sgesv_impl(int n, int nrhs, float* a, int lda, int* ipiv, float* b, int ldb, int* info)
+{
+    *info = 0;
+    if (n < 0) { *info = -1; return; }
+    if (nrhs < 0) { *info = -2; return; }
+    if (lda < std::max(1, n)) { *info = -4; return; }
+    if (ldb < std::max(1, n)) { *info = -7; return; }
+    if (n == 0) return;
+    cudaStream_t s = lapack_stream();
+    slt_options o = lapack_opts();
+    DevBuf dA, dB, dP;
+    if (to_device(a, n, n, lda, dA, s) || to_device(b, n, nrhs, ldb, dB, s) ||
+        dP.alloc(sizeof(int) * size_t(n), s)) { *info = -100; return; }
+    int64_t inf = 0;
+    int rc = slt_sgetrf_device(n, n, dA.as<float>(), n, dP.as<int>(), &o, s, &inf);
+    if (rc) { *info = -1000 + rc; return; }
+    if (inf == 0) {
+        rc = slt_sgetrs_device(n, nrhs, dA.as<float>(), n, dP.as<int>(), dB.as<float>(), n, &o, s);
+        if (rc) { *info = -1000 + rc; return; }
+    }
+    std::vector<int> rel(n);
+    if (to_host(dA, a, n, n, lda, s) || to_host(dB, b, n, nrhs, ldb, s) ||
+        cudaMemcpyAsync(rel.data(), dP.p, sizeof(int) * size_t(n), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+    ipiv_to_lapack(rel, o.nb, ipiv, n);
+    *info = int(inf);
+}
+
+void slate_sgesv(const int* n, const int* nrhs, float* a, const int* lda, int* ipiv, float* b,
+                 const int* ldb, int* info)
+{ lapack_sgesv_impl(*n, *nrhs, a, *lda, ipiv, b, *ldb, info); }
+void slate_sgesv_(const int* n, const int* nrhs, float* a, const int* lda, int* ipiv, float* b,
+                  const int* ldb, int* info)
+{ lapack_sgesv_impl(*n, *nrhs, a, *lda, ipiv, b, *ldb, info); }
+
+} // extern "C"
+
+template <typename T>
+static void lapack_getrf_impl(int m, int n, T* a, int lda, int* ipiv, int* info)
+{
+    *info = 0;
+    if (m < 0) { *info = -1; return; }
+    if (n < 0) { *info = -2; return; }
+    if (lda < std::max(1, m)) { *info = -4; return; }
+    if (m == 0 || n == 0) return;
+    cudaStream_t s = lapack_stream();
+    slt_options o = lapack_opts();
+    const int mn = std::min(m, n);
+    DevBuf dA, dP;
+    if (to_device(a, m, n, lda, dA, s) || dP.alloc(sizeof(int) * size_t(mn), s)) { *info = -100; return; }
+    int64_t inf = 0;
+    int rc = getrf_device_impl<T>(m, n, dA.as<T>(), m, dP.as<int>(), &o, s, &inf);
+    if (rc) { *info = -1000 + rc; return; }
+    std::vector<int> rel(mn);
+    if (to_host(dA, a, m, n, lda, s) ||
+        cudaMemcpyAsync(rel.data(), dP.p, sizeof(int) * size_t(mn), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+    ipiv_to_lapack(rel, o.nb, ipiv, mn);
+    *info = int(inf);
+}
+
+extern "C" {
+
+void slate_dgetrf(const int* m, const int* n, double* a, const int* lda, int* ipiv, int* info)
+{ lapack_getrf_impl<double>(*m, *n, a, *lda, ipiv, info); }
+void slate_dgetrf_(const int* m, const int* n, double* a, const int* lda, int* ipiv, int* info)
+{ lapack_getrf_impl<double>(*m, *n, a, *lda, ipiv, info); }
+void slate_sgetrf(const int* m, const int* n, float* a, const int* lda, int* ipiv, int* info)
+{ lapack_getrf_impl<float>(*m, *n, a, *lda, ipiv, info); }
+void slate_sgetrf_(const int* m, const int* n, float* a, const int* lda, int* ipiv, int* info)
+{ lapack_getrf_impl<float>(*m, *n, a, *lda, ipiv, info); }
+
+static void lapack_getrs_impl(char trans, int n, int nrhs, double* a, int lda, int* ipiv, double* b, int ldb,
+                              int* info)
+{
+    *info = 0;
+    if (trans != 'N' && trans != 'n') { *info = -1; return; }
+    if (n < 0) { *info = -2; return; }
+    if (nrhs < 0) { *info = -3; return; }
+    if (lda < std::max(1, n)) { *info = -5; return; }
+    if (ldb < std::max(1, n)) { *info = -8; return; }
+    if (n == 0 || nrhs == 0) return;
+    cudaStream_t s = lapack_stream();
+    slt_options o = lapack_opts();
+    std::vector<int> rel;
+    ipiv_from_lapack(ipiv, o.nb, rel, n);
+    DevBuf dA, dB, dP;
+    if (to_device(a, n, n, lda, dA, s) || to_device(b, n, nrhs, ldb, dB, s) ||
+        to_device(rel.data(), n, 1, n, dP, s)) { *info = -100; return; }
+    int rc = slt_dgetrs_device(n, nrhs, dA.as<double>(), n, dP.as<int>(), dB.as<double>(), n, &o, s);
+    if (rc) { *info = -1000 + rc; return; }
+    if (to_host(dB, b, n, nrhs, ldb, s) || cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+}
+
+void slate_dgetrs(const char* trans, const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
+                  double* b, const int* ldb, int* info)
+{ lapack_getrs_impl(*trans, *n, *nrhs, a, *lda, ipiv, b, *ldb, info); }
+void slate_dgetrs_(const char* trans, const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
+                   double* b, const int* ldb, int* info)
+{ lapack_getrs_impl(*trans, *n, *nrhs, a, *lda, ipiv, b, *ldb, info); }
+
+static void lapack_dsgesv_impl(int n, int nrhs, double* a, int lda, int* ipiv, double* b, int ldb,
+                               double* x, int ldx, int* iter, int* info)
+{
+    *info = 0;
+    *iter = 0;
+    if (n < 0) { *info = -1; return; }
+    if (nrhs < 0) { *info = -2; return; }
+    if (lda < std::max(1, n)) { *info = -4; return; }
+    if (ldb < std::max(1, n)) { *info = -7; return; }
+    if (ldx < std::max(1, n)) { *info = -9; return; }
+    if (n == 0) return;
+    cudaStream_t s = lapack_stream();
+    slt_options o = lapack_opts();
+    DevBuf dA, dB, dX, dP;
+    if (to_device(a, n, n, lda, dA, s) || to_device(b, n, nrhs, ldb, dB, s) ||
+        dX.alloc(sizeof(double) * size_t(n) * size_t(std::max(nrhs, 1)), s) ||
+        dP.alloc(sizeof(int) * size_t(n), s)) { *info = -100; return; }
+    int64_t inf = 0;
+    int it = 0;
+    int rc = slt_dsgesv_device(n, nrhs, dA.as<double>(), n, dP.as<int>(), dB.as<double>(), n,
+                               dX.as<double>(), n, &o, s, &it, &inf);
+    if (rc) { *info = -1000 + rc; return; }
+    std::vector<int> rel(n);
+    if (to_host(dX, x, n, nrhs, ldx, s) || to_host(dA, a, n, n, lda, s) ||
+        cudaMemcpyAsync(rel.data(), dP.p, sizeof(int) * size_t(n), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+    ipiv_to_lapack(rel, o.nb, ipiv, n);
+    *iter = it;
+    *info = int(inf);
+}
+
+void slate_dsgesv(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv, double* b,
+                  const int* ldb, double* x, const int* ldx, double* work, float* swork, int* iter, int* info)
+{ (void) work; (void) swork; lapack_dsgesv_impl(*n, *nrhs, a, *lda, ipiv, b, *ldb, x, *ldx, iter, info); }
+void slate_dsgesv_(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv, double* b,
+                   const int* ldb, double* x, const int* ldx, double* work, float* swork, int* iter, int* info)
+{ (void) work; (void) swork; lapack_dsgesv_impl(*n, *nrhs, a, *lda, ipiv, b, *ldb, x, *ldx, iter, info); }
+
+// posv / potrf with uplo: an upper-stored matrix is transposed on the device
+// into lower storage (SLATE: A = conj_transpose(A), src/potrf.cc:45-47) and
+// the factor is transposed back.
+static int lower_view(char uplo, int64_t n, DevBuf& dA, DevBuf& tmp, cudaStream_t s)
+{
+    if (uplo == 'L' || uplo == 'l') return SLT_OK;
+    int rc = tmp.alloc(sizeof(double) * size_t(n) * size_t(n), s);
+    if (rc) return rc;
+    rc = slt_dtranspose(n, n, dA.as<double>(), n, tmp.as<double>(), n, s);
+    if (rc) return rc;
+    std::swap(dA.p, tmp.p);
+    return SLT_OK;
+}
+
+static void lapack_potrf_impl(char uplo, int n, double* a, int lda, int* info, int nrhs, double* b, int ldb)
+{
+    *info = 0;
+    bool up = (uplo == 'U' || uplo == 'u');
+    if (!up && uplo != 'L' && uplo != 'l') { *info = -1; return; }
+    if (n < 0) { *info = -2; return; }
+    if (nrhs < 0) { *info = -3; return; }
+    if (lda < std::max(1, n)) { *info = b ? -5 : -4; return; }
+    if (b && ldb < std::max(1, n)) { *info = -7; return; }
+    if (n == 0) return;
+    cudaStream_t s = lapack_stream();
+    slt_options o = lapack_opts();
+    DevBuf dA, dB, tmp;
+    if (to_device(a, n, n, lda, dA, s)) { *info = -100; return; }
+    if (b && to_device(b, n, nrhs, ldb, dB, s)) { *info = -100; return; }
+    if (lower_view(uplo, n, dA, tmp, s)) { *info = -100; return; }
+    int64_t inf = 0;
+    int rc = b ? slt_dposv_device(n, nrhs, dA.as<double>(), n, dB.as<double>(), n, &o, s, &inf)
+               : slt_dpotrf_device(n, dA.as<double>(), n, &o, s, &inf);
+    if (rc) { *info = -1000 + rc; return; }
+    if (up) {
+        rc = slt_dtranspose(n, n, dA.as<double>(), n, tmp.as<double>(), n, s);
+        if (rc) { *info = -1000 + rc; return; }
+        std::swap(dA.p, tmp.p);
+    }
+    // write back only the referenced triangle
+    std::vector<double> h(size_t(n) * size_t(n));
+    if (cudaMemcpyAsync(h.data(), dA.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        (b && to_host(dB, b, n, nrhs, ldb, s)) || cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i)
+            if (up ? (i <= j) : (i >= j)) a[i + size_t(j) * lda] = h[i + size_t(j) * n];
+    *info = int(inf);
+}
+
+void slate_dposv(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda, double* b,
+                 const int* ldb, int* info)
+{ lapack_potrf_impl(*uplo, *n, a, *lda, info, *nrhs, b, *ldb); }
+void slate_dposv_(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda, double* b,
+                  const int* ldb, int* info)
+{ lapack_potrf_impl(*uplo, *n, a, *lda, info, *nrhs, b, *ldb); }
+void slate_dpotrf(const char* uplo, const int* n, double* a, const int* lda, int* info)
+{ lapack_potrf_impl(*uplo, *n, a, *lda, info, 0, nullptr, 1); }
+void slate_dpotrf_(const char* uplo, const int* n, double* a, const int* lda, int* info)
+{ lapack_potrf_impl(*uplo, *n, a, *lda, info, 0, nullptr, 1); }
+
+} // extern "C"

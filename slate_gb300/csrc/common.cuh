@@ -1,0 +1,92 @@
+// common.cuh -- shared device helpers for the slate_gb300 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <algorithm>
+
+#include "slt_kernels.h"
+#include "status.h"
+
+namespace slt {
+
+// Iteration bound for every spin-wait in this library.  With the 64 ns sleep
+// below this is roughly 2-4 seconds, far longer than any legitimate wait, after
+// which the waiting block records SLT_ERR_TIMEOUT and leaves.
+constexpr long long kSpinLimit = 1ll << 25;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned atom_add_acqrel_u32(unsigned* p, unsigned v)
+{
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int ld_volatile_i32(const int* p)
+{
+    return *(const volatile int*) p;
+}
+
+// Grid-wide barrier for a cooperatively launched grid (all blocks are
+// co-resident, guaranteed by cudaLaunchCooperativeKernel).  Counter +
+// generation word in global memory, zeroed before launch.  Every wait is
+// bounded: on timeout the block sets *status = SLT_ERR_TIMEOUT.  Returns
+// false when the kernel must stop (status non-zero).
+struct GridBarrier {
+    unsigned count;
+    unsigned gen;
+};
+
+__device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned nblocks, int* status)
+{
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        unsigned g = ld_acquire_u32(&bar->gen);
+        unsigned arrived = atom_add_acqrel_u32(&bar->count, 1u);
+        if (arrived == nblocks - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            st_release_u32(&bar->gen, g + 1u);
+        }
+        else {
+            long long it = 0;
+            while (ld_acquire_u32(&bar->gen) == g) {
+                if (++it > kSpinLimit) {
+                    atomicCAS(status, 0, SLT_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        s_ok = (ld_volatile_i32(status) == 0);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <typename T> struct Real;
+template <> struct Real<double> {
+    static __device__ __forceinline__ double safe_min() { return 2.2250738585072014e-308; }
+};
+template <> struct Real<float> {
+    static __device__ __forceinline__ float safe_min() { return 1.17549435e-38f; }
+};
+
+__host__ __device__ inline int64_t ceildiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
+__host__ __device__ inline int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
+
+} // namespace slt

@@ -1,0 +1,586 @@
+// drivers.cc -- C++ host drivers of the LU / Cholesky solve path.
+//
+// The drivers issue stream-ordered launches of the kernel layer
+// (slt_kernels.h) and never synchronise inside a factorisation; the only
+// host reads are the ones SLATE's own algorithms need (norms and stopping
+// tests of the refinement loops, the Givens rotations of GMRES, info).
+
+#include "drivers.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace slt {
+
+// ---------------------------------------------------------------------------
+// Timers: the slate::timers keys of the reference drivers, measured with CUDA
+// events on the driver's stream and resolved when the call ends.
+static thread_local std::map<std::string, double> t_timers;
+
+TimerSet::~TimerSet()
+{
+    for (auto& kv : open) cudaEventDestroy(kv.second);
+    if (spans.empty()) return;
+    cudaStreamSynchronize(s);
+    std::map<std::string, double> acc;
+    for (auto& sp : spans) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, sp.a, sp.b) == cudaSuccess) acc[sp.key] += ms * 1e-3;
+        cudaEventDestroy(sp.a);
+        cudaEventDestroy(sp.b);
+    }
+    cudaGetLastError();
+    for (auto& kv : acc) t_timers[kv.first] = kv.second;
+}
+
+double timer_value(const char* name)
+{
+    auto it = t_timers.find(name);
+    return it == t_timers.end() ? -1.0 : it->second;
+}
+
+void timers_clear() { t_timers.clear(); }
+
+#define TRY(expr) do { int rc_ = (expr); if (rc_ != SLT_OK) return rc_; } while (0)
+
+// ---------------------------------------------------------------------------
+// Type dispatch onto the kernel layer.
+static int k_gemm(char tb, int64_t m, int64_t n, int64_t k, double alpha, const double* A, int64_t lda,
+                  const double* B, int64_t ldb, double beta, double* C, int64_t ldc, int lower,
+                  const slt_options& o, cudaStream_t s)
+{ return slt_dgemm(tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower, o.gemm_engine, s); }
+
+static int k_gemm(char tb, int64_t m, int64_t n, int64_t k, float alpha, const float* A, int64_t lda,
+                  const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int lower,
+                  const slt_options& o, cudaStream_t s)
+{
+    int tier = o.factor_precision;
+    if ((tier == SLT_PREC_TF32 || tier == SLT_PREC_BF16 || tier == SLT_PREC_FP16) && alpha == -1.f
+        && beta == 1.f && k >= 16 && m >= 128 && n >= 128)
+        return slt_tc_gemm_update(tier, tb, m, n, k, A, lda, B, ldb, C, ldc, lower, nullptr, 0, s);
+    return slt_sgemm(tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower, s);
+}
+
+static int k_panel(int64_t prows, int64_t nbk, int64_t ib, double* P, int64_t ld, int* ipiv, int* info,
+                   int64_t off, void* ws, int* status, cudaStream_t s)
+{ return slt_dgetrf_panel(prows, nbk, ib, P, ld, ipiv, info, off, ws, status, s); }
+static int k_panel(int64_t prows, int64_t nbk, int64_t ib, float* P, int64_t ld, int* ipiv, int* info,
+                   int64_t off, void* ws, int* status, cudaStream_t s)
+{ return slt_sgetrf_panel(prows, nbk, ib, P, ld, ipiv, info, off, ws, status, s); }
+
+static int k_laswp(const int* plan, int64_t maxc, double* A, int64_t lda, int64_t nc, cudaStream_t s)
+{ return slt_dlaswp_plan(plan, maxc, A, lda, nc, s); }
+static int k_laswp(const int* plan, int64_t maxc, float* A, int64_t lda, int64_t nc, cudaStream_t s)
+{ return slt_slaswp_plan(plan, maxc, A, lda, nc, s); }
+
+static int k_trsm_llnu(int64_t kb, int64_t n, const double* L, int64_t ldl, double* B, int64_t ldb, cudaStream_t s)
+{ return slt_dtrsm_llnu(kb, n, L, ldl, B, ldb, s); }
+static int k_trsm_llnu(int64_t kb, int64_t n, const float* L, int64_t ldl, float* B, int64_t ldb, cudaStream_t s)
+{ return slt_strsm_llnu(kb, n, L, ldl, B, ldb, s); }
+static int k_trsm_lunn(int64_t kb, int64_t n, const double* U, int64_t ldu, double* B, int64_t ldb, cudaStream_t s)
+{ return slt_dtrsm_lunn(kb, n, U, ldu, B, ldb, s); }
+static int k_trsm_lunn(int64_t kb, int64_t n, const float* U, int64_t ldu, float* B, int64_t ldb, cudaStream_t s)
+{ return slt_strsm_lunn(kb, n, U, ldu, B, ldb, s); }
+static int k_trsm_llnn(char tr, int64_t kb, int64_t n, const double* L, int64_t ldl, double* B, int64_t ldb, cudaStream_t s)
+{ return slt_dtrsm_llnn(tr, kb, n, L, ldl, B, ldb, s); }
+static int k_trsm_llnn(char tr, int64_t kb, int64_t n, const float* L, int64_t ldl, float* B, int64_t ldb, cudaStream_t s)
+{ return slt_strsm_llnn(tr, kb, n, L, ldl, B, ldb, s); }
+static int k_trsm_rltn(int64_t m, int64_t kb, const double* L, int64_t ldl, double* B, int64_t ldb, cudaStream_t s)
+{ return slt_dtrsm_rltn(m, kb, L, ldl, B, ldb, s); }
+static int k_trsm_rltn(int64_t m, int64_t kb, const float* L, int64_t ldl, float* B, int64_t ldb, cudaStream_t s)
+{ return slt_strsm_rltn(m, kb, L, ldl, B, ldb, s); }
+static int k_potrf_small(int64_t kb, double* A, int64_t lda, int* info, int64_t off, cudaStream_t s)
+{ return slt_dpotrf_small(kb, A, lda, info, off, s); }
+static int k_potrf_small(int64_t kb, float* A, int64_t lda, int* info, int64_t off, cudaStream_t s)
+{ return slt_spotrf_small(kb, A, lda, info, off, s); }
+
+static int k_skinny(int64_t m, int64_t nrhs, int64_t k, double alpha, const double* A, int64_t lda,
+                    const double* X, int64_t ldx, double beta, double* C, int64_t ldc, void* ws, cudaStream_t s)
+{ return slt_dgemm_skinny(m, nrhs, k, alpha, A, lda, 0, X, ldx, beta, C, ldc, ws, s); }
+static int k_skinny(int64_t m, int64_t nrhs, int64_t k, float alpha, const float* A, int64_t lda,
+                    const float* X, int64_t ldx, float beta, float* C, int64_t ldc, void*, cudaStream_t s)
+{ return slt_sgemm_skinny(m, nrhs, k, alpha, A, lda, X, ldx, beta, C, ldc, s); }
+static int k_skinny_t(int64_t m, int64_t nrhs, int64_t kk, double alpha, const double* A, int64_t lda,
+                      const double* X, int64_t ldx, double beta, double* C, int64_t ldc, cudaStream_t s)
+{ return slt_dgemm_skinny_t(m, nrhs, kk, alpha, A, lda, X, ldx, beta, C, ldc, s); }
+static int k_skinny_t(int64_t m, int64_t nrhs, int64_t kk, float alpha, const float* A, int64_t lda,
+                      const float* X, int64_t ldx, float beta, float* C, int64_t ldc, cudaStream_t s)
+{ return slt_sgemm_skinny_t(m, nrhs, kk, alpha, A, lda, X, ldx, beta, C, ldc, s); }
+static int k_permute(int fwd, const int* perm, int64_t n, int64_t nc, const double* X, int64_t ldx,
+                     double* Y, int64_t ldy, cudaStream_t s)
+{ return slt_dpermute_rows(fwd, perm, n, nc, X, ldx, Y, ldy, s); }
+static int k_permute(int fwd, const int* perm, int64_t n, int64_t nc, const float* X, int64_t ldx,
+                     float* Y, int64_t ldy, cudaStream_t s)
+{ return slt_spermute_rows(fwd, perm, n, nc, X, ldx, Y, ldy, s); }
+
+static int64_t eff_nb(const slt_options& o) { return o.nb > 0 ? o.nb : 512; }
+static int64_t eff_ib(const slt_options& o, int64_t nb)
+{
+    int64_t ib = o.ib > 0 ? o.ib : 32;
+    return std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(ib, 64), nb));
+}
+
+int finish_factor(FactorCtx& fc, int64_t* info, cudaStream_t s)
+{
+    int h[2] = {0, 0};
+    if (fc.d_info) SLT_CUDA_TRY(cudaMemcpyAsync(&h[0], fc.d_info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (fc.d_status) SLT_CUDA_TRY(cudaMemcpyAsync(&h[1], fc.d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SLT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (info) *info = h[0];
+    return h[1] != 0 ? h[1] : SLT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// LU: right-looking, one cooperative panel launch per block column, then the
+// panel's interchanges on both sides, the U12 solve and the trailing GEMM
+// (impl::getrf, src/getrf.cc:22-244).
+template <typename T>
+int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_options& o,
+              FactorCtx& fc, cudaStream_t s)
+{
+    if (m < 0 || n < 0 || lda < std::max<int64_t>(1, m)) return SLT_ERR_ARG;
+    const int64_t nb = eff_nb(o);
+    const int64_t ib = eff_ib(o, nb);
+    const int64_t mn = std::min(m, n);
+    if (mn == 0) return SLT_OK;
+    if (nb > 1024) return SLT_ERR_ARG;
+    DevBuf pws, plan;
+    TRY(pws.alloc(slt_getrf_panel_ws_bytes(m, ib), s));
+    TRY(plan.alloc(sizeof(int) * size_t(1 + 4 * nb), s));
+    for (int64_t r0 = 0; r0 < mn; r0 += nb) {
+        const int64_t nbk = std::min(nb, n - r0);
+        const int64_t prows = m - r0;
+        const int64_t diag = std::min(prows, nbk);
+        T* P = A + r0 + r0 * lda;
+        TRY(k_panel(prows, nbk, ib, P, lda, ipiv + r0, fc.d_info, r0, pws.p, fc.d_status, s));
+        TRY(slt_swap_plan(ipiv + r0, diag, r0, plan.as<int>(), s));
+        const int64_t c1 = r0 + nbk;
+        TRY(k_laswp(plan.as<int>(), 2 * diag, A + c1 * lda, lda, n - c1, s));
+        TRY(k_laswp(plan.as<int>(), 2 * diag, A, lda, r0, s));
+        if (c1 < n) {
+            TRY(k_trsm_llnu(diag, n - c1, P, lda, A + r0 + c1 * lda, lda, s));
+            if (r0 + diag < m)
+                TRY(k_gemm('N', m - r0 - diag, n - c1, diag, T(-1), A + (r0 + diag) + r0 * lda, lda,
+                           A + r0 + c1 * lda, lda, T(1), A + (r0 + diag) + c1 * lda, lda, 0, o, s));
+        }
+    }
+    return SLT_OK;
+}
+
+// getrs NoTrans: W = P B, forward sweep with unit L, backward with U
+// (src/getrs.cc:66-117; work::trsmA, src/work/work_trsmA.cc:147-480).
+template <typename T>
+int getrs_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv, int64_t nb,
+              T* B, int64_t ldb, cudaStream_t s)
+{
+    if (n < 0 || nrhs < 0) return SLT_ERR_ARG;
+    if (n == 0 || nrhs == 0) return SLT_OK;
+    DevBuf perm, W, ws;
+    TRY(perm.alloc(sizeof(int) * size_t(n), s));
+    TRY(W.alloc(sizeof(T) * size_t(n) * size_t(nrhs), s));
+    TRY(ws.alloc(slt_residual_ws_bytes(n, std::min<int64_t>(nrhs, 16)), s));
+    TRY(slt_perm_from_ipiv(ipiv, n, nb, perm.as<int>(), s));
+    T* w = W.as<T>();
+    for (int64_t c0 = 0; c0 < nrhs; c0 += 16) {
+        const int64_t nc = std::min<int64_t>(16, nrhs - c0);
+        TRY(k_permute(1, perm.as<int>(), n, nc, B + c0 * ldb, ldb, w, n, s));
+        for (int64_t r0 = 0; r0 < n; r0 += nb) {
+            const int64_t kb = std::min(nb, n - r0);
+            TRY(k_trsm_llnu(kb, nc, LU + r0 + r0 * lda, lda, w + r0, n, s));
+            if (r0 + kb < n)
+                TRY(k_skinny(n - r0 - kb, nc, kb, T(-1), LU + (r0 + kb) + r0 * lda, lda, w + r0, n, T(1),
+                             w + r0 + kb, n, ws.p, s));
+        }
+        for (int64_t r0 = ((n - 1) / nb) * nb; r0 >= 0; r0 -= nb) {
+            const int64_t kb = std::min(nb, n - r0);
+            TRY(k_trsm_lunn(kb, nc, LU + r0 + r0 * lda, lda, w + r0, n, s));
+            if (r0 > 0)
+                TRY(k_skinny(r0, nc, kb, T(-1), LU + r0 * lda, lda, w + r0, n, T(1), w, n, ws.p, s));
+        }
+        SLT_CUDA_TRY(cudaMemcpy2DAsync(B + c0 * ldb, size_t(ldb) * sizeof(T), w, size_t(n) * sizeof(T),
+                                       size_t(n) * sizeof(T), size_t(nc), cudaMemcpyDeviceToDevice, s));
+    }
+    return SLT_OK;
+}
+
+// Cholesky, lower: block columns of nb; inside a block column, 64-wide
+// steps of small potrf + solve of everything below + update of the rest of
+// the block column; then the herk-shaped trailing update
+// (impl::potrf, src/potrf.cc:22-210).
+template <typename T>
+int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc, cudaStream_t s)
+{
+    if (n < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
+    const int64_t nb = eff_nb(o);
+    const int64_t inner = 64;
+    for (int64_t r0 = 0; r0 < n; r0 += nb) {
+        const int64_t kb = std::min(nb, n - r0);
+        for (int64_t b = 0; b < kb; b += inner) {
+            const int64_t bs = std::min(inner, kb - b);
+            const int64_t c = r0 + b;
+            TRY(k_potrf_small(bs, A + c + c * lda, lda, fc.d_info, c, s));
+            const int64_t below = n - (c + bs);
+            if (below > 0) TRY(k_trsm_rltn(below, bs, A + c + c * lda, lda, A + (c + bs) + c * lda, lda, s));
+            const int64_t ncols = r0 + kb - (c + bs);
+            if (ncols > 0)
+                TRY(k_gemm('T', below, ncols, bs, T(-1), A + (c + bs) + c * lda, lda, A + (c + bs) + c * lda,
+                           lda, T(1), A + (c + bs) + (c + bs) * lda, lda, 1, o, s));
+        }
+        const int64_t t0 = r0 + kb;
+        if (t0 < n)
+            TRY(k_gemm('T', n - t0, n - t0, kb, T(-1), A + t0 + r0 * lda, lda, A + t0 + r0 * lda, lda, T(1),
+                       A + t0 + t0 * lda, lda, 1, o, s));
+    }
+    return SLT_OK;
+}
+
+// potrs lower: forward with L, backward with L^T (src/potrs.cc:55-78).
+template <typename T>
+int potrs_dev(int64_t n, int64_t nrhs, const T* L, int64_t lda, int64_t nb, T* B, int64_t ldb,
+              cudaStream_t s)
+{
+    if (n < 0 || nrhs < 0) return SLT_ERR_ARG;
+    if (n == 0 || nrhs == 0) return SLT_OK;
+    DevBuf ws;
+    TRY(ws.alloc(slt_residual_ws_bytes(n, std::min<int64_t>(nrhs, 16)), s));
+    for (int64_t c0 = 0; c0 < nrhs; c0 += 16) {
+        const int64_t nc = std::min<int64_t>(16, nrhs - c0);
+        T* b = B + c0 * ldb;
+        for (int64_t r0 = 0; r0 < n; r0 += nb) {
+            const int64_t kb = std::min(nb, n - r0);
+            TRY(k_trsm_llnn('N', kb, nc, L + r0 + r0 * lda, lda, b + r0, ldb, s));
+            if (r0 + kb < n)
+                TRY(k_skinny(n - r0 - kb, nc, kb, T(-1), L + (r0 + kb) + r0 * lda, lda, b + r0, ldb, T(1),
+                             b + r0 + kb, ldb, ws.p, s));
+        }
+        for (int64_t r0 = ((n - 1) / nb) * nb; r0 >= 0; r0 -= nb) {
+            const int64_t kb = std::min(nb, n - r0);
+            TRY(k_trsm_llnn('T', kb, nc, L + r0 + r0 * lda, lda, b + r0, ldb, s));
+            if (r0 > 0)
+                TRY(k_skinny_t(r0, nc, kb, T(-1), L + r0, lda, b + r0, ldb, T(1), b, ldb, s));
+        }
+    }
+    return SLT_OK;
+}
+
+template int getrf_dev<double>(int64_t, int64_t, double*, int64_t, int*, const slt_options&, FactorCtx&, cudaStream_t);
+template int getrf_dev<float>(int64_t, int64_t, float*, int64_t, int*, const slt_options&, FactorCtx&, cudaStream_t);
+template int getrs_dev<double>(int64_t, int64_t, const double*, int64_t, const int*, int64_t, double*, int64_t, cudaStream_t);
+template int getrs_dev<float>(int64_t, int64_t, const float*, int64_t, const int*, int64_t, float*, int64_t, cudaStream_t);
+template int potrf_dev<double>(int64_t, double*, int64_t, const slt_options&, FactorCtx&, cudaStream_t);
+template int potrf_dev<float>(int64_t, float*, int64_t, const slt_options&, FactorCtx&, cudaStream_t);
+template int potrs_dev<double>(int64_t, int64_t, const double*, int64_t, int64_t, double*, int64_t, cudaStream_t);
+template int potrs_dev<float>(int64_t, int64_t, const float*, int64_t, int64_t, float*, int64_t, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Mixed precision.
+namespace {
+
+struct LoFactor {
+    int chol;
+    int64_t n, nb;
+    slt_options o;
+    DevBuf A;          // float n x n
+    int* ipiv;
+
+    int factor(const double* Ahi, int64_t lda, FactorCtx& fc, int64_t* info, cudaStream_t s) {
+        TRY(A.alloc(sizeof(float) * size_t(n) * size_t(n), s));
+        TRY(slt_convert_d2s(n, n, Ahi, lda, A.as<float>(), n, s));
+        if (chol) TRY(potrf_dev<float>(n, A.as<float>(), n, o, fc, s));
+        else TRY(getrf_dev<float>(n, n, A.as<float>(), n, ipiv, o, fc, s));
+        return finish_factor(fc, info, s);
+    }
+    // X (double) <- M^{-1} R (double), through FP32.
+    int solve(int64_t nrhs, const double* R, int64_t ldr, double* X, int64_t ldx, float* wlo, cudaStream_t s) {
+        TRY(slt_convert_d2s(n, nrhs, R, ldr, wlo, n, s));
+        if (chol) TRY(potrs_dev<float>(n, nrhs, A.as<float>(), n, nb, wlo, n, s));
+        else TRY(getrs_dev<float>(n, nrhs, A.as<float>(), n, ipiv, nb, wlo, n, s));
+        return slt_convert_s2d(n, nrhs, wlo, n, X, ldx, s);
+    }
+};
+
+int read_doubles(const double* d, double* h, int64_t cnt, cudaStream_t s)
+{
+    SLT_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(double) * size_t(cnt), cudaMemcpyDeviceToHost, s));
+    SLT_CUDA_TRY(cudaStreamSynchronize(s));
+    return SLT_OK;
+}
+
+bool converged(const double* cr, const double* cx, int64_t k, double cte)
+{
+    for (int64_t i = 0; i < k; ++i)
+        if (!(cr[i] <= cx[i] * cte)) return false;
+    return true;
+}
+
+int fallback_fp64(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                  const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,
+                  int64_t* info, TimerSet& tm, const char* pfx, cudaStream_t s)
+{
+    DevBuf st;
+    TRY(st.alloc(2 * sizeof(int), s));
+    SLT_CUDA_TRY(cudaMemsetAsync(st.p, 0, 2 * sizeof(int), s));
+    FactorCtx fc{st.as<int>(), st.as<int>() + 1};
+    slt_options o64 = o;
+    o64.factor_precision = SLT_PREC_FP64;
+    tm.start(std::string(pfx) + (chol ? "::potrf_hi" : "::getrf_hi"));
+    if (chol) TRY(potrf_dev<double>(n, A, lda, o64, fc, s));
+    else TRY(getrf_dev<double>(n, n, A, lda, ipiv, o64, fc, s));
+    tm.stop(std::string(pfx) + (chol ? "::potrf_hi" : "::getrf_hi"));
+    TRY(finish_factor(fc, info, s));
+    if (*info == 0) {
+        tm.start(std::string(pfx) + (chol ? "::potrs_hi" : "::getrs_hi"));
+        TRY(slt_dcopy2d(n, nrhs, B, ldb, X, ldx, s));
+        if (chol) TRY(potrs_dev<double>(n, nrhs, A, lda, eff_nb(o), X, ldx, s));
+        else TRY(getrs_dev<double>(n, nrhs, A, lda, ipiv, eff_nb(o), X, ldx, s));
+        tm.stop(std::string(pfx) + (chol ? "::potrs_hi" : "::getrs_hi"));
+    }
+    return SLT_OK;
+}
+
+} // namespace
+
+// gesv_mixed / posv_mixed (src/gesv_mixed.cc:105-289, src/posv_mixed.cc:105-320).
+int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                   const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,
+                   int* iter, int64_t* info, cudaStream_t s)
+{
+    if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
+    *iter = 0;
+    *info = 0;
+    if (n == 0 || nrhs == 0) return SLT_OK;
+    const char* pfx = chol ? "posv_mixed" : "gesv_mixed";
+    TimerSet tm(s);
+    tm.start(pfx);
+    const double eps = std::numeric_limits<double>::epsilon();
+    const double tol = o.tolerance > 0 ? o.tolerance : eps * std::sqrt(double(n));
+    const int64_t itermax = o.max_iterations;
+    const int64_t nb = eff_nb(o);
+
+    DevBuf nws, scal, R, Wlo, st, col;
+    TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, std::min<int64_t>(nrhs, 16))), s));
+    TRY(scal.alloc(sizeof(double) * 4, s));
+    TRY(R.alloc(sizeof(double) * size_t(n) * size_t(nrhs), s));
+    TRY(Wlo.alloc(sizeof(float) * size_t(n) * size_t(nrhs), s));
+    TRY(st.alloc(2 * sizeof(int), s));
+    TRY(col.alloc(sizeof(double) * 2 * size_t(nrhs), s));
+    SLT_CUDA_TRY(cudaMemsetAsync(st.p, 0, 2 * sizeof(int), s));
+    FactorCtx fc{st.as<int>(), st.as<int>() + 1};
+
+    double Anorm = 0;
+    TRY(slt_dnorm_inf(n, n, A, lda, chol, scal.as<double>(), nws.p, s));
+    TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
+    const double cte = Anorm * tol;
+
+    LoFactor lo{chol, n, nb, o, {}, ipiv};
+    if (lo.o.factor_precision == SLT_PREC_FP64) lo.o.factor_precision = SLT_PREC_FP32;
+    int64_t linfo = 0;
+    tm.start(std::string(pfx) + (chol ? "::potrf_lo" : "::getrf_lo"));
+    TRY(lo.factor(A, lda, fc, &linfo, s));
+    tm.stop(std::string(pfx) + (chol ? "::potrf_lo" : "::getrf_lo"));
+    bool conv = false;
+    std::vector<double> h(2 * nrhs);
+    double* dcx = col.as<double>();
+    double* dcr = dcx + nrhs;
+    const int64_t rhs_chunks = (nrhs + 15) / 16;
+    auto residual = [&]() -> int {
+        tm.start(std::string(pfx) + (chol ? "::hemm_hi" : "::gemm_hi"));
+        for (int64_t c = 0; c < rhs_chunks; ++c) {
+            int64_t c0 = c * 16, nc = std::min<int64_t>(16, nrhs - c0);
+            TRY(slt_dresidual(n, nc, A, lda, chol, B + c0 * ldb, ldb, X + c0 * ldx, ldx,
+                              R.as<double>() + c0 * n, n, nws.p, s));
+        }
+        tm.stop(std::string(pfx) + (chol ? "::hemm_hi" : "::gemm_hi"));
+        TRY(slt_dcolmax(n, nrhs, X, ldx, dcx, s));
+        TRY(slt_dcolmax(n, nrhs, R.as<double>(), n, dcr, s));
+        return read_doubles(dcx, h.data(), 2 * nrhs, s);
+    };
+    if (linfo != 0) {
+        *iter = -3;
+    }
+    else {
+        tm.start(std::string(pfx) + (chol ? "::potrs_lo" : "::getrs_lo"));
+        TRY(lo.solve(nrhs, B, ldb, X, ldx, Wlo.as<float>(), s));
+        tm.stop(std::string(pfx) + (chol ? "::potrs_lo" : "::getrs_lo"));
+        TRY(residual());
+        if (converged(h.data() + nrhs, h.data(), nrhs, cte)) { *iter = 0; conv = true; }
+        for (int64_t it = 0; it < itermax && !conv; ++it) {
+            TRY(lo.solve(nrhs, R.as<double>(), n, R.as<double>(), n, Wlo.as<float>(), s));
+            TRY(slt_dgeadd(n, nrhs, 1.0, R.as<double>(), n, 1.0, X, ldx, s));
+            TRY(residual());
+            if (converged(h.data() + nrhs, h.data(), nrhs, cte)) { *iter = int(it + 1); conv = true; }
+        }
+    }
+    *info = linfo;
+    if (!conv) {
+        if (linfo == 0) *iter = int(-itermax - 1);
+        if (o.use_fallback)
+            TRY(fallback_fp64(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, o, info, tm, pfx, s));
+    }
+    tm.stop(pfx);
+    SLT_CUDA_TRY(cudaStreamSynchronize(s));
+    return SLT_OK;
+}
+
+// gesv_mixed_gmres / posv_mixed_gmres (src/gesv_mixed_gmres.cc:110-410,
+// src/posv_mixed_gmres.cc:109-436): FGMRES(restart) preconditioned by the
+// low-precision factors, CGS2 Arnoldi in FP64, Givens rotations on the
+// host.  Each right-hand side is an independent instance sharing the
+// factorisation.
+int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                         const double* B, int64_t ldb, double* X, int64_t ldx,
+                         const slt_options& o, int* iter, int64_t* info, cudaStream_t s)
+{
+    if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
+    *iter = 0;
+    *info = 0;
+    if (n == 0 || nrhs == 0) return SLT_OK;
+    const char* pfx = chol ? "posv_mixed_gmres" : "gesv_mixed_gmres";
+    TimerSet tm(s);
+    tm.start(pfx);
+    const double eps = std::numeric_limits<double>::epsilon();
+    const double tol = o.tolerance > 0 ? o.tolerance : eps * std::sqrt(double(n));
+    const int64_t itermax = o.max_iterations;
+    const int64_t nb = eff_nb(o);
+    const int64_t restart = std::max<int64_t>(
+        0, std::min<int64_t>(std::min<int64_t>(30, itermax), std::min(nb, n) - 1));
+    const int64_t R1 = restart + 1;
+
+    DevBuf nws, scal, st, V, W, vec, Wlo;
+    TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, 1)), s));
+    TRY(scal.alloc(sizeof(double) * (4 + 4 * R1), s));
+    TRY(st.alloc(2 * sizeof(int), s));
+    TRY(V.alloc(sizeof(double) * size_t(n) * size_t(R1), s));
+    TRY(W.alloc(sizeof(double) * size_t(n) * size_t(R1), s));
+    TRY(vec.alloc(sizeof(double) * size_t(n), s));
+    TRY(Wlo.alloc(sizeof(float) * size_t(n) * size_t(std::max<int64_t>(nrhs, 1)), s));
+    SLT_CUDA_TRY(cudaMemsetAsync(st.p, 0, 2 * sizeof(int), s));
+    FactorCtx fc{st.as<int>(), st.as<int>() + 1};
+    double* dsc = scal.as<double>();
+    double* dh = dsc + 4;
+    double* dz = dh + R1;
+    double* dy = dz + R1;
+
+    double Anorm = 0;
+    TRY(slt_dnorm_inf(n, n, A, lda, chol, dsc, nws.p, s));
+    TRY(read_doubles(dsc, &Anorm, 1, s));
+    const double cte = Anorm * tol;
+
+    LoFactor lo{chol, n, nb, o, {}, ipiv};
+    if (lo.o.factor_precision == SLT_PREC_FP64) lo.o.factor_precision = SLT_PREC_FP32;
+    int64_t linfo = 0;
+    tm.start(std::string(pfx) + (chol ? "::potrf_lo" : "::getrf_lo"));
+    TRY(lo.factor(A, lda, fc, &linfo, s));
+    tm.stop(std::string(pfx) + (chol ? "::potrf_lo" : "::getrf_lo"));
+    *info = linfo;
+    bool all_conv = true;
+    int worst_iter = 0;
+    double* Vd = V.as<double>();
+    double* Wd = W.as<double>();
+    float* wlo = Wlo.as<float>();
+    if (linfo != 0) {
+        *iter = -3;
+        all_conv = false;
+    }
+    else {
+        std::vector<double> H(size_t(R1) * size_t(R1)), S(R1), gc(R1), gs(R1), hh(2 * R1);
+        for (int64_t c = 0; c < nrhs; ++c) {
+            const double* b = B + c * ldb;
+            double* x = X + c * ldx;
+            bool conv = false;
+            int citer = 0;
+            TRY(lo.solve(1, b, ldb, x, ldx, wlo, s));
+            int64_t iiter = 0;
+            double cx = 0, cr = 0;
+            while (iiter < itermax) {
+                // residual and stopping test
+                TRY(slt_dresidual(n, 1, A, lda, chol, b, ldb, x, ldx, Vd, n, nws.p, s));
+                TRY(slt_dcolmax(n, 1, x, ldx, dsc, s));
+                TRY(slt_dcolmax(n, 1, Vd, n, dsc + 1, s));
+                TRY(slt_dnrm2(n, Vd, dsc + 2, s));
+                double hv[3];
+                TRY(read_doubles(dsc, hv, 3, s));
+                cx = hv[0]; cr = hv[1];
+                if (cr <= cx * cte) { citer = int(iiter); conv = true; break; }
+                double ares = hv[2];
+                if (ares == 0) { citer = int(iiter); conv = false; break; }
+                TRY(slt_dgeadd(n, 1, 1.0 / ares, Vd, n, 0.0, Vd, n, s));
+                S.assign(R1, 0.0);
+                S[0] = ares;
+                int64_t j = 0;
+                for (; j < restart && iiter < itermax && !(ares <= cx * cte); ++j, ++iiter) {
+                    double* vj1 = Vd + (j + 1) * n;
+                    double* wj1 = Wd + (j + 1) * n;
+                    TRY(lo.solve(1, Vd + j * n, n, wj1, n, wlo, s));
+                    TRY(slt_dgemm_skinny(n, 1, n, 1.0, A, lda, chol, wj1, n, 0.0, vj1, n, nws.p, s));
+                    // CGS2
+                    TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dh, R1, s));
+                    TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dh, R1, 1.0, vj1, n, nws.p, s));
+                    TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dz, R1, s));
+                    TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dz, R1, 1.0, vj1, n, nws.p, s));
+                    TRY(slt_dnrm2(n, vj1, dsc + 3, s));
+                    TRY(read_doubles(dh, hh.data(), 2 * R1, s));
+                    double nrm = 0;
+                    TRY(read_doubles(dsc + 3, &nrm, 1, s));
+                    TRY(slt_dgeadd(n, 1, 1.0 / nrm, vj1, n, 0.0, vj1, n, s));
+                    double* hj = H.data() + j * R1;
+                    for (int64_t i = 0; i <= j; ++i) hj[i] = hh[i] + hh[R1 + i];
+                    hj[j + 1] = nrm;
+                    auto rot = [](double* xx, double* yy, double cc, double ss) {
+                        double tx = cc * *xx + ss * *yy;
+                        double ty = cc * *yy - ss * *xx;
+                        *xx = tx; *yy = ty;
+                    };
+                    for (int64_t i = 0; i < j; ++i) rot(&hj[i], &hj[i + 1], gc[i], gs[i]);
+                    {
+                        double a = hj[j], bb = hj[j + 1];
+                        double roe = std::fabs(a) > std::fabs(bb) ? a : bb;
+                        double scale = std::fabs(a) + std::fabs(bb);
+                        if (scale == 0) { gc[j] = 1; gs[j] = 0; }
+                        else {
+                            double r = scale * std::sqrt((a / scale) * (a / scale) + (bb / scale) * (bb / scale));
+                            r = std::copysign(1.0, roe) * r;
+                            gc[j] = a / r; gs[j] = bb / r;
+                        }
+                    }
+                    rot(&hj[j], &hj[j + 1], gc[j], gs[j]);
+                    rot(&S[j], &S[j + 1], gc[j], gs[j]);
+                    ares = std::fabs(S[j + 1]);
+                }
+                // X += W(:, 1:j) H(0:j-1, 0:j-1)^{-1} S(0:j-1)
+                if (j > 0) {
+                    std::vector<double> y(S.begin(), S.begin() + j);
+                    for (int64_t r = j - 1; r >= 0; --r) {
+                        double sum = y[r];
+                        for (int64_t cc = r + 1; cc < j; ++cc) sum -= H[r + cc * R1] * y[cc];
+                        y[r] = sum / H[r + r * R1];
+                    }
+                    SLT_CUDA_TRY(cudaMemcpyAsync(dy, y.data(), sizeof(double) * size_t(j),
+                                                 cudaMemcpyHostToDevice, s));
+                    TRY(slt_dgemm_skinny(n, 1, j, 1.0, Wd + n, n, 0, dy, R1, 1.0, x, ldx, nws.p, s));
+                    SLT_CUDA_TRY(cudaStreamSynchronize(s));
+                }
+            }
+            if (!conv) { all_conv = false; citer = int(-itermax - 1); }
+            worst_iter = (c == 0) ? citer : (citer < 0 || worst_iter < 0 ? std::min(worst_iter, citer)
+                                                                        : std::max(worst_iter, citer));
+        }
+        *iter = worst_iter;
+    }
+    if (!all_conv) {
+        if (linfo == 0 && *iter >= 0) *iter = int(-itermax - 1);
+        if (o.use_fallback)
+            TRY(fallback_fp64(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, o, info, tm, pfx, s));
+    }
+    tm.stop(pfx);
+    SLT_CUDA_TRY(cudaStreamSynchronize(s));
+    return SLT_OK;
+}
+
+} // namespace slt

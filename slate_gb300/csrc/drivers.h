@@ -1,0 +1,112 @@
+// drivers.h -- C++ host drivers of the LU / Cholesky solve path (internal).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "slt_kernels.h"
+#include "slate_gb300.h"
+#include "status.h"
+
+#include <map>
+#include <string>
+#include <vector>
+
+extern "C" {
+int slt_dgemm_skinny(int64_t m, int64_t nrhs, int64_t k, double alpha, const double* A, int64_t lda,
+                     int sym_lower, const double* X, int64_t ldx, double beta, double* C, int64_t ldc,
+                     void* ws, cudaStream_t stream);
+int slt_sgemm_skinny(int64_t m, int64_t nrhs, int64_t k, float alpha, const float* A, int64_t lda,
+                     const float* X, int64_t ldx, float beta, float* C, int64_t ldc, cudaStream_t stream);
+int slt_dgemm_skinny_t(int64_t m, int64_t nrhs, int64_t kk, double alpha, const double* A, int64_t lda,
+                       const double* X, int64_t ldx, double beta, double* C, int64_t ldc,
+                       cudaStream_t stream);
+int slt_sgemm_skinny_t(int64_t m, int64_t nrhs, int64_t kk, float alpha, const float* A, int64_t lda,
+                       const float* X, int64_t ldx, float beta, float* C, int64_t ldc,
+                       cudaStream_t stream);
+int slt_dnrm2(int64_t n, const double* x, double* out, cudaStream_t stream);
+int slt_dscal(int64_t n, const double* num, const double* den, double* x, cudaStream_t stream);
+/* Low-precision trailing update of the mixed factorisations:
+ * C (FP32) = C - A op(B) with A, B rounded to the tier's type
+ * (tier: SLT_PREC_TF32 / BF16 / FP16), fp32 accumulation on tcgen05. */
+int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, int64_t k, const float* A,
+                       int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int lower,
+                       void* ws, size_t ws_bytes, cudaStream_t stream);
+size_t slt_tc_gemm_ws_bytes(int64_t m, int64_t n, int64_t k);
+}
+
+namespace slt {
+
+// Device workspace owned by one driver call (stream-ordered pool).
+struct DevBuf {
+    void* p = nullptr;
+    cudaStream_t s = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { if (p) cudaFreeAsync(p, s); }
+    int alloc(size_t bytes, cudaStream_t stream) {
+        s = stream;
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+        if (e != cudaSuccess) { p = nullptr; cudaGetLastError(); return SLT_ERR_NOMEM; }
+        return SLT_OK;
+    }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Timers: the slate::timers keys of the reference drivers, measured with CUDA
+// events on the driver's stream and resolved when the call ends.
+struct TimerSet {
+    struct Span { std::string key; cudaEvent_t a, b; };
+    std::vector<Span> spans;
+    std::map<std::string, cudaEvent_t> open;
+    cudaStream_t s;
+    explicit TimerSet(cudaStream_t st) : s(st) {}
+    void start(const std::string& key) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); return; }
+        cudaEventRecord(e, s);
+        open[key] = e;
+    }
+    void stop(const std::string& key) {
+        auto it = open.find(key);
+        if (it == open.end()) return;
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); return; }
+        cudaEventRecord(e, s);
+        spans.push_back({key, it->second, e});
+        open.erase(it);
+    }
+    ~TimerSet();
+};
+
+
+struct FactorCtx {
+    int* d_info = nullptr;      // first failing column (1-based), 0 = ok
+    int* d_status = nullptr;    // SLT_ERR_TIMEOUT from a bounded wait
+};
+
+template <typename T>
+int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_options& o,
+              FactorCtx& fc, cudaStream_t s);
+template <typename T>
+int getrs_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv, int64_t nb,
+              T* B, int64_t ldb, cudaStream_t s);
+template <typename T>
+int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc, cudaStream_t s);
+template <typename T>
+int potrs_dev(int64_t n, int64_t nrhs, const T* L, int64_t lda, int64_t nb, T* B, int64_t ldb,
+              cudaStream_t s);
+
+int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                   const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,
+                   int* iter, int64_t* info, cudaStream_t s);
+int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                         const double* B, int64_t ldb, double* X, int64_t ldx,
+                         const slt_options& o, int* iter, int64_t* info, cudaStream_t s);
+
+// Read the factorisation status words; returns an slt status (timeout wins).
+int finish_factor(FactorCtx& fc, int64_t* info, cudaStream_t s);
+
+} // namespace slt

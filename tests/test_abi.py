@@ -1,0 +1,48 @@
+"""The C-ABI library builds, loads and exports every declared symbol (no GPU)."""
+import ctypes
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:slt|slate)_\w+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for must in ("slate_dgesv", "slate_dgesv_", "slate_dsgesv", "slate_dposv", "slate_dpotrf",
+                 "slate_dgetrf", "slate_dgetrs", "slt_dgesv_device", "slt_dsgesv_device",
+                 "slt_dsgesv_gmres_device", "slt_dsposv_device", "slt_dsposv_gmres_device",
+                 "slt_dpotrf_device", "slt_dgetrf_device"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(slt):
+    L = ctypes.CDLL(slt.LIB_PATH)
+    missing = [n for n in sorted(declared_symbols()) if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_host_only_calls(slt):
+    L = slt.lib()
+    assert b"sm_103a" in L.slt_version()
+    assert L.slt_status_string(-2) == b"a bounded device wait timed out"
+    o = slt._Options()
+    L.slt_options_default(ctypes.byref(o))
+    assert o.nb == 512 and o.max_iterations == 30 and o.use_fallback == 1
+
+
+def test_options_mirror():
+    import slate_gb300 as s
+    o = s.Options(nb=256, factor_precision="bf16")._c()
+    assert o.nb == 256 and o.factor_precision == s.PREC_BF16

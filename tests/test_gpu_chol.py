@@ -1,0 +1,56 @@
+"""Cholesky parity on the GPU (potrf / potrs / posv) against the oracle."""
+import numpy as np
+import pytest
+
+from gpu_util import EPS, berr, spd, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,nb", [(1, 4), (5, 4), (64, 16), (100, 32), (300, 64), (1000, 256), (1300, 512)])
+def test_potrf_parity(orc, slt, n, nb):
+    import torch
+    A = spd(orc, n, 40 + n)
+    dA = to_dev(A)
+    info = slt.potrf(dA, slt.Options(nb=nb))
+    torch.cuda.synchronize()
+    assert info == 0
+    L = np.tril(to_host(dA))
+    Ao = A.copy(order="F")
+    assert orc.potrf(Ao, nb) == 0
+    np.testing.assert_allclose(L, np.tril(Ao), atol=1e-12 * np.abs(Ao).max())
+    # upper triangle untouched
+    iu = np.triu_indices(n, 1)
+    assert np.array_equal(to_host(dA)[iu], A[iu])
+
+
+@pytest.mark.parametrize("n,nb,nrhs", [(200, 64, 1), (1024, 256, 4), (2048, 512, 16)])
+def test_posv_backward_error(orc, slt, n, nb, nrhs):
+    import torch
+    A = spd(orc, n, 7)
+    B = orc.generate(2, 8, n, nrhs)
+    dA, dB = to_dev(A), to_dev(B)
+    info = slt.posv(dA, dB, slt.Options(nb=nb))
+    torch.cuda.synchronize()
+    assert info == 0
+    assert berr(orc, A, to_host(dB), B, sym=True) <= 3 * EPS
+
+
+def test_potrf_not_spd(orc, slt):
+    import torch
+    n = 200
+    A = spd(orc, n, 3)
+    A[130, 130] = -5.0
+    dA = to_dev(A)
+    info = slt.potrf(dA, slt.Options(nb=64))
+    torch.cuda.synchronize()
+    Ao = A.copy(order="F")
+    assert info == orc.potrf(Ao, 64) == 131
+
+
+def test_potrf_known_answer_minij(orc, slt):
+    import torch
+    dA = to_dev(orc.generate_kind("minij", 70, 70))
+    assert slt.potrf(dA, slt.Options(nb=32)) == 0
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(np.tril(to_host(dA)), np.tril(np.ones((70, 70))), atol=1e-13)

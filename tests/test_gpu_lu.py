@@ -1,0 +1,148 @@
+"""LU parity on the GPU (getrf / getrs / gesv) against the oracle.
+
+Pass bar (BASELINE): scaled backward error ||B - A X||_1 / (n ||A||_1 ||X||_1)
+<= 3 eps64 and pivot sequences identical to the oracle's wherever the pivot
+margin |best| / |second| exceeds 1 + 1e3 n eps (rounding can decide below).
+"""
+import numpy as np
+import pytest
+
+from gpu_util import EPS, berr, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+def _lu_check(orc, slt, m, n, nb, ib, seed=1, engine=0, dist=2):
+    import torch
+    A = orc.generate(dist, seed, m, n)
+    A0 = A.copy(order="F")
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=nb, ib=ib, gemm_engine=engine))
+    torch.cuda.synchronize()
+    LU = to_host(dA)
+    Ao = A0.copy(order="F")
+    oinfo, pt, po, oipiv, mg = orc.getrf(Ao, nb, ib, margins=True)
+    assert info == oinfo
+    gip = slt.ipiv_to_lapack(ipiv, nb)
+    robust = mg > 1 + 1e3 * max(m, n) * EPS
+    assert np.array_equal(gip[robust], oipiv[robust]), np.nonzero(gip != oipiv)[0][:10]
+    if np.array_equal(gip, oipiv):
+        scale = max(1.0, np.abs(Ao).max())
+        assert np.abs(LU - Ao).max() <= 1e-9 * scale
+    return A0, LU, gip
+
+
+@pytest.mark.parametrize("m,n,nb,ib", [(1, 1, 4, 4), (7, 7, 4, 2), (64, 64, 16, 8), (100, 100, 32, 16),
+                                       (257, 257, 64, 16), (300, 200, 64, 32), (200, 300, 64, 32),
+                                       (1000, 1000, 256, 32), (1030, 1030, 512, 64)])
+def test_getrf_parity(orc, slt, m, n, nb, ib):
+    _lu_check(orc, slt, m, n, nb, ib)
+
+
+@pytest.mark.parametrize("engine", [1, 2])
+def test_getrf_both_fp64_engines(orc, slt, engine):
+    _lu_check(orc, slt, 600, 600, 128, 32, seed=9, engine=engine)
+
+
+@pytest.mark.parametrize("n,nb,nrhs", [(1, 4, 1), (33, 16, 2), (500, 128, 1), (777, 256, 5), (1024, 512, 16),
+                                       (1100, 256, 20)])
+def test_gesv_backward_error(orc, slt, n, nb, nrhs):
+    import torch
+    A = orc.generate(2, 100 + n, n, n)
+    B = orc.generate(2, 200 + n, n, nrhs)
+    dA, dB = to_dev(A), to_dev(B)
+    info, ipiv = slt.gesv(dA, dB, slt.Options(nb=nb))
+    torch.cuda.synchronize()
+    assert info == 0
+    X = to_host(dB)
+    assert berr(orc, A, X, B) <= 3 * EPS
+    # same solution as the oracle's gesv to within conditioning
+    Ao, Bo = A.copy(order="F"), B.copy(order="F")
+    orc.gesv(Ao, Bo, nb)
+    assert np.abs(X - Bo).max() <= 1e-8 * max(1.0, np.abs(Bo).max())
+
+
+def test_gesv_config1(orc, slt):
+    """The reference's CPU-runnable configuration: n=4096, nb=256, 1 RHS,
+    A and b uniform(-1,1) from fixed Philox seeds."""
+    import torch
+    n, nb = 4096, 256
+    A = orc.generate(2, 1, n, n)
+    B = orc.generate(2, 2, n, 1)
+    dA, dB = to_dev(A), to_dev(B)
+    info, ipiv = slt.gesv(dA, dB, slt.Options(nb=nb, ib=32))
+    torch.cuda.synchronize()
+    assert info == 0
+    assert berr(orc, A, to_host(dB), B) <= 3 * EPS
+    Ao = A.copy(order="F")
+    oinfo, pt, po, oipiv, mg = orc.getrf(Ao, nb, 16, margins=True)
+    gip = slt.ipiv_to_lapack(ipiv, nb)
+    robust = mg > 1 + 1e3 * n * EPS
+    assert robust.mean() > 0.99
+    assert np.array_equal(gip[robust], oipiv[robust])
+
+
+def test_getrs_separate(orc, slt):
+    import torch
+    n, nb = 700, 128
+    A = orc.generate(2, 31, n, n)
+    B = orc.generate(2, 32, n, 3)
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=nb))
+    dB = to_dev(B)
+    slt.getrs(dA, ipiv, dB, slt.Options(nb=nb))
+    torch.cuda.synchronize()
+    assert berr(orc, A, to_host(dB), B) <= 3 * EPS
+
+
+def test_singular_info(orc, slt):
+    import torch
+    # exactly singular: column 37 zero -> U(37,37) = 0, info = 38 (1-based)
+    n = 100
+    A = orc.generate(2, 5, n, n)
+    A[:, 37] = 0.0
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=32, ib=8))
+    Ao = A.copy(order="F")
+    oinfo = orc.getrf(Ao, 32, 8)[0]
+    assert info == oinfo == 38
+    # ones: rank one
+    dA = to_dev(orc.generate_kind("ones", 40, 40))
+    assert slt.getrf(dA, slt.Options(nb=16, ib=4))[0] == 2
+    # zeros
+    dA = to_dev(np.zeros((10, 10), order="F"))
+    assert slt.getrf(dA, slt.Options(nb=4, ib=2))[0] == 1
+    torch.cuda.synchronize()
+
+
+def test_known_answer_identity_and_ties(orc, slt):
+    import torch
+    dA = to_dev(np.eye(50))
+    info, ipiv = slt.getrf(dA, slt.Options(nb=16, ib=4))
+    assert info == 0 and np.array_equal(slt.ipiv_to_lapack(ipiv, 16), np.arange(1, 51))
+    assert np.array_equal(to_host(dA), np.eye(50))
+    # exact ties: GPU keeps the diagonal on a tie and otherwise the lowest row,
+    # SLATE's order with one panel thread
+    A = np.asfortranarray(np.array([[1., 0, 0, 0], [3, 1, 0, 0], [3, 0, 1, 0], [3, 0, 0, 1]]))
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=4, ib=1))
+    oinfo, pt, po, oipiv, _ = orc.getrf(A.copy(order="F"), 4, 1, panel_threads=1)
+    assert np.array_equal(slt.ipiv_to_lapack(ipiv, 4), oipiv)
+    B = np.asfortranarray(np.array([[2., 1], [-2, 1]]))
+    info, ipiv = slt.getrf(to_dev(B), slt.Options(nb=2, ib=1))
+    assert int(ipiv[0]) == 0
+    torch.cuda.synchronize()
+
+
+def test_float32_getrf(orc, slt):
+    import torch
+    n, nb = 500, 128
+    A = orc.generate(2, 77, n, n, dtype=np.float32)
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=nb, ib=32))
+    torch.cuda.synchronize()
+    Ao = A.copy(order="F")
+    oinfo, pt, po, oipiv, mg = orc.getrf(Ao, nb, 32, margins=True)
+    robust = mg > 1 + 1e3 * n * np.finfo(np.float32).eps
+    gip = slt.ipiv_to_lapack(ipiv, nb)
+    assert np.array_equal(gip[robust], oipiv[robust])

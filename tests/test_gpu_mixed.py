@@ -1,0 +1,57 @@
+"""Mixed-precision solvers on the GPU against the oracle.
+
+Bar: converged (iter >= 0), FP64 backward error <= 3 n eps64, and the same
+refinement behaviour as the oracle's restatement of SLATE's loop (iteration
+counts within one).
+"""
+import numpy as np
+import pytest
+
+from gpu_util import EPS, berr, spd, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(slt, fn, A, B, opts):
+    import torch
+    dA, dB = to_dev(A), to_dev(B)
+    dX = to_dev(np.zeros_like(B))
+    info, it, _ = getattr(slt, fn)(dA, dB, dX, opts)
+    torch.cuda.synchronize()
+    return info, it, to_host(dX), to_host(dA)
+
+
+@pytest.mark.parametrize("fn", ["gesv_mixed", "gesv_mixed_gmres", "posv_mixed", "posv_mixed_gmres"])
+@pytest.mark.parametrize("n,nb", [(300, 64), (1500, 256)])
+def test_mixed_parity(orc, slt, fn, n, nb):
+    chol = fn.startswith("posv")
+    A = spd(orc, n, 21) if chol else orc.generate(2, 22, n, n)
+    nrhs = 1 if "gmres" in fn else 3
+    B = orc.generate(2, 23, n, nrhs)
+    info, it, X, Aout = _run(slt, fn, A, B, slt.Options(nb=nb))
+    assert info == 0 and it >= 0
+    assert berr(orc, A, X, B, sym=chol) <= 3 * n * EPS
+    assert np.array_equal(Aout, A)          # A untouched unless the fallback runs
+    Ao = A.copy(order="F")
+    r = getattr(orc, fn)(Ao, B.copy(order="F") if nrhs > 1 else B[:, 0].copy(), nb)
+    assert r[0] == 0 and abs(r[2] - it) <= 1
+
+
+@pytest.mark.parametrize("fn", ["gesv_mixed", "posv_mixed_gmres"])
+def test_mixed_forced_fallback(orc, slt, fn):
+    chol = fn.startswith("posv")
+    n = 400
+    A = spd(orc, n, 31) if chol else orc.generate(2, 32, n, n)
+    B = orc.generate(2, 33, n, 1)
+    info, it, X, Aout = _run(slt, fn, A, B, slt.Options(nb=128, max_iterations=0))
+    assert it == -1 and info == 0
+    assert berr(orc, A, X, B, sym=chol) <= 3 * EPS
+
+
+def test_mixed_singular(orc, slt):
+    n = 256
+    A = orc.generate(2, 3, n, n)
+    A[:, 10] = 0.0
+    B = orc.generate(2, 4, n, 1)
+    info, it, X, _ = _run(slt, "gesv_mixed", A, B, slt.Options(nb=64, use_fallback=False))
+    assert it == -3 and info == 11
