@@ -1,0 +1,375 @@
+"""Benchmark: posv effective TFLOP/s at FP64 backward error, mixed vs plain FP64.
+
+Workload (N=1, one GB300): SLATE's posv configuration n=16384, nb=512, 4
+right-hand sides, A = G G^T / n + I with G ~ N(0,1) (SLATE's Philox normal
+stream, seed 1), B ~ U(-1,1) (seed 2).  One step = one posv_mixed solve to
+FP64 backward error through the library (A, B resident in HBM, 2.1 GB > L2).
+``value`` = LAPACK posv flop count (n^3/3 + n^2/2 + n/6 + 2 n^2 nrhs) / step
+time; the plain FP64 posv on the same system is timed beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--prec fp32|tf32|bf16|fp16] [--n N] [--nrhs R]
+
+--impl reference times the CPU restatement of SLATE's posv_mixed (the
+oracle; SLATE itself cannot be built here) on the host cores.  Under
+torchrun (N > 1) every rank solves its own replica ("replicas only": one
+factorisation does not shard); value = total solves x flops / max time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def posv_flops(n, nrhs):
+    return n**3 / 3.0 + n**2 / 2.0 + n / 6.0 + 2.0 * n**2 * nrhs
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--prec", default="fp32")
+    p.add_argument("--n", type=int, default=16384)
+    p.add_argument("--nb", type=int, default=512)
+    p.add_argument("--nrhs", type=int, default=4)
+    p.add_argument("--cpu-n", type=int, default=8192, help="CPU sample size")
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_system(slt, torch, n, nrhs, device):
+    """A = G G^T / n + I (G from SLATE's Philox normal stream), B ~ U(-1,1)."""
+    G = slt.colmajor(torch.empty(n, n, dtype=torch.float64, device=device))
+    slt.generate(3, 1, G)
+    Gf = G.to(torch.float32)
+    del G
+    torch.backends.cuda.matmul.allow_tf32 = False
+    S = (Gf @ Gf.t()) / n
+    del Gf
+    A = S.to(torch.float64)
+    del S
+    A.diagonal().add_(1.0)
+    A = slt.colmajor(A)             # symmetric: column-major view of the same values
+    B = slt.colmajor(torch.empty(n, nrhs, dtype=torch.float64, device=device))
+    slt.generate(2, 2, B)
+    torch.cuda.synchronize()
+    return A, B
+
+
+def backward_error(torch, A, X, B):
+    """||B - A X||_1 / (n ||A||_1 ||X||_1) (SLATE tester, test/test_posv.cc)."""
+    n = A.shape[0]
+    R = B - A @ X
+    an = A.abs().sum(0).max()
+    return float(R.abs().sum(0).max() / (n * an * X.abs().sum(0).max()))
+
+
+def run_reference(args):
+    """The CPU restatement of SLATE's posv_mixed<double,float> on host cores."""
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    # one BLAS thread per tile task, as SLATE's HostTask runs tile BLAS inside
+    # OpenMP tasks (nested BLAS threads would oversubscribe the cores)
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    blas = oracle.use_host_blas()
+    n = min(args.cpu_n, args.n)
+    G = oracle.generate(3, 1, n, n)
+    A = np.asfortranarray(G @ G.T / n + np.eye(n))
+    del G
+    B = oracle.generate(2, 2, n, args.nrhs)
+    times = []
+    for i in range(args.warmup + args.steps):
+        Aw = A.copy(order="F")
+        t = time.perf_counter()
+        info, X, it = oracle.posv_mixed(Aw, B.copy(order="F"), args.nb)
+        dt = time.perf_counter() - t
+        if i >= args.warmup:
+            times.append(dt)
+    t = statistics.median(times)
+    val = posv_flops(n, args.nrhs) / t / 1e12
+    sample = ("posv_mixed<double,float> restatement, n=%d nb=%d nrhs=%d (same distribution, "
+              "smaller n), host BLAS %s" % (n, args.nb, args.nrhs, "scipy-openblas" if blas else "built-in"))
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s",
+            "higher_is_better": True, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t * 1e3, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config(args),
+            "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "iter": it, "info": info}
+    print(json.dumps(line))
+
+
+METRIC = "posv effective TFLOP/s at FP64 backward error (posv_mixed vs plain FP64 posv)"
+
+
+def config(args):
+    return {"workload": "posv n=%d nb=%d nrhs=%d, A = G G^T/n + I (G Philox N(0,1)), B U(-1,1)"
+                        % (args.n, args.nb, args.nrhs),
+            "n": args.n, "nb": args.nb, "nrhs": args.nrhs, "factor_precision": args.prec,
+            "l2": "inputs larger than L2 (A is %.1f GB)" % (8.0 * args.n * args.n / 1e9),
+            "parallelism": "replicas x%d" % args.gpus}
+
+
+def cpu_baseline_sample(args):
+    """Oracle posv_mixed on host cores (bounded sample), rank 0 at N=1."""
+    # one BLAS thread per tile task, as SLATE's HostTask runs tile BLAS inside
+    # OpenMP tasks (nested BLAS threads would oversubscribe the cores)
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    blas = oracle.use_host_blas()
+    n = min(args.cpu_n, args.n)
+    G = oracle.generate(3, 1, n, n)
+    A = np.asfortranarray(G @ G.T / n + np.eye(n))
+    del G
+    B = oracle.generate(2, 2, n, args.nrhs)
+    t = time.perf_counter()
+    oracle.posv_mixed(A, B, args.nb)
+    dt = time.perf_counter() - t
+    return {"value": posv_flops(n, args.nrhs) / dt / 1e12, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+            "sample": "posv_mixed<double,float> restatement at n=%d nb=%d nrhs=%d (%.1f s), host BLAS %s"
+                      % (n, args.nb, args.nrhs, dt, "scipy-openblas" if blas else "built-in")}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import slate_gb300 as slt
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    peaks = {}
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        peaks = json.load(open(pp))
+
+    n, nrhs = args.n, args.nrhs
+    A, B = make_system(slt, torch, n, nrhs, dev)
+    X = slt.colmajor(torch.zeros(n, nrhs, dtype=torch.float64, device=dev))
+    opts = slt.Options(nb=args.nb, ib=32, factor_precision=args.prec)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        info, it, _ = slt.posv_mixed(A, B, X, opts)
+    barrier()
+    clk = Clocks(local)
+    clk.start()
+    l0 = slt.lib().slt_launch_count()
+    slt.lib().slt_profile_enable(1)
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    iters = []
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        info, it, _ = slt.posv_mixed(A, B, X, opts)
+        iters.append(it)
+    e1.record(stream)
+    barrier()
+    launches = slt.lib().slt_launch_count() - l0
+    clocks = clk.stop()
+    t_step = e0.elapsed_time(e1) / 1e3 / args.steps
+    # dominant kernel class by event time inside the timed region
+    import ctypes
+    prof = {}
+    for kind, name in ((1, "gemm64"), (2, "gemm32_simt"), (3, "gemm_tc"), (4, "panel"), (5, "trsm"),
+                       (6, "laswp"), (7, "skinny_fp64"), (8, "chol_panel"), (10, "sweep")):
+        f, by, s, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        slt.lib().slt_profile_read(kind, ctypes.byref(f), ctypes.byref(by), ctypes.byref(s), ctypes.byref(c))
+        if c.value:
+            prof[name] = {"flops": f.value, "bytes": by.value, "seconds": s.value, "launches": c.value}
+    slt.lib().slt_profile_enable(0)
+    berr = backward_error(torch, A, X, B)
+
+    tmax = t_step
+    if ws > 1:
+        tt = torch.tensor([t_step], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        tmax = float(tt.item())
+    value = ws * posv_flops(n, nrhs) / tmax / 1e12
+
+    # plain FP64 posv on the same system (A restored outside the timing)
+    plain = None
+    if not args.no_plain:
+        A2 = A.clone()
+        X2 = B.clone()
+        slt.posv(slt.colmajor(A2), slt.colmajor(X2), slt.Options(nb=args.nb))
+        torch.cuda.synchronize()
+        A2.copy_(A)
+        X2.copy_(B)
+        torch.cuda.synchronize()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        pinfo = slt.posv(slt.colmajor(A2), slt.colmajor(X2), slt.Options(nb=args.nb))
+        p1.record(stream)
+        torch.cuda.synchronize()
+        tp = p0.elapsed_time(p1) / 1e3
+        plain = {"value": posv_flops(n, nrhs) / tp / 1e12, "unit": "TFLOP/s", "ms": tp * 1e3,
+                 "backward_error": backward_error(torch, A, X2, B), "info": pinfo}
+        del A2, X2
+
+    # end to end through the LAPACK-compatible host entry point (pinned host buffers)
+    e2e = None
+    if not args.no_e2e:
+        hA = torch.empty(n, n, dtype=torch.float64, pin_memory=True)
+        hA.copy_(A.t())
+        hB = torch.empty(nrhs, n, dtype=torch.float64, pin_memory=True)
+        hB.copy_(B.t())
+        hX = torch.zeros(nrhs, n, dtype=torch.float64, pin_memory=True)
+        a_np, b_np, x_np = hA.numpy().T, hB.numpy().T, hX.numpy().T
+        ts = []
+        for i in range(2 + args.steps):
+            t = time.perf_counter()
+            ip = _dsposv(slt, a_np, b_np, x_np, args)
+            dt = time.perf_counter() - t
+            if i >= 2:
+                ts.append(dt)
+        te = statistics.median(ts)
+        e2e = {"value": ws * posv_flops(n, nrhs) / te / 1e12, "unit": "TFLOP/s",
+               "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
+               "ms_per_step": te * 1e3, "iter": ip}
+
+    if rank != 0:
+        return
+    dom = max(prof.items(), key=lambda kv: kv[1]["seconds"]) if prof else (None, None)
+    roof = None
+    if dom[0] is not None:
+        d = dom[1]
+        if dom[0] in ("gemm_tc",):
+            peak, bound, unit = peaks.get("bf16_tflops", 1900.0), "tensor", "TFLOP/s"
+            src = "MEASURED_PEAKS.json bf16_tflops (burst)"
+            achieved = d["flops"] / d["seconds"] / 1e12
+        elif dom[0] in ("gemm32_simt",):
+            peak, bound, unit = 69.8, "tensor", "TFLOP/s"
+            src = "FP32 SIMT: cuBLAS SGEMM n=8192 measured on this pool (69.8 TF/s); no tensor pipe"
+            achieved = d["flops"] / d["seconds"] / 1e12
+        elif dom[0] in ("gemm64",):
+            peak, bound, unit = 1.24, "tensor", "TFLOP/s"
+            src = "FP64: best measured FP64 GEMM on this pool (our DFMA kernel 1.24, cuBLAS 1.10 TF/s)"
+            achieved = d["flops"] / d["seconds"] / 1e12
+        else:
+            peak, bound, unit = peaks.get("hbm_gbs", 6800.0), "hbm", "GB/s"
+            src = "MEASURED_PEAKS.json hbm_gbs"
+            achieved = d["bytes"] / d["seconds"] / 1e9
+        roof = {"kernel": dom[0], "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": achieved / peak, "traffic": None, "peak_source": src,
+                "launches_per_step": d["launches"] / args.steps,
+                "share_of_step": d["seconds"] / (t_step * args.steps)}
+    cpu = cpu_baseline_sample(args) if (ws == 1 and rank == 0 and not args.no_cpu) else None
+    line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tmax * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(args),
+            "iter": iters[-1], "info": info, "backward_error": berr,
+            "backward_error_bound_3n_eps": 3 * n * np.finfo(np.float64).eps,
+            "plain_fp64": plain,
+            "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
+            "e2e": e2e, "gpu_launches": launches, "clocks": clocks, "roofline": roof,
+            "kernel_profile": prof, "cpu_baseline": cpu}
+    print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _dsposv(slt, a, b, x, args):
+    import ctypes
+    c = ctypes.c_int
+    n, nrhs = a.shape[0], b.shape[1]
+    os.environ["SLATE_LAPACK_NB"] = str(args.nb)
+    os.environ["SLATE_LAPACK_FACTOR_PRECISION"] = args.prec
+    it, info = c(0), c(0)
+    slt.lib().slate_dsposv(ctypes.c_char_p(b"L"), ctypes.byref(c(n)), ctypes.byref(c(nrhs)),
+                           a.ctypes.data_as(ctypes.c_void_p), ctypes.byref(c(n)),
+                           b.ctypes.data_as(ctypes.c_void_p), ctypes.byref(c(n)),
+                           x.ctypes.data_as(ctypes.c_void_p), ctypes.byref(c(n)), None, None,
+                           ctypes.byref(it), ctypes.byref(info))
+    if info.value != 0:
+        raise RuntimeError("slate_dsposv info %d" % info.value)
+    return it.value
+
+
+if __name__ == "__main__":
+    main()

@@ -114,6 +114,17 @@ int slt_dsposv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, co
 int slt_dgenerate_device(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
                          double* dA, int64_t lda, slt_stream_t stream);
 
+/* Launch accounting: number of kernels this library has launched so far
+ * (all classes), and optional CUDA-event timing of each launch by kernel
+ * class (1 FP64 update GEMM, 2 FP32 update GEMM, 3 tensor-core update GEMM,
+ * 4 LU panel, 5 triangular solves, 6 row interchanges, 7 skinny products,
+ * 8 diagonal-block Cholesky).  slt_profile_enable(1) clears and starts
+ * recording; slt_profile_read synchronises the device and sums one class:
+ * algorithmic flops and bytes, event-timed seconds and launches. */
+long long slt_launch_count(void);
+void slt_profile_enable(int on);
+int slt_profile_read(int kind, double* flops, double* bytes, double* seconds, long long* launches);
+
 /* Seconds spent in named phases of the last driver call on this thread
  * (the keys of SLATE's slate::timers map, e.g. "gesv_mixed::getrf_lo");
  * returns -1 if the key is unknown. */
@@ -122,7 +133,8 @@ double slt_timer(const char* name);
 /* ------------------------------------------------------------------------- */
 /* LAPACK-compatible entry points (lapack_api/lapack_*.cc).  Host memory.     */
 /* Tile size from SLATE_LAPACK_NB (default 512), inner blocking from          */
-/* SLATE_LAPACK_IB (default 32).                                              */
+/* SLATE_LAPACK_IB (default 32), factorisation precision of the mixed solvers */
+/* from SLATE_LAPACK_FACTOR_PRECISION (fp32 | tf32 | bf16 | fp16, default fp32).*/
 
 /* lapack_api/lapack_gesv.cc:32 */
 void slate_dgesv(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
@@ -137,6 +149,11 @@ void slate_dgetrs(const char* trans, const int* n, const int* nrhs, double* a, c
                   int* ipiv, double* b, const int* ldb, int* info);
 /* lapack_api/lapack_gesv_mixed.cc:24 (dsgesv signature; x receives the solution) */
 void slate_dsgesv(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
+                  double* b, const int* ldb, double* x, const int* ldx, double* work,
+                  float* swork, int* iter, int* info);
+/* LAPACK dsposv signature (mixed-precision Cholesky solve; SLATE's C++
+ * posv_mixed, src/posv_mixed.cc:105-320, has no lapack_api wrapper) */
+void slate_dsposv(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda,
                   double* b, const int* ldb, double* x, const int* ldx, double* work,
                   float* swork, int* iter, int* info);
 /* lapack_api/lapack_posv.cc:32 (uplo 'L' or 'U') */
@@ -154,6 +171,9 @@ void slate_sgetrf_(const int* m, const int* n, float* a, const int* lda, int* ip
 void slate_dgetrs_(const char* trans, const int* n, const int* nrhs, double* a, const int* lda,
                    int* ipiv, double* b, const int* ldb, int* info);
 void slate_dsgesv_(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,
+                   double* b, const int* ldb, double* x, const int* ldx, double* work,
+                   float* swork, int* iter, int* info);
+void slate_dsposv_(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda,
                    double* b, const int* ldb, double* x, const int* ldx, double* work,
                    float* swork, int* iter, int* info);
 void slate_dposv_(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda,

@@ -113,6 +113,54 @@ typedef void (*sgemm_f)(const char*, const char*, const int*, const int*, const 
                         const float*, float*, const int*);
 dgemm_f g_dgemm = nullptr;
 sgemm_f g_sgemm = nullptr;
+typedef void (*dtrsm_f)(const char*, const char*, const char*, const char*, const int*, const int*,
+                        const double*, const double*, const int*, double*, const int*);
+typedef void (*strsm_f)(const char*, const char*, const char*, const char*, const int*, const int*,
+                        const float*, const float*, const int*, float*, const int*);
+typedef void (*dpotrf_f)(const char*, const int*, double*, const int*, int*);
+typedef void (*spotrf_f)(const char*, const int*, float*, const int*, int*);
+dtrsm_f g_dtrsm = nullptr;
+strsm_f g_strsm = nullptr;
+dpotrf_f g_dpotrf = nullptr;
+spotrf_f g_spotrf = nullptr;
+
+// Host BLAS/LAPACK tile calls (the calls SLATE's HostTask makes), when set.
+bool host_trsm(char side, char uplo, char trans, char diag, int64_t m, int64_t n, const double* A,
+               int64_t lda, double* B, int64_t ldb)
+{
+    if (!g_dtrsm || m <= 0 || n <= 0) return false;
+    int mi = int(m), ni = int(n), la = int(lda), lb = int(ldb);
+    double one = 1.0;
+    g_dtrsm(&side, &uplo, &trans, &diag, &mi, &ni, &one, A, &la, B, &lb);
+    return true;
+}
+bool host_trsm(char side, char uplo, char trans, char diag, int64_t m, int64_t n, const float* A,
+               int64_t lda, float* B, int64_t ldb)
+{
+    if (!g_strsm || m <= 0 || n <= 0) return false;
+    int mi = int(m), ni = int(n), la = int(lda), lb = int(ldb);
+    float one = 1.0f;
+    g_strsm(&side, &uplo, &trans, &diag, &mi, &ni, &one, A, &la, B, &lb);
+    return true;
+}
+bool host_potrf(int64_t n, double* A, int64_t lda, int64_t* info)
+{
+    if (!g_dpotrf) return false;
+    int ni = int(n), la = int(lda), inf = 0;
+    char u = 'L';
+    g_dpotrf(&u, &ni, A, &la, &inf);
+    *info = inf;
+    return true;
+}
+bool host_potrf(int64_t n, float* A, int64_t lda, int64_t* info)
+{
+    if (!g_spotrf) return false;
+    int ni = int(n), la = int(lda), inf = 0;
+    char u = 'L';
+    g_spotrf(&u, &ni, A, &la, &inf);
+    *info = inf;
+    return true;
+}
 
 // C = alpha op(A) op(B) + beta C ; ta/tb in {'N','T'}.
 template <typename T>
@@ -193,6 +241,7 @@ template <typename T>
 void trsm_left(char uplo, char trans, char diag, int64_t m, int64_t n,
                const T* A, int64_t lda, T* B, int64_t ldb)
 {
+    if (host_trsm('L', uplo, trans, diag, m, n, A, lda, B, ldb)) return;
     bool lower_eff = (uplo == 'L') == (trans == 'N');
     for (int64_t j = 0; j < n; ++j) {
         T* b = B + j*ldb;
@@ -220,6 +269,7 @@ void trsm_left(char uplo, char trans, char diag, int64_t m, int64_t n,
 template <typename T>
 void trsm_right_lower_trans(int64_t m, int64_t n, const T* L, int64_t ldl, T* B, int64_t ldb)
 {
+    if (host_trsm('R', 'L', 'T', 'N', m, n, L, ldl, B, ldb)) return;
     for (int64_t j = 0; j < n; ++j) {
         T d = L[j + j*ldl];
         for (int64_t l = 0; l < j; ++l) {
@@ -469,6 +519,8 @@ void getrs(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int64_t* piv
 template <typename T>
 int64_t potf2_lower(int64_t n, T* A, int64_t lda)
 {
+    int64_t hinfo = 0;
+    if (host_potrf(n, A, lda, &hinfo)) return hinfo;
     for (int64_t j = 0; j < n; ++j) {
         T ajj = A[j + j*lda];
         for (int64_t l = 0; l < j; ++l) ajj -= A[j + l*lda] * A[j + l*lda];
@@ -588,19 +640,22 @@ void residual(int64_t n, int64_t nrhs, const double* A, int64_t lda, bool sym_lo
         gemm('N', 'N', n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, R, n);
         return;
     }
-    #pragma omp parallel for schedule(static)
-    for (int64_t j = 0; j < nrhs; ++j) {
-        const double* x = X + j*ldx;
-        double* r = R + j*n;
-        for (int64_t c = 0; c < n; ++c) {
-            double acc = 0;
-            r[c] -= A[c + c*lda] * x[c];
-            for (int64_t i = c + 1; i < n; ++i) {
-                double a = A[i + c*lda];
-                r[i] -= a * x[c];
-                acc += a * x[i];
-            }
-            r[c] -= acc;
+    // Symmetric A with lower storage (SLATE's hemm on a HermitianMatrix):
+    // tile (I,J), I > J, contributes A_IJ X_J to R_I and A_IJ^T X_I to R_J;
+    // diagonal tiles are expanded to full symmetric blocks.
+    const int64_t nb = 512;
+    std::vector<double> D(size_t(nb) * nb);
+    for (int64_t J = 0; J < n; J += nb) {
+        int64_t jb = std::min(nb, n - J);
+        for (int64_t c = 0; c < jb; ++c)
+            for (int64_t r = 0; r < jb; ++r)
+                D[r + c * jb] = (r >= c) ? A[J + r + (J + c) * lda] : A[J + c + (J + r) * lda];
+        gemm('N', 'N', jb, nrhs, jb, -1.0, D.data(), jb, X + J, ldx, 1.0, R + J, n);
+        if (J + jb < n) {
+            int64_t rows = n - J - jb;
+            const double* Ab = A + (J + jb) + J * lda;
+            gemm('N', 'N', rows, nrhs, jb, -1.0, Ab, lda, X + J, ldx, 1.0, R + J + jb, n);
+            gemm('T', 'N', jb, nrhs, rows, -1.0, Ab, lda, X + J + jb, ldx, 1.0, R + J, n);
         }
     }
 }
@@ -832,6 +887,15 @@ void orc_set_blas(void* dgemm_ptr, void* sgemm_ptr)
 {
     g_dgemm = (dgemm_f) dgemm_ptr;
     g_sgemm = (sgemm_f) sgemm_ptr;
+}
+
+// Host trsm / potrf (Fortran ABI) for the tile solves and diagonal tiles.
+void orc_set_lapack(void* dtrsm_ptr, void* strsm_ptr, void* dpotrf_ptr, void* spotrf_ptr)
+{
+    g_dtrsm = (dtrsm_f) dtrsm_ptr;
+    g_strsm = (strsm_f) strsm_ptr;
+    g_dpotrf = (dpotrf_f) dpotrf_ptr;
+    g_spotrf = (spotrf_f) spotrf_ptr;
 }
 
 void orc_philox(uint64_t s0, uint64_t s1, uint64_t key, uint64_t* out)

@@ -84,11 +84,18 @@ def use_host_blas():
     get.argtypes = [ctypes.py_object, ctypes.c_char_p]
     capi = cb.__pyx_capi__
     try:
+        import scipy.linalg.cython_lapack as cl
         pd = get(capi["dgemm"], _capsule_name(capi["dgemm"]))
         ps = get(capi["sgemm"], _capsule_name(capi["sgemm"]))
+        td = get(capi["dtrsm"], _capsule_name(capi["dtrsm"]))
+        ts = get(capi["strsm"], _capsule_name(capi["strsm"]))
+        lcapi = cl.__pyx_capi__
+        fd = get(lcapi["dpotrf"], _capsule_name(lcapi["dpotrf"]))
+        fs = get(lcapi["spotrf"], _capsule_name(lcapi["spotrf"]))
     except Exception:
         return False
     lib().orc_set_blas(ctypes.c_void_p(pd), ctypes.c_void_p(ps))
+    lib().orc_set_lapack(ctypes.c_void_p(td), ctypes.c_void_p(ts), ctypes.c_void_p(fd), ctypes.c_void_p(fs))
     return True
 
 
@@ -101,6 +108,7 @@ def _capsule_name(cap):
 
 def use_builtin_blas():
     lib().orc_set_blas(None, None)
+    lib().orc_set_lapack(None, None, None, None)
 
 
 def philox(s0, s1, key):

@@ -16,6 +16,7 @@
 // memory.
 
 #include "common.cuh"
+#include "prof.h"
 
 namespace slt {
 
@@ -25,7 +26,7 @@ constexpr int kMaxRhs = 16;
 // y_seg(i, r) = sum_{j in segment} op(A)(i, j) X(j, r)   (MODE 0)
 // y_seg(i, 0) = sum_{j in segment} |op(A)(i, j)|         (MODE 1)
 // Tiles of 64 x 64; SYM: A symmetric with lower storage.
-template <int MODE, bool SYM>
+template <int MODE, bool SYM, int NR>
 __global__ void __launch_bounds__(256)
 rowop_kernel(int64_t m, int64_t k, int nrhs, const double* __restrict__ A, int64_t lda,
              const double* __restrict__ X, int64_t ldx, int64_t tiles_per_seg,
@@ -44,11 +45,12 @@ rowop_kernel(int64_t m, int64_t k, int nrhs, const double* __restrict__ A, int64
     const int64_t ktiles = ceildiv(k, 64);
     const int64_t J0 = seg * tiles_per_seg;
     const int64_t J1 = min(ktiles, J0 + tiles_per_seg);
+    // NR: compile-time right-hand-side count (1, 2, 4, 8 or 16); MODE 1 uses 1.
     const int nr = (MODE == 0) ? nrhs : 1;
 
-    double acc[kMaxRhs];
+    double acc[NR];
     #pragma unroll
-    for (int q = 0; q < kMaxRhs; ++q) acc[q] = 0.0;
+    for (int q = 0; q < NR; ++q) acc[q] = 0.0;
 
     for (int64_t J = J0; J < J1; ++J) {
         const int64_t col0 = J * 64;
@@ -84,11 +86,11 @@ rowop_kernel(int64_t m, int64_t k, int nrhs, const double* __restrict__ A, int64
         __syncthreads();
         // group g takes tile columns c = g, g+4, ...
         if (MODE == 0) {
+            #pragma unroll 4
             for (int c = g; c < 64; c += 4) {
                 double a = As[c][r];
                 #pragma unroll
-                for (int q = 0; q < kMaxRhs; ++q)
-                    if (q < nr) acc[q] = fma(a, xs[c][q], acc[q]);
+                for (int q = 0; q < NR; ++q) acc[q] = fma(a, xs[c][q], acc[q]);
             }
         }
         else {
@@ -96,7 +98,7 @@ rowop_kernel(int64_t m, int64_t k, int nrhs, const double* __restrict__ A, int64
         }
     }
     #pragma unroll
-    for (int q = 0; q < kMaxRhs; ++q)
+    for (int q = 0; q < NR; ++q)
         if (q < nr) red[g][r][q] = acc[q];
     __syncthreads();
     for (int e = t; e < 64 * nr; e += 256) {
@@ -142,17 +144,34 @@ __global__ void max_reduce_kernel(int64_t m, int64_t nseg, const double* __restr
 
 constexpr size_t kRowopSmem = sizeof(double) * (64 * 65 + 64 * kMaxRhs + 4 * 64 * (kMaxRhs + 1));
 
+template <int MODE, bool SYM, int NR>
+static int launch_rowop_nr(dim3 grid, cudaStream_t stream, int64_t m, int64_t k, int nrhs, const double* A,
+                           int64_t lda, const double* X, int64_t ldx, int64_t tps, double* part)
+{
+    static bool configured = false;
+    if (!configured) {
+        SLT_CUDA_TRY(cudaFuncSetAttribute(rowop_kernel<MODE, SYM, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          int(kRowopSmem)));
+        configured = true;
+    }
+    rowop_kernel<MODE, SYM, NR><<<grid, 256, kRowopSmem, stream>>>(m, k, nrhs, A, lda, X, ldx, tps, part);
+    return SLT_OK;
+}
+
 template <int MODE, bool SYM>
 static int launch_rowop(dim3 grid, cudaStream_t stream, int64_t m, int64_t k, int nrhs, const double* A,
                         int64_t lda, const double* X, int64_t ldx, int64_t tps, double* part)
 {
-    static bool configured = false;
-    if (!configured) {
-        SLT_CUDA_TRY(cudaFuncSetAttribute(rowop_kernel<MODE, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          int(kRowopSmem)));
-        configured = true;
-    }
-    rowop_kernel<MODE, SYM><<<grid, 256, kRowopSmem, stream>>>(m, k, nrhs, A, lda, X, ldx, tps, part);
+    const int pidx = prof_begin(SLT_PROF_SKINNY, stream);
+    int rc;
+    if (MODE == 1 || nrhs == 1) rc = launch_rowop_nr<MODE, SYM, 1>(grid, stream, m, k, nrhs, A, lda, X, ldx, tps, part);
+    else if (nrhs == 2) rc = launch_rowop_nr<MODE, SYM, 2>(grid, stream, m, k, nrhs, A, lda, X, ldx, tps, part);
+    else if (nrhs <= 4) rc = launch_rowop_nr<MODE, SYM, 4>(grid, stream, m, k, nrhs, A, lda, X, ldx, tps, part);
+    else if (nrhs <= 8) rc = launch_rowop_nr<MODE, SYM, 8>(grid, stream, m, k, nrhs, A, lda, X, ldx, tps, part);
+    else rc = launch_rowop_nr<MODE, SYM, 16>(grid, stream, m, k, nrhs, A, lda, X, ldx, tps, part);
+    if (rc) return rc;
+    slt::count_launch();
+    prof_end(pidx, stream, 2.0 * double(m) * double(k) * (MODE == 0 ? nrhs : 1), 8.0 * (SYM ? double(m) * double(k) / 2 + 64.0 * m : double(m) * double(k)));
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -363,7 +382,7 @@ extern "C" int slt_dgemm_skinny(int64_t m, int64_t nrhs, int64_t k, double alpha
     if (k <= 0) {
         // C = beta C
         dim3 grid(unsigned(ceildiv(m, 256)), unsigned(nrhs));
-        reduce_segments_kernel<<<grid, 256, 0, stream>>>(m, int(nrhs), 0, nullptr, alpha, beta, C, ldc);
+        reduce_segments_kernel<<<grid, 256, 0, stream>>>(m, int(nrhs), 0, nullptr, alpha, beta, C, ldc); slt::count_launch();
         return slt_from_cuda(cudaGetLastError());
     }
     int64_t nseg, tps;
@@ -374,7 +393,7 @@ extern "C" int slt_dgemm_skinny(int64_t m, int64_t nrhs, int64_t k, double alpha
                        : launch_rowop<0, false>(grid, stream, m, k, int(nrhs), A, lda, X, ldx, tps, part);
     if (rc) return rc;
     dim3 g2(unsigned(ceildiv(m, 256)), unsigned(nrhs));
-    reduce_segments_kernel<<<g2, 256, 0, stream>>>(m, int(nrhs), nseg, part, alpha, beta, C, ldc);
+    reduce_segments_kernel<<<g2, 256, 0, stream>>>(m, int(nrhs), nseg, part, alpha, beta, C, ldc); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -398,7 +417,7 @@ extern "C" int slt_dnorm_inf(int64_t m, int64_t n, const double* A, int64_t lda,
     int rc = sym_lower ? launch_rowop<1, true>(grid, stream, m, n, 1, A, lda, nullptr, 0, tps, part)
                        : launch_rowop<1, false>(grid, stream, m, n, 1, A, lda, nullptr, 0, tps, part);
     if (rc) return rc;
-    max_reduce_kernel<<<1, 256, 0, stream>>>(m, nseg, part, out);
+    max_reduce_kernel<<<1, 256, 0, stream>>>(m, nseg, part, out); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -408,7 +427,7 @@ extern "C" int slt_dgemm_skinny_t(int64_t m, int64_t nrhs, int64_t kk, double al
 {
     if (m <= 0 || nrhs <= 0) return SLT_OK;
     unsigned grid = unsigned(ceildiv(m * 32, 256));
-    skinny_t_kernel<double><<<grid, 256, 0, stream>>>(m, kk, int(nrhs), alpha, A, lda, X, ldx, beta, C, ldc);
+    skinny_t_kernel<double><<<grid, 256, 0, stream>>>(m, kk, int(nrhs), alpha, A, lda, X, ldx, beta, C, ldc); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -418,7 +437,7 @@ extern "C" int slt_sgemm_skinny_t(int64_t m, int64_t nrhs, int64_t kk, float alp
 {
     if (m <= 0 || nrhs <= 0) return SLT_OK;
     unsigned grid = unsigned(ceildiv(m * 32, 256));
-    skinny_t_kernel<float><<<grid, 256, 0, stream>>>(m, kk, int(nrhs), alpha, A, lda, X, ldx, beta, C, ldc);
+    skinny_t_kernel<float><<<grid, 256, 0, stream>>>(m, kk, int(nrhs), alpha, A, lda, X, ldx, beta, C, ldc); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -428,7 +447,7 @@ extern "C" int slt_sgemm_skinny(int64_t m, int64_t nrhs, int64_t k, float alpha,
 {
     if (m <= 0 || nrhs <= 0) return SLT_OK;
     if (nrhs > kMaxRhs) return SLT_ERR_ARG;
-    sskinny_n_kernel<<<unsigned(ceildiv(m, 256)), 256, 0, stream>>>(m, k, int(nrhs), alpha, A, lda, X, ldx, beta, C, ldc);
+    sskinny_n_kernel<<<unsigned(ceildiv(m, 256)), 256, 0, stream>>>(m, k, int(nrhs), alpha, A, lda, X, ldx, beta, C, ldc); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -437,7 +456,7 @@ extern "C" int slt_convert_d2s(int64_t m, int64_t n, const double* A, int64_t ld
 {
     if (m <= 0 || n <= 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(m, 256)), unsigned(std::min<int64_t>(n, 65535)));
-    convert_kernel<double, float><<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb);
+    convert_kernel<double, float><<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -446,7 +465,7 @@ extern "C" int slt_convert_s2d(int64_t m, int64_t n, const float* A, int64_t lda
 {
     if (m <= 0 || n <= 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(m, 256)), unsigned(std::min<int64_t>(n, 65535)));
-    convert_kernel<float, double><<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb);
+    convert_kernel<float, double><<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -464,7 +483,7 @@ extern "C" int slt_dgeadd(int64_t m, int64_t n, double alpha, const double* A, i
 {
     if (m <= 0 || n <= 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(m, 256)), unsigned(std::min<int64_t>(n, 65535)));
-    geadd_kernel<<<grid, 256, 0, stream>>>(m, n, alpha, A, lda, beta, B, ldb);
+    geadd_kernel<<<grid, 256, 0, stream>>>(m, n, alpha, A, lda, beta, B, ldb); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -472,7 +491,7 @@ extern "C" int slt_dcolmax(int64_t m, int64_t n, const double* A, int64_t lda, d
                            cudaStream_t stream)
 {
     if (n <= 0) return SLT_OK;
-    colmax_kernel<<<unsigned(n), 256, 0, stream>>>(m, A, lda, out);
+    colmax_kernel<<<unsigned(n), 256, 0, stream>>>(m, A, lda, out); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -481,14 +500,14 @@ extern "C" int slt_dgenerate(int dist, int64_t seed, int64_t m, int64_t n, int64
 {
     if (m <= 0 || n <= 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(m, 256)), unsigned(std::min<int64_t>(n, 65535)));
-    generate_kernel<<<grid, 256, 0, stream>>>(dist, seed, m, n, ioff, joff, A, lda);
+    generate_kernel<<<grid, 256, 0, stream>>>(dist, seed, m, n, ioff, joff, A, lda); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
 extern "C" int slt_dshift_diag(int64_t n, double alpha, double* A, int64_t lda, cudaStream_t stream)
 {
     if (n <= 0) return SLT_OK;
-    shift_diag_kernel<<<unsigned(ceildiv(n, 256)), 256, 0, stream>>>(n, alpha, A, lda);
+    shift_diag_kernel<<<unsigned(ceildiv(n, 256)), 256, 0, stream>>>(n, alpha, A, lda); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -496,7 +515,7 @@ extern "C" int slt_dsymmetrize_lower(int64_t n, double* A, int64_t lda, cudaStre
 {
     if (n <= 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(n, 32)), unsigned(ceildiv(n, 32)));
-    symmetrize_lower_kernel<<<grid, 256, 0, stream>>>(n, A, lda);
+    symmetrize_lower_kernel<<<grid, 256, 0, stream>>>(n, A, lda); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -539,7 +558,7 @@ __global__ void transpose_kernel(int64_t m, int64_t n, const double* __restrict_
 
 extern "C" int slt_dnrm2(int64_t n, const double* x, double* out, cudaStream_t stream)
 {
-    nrm2_kernel<<<1, 1024, 0, stream>>>(n, x, out);
+    nrm2_kernel<<<1, 1024, 0, stream>>>(n, x, out); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -548,6 +567,6 @@ extern "C" int slt_dtranspose(int64_t m, int64_t n, const double* A, int64_t lda
 {
     if (m <= 0 || n <= 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(m, 32)), unsigned(ceildiv(n, 32)));
-    transpose_kernel<<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb);
+    transpose_kernel<<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }

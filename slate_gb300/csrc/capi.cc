@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 namespace slt {
@@ -65,6 +66,13 @@ slt_options lapack_opts()
     slt_options_default(&o);
     o.nb = env_int("SLATE_LAPACK_NB", 512);
     o.ib = std::min<int64_t>(env_int("SLATE_LAPACK_IB", 32), o.nb);
+    if (const char* p = std::getenv("SLATE_LAPACK_FACTOR_PRECISION")) {
+        std::string v(p);
+        if (v == "fp32") o.factor_precision = SLT_PREC_FP32;
+        else if (v == "tf32") o.factor_precision = SLT_PREC_TF32;
+        else if (v == "bf16") o.factor_precision = SLT_PREC_BF16;
+        else if (v == "fp16") o.factor_precision = SLT_PREC_FP16;
+    }
     return o;
 }
 
@@ -178,9 +186,12 @@ int slt_dgetrs_device(int64_t n, int64_t nrhs, const double* dLU, int64_t lda, c
 {
     cudaStream_t s = as_stream(stream);
     slt_options o = resolve(opts);
-    int rc = getrs_dev<double>(n, nrhs, dLU, lda, d_ipiv, o.nb, dB, ldb, s);
+    Status st;
+    int rc = st.init(s);
     if (rc) return rc;
-    return slt_from_cuda(cudaStreamSynchronize(s));
+    rc = getrs_dev<double>(n, nrhs, dLU, lda, d_ipiv, o.nb, dB, ldb, st.fc.d_status, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, nullptr, s);
 }
 
 int slt_sgetrs_device(int64_t n, int64_t nrhs, const float* dLU, int64_t lda, const int* d_ipiv,
@@ -188,9 +199,12 @@ int slt_sgetrs_device(int64_t n, int64_t nrhs, const float* dLU, int64_t lda, co
 {
     cudaStream_t s = as_stream(stream);
     slt_options o = resolve(opts);
-    int rc = getrs_dev<float>(n, nrhs, dLU, lda, d_ipiv, o.nb, dB, ldb, s);
+    Status st;
+    int rc = st.init(s);
     if (rc) return rc;
-    return slt_from_cuda(cudaStreamSynchronize(s));
+    rc = getrs_dev<float>(n, nrhs, dLU, lda, d_ipiv, o.nb, dB, ldb, st.fc.d_status, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, nullptr, s);
 }
 
 int slt_dgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv, double* dB,
@@ -211,12 +225,12 @@ int slt_dgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ip
     if (rc) return rc;
     tm.start("gesv::getrs");
     if (*info == 0) {
-        rc = getrs_dev<double>(n, nrhs, dA, lda, d_ipiv, o.nb, dB, ldb, s);
+        rc = getrs_dev<double>(n, nrhs, dA, lda, d_ipiv, o.nb, dB, ldb, st.fc.d_status, s);
         if (rc) return rc;
     }
     tm.stop("gesv::getrs");
     tm.stop("gesv");
-    return slt_from_cuda(cudaStreamSynchronize(s));
+    return finish_factor(st.fc, nullptr, s);
 }
 
 int slt_dpotrf_device(int64_t n, double* dA, int64_t lda, const slt_options* opts, slt_stream_t stream,
@@ -250,9 +264,12 @@ int slt_dpotrs_device(int64_t n, int64_t nrhs, const double* dL, int64_t lda, do
 {
     cudaStream_t s = as_stream(stream);
     slt_options o = resolve(opts);
-    int rc = potrs_dev<double>(n, nrhs, dL, lda, o.nb, dB, ldb, s);
+    Status st;
+    int rc = st.init(s);
     if (rc) return rc;
-    return slt_from_cuda(cudaStreamSynchronize(s));
+    rc = potrs_dev<double>(n, nrhs, dL, lda, o.nb, dB, ldb, st.fc.d_status, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, nullptr, s);
 }
 
 int slt_dposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, double* dB, int64_t ldb,
@@ -273,12 +290,12 @@ int slt_dposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, double* d
     if (rc) return rc;
     tm.start("posv::potrs");
     if (*info == 0) {
-        rc = potrs_dev<double>(n, nrhs, dA, lda, o.nb, dB, ldb, s);
+        rc = potrs_dev<double>(n, nrhs, dA, lda, o.nb, dB, ldb, st.fc.d_status, s);
         if (rc) return rc;
     }
     tm.stop("posv::potrs");
     tm.stop("posv");
-    return slt_from_cuda(cudaStreamSynchronize(s));
+    return finish_factor(st.fc, nullptr, s);
 }
 
 int slt_dsgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv, const double* dB,
@@ -545,6 +562,56 @@ static void lapack_potrf_impl(char uplo, int n, double* a, int lda, int* info, i
             if (up ? (i <= j) : (i >= j)) a[i + size_t(j) * lda] = h[i + size_t(j) * n];
     *info = int(inf);
 }
+
+static void lapack_dsposv_impl(char uplo, int n, int nrhs, double* a, int lda, double* b, int ldb,
+                               double* x, int ldx, int* iter, int* info)
+{
+    *info = 0;
+    *iter = 0;
+    bool up = (uplo == 'U' || uplo == 'u');
+    if (!up && uplo != 'L' && uplo != 'l') { *info = -1; return; }
+    if (n < 0) { *info = -2; return; }
+    if (nrhs < 0) { *info = -3; return; }
+    if (lda < std::max(1, n)) { *info = -5; return; }
+    if (ldb < std::max(1, n)) { *info = -7; return; }
+    if (ldx < std::max(1, n)) { *info = -9; return; }
+    if (n == 0) return;
+    cudaStream_t s = lapack_stream();
+    slt_options o = lapack_opts();
+    DevBuf dA, dB, dX, tmp;
+    if (to_device(a, n, n, lda, dA, s) || to_device(b, n, nrhs, ldb, dB, s) ||
+        dX.alloc(sizeof(double) * size_t(n) * size_t(std::max(nrhs, 1)), s)) { *info = -100; return; }
+    if (lower_view(uplo, n, dA, tmp, s)) { *info = -100; return; }
+    int64_t inf = 0;
+    int it = 0;
+    int rc = slt_dsposv_device(n, nrhs, dA.as<double>(), n, dB.as<double>(), n, dX.as<double>(), n, &o, s,
+                               &it, &inf);
+    if (rc) { *info = -1000 + rc; return; }
+    if (to_host(dX, x, n, nrhs, ldx, s) || cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+    if (it < 0) {
+        // the FP64 fallback ran: A holds its Cholesky factor (referenced triangle)
+        if (up) {
+            rc = slt_dtranspose(n, n, dA.as<double>(), n, tmp.as<double>(), n, s);
+            if (rc) { *info = -1000 + rc; return; }
+            std::swap(dA.p, tmp.p);
+        }
+        std::vector<double> h(size_t(n) * size_t(n));
+        if (cudaMemcpyAsync(h.data(), dA.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i)
+                if (up ? (i <= j) : (i >= j)) a[i + size_t(j) * lda] = h[i + size_t(j) * n];
+    }
+    *iter = it;
+    *info = int(inf);
+}
+
+void slate_dsposv(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda, double* b,
+                  const int* ldb, double* x, const int* ldx, double* work, float* swork, int* iter, int* info)
+{ (void) work; (void) swork; lapack_dsposv_impl(*uplo, *n, *nrhs, a, *lda, b, *ldb, x, *ldx, iter, info); }
+void slate_dsposv_(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda, double* b,
+                   const int* ldb, double* x, const int* ldx, double* work, float* swork, int* iter, int* info)
+{ (void) work; (void) swork; lapack_dsposv_impl(*uplo, *n, *nrhs, a, *lda, b, *ldb, x, *ldx, iter, info); }
 
 void slate_dposv(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda, double* b,
                  const int* ldb, int* info)

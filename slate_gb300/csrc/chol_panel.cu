@@ -1,0 +1,233 @@
+// chol_panel.cu -- Cholesky column panel in one cooperative launch.
+//
+// SLATE factors a column panel as potrf of the diagonal tile on the device
+// queue (cuSOLVER, with a blocking info copy, src/internal/internal_potrf.cc:
+// 56-81) followed by a batched trsm of the tiles below (src/potrf.cc:109-120).
+// Here the whole nb-wide panel (rows r0..n-1, columns r0..r0+nb-1) is one
+// cooperative persistent launch.  Block b owns a band of R rows (R a
+// multiple of 64).  For each 64-column step:
+//   1. every block loads the 64 x 64 diagonal block and factors it in shared
+//      memory (the owner of those rows records info, and writes the factor
+//      back after the next barrier, once every block has read the block);
+//   2. every block solves its own rows below it, X = B L^{-T};
+//   3. grid barrier; every block updates its rows in the remaining panel
+//      columns with the freshly solved rows (rank-64 update);
+//   4. grid barrier.
+// Barriers are the bounded grid barriers of common.cuh.
+
+#include "common.cuh"
+#include "prof.h"
+
+namespace slt {
+
+constexpr int kCpThreads = 256;
+constexpr int kCpIB = 64;
+
+template <typename T>
+struct CholPanelArgs {
+    int64_t m, nbk, ld, rows_per_block, info_offset;
+    T* P;
+    int* info;
+    int* status;
+    GridBarrier* bar;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kCpThreads)
+chol_panel_kernel(CholPanelArgs<T> a)
+{
+    extern __shared__ unsigned char cp_smem_raw[];
+    T* D = reinterpret_cast<T*>(cp_smem_raw);             // [64][65] factor, D[i*65 + l] = L(i,l)
+    T* Xs = D + kCpIB * (kCpIB + 1);                        // [64][68] solved rows staging
+    T* Us = Xs + kCpIB * 68;                                // [64][68] update operand
+    __shared__ int s_fail;
+    const int G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
+    const int64_t ld = a.ld;
+    T* P = a.P;
+    const int64_t rb = int64_t(b) * a.rows_per_block;
+    const int64_t re = min64(a.m, rb + a.rows_per_block);
+
+    for (int64_t c0 = 0; c0 < a.nbk; c0 += kCpIB) {
+        const int kb = int(min64(kCpIB, a.nbk - c0));
+        // ---- 1. factor the diagonal block in shared memory (every block)
+        for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+            int i = e % kCpIB, l = e / kCpIB;
+            D[i * (kCpIB + 1) + l] = (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
+        }
+        if (t == 0) s_fail = 0;
+        __syncthreads();
+        for (int j = 0; j < kb; ++j) {
+            const T d = D[j * (kCpIB + 1) + j];
+            if (!(d > T(0))) {
+                if (t == 0 && !s_fail) {
+                    s_fail = 1;
+                    if (c0 >= rb && c0 < re) atomicCAS(a.info, 0, int(a.info_offset + c0 + j + 1));
+                }
+                break;
+            }
+            const T sd = sqrt(d);
+            for (int i = j + 1 + t; i < kb; i += kCpThreads) D[i * (kCpIB + 1) + j] /= sd;
+            __syncthreads();
+            if (t == 0) D[j * (kCpIB + 1) + j] = sd;
+            {
+                // rows i = j+1+(t&63), columns l = j+1+(t>>6), +4, ... up to i
+                const int i = j + 1 + (t & 63);
+                if (i < kb) {
+                    const T dij = D[i * (kCpIB + 1) + j];
+                    for (int l = j + 1 + (t >> 6); l <= i; l += 4)
+                        D[i * (kCpIB + 1) + l] -= dij * D[l * (kCpIB + 1) + j];
+                }
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+        const bool failed = s_fail != 0;
+        // ---- 2. solve the owned rows below the block: X L^T = B, 64 rows at a time
+        if (!failed) {
+            const int64_t r0 = max64(rb, c0 + kb);
+            for (int64_t rr = r0; rr < re; rr += kCpIB) {
+                const int nr = int(min64(kCpIB, re - rr));
+                __syncthreads();
+                for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+                    int i = e % kCpIB, l = e / kCpIB;
+                    Xs[i * (kCpIB + 1) + l] = (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
+                }
+                __syncthreads();
+                // 4 lanes per row, 64 rows: forward substitution over the kb columns
+                const int row = t >> 2, q = t & 3;
+                for (int j = 0; j < kb; ++j) {
+                    T part = T(0);
+                    for (int l = q; l < j; l += 4) part = fma(Xs[row * (kCpIB + 1) + l], D[j * (kCpIB + 1) + l], part);
+                    part += __shfl_xor_sync(0xffffffffu, part, 2);
+                    part += __shfl_xor_sync(0xffffffffu, part, 1);
+                    if (q == 0) Xs[row * (kCpIB + 1) + j] = (Xs[row * (kCpIB + 1) + j] - part) / D[j * (kCpIB + 1) + j];
+                    __syncwarp();
+                }
+                __syncthreads();
+                for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+                    int i = e % kCpIB, l = e / kCpIB;
+                    if (i < nr && l < kb) P[rr + i + (c0 + l) * ld] = Xs[i * (kCpIB + 1) + l];
+                }
+            }
+        }
+        __threadfence();
+        if (!grid_sync(a.bar, unsigned(G), a.status)) return;
+        // every block has read the diagonal block: its owner writes the factor back
+        if (c0 >= rb && c0 < re)
+            for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+                int i = e % kCpIB, l = e / kCpIB;
+                if (i < kb && l < kb && i >= l) P[c0 + i + (c0 + l) * ld] = D[i * (kCpIB + 1) + l];
+            }
+        // ---- 3. rank-kb update of the owned rows in panel columns [c0+kb, nbk):
+        //      64 x 64 output tiles, 4 x 4 per thread, operands staged [l][row]
+        //      and [l][col] (row stride 68) so each thread reads two 4-vectors
+        //      per k step for 16 FMAs.
+        const int64_t cbeg = c0 + kb;
+        if (cbeg < a.nbk && !failed) {
+            T* X3 = Xs;                                  // [64][68]
+            T* U3 = Us;                                  // [64][68]
+            const int64_t r0 = max64(rb, cbeg);
+            // rows tr + 16 i and columns tc + 16 j: lanes run along rows, so
+            // the final read-modify-write of P is two 64-byte segments per warp
+            const int tr = t & 15, tc = t >> 4;
+            for (int64_t cb = cbeg; cb < a.nbk; cb += kCpIB) {
+                const int nc = int(min64(kCpIB, a.nbk - cb));
+                __syncthreads();
+                for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+                    int c = e % kCpIB, l = e / kCpIB;
+                    U3[l * 68 + c] = (c < nc && l < kb) ? __ldcg(&P[cb + c + (c0 + l) * ld]) : T(0);
+                }
+                for (int64_t rr = max64(r0, cb); rr < re; rr += kCpIB) {
+                    const int nr = int(min64(kCpIB, re - rr));
+                    __syncthreads();
+                    for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+                        int i = e % kCpIB, l = e / kCpIB;
+                        X3[l * 68 + i] = (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
+                    }
+                    __syncthreads();
+                    T acc[4][4];
+                    #pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+                    #pragma unroll 4
+                    for (int l = 0; l < kb; ++l) {
+                        T xr[4], uc[4];
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i) { xr[i] = X3[l * 68 + tr + 16 * i]; uc[i] = U3[l * 68 + tc + 16 * i]; }
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            #pragma unroll
+                            for (int j = 0; j < 4; ++j) acc[i][j] = fma(xr[i], uc[j], acc[i][j]);
+                    }
+                    #pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int c = tc + 16 * j;
+                        if (c >= nc) continue;
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const int ii = tr + 16 * i;
+                            const int64_t gi = rr + ii;
+                            if (ii < nr && gi >= cb + c) {
+                                T* p = &P[gi + (cb + c) * ld];
+                                *p = __ldcg(p) - acc[i][j];
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __threadfence();
+        if (!grid_sync(a.bar, unsigned(G), a.status)) return;
+        if (failed) return;       // every block saw the same failing diagonal block
+    }
+}
+
+template <typename T>
+static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info, int64_t info_offset,
+                             void* ws, int* status, cudaStream_t stream)
+{
+    if (m <= 0 || nbk <= 0) return SLT_OK;
+    int dev = 0, sms = 0, coop = 0;
+    SLT_CUDA_TRY(cudaGetDevice(&dev));
+    SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SLT_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return SLT_ERR_NOT_SUPPORTED;
+    const size_t smem = (size_t(kCpIB) * (kCpIB + 1) + size_t(2) * kCpIB * 68) * sizeof(T);
+    static bool cfg = false;
+    if (!cfg) {
+        SLT_CUDA_TRY(cudaFuncSetAttribute(chol_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        cfg = true;
+    }
+    int per_sm = 0;
+    SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chol_panel_kernel<T>, kCpThreads, smem));
+    if (per_sm < 1) return SLT_ERR_NOT_SUPPORTED;
+    const int64_t maxg = int64_t(sms) * per_sm;             // all blocks co-resident
+    int64_t R = ceildiv(ceildiv(m, maxg), kCpIB) * kCpIB;     // multiple of 64
+    int64_t G = ceildiv(m, R);
+    GridBarrier* bar = static_cast<GridBarrier*>(ws);
+    SLT_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), stream));
+    CholPanelArgs<T> args{m, nbk, ld, R, info_offset, P, info, status, bar};
+    void* kargs[] = { &args };
+    const int pidx = prof_begin(SLT_PROF_POTRF, stream);
+    SLT_CUDA_TRY(cudaLaunchCooperativeKernel((const void*) chol_panel_kernel<T>, dim3(unsigned(G)),
+                                             dim3(kCpThreads), kargs, smem, stream));
+    count_launch();
+    prof_end(pidx, stream, double(m) * double(nbk) * double(nbk), 2.0 * sizeof(T) * double(m) * double(nbk));
+    return SLT_OK;
+}
+
+} // namespace slt
+
+using namespace slt;
+
+// Factor the Cholesky column panel with top-left P (the diagonal element),
+// m rows (to the bottom of the matrix), nbk columns.  ws: >= 256 bytes of
+// device scratch for the grid barrier.
+extern "C" int slt_dchol_panel(int64_t m, int64_t nbk, double* P, int64_t ld, int* info, int64_t info_offset,
+                               void* ws, int* status, cudaStream_t stream)
+{ return launch_chol_panel<double>(m, nbk, P, ld, info, info_offset, ws, status, stream); }
+
+extern "C" int slt_schol_panel(int64_t m, int64_t nbk, float* P, int64_t ld, int* info, int64_t info_offset,
+                               void* ws, int* status, cudaStream_t stream)
+{ return launch_chol_panel<float>(m, nbk, P, ld, info, info_offset, ws, status, stream); }

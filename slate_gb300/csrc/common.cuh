@@ -10,10 +10,17 @@
 
 namespace slt {
 
-// Iteration bound for every spin-wait in this library.  With the 64 ns sleep
-// below this is roughly 2-4 seconds, far longer than any legitimate wait, after
-// which the waiting block records SLT_ERR_TIMEOUT and leaves.
-constexpr long long kSpinLimit = 1ll << 25;
+// Bound for every spin-wait in this library: about two seconds of wall time
+// (%globaltimer), far longer than any legitimate wait, after which the
+// waiting block records SLT_ERR_TIMEOUT and leaves.
+constexpr unsigned long long kWaitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned long long globaltimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
 {
@@ -62,13 +69,13 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned nblocks, in
             st_release_u32(&bar->gen, g + 1u);
         }
         else {
-            long long it = 0;
-            while (ld_acquire_u32(&bar->gen) == g) {
-                if (++it > kSpinLimit) {
+            const unsigned long long t0 = globaltimer();
+            for (unsigned it = 1; ld_acquire_u32(&bar->gen) == g; ++it) {
+                if ((it & 63u) == 0 && (ld_volatile_i32(status) != 0 || globaltimer() - t0 > kWaitNs)) {
                     atomicCAS(status, 0, SLT_ERR_TIMEOUT);
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(32);
             }
         }
         s_ok = (ld_volatile_i32(status) == 0);

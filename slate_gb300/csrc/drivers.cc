@@ -174,35 +174,32 @@ int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_opti
 }
 
 // getrs NoTrans: W = P B, forward sweep with unit L, backward with U
-// (src/getrs.cc:66-117; work::trsmA, src/work/work_trsmA.cc:147-480).
+// (src/getrs.cc:66-117; work::trsmA, src/work/work_trsmA.cc:147-480), each
+// sweep one persistent launch.
+static int k_sweep(int kind, int64_t n, int64_t nrhs, const double* M, int64_t ldm, double* X, int64_t ldx,
+                   int* flags, int* status, cudaStream_t s)
+{ return slt_dsweep(kind, n, nrhs, M, ldm, X, ldx, flags, status, s); }
+static int k_sweep(int kind, int64_t n, int64_t nrhs, const float* M, int64_t ldm, float* X, int64_t ldx,
+                   int* flags, int* status, cudaStream_t s)
+{ return slt_ssweep(kind, n, nrhs, M, ldm, X, ldx, flags, status, s); }
+
 template <typename T>
 int getrs_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv, int64_t nb,
-              T* B, int64_t ldb, cudaStream_t s)
+              T* B, int64_t ldb, int* d_status, cudaStream_t s)
 {
     if (n < 0 || nrhs < 0) return SLT_ERR_ARG;
     if (n == 0 || nrhs == 0) return SLT_OK;
-    DevBuf perm, W, ws;
+    DevBuf perm, W, flags;
     TRY(perm.alloc(sizeof(int) * size_t(n), s));
-    TRY(W.alloc(sizeof(T) * size_t(n) * size_t(nrhs), s));
-    TRY(ws.alloc(slt_residual_ws_bytes(n, std::min<int64_t>(nrhs, 16)), s));
+    TRY(W.alloc(sizeof(T) * size_t(n) * size_t(std::min<int64_t>(nrhs, 16)), s));
+    TRY(flags.alloc(slt_sweep_flags_bytes(n), s));
     TRY(slt_perm_from_ipiv(ipiv, n, nb, perm.as<int>(), s));
     T* w = W.as<T>();
     for (int64_t c0 = 0; c0 < nrhs; c0 += 16) {
         const int64_t nc = std::min<int64_t>(16, nrhs - c0);
         TRY(k_permute(1, perm.as<int>(), n, nc, B + c0 * ldb, ldb, w, n, s));
-        for (int64_t r0 = 0; r0 < n; r0 += nb) {
-            const int64_t kb = std::min(nb, n - r0);
-            TRY(k_trsm_llnu(kb, nc, LU + r0 + r0 * lda, lda, w + r0, n, s));
-            if (r0 + kb < n)
-                TRY(k_skinny(n - r0 - kb, nc, kb, T(-1), LU + (r0 + kb) + r0 * lda, lda, w + r0, n, T(1),
-                             w + r0 + kb, n, ws.p, s));
-        }
-        for (int64_t r0 = ((n - 1) / nb) * nb; r0 >= 0; r0 -= nb) {
-            const int64_t kb = std::min(nb, n - r0);
-            TRY(k_trsm_lunn(kb, nc, LU + r0 + r0 * lda, lda, w + r0, n, s));
-            if (r0 > 0)
-                TRY(k_skinny(r0, nc, kb, T(-1), LU + r0 * lda, lda, w + r0, n, T(1), w, n, ws.p, s));
-        }
+        TRY(k_sweep(0, n, nc, LU, lda, w, n, flags.as<int>(), d_status, s));
+        TRY(k_sweep(1, n, nc, LU, lda, w, n, flags.as<int>(), d_status, s));
         SLT_CUDA_TRY(cudaMemcpy2DAsync(B + c0 * ldb, size_t(ldb) * sizeof(T), w, size_t(n) * sizeof(T),
                                        size_t(n) * sizeof(T), size_t(nc), cudaMemcpyDeviceToDevice, s));
     }
@@ -213,25 +210,24 @@ int getrs_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv
 // steps of small potrf + solve of everything below + update of the rest of
 // the block column; then the herk-shaped trailing update
 // (impl::potrf, src/potrf.cc:22-210).
+static int k_chol_panel(int64_t m, int64_t nbk, double* P, int64_t ld, int* info, int64_t off, void* ws,
+                        int* status, cudaStream_t s)
+{ return slt_dchol_panel(m, nbk, P, ld, info, off, ws, status, s); }
+static int k_chol_panel(int64_t m, int64_t nbk, float* P, int64_t ld, int* info, int64_t off, void* ws,
+                        int* status, cudaStream_t s)
+{ return slt_schol_panel(m, nbk, P, ld, info, off, ws, status, s); }
+
 template <typename T>
 int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc, cudaStream_t s)
 {
     if (n < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
     const int64_t nb = eff_nb(o);
-    const int64_t inner = 64;
+    DevBuf bar;
+    TRY(bar.alloc(256, s));
     for (int64_t r0 = 0; r0 < n; r0 += nb) {
         const int64_t kb = std::min(nb, n - r0);
-        for (int64_t b = 0; b < kb; b += inner) {
-            const int64_t bs = std::min(inner, kb - b);
-            const int64_t c = r0 + b;
-            TRY(k_potrf_small(bs, A + c + c * lda, lda, fc.d_info, c, s));
-            const int64_t below = n - (c + bs);
-            if (below > 0) TRY(k_trsm_rltn(below, bs, A + c + c * lda, lda, A + (c + bs) + c * lda, lda, s));
-            const int64_t ncols = r0 + kb - (c + bs);
-            if (ncols > 0)
-                TRY(k_gemm('T', below, ncols, bs, T(-1), A + (c + bs) + c * lda, lda, A + (c + bs) + c * lda,
-                           lda, T(1), A + (c + bs) + (c + bs) * lda, lda, 1, o, s));
-        }
+        // the whole column panel (diagonal block and everything below) in one launch
+        TRY(k_chol_panel(n - r0, kb, A + r0 + r0 * lda, lda, fc.d_info, r0, bar.p, fc.d_status, s));
         const int64_t t0 = r0 + kb;
         if (t0 < n)
             TRY(k_gemm('T', n - t0, n - t0, kb, T(-1), A + t0 + r0 * lda, lda, A + t0 + r0 * lda, lda, T(1),
@@ -243,40 +239,30 @@ int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc,
 // potrs lower: forward with L, backward with L^T (src/potrs.cc:55-78).
 template <typename T>
 int potrs_dev(int64_t n, int64_t nrhs, const T* L, int64_t lda, int64_t nb, T* B, int64_t ldb,
-              cudaStream_t s)
+              int* d_status, cudaStream_t s)
 {
+    (void) nb;
     if (n < 0 || nrhs < 0) return SLT_ERR_ARG;
     if (n == 0 || nrhs == 0) return SLT_OK;
-    DevBuf ws;
-    TRY(ws.alloc(slt_residual_ws_bytes(n, std::min<int64_t>(nrhs, 16)), s));
+    DevBuf flags;
+    TRY(flags.alloc(slt_sweep_flags_bytes(n), s));
     for (int64_t c0 = 0; c0 < nrhs; c0 += 16) {
         const int64_t nc = std::min<int64_t>(16, nrhs - c0);
         T* b = B + c0 * ldb;
-        for (int64_t r0 = 0; r0 < n; r0 += nb) {
-            const int64_t kb = std::min(nb, n - r0);
-            TRY(k_trsm_llnn('N', kb, nc, L + r0 + r0 * lda, lda, b + r0, ldb, s));
-            if (r0 + kb < n)
-                TRY(k_skinny(n - r0 - kb, nc, kb, T(-1), L + (r0 + kb) + r0 * lda, lda, b + r0, ldb, T(1),
-                             b + r0 + kb, ldb, ws.p, s));
-        }
-        for (int64_t r0 = ((n - 1) / nb) * nb; r0 >= 0; r0 -= nb) {
-            const int64_t kb = std::min(nb, n - r0);
-            TRY(k_trsm_llnn('T', kb, nc, L + r0 + r0 * lda, lda, b + r0, ldb, s));
-            if (r0 > 0)
-                TRY(k_skinny_t(r0, nc, kb, T(-1), L + r0, lda, b + r0, ldb, T(1), b, ldb, s));
-        }
+        TRY(k_sweep(2, n, nc, L, lda, b, ldb, flags.as<int>(), d_status, s));
+        TRY(k_sweep(3, n, nc, L, lda, b, ldb, flags.as<int>(), d_status, s));
     }
     return SLT_OK;
 }
 
 template int getrf_dev<double>(int64_t, int64_t, double*, int64_t, int*, const slt_options&, FactorCtx&, cudaStream_t);
 template int getrf_dev<float>(int64_t, int64_t, float*, int64_t, int*, const slt_options&, FactorCtx&, cudaStream_t);
-template int getrs_dev<double>(int64_t, int64_t, const double*, int64_t, const int*, int64_t, double*, int64_t, cudaStream_t);
-template int getrs_dev<float>(int64_t, int64_t, const float*, int64_t, const int*, int64_t, float*, int64_t, cudaStream_t);
+template int getrs_dev<double>(int64_t, int64_t, const double*, int64_t, const int*, int64_t, double*, int64_t, int*, cudaStream_t);
+template int getrs_dev<float>(int64_t, int64_t, const float*, int64_t, const int*, int64_t, float*, int64_t, int*, cudaStream_t);
 template int potrf_dev<double>(int64_t, double*, int64_t, const slt_options&, FactorCtx&, cudaStream_t);
 template int potrf_dev<float>(int64_t, float*, int64_t, const slt_options&, FactorCtx&, cudaStream_t);
-template int potrs_dev<double>(int64_t, int64_t, const double*, int64_t, int64_t, double*, int64_t, cudaStream_t);
-template int potrs_dev<float>(int64_t, int64_t, const float*, int64_t, int64_t, float*, int64_t, cudaStream_t);
+template int potrs_dev<double>(int64_t, int64_t, const double*, int64_t, int64_t, double*, int64_t, int*, cudaStream_t);
+template int potrs_dev<float>(int64_t, int64_t, const float*, int64_t, int64_t, float*, int64_t, int*, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Mixed precision.
@@ -286,21 +272,26 @@ struct LoFactor {
     int chol;
     int64_t n, nb;
     slt_options o;
-    DevBuf A;          // float n x n
+    DevBuf A;          // float n x n, leading dimension ld (a multiple of 32 so the
+                       // tensor-core update can address it with TMA)
     int* ipiv;
+    int64_t ld = 0;
+    int* status = nullptr;
 
     int factor(const double* Ahi, int64_t lda, FactorCtx& fc, int64_t* info, cudaStream_t s) {
-        TRY(A.alloc(sizeof(float) * size_t(n) * size_t(n), s));
-        TRY(slt_convert_d2s(n, n, Ahi, lda, A.as<float>(), n, s));
-        if (chol) TRY(potrf_dev<float>(n, A.as<float>(), n, o, fc, s));
-        else TRY(getrf_dev<float>(n, n, A.as<float>(), n, ipiv, o, fc, s));
+        ld = ((n + 31) / 32) * 32;
+        TRY(A.alloc(sizeof(float) * size_t(ld) * size_t(n), s));
+        TRY(slt_convert_d2s(n, n, Ahi, lda, A.as<float>(), ld, s));
+        status = fc.d_status;
+        if (chol) TRY(potrf_dev<float>(n, A.as<float>(), ld, o, fc, s));
+        else TRY(getrf_dev<float>(n, n, A.as<float>(), ld, ipiv, o, fc, s));
         return finish_factor(fc, info, s);
     }
     // X (double) <- M^{-1} R (double), through FP32.
     int solve(int64_t nrhs, const double* R, int64_t ldr, double* X, int64_t ldx, float* wlo, cudaStream_t s) {
         TRY(slt_convert_d2s(n, nrhs, R, ldr, wlo, n, s));
-        if (chol) TRY(potrs_dev<float>(n, nrhs, A.as<float>(), n, nb, wlo, n, s));
-        else TRY(getrs_dev<float>(n, nrhs, A.as<float>(), n, ipiv, nb, wlo, n, s));
+        if (chol) TRY(potrs_dev<float>(n, nrhs, A.as<float>(), ld, nb, wlo, n, status, s));
+        else TRY(getrs_dev<float>(n, nrhs, A.as<float>(), ld, ipiv, nb, wlo, n, status, s));
         return slt_convert_s2d(n, nrhs, wlo, n, X, ldx, s);
     }
 };
@@ -337,8 +328,8 @@ int fallback_fp64(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int
     if (*info == 0) {
         tm.start(std::string(pfx) + (chol ? "::potrs_hi" : "::getrs_hi"));
         TRY(slt_dcopy2d(n, nrhs, B, ldb, X, ldx, s));
-        if (chol) TRY(potrs_dev<double>(n, nrhs, A, lda, eff_nb(o), X, ldx, s));
-        else TRY(getrs_dev<double>(n, nrhs, A, lda, ipiv, eff_nb(o), X, ldx, s));
+        if (chol) TRY(potrs_dev<double>(n, nrhs, A, lda, eff_nb(o), X, ldx, fc.d_status, s));
+        else TRY(getrs_dev<double>(n, nrhs, A, lda, ipiv, eff_nb(o), X, ldx, fc.d_status, s));
         tm.stop(std::string(pfx) + (chol ? "::potrs_hi" : "::getrs_hi"));
     }
     return SLT_OK;
@@ -424,8 +415,7 @@ int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, in
             TRY(fallback_fp64(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, o, info, tm, pfx, s));
     }
     tm.stop(pfx);
-    SLT_CUDA_TRY(cudaStreamSynchronize(s));
-    return SLT_OK;
+    return finish_factor(fc, nullptr, s);   // bounded-wait status of every launch above
 }
 
 // gesv_mixed_gmres / posv_mixed_gmres (src/gesv_mixed_gmres.cc:110-410,
@@ -579,8 +569,7 @@ int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t l
             TRY(fallback_fp64(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, o, info, tm, pfx, s));
     }
     tm.stop(pfx);
-    SLT_CUDA_TRY(cudaStreamSynchronize(s));
-    return SLT_OK;
+    return finish_factor(fc, nullptr, s);   // bounded-wait status of every launch above
 }
 
 } // namespace slt

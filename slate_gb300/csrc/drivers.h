@@ -24,15 +24,17 @@ int slt_dgemm_skinny_t(int64_t m, int64_t nrhs, int64_t kk, double alpha, const 
 int slt_sgemm_skinny_t(int64_t m, int64_t nrhs, int64_t kk, float alpha, const float* A, int64_t lda,
                        const float* X, int64_t ldx, float beta, float* C, int64_t ldc,
                        cudaStream_t stream);
+int slt_dsweep(int kind, int64_t n, int64_t nrhs, const double* M, int64_t ldm, double* X, int64_t ldx,
+               int* flags, int* status, cudaStream_t s);
+int slt_ssweep(int kind, int64_t n, int64_t nrhs, const float* M, int64_t ldm, float* X, int64_t ldx,
+               int* flags, int* status, cudaStream_t s);
+size_t slt_sweep_flags_bytes(int64_t n);
+int slt_dchol_panel(int64_t m, int64_t nbk, double* P, int64_t ld, int* info, int64_t info_offset, void* ws,
+                    int* status, cudaStream_t stream);
+int slt_schol_panel(int64_t m, int64_t nbk, float* P, int64_t ld, int* info, int64_t info_offset, void* ws,
+                    int* status, cudaStream_t stream);
 int slt_dnrm2(int64_t n, const double* x, double* out, cudaStream_t stream);
 int slt_dscal(int64_t n, const double* num, const double* den, double* x, cudaStream_t stream);
-/* Low-precision trailing update of the mixed factorisations:
- * C (FP32) = C - A op(B) with A, B rounded to the tier's type
- * (tier: SLT_PREC_TF32 / BF16 / FP16), fp32 accumulation on tcgen05. */
-int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, int64_t k, const float* A,
-                       int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int lower,
-                       void* ws, size_t ws_bytes, cudaStream_t stream);
-size_t slt_tc_gemm_ws_bytes(int64_t m, int64_t n, int64_t k);
 }
 
 namespace slt {
@@ -92,12 +94,12 @@ int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_opti
               FactorCtx& fc, cudaStream_t s);
 template <typename T>
 int getrs_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv, int64_t nb,
-              T* B, int64_t ldb, cudaStream_t s);
+              T* B, int64_t ldb, int* d_status, cudaStream_t s);
 template <typename T>
 int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc, cudaStream_t s);
 template <typename T>
 int potrs_dev(int64_t n, int64_t nrhs, const T* L, int64_t lda, int64_t nb, T* B, int64_t ldb,
-              cudaStream_t s);
+              int* d_status, cudaStream_t s);
 
 int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
                    const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,

@@ -12,6 +12,7 @@
 // the only FP64 tensor instruction on this part.
 
 #include "common.cuh"
+#include "prof.h"
 
 namespace slt {
 
@@ -244,13 +245,15 @@ extern "C" int slt_dgemm(char transb, int64_t m, int64_t n, int64_t k, double al
 {
     if (m < 0 || n < 0 || k < 0 || (transb != 'N' && transb != 'T')) return SLT_ERR_ARG;
     if (m == 0 || n == 0) return SLT_OK;
-    if (engine == 0) engine = g_dgemm_engine ? g_dgemm_engine : 2;
+    if (engine == 0) engine = g_dgemm_engine ? g_dgemm_engine : 1;
+    const int pidx = prof_begin(SLT_PROF_GEMM64, stream);
     if (engine == 2) {
         dim3 grid(unsigned(ceildiv(m, 64)), unsigned(ceildiv(n, 64)));
         if (transb == 'N')
             dgemm_dmma_kernel<false><<<grid, 128, 0, stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
         else
             dgemm_dmma_kernel<true><<<grid, 128, 0, stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+    slt::count_launch();
     }
     else {
         dim3 grid(unsigned(ceildiv(m, 64)), unsigned(ceildiv(n, 64)));
@@ -260,6 +263,11 @@ extern "C" int slt_dgemm(char transb, int64_t m, int64_t n, int64_t k, double al
         else
             gemm_simt_kernel<double, 64, 64, 8, 4, 4, true><<<grid, 256, 0, stream>>>(
                 m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+    slt::count_launch();
+    }
+    {
+        double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);
+        prof_end(pidx, stream, 2.0 * mn * double(k), 8.0 * (2.0 * mn + double(k) * double(m + n)));
     }
     return slt_from_cuda(cudaGetLastError());
 }
@@ -271,11 +279,17 @@ extern "C" int slt_sgemm(char transb, int64_t m, int64_t n, int64_t k, float alp
     if (m < 0 || n < 0 || k < 0 || (transb != 'N' && transb != 'T')) return SLT_ERR_ARG;
     if (m == 0 || n == 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(m, 128)), unsigned(ceildiv(n, 128)));
+    const int pidx = prof_begin(SLT_PROF_GEMM32, stream);
     if (transb == 'N')
         gemm_simt_kernel<float, 128, 128, 8, 8, 8, false><<<grid, 256, 0, stream>>>(
             m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
     else
         gemm_simt_kernel<float, 128, 128, 8, 8, 8, true><<<grid, 256, 0, stream>>>(
             m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+    slt::count_launch();
+    {
+        double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);
+        prof_end(pidx, stream, 2.0 * mn * double(k), 4.0 * (2.0 * mn + double(k) * double(m + n)));
+    }
     return slt_from_cuda(cudaGetLastError());
 }

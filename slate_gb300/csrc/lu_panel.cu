@@ -23,6 +23,7 @@
 // then one launch moves every affected row of every column.
 
 #include "common.cuh"
+#include "prof.h"
 #include <climits>
 
 namespace slt {
@@ -415,8 +416,14 @@ static int launch_panel(int64_t prows, int64_t nbk, int64_t ib, T* P, int64_t ld
     args.P = P; args.ipiv = ipiv; args.info = info; args.status = status;
     args.bar = bar; args.ex = ex;
     void* kargs[] = { &args };
+    const int pidx = prof_begin(SLT_PROF_PANEL, stream);
     SLT_CUDA_TRY(cudaLaunchCooperativeKernel((const void*) getrf_panel_kernel<T>, dim3(unsigned(G)),
                                              dim3(kPanelThreads), kargs, 0, stream));
+    count_launch();
+    {
+        const double nb_ = double(nbk), m_ = double(prows);
+        prof_end(pidx, stream, m_ * nb_ * nb_ - nb_ * nb_ * nb_ / 3.0, 2.0 * m_ * nb_ * sizeof(T));
+    }
     return SLT_OK;
 }
 
@@ -432,7 +439,9 @@ static int launch_laswp(const int* plan, int64_t maxcount, T* A, int64_t lda, in
         SLT_CUDA_TRY(cudaFuncSetAttribute(laswp_plan_kernel<T, CB>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     unsigned grid = unsigned(ceildiv(ncols, CB));
-    laswp_plan_kernel<T, CB><<<grid, 256, smem, stream>>>(plan, int(maxcount), A, lda, ncols);
+    const int pidx = prof_begin(SLT_PROF_LASWP, stream);
+    laswp_plan_kernel<T, CB><<<grid, 256, smem, stream>>>(plan, int(maxcount), A, lda, ncols); slt::count_launch();
+    prof_end(pidx, stream, 0.0, 2.0 * sizeof(T) * double(maxcount) * double(ncols));
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -465,7 +474,7 @@ extern "C" int slt_swap_plan(const int* ipiv, int64_t len, int64_t r0, int* plan
     if (len <= 0) return SLT_OK;
     if (len > 1024) return SLT_ERR_ARG;
     size_t smem = size_t(4 * len) * sizeof(int);
-    swap_plan_kernel<<<1, 256, smem, stream>>>(ipiv, int(len), r0, plan);
+    swap_plan_kernel<<<1, 256, smem, stream>>>(ipiv, int(len), r0, plan); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -484,7 +493,7 @@ extern "C" int slt_slaswp_plan(const int* plan, int64_t maxcount, float* A, int6
 extern "C" int slt_perm_from_ipiv(const int* ipiv, int64_t n, int64_t nb, int* perm, cudaStream_t stream)
 {
     if (n <= 0) return SLT_OK;
-    perm_from_ipiv_kernel<<<unsigned(ceildiv(n, 256)), 256, 0, stream>>>(ipiv, int(n), int(nb), perm);
+    perm_from_ipiv_kernel<<<unsigned(ceildiv(n, 256)), 256, 0, stream>>>(ipiv, int(n), int(nb), perm); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -493,7 +502,7 @@ extern "C" int slt_dpermute_rows(int forward, const int* perm, int64_t n, int64_
 {
     if (n <= 0 || ncols <= 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(n, 256)), unsigned(ncols));
-    permute_rows_kernel<double><<<grid, 256, 0, stream>>>(forward, perm, n, ncols, X, ldx, Y, ldy);
+    permute_rows_kernel<double><<<grid, 256, 0, stream>>>(forward, perm, n, ncols, X, ldx, Y, ldy); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -502,6 +511,6 @@ extern "C" int slt_spermute_rows(int forward, const int* perm, int64_t n, int64_
 {
     if (n <= 0 || ncols <= 0) return SLT_OK;
     dim3 grid(unsigned(ceildiv(n, 256)), unsigned(ncols));
-    permute_rows_kernel<float><<<grid, 256, 0, stream>>>(forward, perm, n, ncols, X, ldx, Y, ldy);
+    permute_rows_kernel<float><<<grid, 256, 0, stream>>>(forward, perm, n, ncols, X, ldx, Y, ldy); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }

@@ -37,6 +37,18 @@ int slt_sgemm(char transb, int64_t m, int64_t n, int64_t k, float alpha,
               const float* A, int64_t lda, const float* B, int64_t ldb,
               float beta, float* C, int64_t ldc, int lower, cudaStream_t stream);
 
+/* ---- low-precision tensor-core update (tcgen05) ----------------------------
+ * C (fp32, m x n) -= A (m x k) op(B), operands rounded to the tier's type
+ * (2 TF32, 3 BF16, 4 FP16), fp32 accumulation in TMEM.  transb 'N': B is
+ * k x n; 'T': B is n x k.  lower: only C(i,j), i >= j, is updated.  ws may be
+ * null.  slt_tc_status() returns (and clears) SLT_ERR_TIMEOUT after a tile
+ * gave up waiting. */
+int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, int64_t k, const float* A,
+                       int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int lower,
+                       void* ws, size_t ws_bytes, cudaStream_t stream);
+size_t slt_tc_gemm_ws_bytes(int64_t m, int64_t n, int64_t k);
+int slt_tc_status(void);
+
 /* ---- LU panel -------------------------------------------------------------
  * Factor the prows x nbk panel P (top-left = diagonal element) with partial
  * pivoting.  ipiv[j] receives the pivot row of column j relative to the

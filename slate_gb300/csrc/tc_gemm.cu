@@ -1,13 +1,742 @@
-// tc_gemm.cu -- low-precision tensor-core trailing update (tcgen05).
+// tc_gemm.cu -- low-precision tensor-core trailing update on tcgen05 (sm_103a).
+//
+// The O(n^3) part of the mixed-precision factorisations: SLATE's trailing
+// update (internal::gemm / internal::herk, src/internal/internal_gemm.cc:
+// 354-518, src/internal/internal_herk.cc:350-540) runs in FP32 there
+// (gesv_mixed<double,float>, src/gesv_mixed.cc:183).  Here the trailing matrix
+// stays FP32 in HBM while the two panel operands are rounded to BF16 / FP16
+// (or TF32) and multiplied on the 5th-generation tensor cores with FP32
+// accumulation:
+//
+//     C (fp32, m x n) -= A (m x k) * op(B),  op(B) = B (k x n) or B^T.
+//
+// 1. pack_kernel: cast the operands to the tier's type, K-contiguous rows
+//    ("K-major"), zero-padded to the tile grid.
+// 2. tc_update_kernel: one 128 x BN output tile per CTA.  One thread issues
+//    TMA loads (cp.async.bulk.tensor, 128B swizzle) into a ring of smem
+//    stages guarded by mbarriers; one thread issues tcgen05.mma into a TMEM
+//    accumulator and frees stages with tcgen05.commit; then all four warps
+//    read the accumulator with tcgen05.ld (32 lanes x 32 columns per
+//    instruction) and update C with coalesced column segments.
+// Every mbarrier wait is bounded: on timeout the CTA records
+// SLT_ERR_TIMEOUT, drains its own TMA copies (bounded), frees its TMEM and
+// returns.
+
 #include "common.cuh"
+#include "prof.h"
+#include "slate_gb300.h"
 
-extern "C" size_t slt_tc_gemm_ws_bytes(int64_t, int64_t, int64_t) { return 0; }
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
+#include <mutex>
+
+namespace slt {
+
+constexpr int kTcBM = 128;
+constexpr int kTcBN = 128;
+constexpr int kTcStages = 4;
+constexpr int kTcThreads = 128;
+constexpr long long kTcSpin = 1ll << 24;
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred P1;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+                 "selp.b32 %0, 1, 0, P1;\n\t}"
+                 : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait (about two seconds of wall time, and an iteration cap);
+// returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (long long it = 0; it < kTcSpin; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63) == 0 && globaltimer_ns() - t0 > 2000000000ull) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%3, %4}], [%2];"
+                 :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(dst_smem), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(ncols) : "memory");
+}
+
+template <int KIND>   // 0: kind::f16 (BF16/FP16 operands), 1: kind::tf32
+__device__ __forceinline__ void umma(uint32_t taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
+{
+    if (KIND == 0)
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                     :: "r"(taddr), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
+    else
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                     :: "r"(taddr), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(bar) : "memory");
+}
+
+// 32 lanes x 32 consecutive fp32 columns of TMEM into registers.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+                 "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+                   "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+                   "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    #pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), start address in 16-byte units.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= uint64_t((saddr >> 4) & 0x3FFFu);          // start address
+    d |= uint64_t(1) << 16;                          // leading byte offset (unused for SW128 K-major)
+    d |= uint64_t(1024 >> 4) << 32;                  // stride byte offset
+    d |= uint64_t(1) << 46;                          // descriptor version
+    d |= uint64_t(2) << 61;                          // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor: D fp32, A/B format, both K-major, M = 128, N = BN.
+__host__ __device__ constexpr uint32_t make_idesc(uint32_t ab_format, int M, int N)
+{
+    return (1u << 4) | (ab_format << 7) | (ab_format << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
+
+struct TcArgs {
+    int64_t m, n, kpad;
+    float* C;
+    int64_t ldc;
+    int lower;
+    int* status;
+};
+
+// KIND 0: 16-bit operands (BF16 or FP16 per fmt), KIND 1: TF32.
+template <int KIND>
+__global__ void __launch_bounds__(kTcThreads, 1)
+tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                 TcArgs a, uint32_t idesc)
+{
+    constexpr int BM = kTcBM, BN = kTcBN, S = kTcStages;
+    constexpr int A_BYTES = BM * 128;   // 128 rows x 128 B (one swizzle atom of K)
+    constexpr int B_BYTES = BN * 128;
+    constexpr int STAGE = A_BYTES + B_BYTES;
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    // 1024-byte aligned base for the swizzled tiles
+    const uint32_t raw = smem_u32(tc_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char* gbase = tc_smem_raw + (base - raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + S * STAGE);   // full[S], empty[S], accum
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 1);
+    __shared__ int s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t row0 = int64_t(blockIdx.x) * BM;
+    const int64_t col0 = int64_t(blockIdx.y) * BN;
+    if (a.lower && row0 + BM - 1 < col0) return;       // tile strictly above the diagonal
+    const int KT = int(a.kpad / (KIND == 0 ? 64 : 32));
+
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S), accum = smem_u32(bars + 2 * S);
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        for (int s = 0; s < S; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(accum, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(smem_u32(tmem_slot), BN);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = *tmem_slot;
+
+    int issued = 0;   // TMA stages armed by the producer
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer
+        for (int kt = 0; kt < KT; ++kt) {
+            const int s = kt % S;
+            const uint32_t par = ((kt / S) & 1) ^ 1;
+            if (!mbar_wait(empty0 + 8 * s, par)) { atomicCAS(a.status, 0, SLT_ERR_TIMEOUT); s_abort = 1; break; }
+            if (*(volatile int*) &s_abort) break;
+            const uint32_t sa = base + s * STAGE, sb = sa + A_BYTES;
+            mbar_expect_tx(full0 + 8 * s, STAGE);
+            tma_load_2d(sa, &mapA, full0 + 8 * s, kt * (KIND == 0 ? 64 : 32), int(row0));
+            tma_load_2d(sb, &mapB, full0 + 8 * s, kt * (KIND == 0 ? 64 : 32), int(col0));
+            issued = kt + 1;
+        }
+    }
+    else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer
+        bool ok = true;
+        for (int kt = 0; kt < KT; ++kt) {
+            const int s = kt % S;
+            const uint32_t par = (kt / S) & 1;
+            if (!mbar_wait(full0 + 8 * s, par)) { atomicCAS(a.status, 0, SLT_ERR_TIMEOUT); ok = false; break; }
+            if (*(volatile int*) &s_abort) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t sa = base + s * STAGE, sb = sa + A_BYTES;
+            const uint64_t da = sw128_desc(sa), db = sw128_desc(sb);
+            #pragma unroll
+            for (int k = 0; k < 4; ++k)   // 4 MMAs of K = 16 (16-bit) or 8 (tf32): 32 bytes each
+                umma<KIND>(taddr, da + uint64_t(2 * k), db + uint64_t(2 * k), idesc, (kt | k) != 0 ? 1u : 0u);
+            umma_commit(empty0 + 8 * s);
+        }
+        if (ok) umma_commit(accum);
+        else s_abort = 1;
+    }
+    __syncwarp();
+
+    // ---- epilogue: all four warps
+    bool ready = mbar_wait(accum, 0);
+    ready = __all_sync(0xffffffffu, ready);          // tcgen05.ld below is warp-collective
+    if (!ready && lane == 0) atomicCAS(a.status, 0, SLT_ERR_TIMEOUT);
+    tc_fence_after();
+    if (ready) {
+        const int64_t r = row0 + warp * 32 + lane;
+        #pragma unroll 1
+        for (int cc = 0; cc < BN; cc += 32) {
+            float v[32];
+            tmem_ld32(taddr + (uint32_t(warp * 32) << 16) + uint32_t(cc), v);
+            if (r < a.m) {
+                #pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const int64_t c = col0 + cc + i;
+                    if (c < a.n && !(a.lower && r < c)) {
+                        float* p = a.C + r + c * a.ldc;
+                        *p = *p - v[i];
+                    }
+                }
+            }
+        }
+    }
+    // drain this CTA's own TMA copies if the pipeline was abandoned
+    if (warp == 0 && lane == 0 && !ready) {
+        for (int s = 0; s < S && s < issued; ++s) {
+            const int last = s + ((issued - 1 - s) / S) * S;   // last armed phase of stage s
+            mbar_wait(full0 + 8 * s, (last / S) & 1);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(taddr, BN);
+}
+
+// Persistent, warp-specialised variant.  Warp 0: TMA producer; warp 1: MMA
+// issuer (and TMEM owner); warps 2-5: epilogue, one TMEM lane quarter each.
+// Two TMEM accumulators (2 x BN columns) let the epilogue of one tile overlap
+// the MMAs of the next.  The epilogue stages -acc in shared memory and adds
+// it to C with a TMA tensor reduce (cp.reduce.async.bulk.tensor .add), so the
+// read-modify-write of C is done by the memory system with full overlap.
+constexpr int kPThreads = 192;
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, uint32_t src, int x, int y)
+{
+    asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%2, %3}], [%1];"
+                 :: "l"(reinterpret_cast<uint64_t>(map)), "r"(src), "r"(x), "r"(y) : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void bulk_wait_read_le1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+template <int KIND>
+__global__ void __launch_bounds__(kPThreads, 1)
+tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                     const __grid_constant__ CUtensorMap mapC, TcArgs a, uint32_t idesc)
+{
+    constexpr int BM = kTcBM, BN = kTcBN, S = kTcStages;
+    constexpr int A_BYTES = BM * 128;
+    constexpr int B_BYTES = BN * 128;
+    constexpr int STAGE = A_BYTES + B_BYTES;
+    constexpr int STG = 32 * 32 * 4;               // one 32 x 32 fp32 staging box
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    const uint32_t raw = smem_u32(tc_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char* gbase = tc_smem_raw + (base - raw);
+    float* stage_c = reinterpret_cast<float*>(gbase + S * STAGE);          // [4 warps][2][32*32]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + S * STAGE + 8 * STG);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 4);
+    __shared__ int s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t mt = ceildiv(a.m, BM), nt = ceildiv(a.n, BN);
+    const int64_t ntiles = mt * nt;
+    const int KT = int(a.kpad / (KIND == 0 ? 64 : 32));
+
+    const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S);
+    const uint32_t tfull0 = smem_u32(bars + 2 * S), tempty0 = smem_u32(bars + 2 * S + 2);
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        for (int s = 0; s < S; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(tfull0 + 8 * b, 1);
+            mbar_init(tempty0 + 8 * b, 4);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) tmem_alloc(smem_u32(tmem_slot), 2 * BN);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = *tmem_slot;
+
+    auto skip = [&](int64_t t) {
+        const int64_t r0 = (t % mt) * BM, c0 = (t / mt) * BN;
+        return a.lower && r0 + BM - 1 < c0;
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer
+            long long it = 0;
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                if (skip(t)) continue;
+                const int row0 = int((t % mt) * BM), col0 = int((t / mt) * BN);
+                for (int kt = 0; kt < KT; ++kt, ++it) {
+                    const int s = int(it % S);
+                    const uint32_t par = uint32_t((it / S) & 1) ^ 1u;
+                    if (!mbar_wait(empty0 + 8 * s, par) || *(volatile int*) &s_abort) {
+                        atomicCAS(a.status, 0, SLT_ERR_TIMEOUT);
+                        s_abort = 1;
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t sa = base + s * STAGE, sb = sa + A_BYTES;
+                    mbar_expect_tx(full0 + 8 * s, STAGE);
+                    tma_load_2d(sa, &mapA, full0 + 8 * s, kt * (KIND == 0 ? 64 : 32), row0);
+                    tma_load_2d(sb, &mapB, full0 + 8 * s, kt * (KIND == 0 ? 64 : 32), col0);
+                }
+            }
+            // drain: the last armed phase of every stage must land before exit
+            const long long issued = it;
+            for (int s = 0; s < S && s < issued; ++s) {
+                const long long last = s + ((issued - 1 - s) / S) * S;
+                mbar_wait(full0 + 8 * s, uint32_t((last / S) & 1));
+            }
+        }
+    }
+    else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer
+            long long it = 0;
+            int lt = 0;
+            for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+                if (skip(t)) continue;
+                const int buf = lt & 1;
+                const uint32_t upar = uint32_t((lt >> 1) & 1) ^ 1u;
+                if (!mbar_wait(tempty0 + 8 * buf, upar) || *(volatile int*) &s_abort) {
+                    atomicCAS(a.status, 0, SLT_ERR_TIMEOUT);
+                    s_abort = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t tacc = taddr + uint32_t(buf * BN);
+                bool ok = true;
+                for (int kt = 0; kt < KT; ++kt, ++it) {
+                    const int s = int(it % S);
+                    const uint32_t par = uint32_t((it / S) & 1);
+                    if (!mbar_wait(full0 + 8 * s, par) || *(volatile int*) &s_abort) {
+                        atomicCAS(a.status, 0, SLT_ERR_TIMEOUT);
+                        s_abort = 1;
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = base + s * STAGE, sb = sa + A_BYTES;
+                    const uint64_t da = sw128_desc(sa), db = sw128_desc(sb);
+                    #pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        umma<KIND>(tacc, da + uint64_t(2 * k), db + uint64_t(2 * k), idesc, (kt | k) != 0 ? 1u : 0u);
+                    umma_commit(empty0 + 8 * s);
+                }
+                if (!ok) break;
+                umma_commit(tfull0 + 8 * buf);
+                ++lt;
+            }
+        }
+    }
+    else {
+        // ---- epilogue warps 2..5: TMEM lane quarter q = warp % 4
+        const int q = warp & 3;
+        float* stg = stage_c + (warp - 2) * 2 * (32 * 32);
+        int lt = 0, chunk = 0;
+        bool prev_committed = true;     // did the previous chunk commit a bulk group?
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            if (skip(t)) continue;
+            const int buf = lt & 1;
+            bool ready = mbar_wait(tfull0 + 8 * buf, uint32_t((lt >> 1) & 1));
+            ready = __all_sync(0xffffffffu, ready) && !*(volatile int*) &s_abort;
+            if (!ready) {
+                if (lane == 0) { atomicCAS(a.status, 0, SLT_ERR_TIMEOUT); s_abort = 1; }
+                break;
+            }
+            tc_fence_after();
+            const int64_t row0 = (t % mt) * BM, col0 = (t / mt) * BN;
+            const int64_t r = row0 + q * 32 + lane;
+            #pragma unroll 1
+            for (int cc = 0; cc < BN; cc += 32, ++chunk) {
+                float v[32];
+                tmem_ld32(taddr + (uint32_t(q * 32) << 16) + uint32_t(buf * BN + cc), v);
+                float* sb = stg + (chunk & 1) * (32 * 32);
+                // this buffer was last read by the group two chunks back: if the
+                // previous chunk committed a group, allowing one pending group
+                // leaves exactly that newer one in flight; otherwise wait for all
+                if (lane == 0) {
+                    if (prev_committed) bulk_wait_read_le1();
+                    else asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                }
+                __syncwarp();
+                #pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const int64_t c = col0 + cc + i;
+                    sb[i * 32 + lane] = (a.lower && r < c) ? 0.f : -v[i];
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                prev_committed = (row0 + q * 32 < a.m && col0 + cc < a.n);
+                if (lane == 0 && prev_committed)
+                    tma_reduce_add_2d(&mapC, smem_u32(sb), int(row0 + q * 32), int(col0 + cc));
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
+            ++lt;
+        }
+        if (lane == 0) bulk_wait_all();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) tmem_dealloc(taddr, 2 * BN);
+}
+
+// Cast + K-major packing: dst[r][c] (row stride kpad) = src element (r, c);
+// TRANS: src is column-major rows x k (element (r, c) at src[r + c*ld]),
+// else src "row" r is contiguous over c (element (r, c) at src[c + r*ld]).
+// Zero fill up to rpad x kpad.
+template <typename TO, bool TRANS>
+__global__ void __launch_bounds__(256)
+pack_kernel(int64_t rows, int64_t k, const float* __restrict__ src, int64_t ld, TO* __restrict__ dst,
+            int64_t rpad, int64_t kpad)
+{
+    __shared__ float t[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;   // 32 x 8
+    const int64_t r0 = int64_t(blockIdx.y) * 32, c0 = int64_t(blockIdx.x) * 32;
+    if (TRANS) {
+        for (int q = ty; q < 32; q += 8) {            // read column c0+q, rows r0+tx (coalesced)
+            int64_t r = r0 + tx, c = c0 + q;
+            t[q][tx] = (r < rows && c < k) ? src[r + c * ld] : 0.f;
+        }
+        __syncthreads();
+        for (int q = ty; q < 32; q += 8) {            // write row r0+q, cols c0+tx (coalesced)
+            int64_t r = r0 + q, c = c0 + tx;
+            if (r < rpad && c < kpad) {
+                float v = t[tx][q];
+                if constexpr (sizeof(TO) == 4) {
+                    uint32_t u;
+                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(v));
+                    dst[r * kpad + c] = __uint_as_float(u);
+                }
+                else {
+                    dst[r * kpad + c] = TO(v);
+                }
+            }
+        }
+    }
+    else {
+        for (int q = ty; q < 32; q += 8) {
+            int64_t r = r0 + q, c = c0 + tx;
+            if (r < rpad && c < kpad) {
+                float v = (r < rows && c < k) ? src[c + r * ld] : 0.f;
+                if constexpr (sizeof(TO) == 4) {
+                    uint32_t u;
+                    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(v));
+                    dst[r * kpad + c] = __uint_as_float(u);
+                }
+                else {
+                    dst[r * kpad + c] = TO(v);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+static std::once_flag g_encode_once;
+
+static int get_encode()
+{
+    std::call_once(g_encode_once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &fn, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        cudaGetLastError();
+    });
+    return g_encode ? SLT_OK : SLT_ERR_NOT_SUPPORTED;
+}
+
+// 2-D map over a packed operand: inner dim = kpad elements, outer = rpad rows,
+// box = (128 bytes of K) x box_rows, 128B swizzle.
+static int make_map(CUtensorMap* map, void* ptr, CUtensorMapDataType dt, int esize, int64_t kpad,
+                    int64_t rpad, int box_rows)
+{
+    cuuint64_t dims[2] = {cuuint64_t(kpad), cuuint64_t(rpad)};
+    cuuint64_t strides[1] = {cuuint64_t(kpad) * cuuint64_t(esize)};
+    cuuint32_t box[2] = {cuuint32_t(128 / esize), cuuint32_t(box_rows)};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, dt, 2, ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? SLT_OK : SLT_ERR_ARG;
+}
+
+template <typename TO, bool TRANS>
+static int launch_pack(int64_t rows, int64_t k, const float* src, int64_t ld, TO* dst, int64_t rpad,
+                       int64_t kpad, cudaStream_t s)
+{
+    dim3 grid(unsigned(ceildiv(kpad, 32)), unsigned(ceildiv(rpad, 32)));
+    pack_kernel<TO, TRANS><<<grid, 256, 0, s>>>(rows, k, src, ld, dst, rpad, kpad);
+    count_launch();
+    return slt_from_cuda(cudaGetLastError());
+}
+
+static size_t tc_smem_bytes()
+{
+    return size_t(kTcStages) * (kTcBM + kTcBN) * 128 + 1024 + 256;
+}
+
+static size_t tcp_smem_bytes()
+{
+    return size_t(kTcStages) * (kTcBM + kTcBN) * 128 + 8 * 32 * 32 * 4 + 1024 + 256;
+}
+
+// fp32 column-major C: inner dim m (rows), outer n, box 32 x 32, no swizzle.
+static int make_map_c(CUtensorMap* map, float* C, int64_t m, int64_t n, int64_t ldc)
+{
+    cuuint64_t dims[2] = {cuuint64_t(m), cuuint64_t(n)};
+    cuuint64_t strides[1] = {cuuint64_t(ldc) * 4};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, C, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                          CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? SLT_OK : SLT_ERR_ARG;
+}
+
+static int g_sms = 0;
+
+// device status word for the tensor-core path (timeouts)
+static int* g_tc_status = nullptr;
+
+} // namespace slt
+
+using namespace slt;
+
+extern "C" size_t slt_tc_gemm_ws_bytes(int64_t m, int64_t n, int64_t k)
+{
+    int64_t kpad = ceildiv(k, 64) * 64;
+    int64_t mp = ceildiv(m, kTcBM) * kTcBM, np = ceildiv(n, kTcBN) * kTcBN;
+    return size_t(mp + np) * size_t(kpad) * 4 + 2048;
+}
+
+// C (fp32) -= A op(B), operands rounded to the tier's type.  transb 'N':
+// B is k x n (column-major); 'T': B is n x k (C -= A B^T).  ws may be null
+// (allocated from the stream-ordered pool).
 extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, int64_t k, const float* A,
                                   int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int lower,
                                   void* ws, size_t ws_bytes, cudaStream_t stream)
 {
-    (void) tier; (void) transb; (void) m; (void) n; (void) k; (void) A; (void) lda; (void) B; (void) ldb;
-    (void) C; (void) ldc; (void) lower; (void) ws; (void) ws_bytes; (void) stream;
-    return SLT_ERR_NOT_SUPPORTED;
+    if (m < 0 || n < 0 || k < 0 || (transb != 'N' && transb != 'T')) return SLT_ERR_ARG;
+    if (tier != SLT_PREC_TF32 && tier != SLT_PREC_BF16 && tier != SLT_PREC_FP16) return SLT_ERR_ARG;
+    if (m == 0 || n == 0 || k == 0) return SLT_OK;
+    int rc = get_encode();
+    if (rc) return rc;
+    if (!g_tc_status) {
+        SLT_CUDA_TRY(cudaMalloc(&g_tc_status, sizeof(int)));
+        SLT_CUDA_TRY(cudaMemset(g_tc_status, 0, sizeof(int)));
+    }
+    const bool tf32 = tier == SLT_PREC_TF32;
+    const int esize = tf32 ? 4 : 2;
+    const int64_t kpad = ceildiv(k, tf32 ? 32 : 64) * (tf32 ? 32 : 64);
+    const int64_t mp = ceildiv(m, kTcBM) * kTcBM, np = ceildiv(n, kTcBN) * kTcBN;
+    const size_t need = size_t(mp + np) * size_t(kpad) * esize + 2048;
+    void* owned = nullptr;
+    if (!ws || ws_bytes < need) {
+        if (cudaMallocAsync(&owned, need, stream) != cudaSuccess) { cudaGetLastError(); return SLT_ERR_NOMEM; }
+        ws = owned;
+    }
+    char* pa = static_cast<char*>(ws);
+    char* pb = pa + ((size_t(mp) * kpad * esize + 1023) & ~size_t(1023));
+    // pack operands
+    if (tier == SLT_PREC_BF16) {
+        rc = launch_pack<__nv_bfloat16, true>(m, k, A, lda, reinterpret_cast<__nv_bfloat16*>(pa), mp, kpad, stream);
+        if (!rc) rc = (transb == 'N')
+            ? launch_pack<__nv_bfloat16, false>(n, k, B, ldb, reinterpret_cast<__nv_bfloat16*>(pb), np, kpad, stream)
+            : launch_pack<__nv_bfloat16, true>(n, k, B, ldb, reinterpret_cast<__nv_bfloat16*>(pb), np, kpad, stream);
+    }
+    else if (tier == SLT_PREC_FP16) {
+        rc = launch_pack<__half, true>(m, k, A, lda, reinterpret_cast<__half*>(pa), mp, kpad, stream);
+        if (!rc) rc = (transb == 'N')
+            ? launch_pack<__half, false>(n, k, B, ldb, reinterpret_cast<__half*>(pb), np, kpad, stream)
+            : launch_pack<__half, true>(n, k, B, ldb, reinterpret_cast<__half*>(pb), np, kpad, stream);
+    }
+    else {
+        rc = launch_pack<float, true>(m, k, A, lda, reinterpret_cast<float*>(pa), mp, kpad, stream);
+        if (!rc) rc = (transb == 'N')
+            ? launch_pack<float, false>(n, k, B, ldb, reinterpret_cast<float*>(pb), np, kpad, stream)
+            : launch_pack<float, true>(n, k, B, ldb, reinterpret_cast<float*>(pb), np, kpad, stream);
+    }
+    if (!rc) {
+        CUtensorMap mapA, mapB;
+        CUtensorMapDataType dt = tier == SLT_PREC_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                               : tier == SLT_PREC_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                       : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+        rc = make_map(&mapA, pa, dt, esize, kpad, mp, kTcBM);
+        if (!rc) rc = make_map(&mapB, pb, dt, esize, kpad, np, kTcBN);
+        if (!rc) {
+            TcArgs args{m, n, kpad, C, ldc, lower, g_tc_status};
+            const int pidx = prof_begin(SLT_PROF_GEMM_TC, stream);
+            const bool tma_c = (reinterpret_cast<uintptr_t>(C) % 16 == 0) && (ldc % 4 == 0);
+            CUtensorMap mapC;
+            if (tma_c) rc = make_map_c(&mapC, C, m, n, ldc);
+            if (rc) {
+                // not reachable for aligned C; keep the status
+            }
+            else if (tma_c) {
+                if (!g_sms) {
+                    int dev = 0;
+                    cudaGetDevice(&dev);
+                    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+                }
+                const size_t psm = tcp_smem_bytes();
+                const int64_t tiles = (mp / kTcBM) * (np / kTcBN);
+                const unsigned grid1 = unsigned(std::min<int64_t>(tiles, g_sms));
+                if (tf32) {
+                    static bool cfg = false;
+                    if (!cfg) { cudaFuncSetAttribute(tc_update_persistent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psm)); cfg = true; }
+                    tc_update_persistent<1><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(2, kTcBM, kTcBN));
+                }
+                else {
+                    static bool cfg = false;
+                    if (!cfg) { cudaFuncSetAttribute(tc_update_persistent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psm)); cfg = true; }
+                    const uint32_t fmt = tier == SLT_PREC_BF16 ? 1u : 0u;
+                    tc_update_persistent<0><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(fmt, kTcBM, kTcBN));
+                }
+            }
+            else {
+            const size_t smem = tc_smem_bytes();
+            dim3 grid(unsigned(mp / kTcBM), unsigned(np / kTcBN));
+            if (tf32) {
+                static bool cfg = false;
+                if (!cfg) { cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); cfg = true; }
+                tc_update_kernel<1><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(2, kTcBM, kTcBN));
+            }
+            else {
+                static bool cfg = false;
+                if (!cfg) { cudaFuncSetAttribute(tc_update_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); cfg = true; }
+                const uint32_t fmt = tier == SLT_PREC_BF16 ? 1u : 0u;
+                tc_update_kernel<0><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(fmt, kTcBM, kTcBN));
+            }
+            }
+            count_launch();
+            rc = slt_from_cuda(cudaGetLastError());
+            double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);
+            prof_end(pidx, stream, 2.0 * mn * double(k), 8.0 * mn + double(esize) * double(k) * double(m + n));
+        }
+    }
+    if (owned) cudaFreeAsync(owned, stream);
+    return rc;
+}
+
+// Status of the tensor-core path (SLT_ERR_TIMEOUT after an abandoned tile);
+// reading clears it.
+extern "C" int slt_tc_status(void)
+{
+    if (!g_tc_status) return SLT_OK;
+    int h = 0;
+    if (cudaMemcpy(&h, g_tc_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return SLT_ERR_CUDA_BASE;
+    if (h) cudaMemset(g_tc_status, 0, sizeof(int));
+    return h;
 }

@@ -17,6 +17,7 @@
 // block staged in shared memory with 8 lanes per vector.
 
 #include "common.cuh"
+#include "prof.h"
 
 namespace slt {
 
@@ -128,7 +129,9 @@ static int launch_trsm(int64_t kb, int64_t nvec, const T* Tm, int64_t ldt, T* B,
     if (smem > 48 * 1024)
         SLT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     unsigned grid = unsigned(ceildiv(nvec, kTrsmCols));
-    fn<<<grid, 256, smem, stream>>>(int(kb), nvec, Tm, ldt, B, ldb);
+    const int pidx = prof_begin(SLT_PROF_TRSM, stream);
+    fn<<<grid, 256, smem, stream>>>(int(kb), nvec, Tm, ldt, B, ldb); slt::count_launch();
+    prof_end(pidx, stream, double(kb) * double(kb) * double(nvec), sizeof(T) * (double(kb) * kb / 2 + 2.0 * kb * nvec));
     return slt_from_cuda(cudaGetLastError());
 }
 
@@ -187,7 +190,9 @@ static int launch_potrf_small(int64_t kb, T* A, int64_t lda, int* info, int64_t 
     auto fn = potrf_small_kernel<T>;
     if (smem > 48 * 1024)
         SLT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    fn<<<1, 256, smem, stream>>>(int(kb), A, lda, info, info_offset);
+    const int pidx = prof_begin(SLT_PROF_POTRF, stream);
+    fn<<<1, 256, smem, stream>>>(int(kb), A, lda, info, info_offset); slt::count_launch();
+    prof_end(pidx, stream, double(kb) * kb * kb / 3.0, sizeof(T) * double(kb) * kb);
     return slt_from_cuda(cudaGetLastError());
 }
 

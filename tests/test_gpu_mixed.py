@@ -55,3 +55,36 @@ def test_mixed_singular(orc, slt):
     B = orc.generate(2, 4, n, 1)
     info, it, X, _ = _run(slt, "gesv_mixed", A, B, slt.Options(nb=64, use_fallback=False))
     assert it == -3 and info == 11
+
+
+@pytest.mark.parametrize("prec", ["tf32", "bf16", "fp16"])
+@pytest.mark.parametrize("fn", ["gesv_mixed", "posv_mixed", "gesv_mixed_gmres"])
+def test_tensor_core_tiers(orc, slt, fn, prec):
+    """Low-precision tensor-core factorisations refined to FP64 accuracy."""
+    chol = fn.startswith("posv")
+    n, nb = 1536, 512
+    A = spd(orc, n, 41) if chol else orc.generate(2, 42, n, n)
+    nrhs = 1 if "gmres" in fn else 2
+    B = orc.generate(2, 43, n, nrhs)
+    info, it, X, Aout = _run(slt, fn, A, B, slt.Options(nb=nb, factor_precision=prec))
+    assert info == 0
+    if prec == "bf16" and not chol:
+        # uniform random LU: kappa * u_bf16 > 1, refinement may stall; SLATE's
+        # contract is then iter = -(itermax+1) and an FP64 fallback solution
+        assert it >= 0 or it == -31
+    else:
+        assert it >= 0
+    assert berr(orc, A, X, B, sym=chol) <= 3 * n * EPS
+    if it >= 0:
+        assert np.array_equal(Aout, A)
+
+
+@pytest.mark.parametrize("fn", ["gesv_mixed", "gesv_mixed_gmres"])
+def test_bf16_lu_converges_when_well_conditioned(orc, slt, fn):
+    n, nb = 1024, 256
+    A = orc.generate(2, 44, n, n) + np.eye(n) * (n / 8.0)
+    A = np.asfortranarray(A)
+    B = orc.generate(2, 45, n, 1)
+    info, it, X, Aout = _run(slt, fn, A, B, slt.Options(nb=nb, factor_precision="bf16"))
+    assert info == 0 and it >= 0
+    assert berr(orc, A, X, B) <= 3 * n * EPS
