@@ -109,6 +109,21 @@ int slt_dsposv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, co
                             int64_t ldb, double* dX, int64_t ldx, const slt_options* opts,
                             slt_stream_t stream, int* iter, int64_t* info);
 
+/* FP64 residual R = B - A X (A n x n general, or symmetric with lower
+ * storage when sym_lower != 0), as the kernel layer's slt_dresidual
+ * computes it, but with no device allocation and no caller scratch, for
+ * callers that cannot allocate where they need it: inside a stream capture,
+ * under an allocator that forbids side allocations, or in a latency-bound
+ * loop that cannot pay cudaMalloc's device synchronisation.  Its partial sums
+ * live in one 16 MiB library-owned __device__ array per device, so
+ * n * min(nrhs, 16) may not exceed 2,097,152 (else SLT_ERR_LIMIT, nothing
+ * launched).  Calls that overlap on the GPU share that array and race; the
+ * first call on a device looks up the array's address and should come before
+ * any stream capture.  No counterpart in SLATE. */
+int slt_dresidual_noalloc(int64_t n, int64_t nrhs, const double* dA, int64_t lda, int sym_lower,
+                          const double* dB, int64_t ldb, const double* dX, int64_t ldx,
+                          double* dR, int64_t ldr, slt_stream_t stream);
+
 /* Philox test-matrix generator, same values as slate::random::generate
  * (matgen/random.cc:197-230) for the uniform distributions. */
 int slt_dgenerate_device(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,

@@ -570,3 +570,42 @@ extern "C" int slt_dtranspose(int64_t m, int64_t n, const double* A, int64_t lda
     transpose_kernel<<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
+
+// ---------------------------------------------------------------------------
+// Residual into caller-provided partial-sum scratch (ws_doubles doubles): the
+// column-segment count is lowered until the partial sums fit.  Used by the
+// allocation-free entry point; returns SLT_ERR_LIMIT when a single segment
+// (n x min(nrhs, 16) doubles) does not fit.
+namespace slt {
+int dresidual_into(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower, const double* B,
+                   int64_t ldb, const double* X, int64_t ldx, double* R, int64_t ldr, double* ws,
+                   size_t ws_doubles, cudaStream_t stream)
+{
+    if (n < 0 || nrhs < 0) return SLT_ERR_ARG;
+    if (n == 0 || nrhs == 0) return SLT_OK;
+    const int64_t chunk = std::min<int64_t>(nrhs, kMaxRhs);
+    if (size_t(n) * size_t(chunk) > ws_doubles) return SLT_ERR_LIMIT;
+    SLT_CUDA_TRY(cudaMemcpy2DAsync(R, size_t(ldr) * sizeof(double), B, size_t(ldb) * sizeof(double),
+                                   size_t(n) * sizeof(double), size_t(nrhs), cudaMemcpyDeviceToDevice, stream));
+    for (int64_t c0 = 0; c0 < nrhs; c0 += kMaxRhs) {
+        const int64_t nc = std::min<int64_t>(kMaxRhs, nrhs - c0);
+        int64_t nseg, tps;
+        plan_segments(n, n, &nseg, &tps);
+        const int64_t ktiles = ceildiv(n, 64);
+        const int64_t fit = int64_t(ws_doubles / (size_t(n) * size_t(nc)));
+        if (nseg > fit) {
+            tps = ceildiv(ktiles, fit);
+            nseg = ceildiv(ktiles, tps);
+        }
+        dim3 grid(unsigned(ceildiv(n, 64)), unsigned(nseg));
+        int rc = sym_lower ? launch_rowop<0, true>(grid, stream, n, n, int(nc), A, lda, X + c0 * ldx, ldx, tps, ws)
+                           : launch_rowop<0, false>(grid, stream, n, n, int(nc), A, lda, X + c0 * ldx, ldx, tps, ws);
+        if (rc) return rc;
+        dim3 g2(unsigned(ceildiv(n, 256)), unsigned(nc));
+        reduce_segments_kernel<<<g2, 256, 0, stream>>>(n, int(nc), nseg, ws, -1.0, 1.0, R + c0 * ldr, ldr);
+        slt::count_launch();
+        SLT_CUDA_TRY(cudaGetLastError());
+    }
+    return SLT_OK;
+}
+} // namespace slt
