@@ -260,6 +260,18 @@ def generate(dist, seed, A, ioff=0, joff=0):
                                       _dev(A), _ld(A), _stream()))
 
 
+def generate_sigma(A, cond, dist="geo", spd=False, seed=1):
+    """Prescribed-spectrum test matrix on the device: A = Q1 diag(sigma) Q2^T,
+    or Q diag(sigma) Q^T when spd, with SLATE's "geo" / "logrand" sigma of
+    condition number cond (matgen/generate_sigma.hh:73-125)."""
+    f = lib().slt_dgenerate_sigma
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
+                  ctypes.c_int64, ctypes.c_void_p]
+    _check(f(A.shape[0], float(cond), {"geo": 0, "logrand": 1}[dist], int(bool(spd)), int(seed), _dev(A), _ld(A),
+             _stream()))
+
+
 def ipiv_to_lapack(ipiv, nb):
     """Per-panel pivots -> LAPACK 1-based ipiv (lapack_api/lapack_gesv.cc:90-100)."""
     p = np.asarray(ipiv.cpu() if hasattr(ipiv, "cpu") else ipiv, dtype=np.int64)

@@ -143,6 +143,12 @@ int slt_dresidual(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym
 /* Philox matrix generator identical to SLATE's slate::random::generate. */
 int slt_dgenerate(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
                   double* A, int64_t lda, cudaStream_t stream);
+/* Test matrix with prescribed singular values (spd = 0: Q1 diag(sigma) Q2^T)
+ * or eigenvalues (spd = 1: Q diag(sigma) Q^T), sigma from SLATE's "geo"
+ * (dist 0) or "logrand" (dist 1) distribution with condition number cond;
+ * Q from log2(n) random butterfly levels (see matgen.cu). */
+int slt_dgenerate_sigma(int64_t n, double cond, int dist, int spd, int64_t seed, double* A, int64_t lda,
+                        cudaStream_t stream);
 /* A(i,i) += alpha for i < n */
 int slt_dshift_diag(int64_t n, double alpha, double* A, int64_t lda, cudaStream_t stream);
 /* Symmetrise from the lower triangle: A(j,i) = A(i,j) for i > j. */

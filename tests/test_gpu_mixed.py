@@ -88,3 +88,51 @@ def test_bf16_lu_converges_when_well_conditioned(orc, slt, fn):
     info, it, X, Aout = _run(slt, fn, A, B, slt.Options(nb=nb, factor_precision="bf16"))
     assert info == 0 and it >= 0
     assert berr(orc, A, X, B) <= 3 * n * EPS
+
+
+def _butterfly_reference(n, cond, dist, spd, seed):
+    """numpy restatement of the device generator (matgen.cu) for small n."""
+    import oracle as O
+    def unit_pair(i, level, key):
+        a, b = O.philox(i, level, key)
+        return (a >> 11) / float(1 << 53), b & 1
+    if dist == "geo":
+        s = cond ** (-np.arange(n) / (n - 1))
+    else:
+        s = np.array([np.exp(unit_pair(i, 0, seed)[0] * np.log(1.0 / cond)) for i in range(n)])
+        s[0], s[1] = 1.0, 1.0 / cond
+    A = np.diag(s)
+    levels = int(np.ceil(np.log2(n)))
+    for l in range(levels):
+        h = 1 << l
+        for side, key in (("rows", seed + 101), ("cols", seed + 101 if spd else seed + 202)):
+            for blk in range(0, n, 2 * h):
+                for i in range(blk, min(blk + h, n - h)):
+                    k = i + h
+                    u, bit = unit_pair(i, l, key)
+                    th = 2 * np.pi * u
+                    c, sn, si = np.cos(th), np.sin(th), (-1.0 if bit else 1.0)
+                    if side == "rows":
+                        x, y = si * A[i, :].copy(), A[k, :].copy()
+                        A[i, :], A[k, :] = c * x + sn * y, -sn * x + c * y
+                    else:
+                        x, y = si * A[:, i].copy(), A[:, k].copy()
+                        A[:, i], A[:, k] = c * x + sn * y, -sn * x + c * y
+    return A, s
+
+
+@pytest.mark.parametrize("dist,spd", [("geo", False), ("logrand", True)])
+def test_generate_sigma_matches_restatement(orc, slt, dist, spd):
+    import torch
+    n, cond = 100, 1e4
+    dA = slt.colmajor(torch.zeros(n, n, dtype=torch.float64, device="cuda"))
+    slt.generate_sigma(dA, cond, dist, spd, seed=7)
+    torch.cuda.synchronize()
+    A = to_host(dA)
+    R, s = _butterfly_reference(n, cond, dist, spd, 7)
+    assert np.abs(A - R).max() <= 1e-12
+    sv = np.linalg.svd(A, compute_uv=False)
+    np.testing.assert_allclose(np.sort(sv), np.sort(s), rtol=1e-10)
+    if spd:
+        np.testing.assert_allclose(A, A.T, atol=1e-14)
+        assert np.linalg.eigvalsh(A).min() > 0
