@@ -14,6 +14,22 @@ time; the plain FP64 posv on the same system is timed beside it.
 oracle; SLATE itself cannot be built here) on the host cores.  Under
 torchrun (N > 1) every rank solves its own replica ("replicas only": one
 factorisation does not shard); value = total solves x flops / max time.
+
+--config 1|3|4 measures SLATE's other solve configurations instead and prints
+one JSON record per case (not the headline line):
+  1  plain FP64 gesv, n=4096 nb=256, 1 RHS, A and b U(-1,1); pivots and
+     backward error against the oracle, the oracle's gesv timed beside it;
+  3  gesv_mixed, n=32768 nb=512, 1 RHS, A = U diag(s) V^T with s geometric
+     from 1 to 1/kappa, kappa in {1e2, 1e4, 1e6}, FP32/BF16/FP16 factors,
+     b = A x_true; plain FP64 gesv timed on the same system;
+  4  posv_mixed_gmres, n=65536 nb=512, 16 RHS, A = Q diag(s) Q^T with s
+     log-uniform in [1/kappa, 1], kappa in {1e2, 1e5, 1e8}, FP16/BF16
+     factors; plain FP64 posv timed on the same system;
+  5  20000 independent systems, n log-uniform in [32, 1024], 1-8 RHS, half
+     general (U(-1,1), LU) and half SPD (G G^T/n + I, Cholesky): the batched
+     FP64 solve and the batched FP32-factor + FP64-refinement solve (one
+     launch each plus the refinement graph) against a loop of per-system
+     gesv / posv calls.
 """
 import argparse
 import json
@@ -47,6 +63,11 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
+    p.add_argument("--batch", type=int, default=20000, help="config 5: number of systems")
+    p.add_argument("--kappas", default=None, help="comma list (configs 3, 4)")
+    p.add_argument("--precs", default=None, help="comma list (configs 3, 4)")
+    p.add_argument("--refine", default="ir+gmres", help="configs 3: ir | ir+gmres")
     return p.parse_args()
 
 
@@ -203,12 +224,238 @@ def cpu_baseline_sample(args):
                       % (n, args.nb, args.nrhs, dt, "scipy-openblas" if blas else "built-in")}
 
 
+def gesv_flops(n, nrhs):
+    return 2.0 * n**3 / 3.0 - n**2 / 2.0 + 5.0 * n / 6.0 + 2.0 * n**2 * nrhs
+
+
+def _event_time(torch, fn):
+    """Seconds of fn() between CUDA events on the current stream."""
+    st = torch.cuda.current_stream()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(st)
+    r = fn()
+    b.record(st)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3, r
+
+
+def _rel_fwd(torch, X, Xt):
+    return float((X - Xt).abs().max() / Xt.abs().max())
+
+
+def run_config1(args, slt, torch, dev):
+    """Plain FP64 gesv n=4096 nb=256 (SLATE's HostTask tester configuration)."""
+    n, nb, nrhs = 4096, 256, 1
+    A0 = slt.colmajor(torch.empty(n, n, dtype=torch.float64, device=dev))
+    B0 = slt.colmajor(torch.empty(n, nrhs, dtype=torch.float64, device=dev))
+    slt.generate(2, 1, A0)
+    slt.generate(2, 2, B0)
+    A = slt.colmajor(A0.clone())
+    B = slt.colmajor(B0.clone())
+    opts = slt.Options(nb=nb, ib=32)
+    times = []
+    for i in range(args.warmup + args.steps):
+        A.copy_(A0)
+        B.copy_(B0)
+        t, (info, ipiv) = _event_time(torch, lambda: slt.gesv(A, B, opts))
+        if i >= args.warmup:
+            times.append(t)
+    t = statistics.median(times)
+    berr = backward_error(torch, A0, B, B0)
+    rec = {"config": 1, "workload": "gesv n=4096 nb=256 nrhs=1, A, b Philox U(-1,1) seeds 1, 2",
+           "dtype": "f64", "steps": args.steps, "warmup": args.warmup, "ms": t * 1e3,
+           "tflops": gesv_flops(n, nrhs) / t / 1e12, "getrf_ms": slt.timer("gesv::getrf") * 1e3,
+           "info": info, "backward_error": berr, "bound_3eps": 3 * np.finfo(np.float64).eps}
+    if not args.no_cpu:
+        os.environ["OPENBLAS_NUM_THREADS"] = "1"
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        cores = os.cpu_count() or 1
+        oracle.set_threads(cores)
+        oracle.use_host_blas()
+        Ah = oracle.generate(2, 1, n, n)
+        Bh = oracle.generate(2, 2, n, nrhs)
+        t0 = time.perf_counter()
+        oinfo, pt, po = oracle.gesv(Ah, Bh, nb)
+        tc = time.perf_counter() - t0
+        k = np.arange(n) // nb
+        oip = (k + pt) * nb + po + 1                      # LAPACK ipiv of the oracle's pivots
+        gip = np.asarray(slt.ipiv_to_lapack(ipiv, nb)).astype(np.int64)
+        rec["cpu_baseline"] = {"ms": tc * 1e3, "tflops": gesv_flops(n, nrhs) / tc / 1e12, "cores": cores,
+                               "kind": "port", "sample": "oracle gesv, same n and inputs"}
+        rec["pivot_mismatches_vs_oracle"] = int(np.count_nonzero(oip != gip))
+        rec["solution_max_diff_vs_oracle"] = float(np.abs(Bh[:, 0] - B.cpu().numpy()[:, 0]).max())
+    print(json.dumps(rec))
+
+
+def run_mixed_sweep(args, slt, torch, dev, cfg):
+    """Configs 3 (gesv_mixed) and 4 (posv_mixed_gmres): kappa x precision."""
+    chol = cfg == 4
+    n = args.n if args.n != 16384 else (65536 if chol else 32768)
+    nb, nrhs = 512, (16 if chol else 1)
+    kappas = [float(k) for k in (args.kappas or ("1e2,1e5,1e8" if chol else "1e2,1e4,1e6")).split(",")]
+    precs = (args.precs or ("fp16,bf16" if chol else "fp32,bf16,fp16")).split(",")
+    fn = slt.posv_mixed_gmres if chol else slt.gesv_mixed
+    flops = posv_flops(n, nrhs) if chol else gesv_flops(n, nrhs)
+    A0 = slt.colmajor(torch.empty(n, n, dtype=torch.float64, device=dev))
+    A = slt.colmajor(torch.empty(n, n, dtype=torch.float64, device=dev))
+    Xt = slt.colmajor(torch.empty(n, nrhs, dtype=torch.float64, device=dev))
+    slt.generate(2, 5, Xt)
+    X = slt.colmajor(torch.zeros(n, nrhs, dtype=torch.float64, device=dev))
+    plain_t = None
+    for kappa in kappas:
+        slt.generate_sigma(A0, kappa, "logrand" if chol else "geo", chol, seed=3)
+        B = slt.colmajor(A0 @ Xt)         # b = A x_true (cuBLAS FP64, a cross-check product)
+        for prec in precs:
+            opts = slt.Options(nb=nb, ib=32, factor_precision=prec, refine=args.refine)
+            # A is restored before every run: an FP64 fallback overwrites it with its factors
+            for _ in range(max(1, min(args.warmup, 1))):
+                A.copy_(A0)
+                X.zero_()
+                fn(A, B, X, opts)
+            A.copy_(A0)
+            X.zero_()
+            t, (info, it, _) = _event_time(torch, lambda: fn(A, B, X, opts))
+            rec = {"config": cfg, "routine": "posv_mixed_gmres" if chol else "gesv_mixed", "n": n, "nb": nb,
+                   "nrhs": nrhs, "kappa": kappa, "factor_precision": prec,
+                   "refine": "gmres" if chol else args.refine, "ms": t * 1e3, "iter": it, "info": info,
+                   "effective_tflops": flops / t / 1e12,
+                   "factor_ms": slt.timer(("posv_mixed_gmres::potrf_lo" if chol else "gesv_mixed::getrf_lo")) * 1e3,
+                   "backward_error": backward_error(torch, A0, X, B), "forward_error": _rel_fwd(torch, X, Xt),
+                   "bound_3n_eps": 3 * n * np.finfo(np.float64).eps}
+            print(json.dumps(rec), flush=True)
+        if plain_t is None and not args.no_plain:
+            A2 = A
+            A2.copy_(A0)
+            X2 = slt.colmajor(B.clone())
+            if chol:
+                t, info = _event_time(torch, lambda: slt.posv(A2, X2, slt.Options(nb=nb, ib=32)))
+                fkey = "posv::potrf"
+            else:
+                t, (info, _) = _event_time(torch, lambda: slt.gesv(A2, X2, slt.Options(nb=nb, ib=32)))
+                fkey = "gesv::getrf"
+            fact = slt.timer(fkey)
+            fflops = (n**3 / 3.0) if chol else (2.0 * n**3 / 3.0)
+            plain_t = t
+            print(json.dumps({"config": cfg, "routine": "posv" if chol else "gesv", "n": n, "nb": nb,
+                              "nrhs": nrhs, "kappa": kappa, "factor_precision": "fp64", "ms": t * 1e3,
+                              "info": info, "tflops": flops / t / 1e12, "factor_ms": fact * 1e3,
+                              "factor_tflops": fflops / fact / 1e12,
+                              "backward_error": backward_error(torch, A0, X2, B),
+                              "forward_error": _rel_fwd(torch, X2, Xt)}), flush=True)
+            del X2
+        del B
+
+
+def run_config5(args, slt, torch, dev):
+    """Variable-size batch: batched FP64, batched mixed, per-system loop."""
+    rng = np.random.default_rng(12345)
+    cnt = args.batch
+    ns = np.exp(rng.uniform(np.log(32), np.log(1024), cnt)).astype(np.int64)
+    rs = rng.integers(1, 9, cnt)
+    kinds = (np.arange(cnt) % 2).astype(np.int64)        # even: general, odd: SPD
+    offA = np.concatenate([[0], np.cumsum(ns * ns)])
+    offB = np.concatenate([[0], np.cumsum(ns * rs)])
+    A0 = torch.empty(int(offA[-1]), dtype=torch.float64, device=dev)
+    B0 = torch.empty(int(offB[-1]), dtype=torch.float64, device=dev)
+    for i in range(cnt):
+        n, r = int(ns[i]), int(rs[i])
+        a = A0[offA[i]:offA[i + 1]].view(n, n).t()
+        if kinds[i] == 0:
+            slt.generate(2, 10 * i + 1, slt.colmajor(a))
+        else:
+            g = slt.colmajor(torch.empty(n, n, dtype=torch.float64, device=dev))
+            slt.generate(3, 10 * i + 1, g)
+            a.copy_((g @ g.t()) / n + torch.eye(n, dtype=torch.float64, device=dev))
+        slt.generate(2, 10 * i + 2, slt.colmajor(B0[offB[i]:offB[i + 1]].view(r, n).t()))
+    A = A0.clone()
+    B = B0.clone()
+    X = torch.zeros_like(B0)
+
+    def views(Abuf, Bbuf):
+        return [(int(kinds[i]), Abuf[offA[i]:offA[i + 1]].view(int(ns[i]), int(ns[i])).t(),
+                 Bbuf[offB[i]:offB[i + 1]].view(int(rs[i]), int(ns[i])).t()) for i in range(cnt)]
+
+    sysv = views(A, B)
+    Xv = [X[offB[i]:offB[i + 1]].view(int(rs[i]), int(ns[i])).t() for i in range(cnt)]
+    vb = slt.VBatch(sysv, X=Xv)
+    flops = float(np.sum(np.where(kinds == 0, 2.0 * ns**3 / 3, ns**3 / 3.0) + 2.0 * ns * ns * rs))
+
+    def berr_max(Xbuf):
+        worst = 0.0
+        for i in range(0, cnt, max(1, cnt // 2000)):      # every system up to 2000, else a stride sample
+            k, a, b = int(kinds[i]), A0[offA[i]:offA[i + 1]].view(int(ns[i]), int(ns[i])).t(), \
+                B0[offB[i]:offB[i + 1]].view(int(rs[i]), int(ns[i])).t()
+            x = Xbuf[offB[i]:offB[i + 1]].view(int(rs[i]), int(ns[i])).t()
+            if k == 1:
+                a = torch.tril(a) + torch.tril(a, -1).t()
+            rr = b - a @ x
+            e = float(rr.abs().sum(0).max() / (a.shape[0] * a.abs().sum(0).max() * x.abs().sum(0).max()))
+            worst = max(worst, e)
+        return worst
+
+    rec = {"config": 5, "workload": "%d systems, n log-uniform [32,1024], 1-8 RHS, half LU half SPD" % cnt,
+           "flops": flops, "fp64_gb": 8.0 * float(offA[-1]) / 1e9}
+    # batched FP64 (A, B restored outside the timing)
+    ts = []
+    for it in range(2):
+        A.copy_(A0)
+        B.copy_(B0)
+        t, info = _event_time(torch, lambda: slt.solve_vbatched(vb))
+        ts.append(t)
+    rec["batched_fp64_ms"] = ts[-1] * 1e3
+    rec["batched_fp64_tflops"] = flops / ts[-1] / 1e12
+    rec["batched_fp64_info_nonzero"] = int((info != 0).sum())
+    rec["batched_fp64_berr_max"] = berr_max(B)
+    # batched mixed
+    A.copy_(A0)
+    B.copy_(B0)
+    ts = []
+    for it in range(2):
+        X.zero_()
+        t, (info, iters) = _event_time(torch, lambda: slt.solve_mixed_vbatched(vb, slt.Options()))
+        ts.append(t)
+    rec["batched_mixed_ms"] = ts[-1] * 1e3
+    rec["batched_mixed_effective_tflops"] = flops / ts[-1] / 1e12
+    rec["batched_mixed_iter_hist"] = {str(int(v)): int(c) for v, c in zip(*np.unique(iters, return_counts=True))}
+    rec["batched_mixed_berr_max"] = berr_max(X)
+    # per-system loop of the library's own gesv / posv (FP64), A, B restored first
+    A.copy_(A0)
+    B.copy_(B0)
+    torch.cuda.synchronize()
+    o = slt.Options(nb=256, ib=32)
+    t0 = time.perf_counter()
+    for k, a, b in sysv:
+        if k == 0:
+            slt.gesv(a, b, o)
+        else:
+            slt.posv(a, b, o)
+    torch.cuda.synchronize()
+    tl = time.perf_counter() - t0
+    rec["loop_fp64_ms"] = tl * 1e3
+    rec["loop_fp64_berr_max"] = berr_max(B)
+    rec["speedup_batched_fp64_vs_loop"] = tl / (rec["batched_fp64_ms"] / 1e3)
+    rec["speedup_batched_mixed_vs_loop"] = tl / (rec["batched_mixed_ms"] / 1e3)
+    print(json.dumps(rec))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     import torch
     import slate_gb300 as slt
+    if args.config != 2:
+        torch.cuda.set_device(0)
+        dev = torch.device("cuda", 0)
+        if args.config == 1:
+            return run_config1(args, slt, torch, dev)
+        if args.config == 5:
+            return run_config5(args, slt, torch, dev)
+        return run_mixed_sweep(args, slt, torch, dev, args.config)
     ws, rank, local = dist_env()
     if ws > 1:
         import torch.distributed as dist

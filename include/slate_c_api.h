@@ -1,0 +1,118 @@
+/* slate_c_api.h -- SLATE's C API (opaque matrices, pivots and options) for
+ * the single-GPU LU / Cholesky solve path, served by libslate_gb300.so.
+ *
+ * Names and argument meaning follow SLATE's generated C API
+ * (tools/c_api/generate_matrix.py, src/c_api/wrappers.cc:692-1080,
+ * include/slate/c_api/types.h), for real single and double precision:
+ *   slate_Options_create / _destroy / _copy / _set_<Option> / _get_<Option>
+ *   slate_Pivots_create / _destroy
+ *   slate_Matrix_create_fromScaLAPACK_{r32,r64} / slate_Matrix_destroy_*
+ *   slate_HermitianMatrix_create_fromScaLAPACK_r64 / _destroy_r64
+ *   slate_lu_solve_*, slate_lu_factor_*, slate_lu_solve_using_factor_*
+ *   slate_chol_solve_r64, slate_chol_factor_r64, slate_chol_solve_using_factor_r64
+ *
+ * Differences a caller sees:
+ *  - the process grid must be 1 x 1 (p = q = 1) and mb = nb; the MPI
+ *    communicator argument is accepted and ignored (no MPI is needed);
+ *  - the wrapped memory may be host or device memory (any pointer the CUDA
+ *    runtime can address); host data are staged to the GPU for each call;
+ *  - SLATE's C wrappers return void and report errors by C++ exceptions; here
+ *    the calls return void as well and the outcome of the last call on the
+ *    calling thread is read with slate_gb300_last_info() (SLATE's info) and
+ *    slate_gb300_last_status() (0, or an slt status code).
+ */
+#ifndef SLATE_GB300_C_API_H
+#define SLATE_GB300_C_API_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef intptr_t slate_mpi_comm_t;   /* MPI_Comm placeholder, ignored */
+
+typedef char slate_Uplo;             /* 'U', 'L' (include/slate/c_api/types.h) */
+typedef char slate_Target;           /* 'H', 'T', 'N', 'B', 'D' */
+typedef char slate_MethodLU;         /* '*', 'P' supported; 'C', 'N', 'R', 'B' rejected */
+
+typedef void* slate_Options;
+typedef struct slate_Pivots_struct* slate_Pivots;
+typedef struct slate_Matrix_struct_r64* slate_Matrix_r64;
+typedef struct slate_Matrix_struct_r32* slate_Matrix_r32;
+typedef struct slate_HermitianMatrix_struct_r64* slate_HermitianMatrix_r64;
+
+slate_Options slate_Options_create(void);
+void slate_Options_destroy(slate_Options opts);
+void slate_Options_copy(slate_Options opts1, slate_Options opts2);   /* opts1 = opts2 */
+
+void    slate_Options_set_ChunkSize(slate_Options opts, int64_t value);
+int64_t slate_Options_get_ChunkSize(slate_Options opts, int64_t defval);
+void    slate_Options_set_Lookahead(slate_Options opts, int64_t value);
+int64_t slate_Options_get_Lookahead(slate_Options opts, int64_t defval);
+void    slate_Options_set_BlockSize(slate_Options opts, int64_t value);
+int64_t slate_Options_get_BlockSize(slate_Options opts, int64_t defval);
+void    slate_Options_set_InnerBlocking(slate_Options opts, int64_t value);
+int64_t slate_Options_get_InnerBlocking(slate_Options opts, int64_t defval);
+void    slate_Options_set_MaxPanelThreads(slate_Options opts, int64_t value);
+int64_t slate_Options_get_MaxPanelThreads(slate_Options opts, int64_t defval);
+void    slate_Options_set_Tolerance(slate_Options opts, double value);
+double  slate_Options_get_Tolerance(slate_Options opts, double defval);
+void    slate_Options_set_Target(slate_Options opts, slate_Target value);
+slate_Target slate_Options_get_Target(slate_Options opts, slate_Target defval);
+void    slate_Options_set_HoldLocalWorkspace(slate_Options opts, bool value);
+bool    slate_Options_get_HoldLocalWorkspace(slate_Options opts, bool defval);
+void    slate_Options_set_Depth(slate_Options opts, int64_t value);
+int64_t slate_Options_get_Depth(slate_Options opts, int64_t defval);
+void    slate_Options_set_MaxIterations(slate_Options opts, int64_t value);
+int64_t slate_Options_get_MaxIterations(slate_Options opts, int64_t defval);
+void    slate_Options_set_UseFallbackSolver(slate_Options opts, bool value);
+bool    slate_Options_get_UseFallbackSolver(slate_Options opts, bool defval);
+void    slate_Options_set_PivotThreshold(slate_Options opts, double value);
+double  slate_Options_get_PivotThreshold(slate_Options opts, double defval);
+void    slate_Options_set_MethodLU(slate_Options opts, slate_MethodLU value);
+slate_MethodLU slate_Options_get_MethodLU(slate_Options opts, slate_MethodLU defval);
+
+slate_Pivots slate_Pivots_create(void);
+void slate_Pivots_destroy(slate_Pivots pivots);
+
+slate_Matrix_r64 slate_Matrix_create_fromScaLAPACK_r64(int64_t m, int64_t n, double* A, int64_t lda, int64_t mb,
+                                                       int64_t nb, int p, int q, slate_mpi_comm_t mpi_comm);
+slate_Matrix_r32 slate_Matrix_create_fromScaLAPACK_r32(int64_t m, int64_t n, float* A, int64_t lda, int64_t mb,
+                                                       int64_t nb, int p, int q, slate_mpi_comm_t mpi_comm);
+void slate_Matrix_destroy_r64(slate_Matrix_r64 A);
+void slate_Matrix_destroy_r32(slate_Matrix_r32 A);
+int64_t slate_Matrix_m_r64(slate_Matrix_r64 A);
+int64_t slate_Matrix_n_r64(slate_Matrix_r64 A);
+
+slate_HermitianMatrix_r64 slate_HermitianMatrix_create_fromScaLAPACK_r64(slate_Uplo uplo, int64_t n, double* A,
+                                                                         int64_t lda, int64_t nb, int p, int q,
+                                                                         slate_mpi_comm_t mpi_comm);
+void slate_HermitianMatrix_destroy_r64(slate_HermitianMatrix_r64 A);
+
+/* slate::lu_solve = gesv, lu_factor = getrf, lu_solve_using_factor = getrs */
+void slate_lu_solve_r64(slate_Matrix_r64 A, slate_Matrix_r64 B, slate_Options opts);
+void slate_lu_factor_r64(slate_Matrix_r64 A, slate_Pivots pivots, slate_Options opts);
+void slate_lu_solve_using_factor_r64(slate_Matrix_r64 A, slate_Pivots pivots, slate_Matrix_r64 B,
+                                     slate_Options opts);
+void slate_lu_solve_r32(slate_Matrix_r32 A, slate_Matrix_r32 B, slate_Options opts);
+void slate_lu_factor_r32(slate_Matrix_r32 A, slate_Pivots pivots, slate_Options opts);
+void slate_lu_solve_using_factor_r32(slate_Matrix_r32 A, slate_Pivots pivots, slate_Matrix_r32 B,
+                                     slate_Options opts);
+
+/* slate::chol_solve = posv, chol_factor = potrf, chol_solve_using_factor = potrs */
+void slate_chol_solve_r64(slate_HermitianMatrix_r64 A, slate_Matrix_r64 B, slate_Options opts);
+void slate_chol_factor_r64(slate_HermitianMatrix_r64 A, slate_Options opts);
+void slate_chol_solve_using_factor_r64(slate_HermitianMatrix_r64 A, slate_Matrix_r64 B, slate_Options opts);
+
+/* Outcome of the last C-API call on this thread (no counterpart in SLATE,
+ * whose C wrappers throw). */
+int64_t slate_gb300_last_info(void);
+int slate_gb300_last_status(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -49,7 +49,23 @@ typedef struct slt_options {
     double  pivot_threshold;  /* Option::PivotThreshold, default 1 (partial piv.) */
     int     factor_precision; /* slt_precision of mixed solvers, default FP32     */
     int     gemm_engine;      /* FP64 update engine: 0 auto, 1 SIMT, 2 DMMA       */
+    int     refine;           /* mixed solvers: slt_refine, default SLT_REFINE_IR */
+    int     equilibrate;      /* mixed solvers: -1 auto (on for BF16/FP16), 0, 1  */
+    int     lo_retry;         /* 16-bit factor failed or did not converge: retry
+                                 with an FP32 factor before the FP64 fallback;
+                                 -1 auto (on for BF16/FP16), 0, 1               */
 } slt_options;
+
+/* Refinement of the mixed solvers.  SLT_REFINE_IR is SLATE's gesv_mixed loop
+ * (src/gesv_mixed.cc:210-262); SLT_REFINE_IR_GMRES runs that loop while the
+ * residual falls by at least half per step and, once it stalls, continues
+ * each unconverged column with FGMRES-IR preconditioned by the same
+ * low-precision factors (the gesv_mixed_gmres iteration) before any FP64
+ * fallback.  The gmres entry points always run FGMRES-IR. */
+enum slt_refine {
+    SLT_REFINE_IR = 0,
+    SLT_REFINE_IR_GMRES = 2
+};
 
 void slt_options_default(slt_options* opts);
 
@@ -123,6 +139,33 @@ int slt_dsposv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, co
 int slt_dresidual_noalloc(int64_t n, int64_t nrhs, const double* dA, int64_t lda, int sym_lower,
                           const double* dB, int64_t ldb, const double* dX, int64_t ldx,
                           double* dR, int64_t ldr, slt_stream_t stream);
+
+/* ------------------------------------------------------------------------- */
+/* Variable-size batched solves.  No counterpart in SLATE, which has no      */
+/* batched routine; each system follows slate::gesv (kind 0: LU with partial */
+/* pivoting, lowest row index on ties) or slate::posv (kind 1: SPD, lower    */
+/* Cholesky).  Every argument array is a DEVICE array of `batch` entries:    */
+/* kind, n (0..2048), nrhs, the column-major matrices A[i] (lda[i] >= n[i]),  */
+/* pivots ipiv[i] (LU only, n[i] ints, LAPACK 1-based), right-hand sides     */
+/* B[i] (ldb[i]).  The call copies the size and pointer arrays to the host   */
+/* once, orders the systems largest first and runs one persistent launch.    */
+
+/* FP64: A[i] <- factors, B[i] <- X[i]; info[i] as slate::gesv / posv. */
+int slt_dsolve_vbatched(int64_t batch, const int* d_kind, const int* d_n, const int* d_nrhs,
+                        double* const* d_A, const int* d_lda, int* const* d_ipiv,
+                        double* const* d_B, const int* d_ldb, int* d_info, slt_stream_t stream);
+
+/* Mixed: FP32 factors (one launch), FP64 refinement with slate::gesv_mixed's
+ * stopping test replayed itermax + 1 times from a CUDA graph, FP64 fallback
+ * for the systems that do not converge (their A[i] then holds FP64 factors;
+ * A[i] and B[i] are untouched otherwise).  X[i] (ldx[i]) receives the
+ * solution, iter[i] / info[i] follow slate::gesv_mixed (0..itermax, -3,
+ * -(itermax+1)).  nrhs[i] <= 8; tolerance <= 0 means eps * sqrt(n[i]). */
+int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const int* d_n, const int* d_nrhs,
+                              double* const* d_A, const int* d_lda, int* const* d_ipiv,
+                              double* const* d_B, const int* d_ldb, double* const* d_X,
+                              const int* d_ldx, int* d_iter, int* d_info, int64_t itermax,
+                              double tolerance, int use_fallback, slt_stream_t stream);
 
 /* Philox test-matrix generator, same values as slate::random::generate
  * (matgen/random.cc:197-230) for the uniform distributions. */

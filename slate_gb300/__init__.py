@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(_HERE, "libslate_gb300.so")
 
 PREC_FP64, PREC_FP32, PREC_TF32, PREC_BF16, PREC_FP16 = 0, 1, 2, 3, 4
 _PREC_NAMES = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "fp16": 4}
+_REFINE_NAMES = {"ir": 0, "ir+gmres": 2}
 
 
 class SlateError(RuntimeError):
@@ -32,7 +33,8 @@ class _Options(ctypes.Structure):
     _fields_ = [("nb", ctypes.c_int64), ("ib", ctypes.c_int64), ("lookahead", ctypes.c_int64),
                 ("max_iterations", ctypes.c_int64), ("tolerance", ctypes.c_double),
                 ("use_fallback", ctypes.c_int), ("pivot_threshold", ctypes.c_double),
-                ("factor_precision", ctypes.c_int), ("gemm_engine", ctypes.c_int)]
+                ("factor_precision", ctypes.c_int), ("gemm_engine", ctypes.c_int),
+                ("refine", ctypes.c_int), ("equilibrate", ctypes.c_int), ("lo_retry", ctypes.c_int)]
 
 
 @dataclass
@@ -47,13 +49,18 @@ class Options:
     pivot_threshold: float = 1.0
     factor_precision: object = "fp32"
     gemm_engine: int = 0
+    refine: object = "ir"          # "ir" (SLATE) or "ir+gmres" (GMRES-IR once IR stalls)
+    equilibrate: int = -1          # -1 auto (on for bf16/fp16), 0 off, 1 on
+    lo_retry: int = -1             # -1 auto (on for bf16/fp16): FP32 retry before the FP64 fallback
 
     def _c(self):
         p = self.factor_precision
         p = _PREC_NAMES[p] if isinstance(p, str) else int(p)
         return _Options(int(self.nb), int(self.ib), int(self.lookahead), int(self.max_iterations),
                         float(self.tolerance), int(bool(self.use_fallback)),
-                        float(self.pivot_threshold), p, int(self.gemm_engine))
+                        float(self.pivot_threshold), p, int(self.gemm_engine),
+                        _REFINE_NAMES[self.refine] if isinstance(self.refine, str) else int(self.refine),
+                        int(self.equilibrate), int(self.lo_retry))
 
 
 _lib = None
@@ -270,6 +277,64 @@ def generate_sigma(A, cond, dist="geo", spd=False, seed=1):
                   ctypes.c_int64, ctypes.c_void_p]
     _check(f(A.shape[0], float(cond), {"geo": 0, "logrand": 1}[dist], int(bool(spd)), int(seed), _dev(A), _ld(A),
              _stream()))
+
+
+class VBatch:
+    """Device descriptor arrays of a variable-size batch.
+
+    systems: list of (kind, A, B) with kind 0 (general, LU) or 1 (SPD,
+    Cholesky, lower triangle used), A an n x n and B an n x nrhs
+    column-major float64 CUDA tensor (see colmajor).  X: optional list of
+    solution tensors shaped like B (mixed solver).  The pointer arrays refer
+    to the caller's tensors, which must outlive the call."""
+
+    def __init__(self, systems, X=None):
+        import torch
+        dev = systems[0][1].device if systems else torch.device("cuda")
+        i32 = dict(dtype=torch.int32, device=dev)
+        i64 = dict(dtype=torch.int64, device=dev)
+        self.batch = len(systems)
+        self.kind = torch.tensor([k for k, _, _ in systems], **i32)
+        self.n = torch.tensor([a.shape[0] for _, a, _ in systems], **i32)
+        self.nrhs = torch.tensor([b.shape[1] for _, _, b in systems], **i32)
+        self.lda = torch.tensor([_ld(a) for _, a, _ in systems], **i32)
+        self.ldb = torch.tensor([_ld(b) for _, _, b in systems], **i32)
+        self.A = torch.tensor([a.data_ptr() for _, a, _ in systems], **i64)
+        self.B = torch.tensor([b.data_ptr() for _, _, b in systems], **i64)
+        self.ipiv_t = [torch.zeros(max(1, a.shape[0]), **i32) if k == 0 else None for k, a, _ in systems]
+        self.ipiv = torch.tensor([p.data_ptr() if p is not None else 0 for p in self.ipiv_t], **i64)
+        self.info = torch.zeros(self.batch, **i32)
+        self.iter = torch.zeros(self.batch, **i32)
+        if X is not None:
+            self.X = torch.tensor([x.data_ptr() for x in X], **i64)
+            self.ldx = torch.tensor([_ld(x) for x in X], **i32)
+
+
+def solve_vbatched(vb):
+    """FP64 variable-size batched gesv/posv: A <- factors, B <- X.
+    Returns the info array (CPU numpy)."""
+    f = lib().slt_dsolve_vbatched
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int64] + [ctypes.c_void_p] * 9 + [ctypes.c_void_p]
+    _check(f(vb.batch, vb.kind.data_ptr(), vb.n.data_ptr(), vb.nrhs.data_ptr(), vb.A.data_ptr(),
+             vb.lda.data_ptr(), vb.ipiv.data_ptr(), vb.B.data_ptr(), vb.ldb.data_ptr(), vb.info.data_ptr(),
+             _stream()))
+    return vb.info.cpu().numpy()
+
+
+def solve_mixed_vbatched(vb, opts=None):
+    """Mixed variable-size batched solve (FP32 factors + FP64 refinement).
+    Returns (info, iter) as CPU numpy arrays."""
+    o = opts or Options()
+    f = lib().slt_dsolve_mixed_vbatched
+    f.restype = ctypes.c_int
+    f.argtypes = ([ctypes.c_int64] + [ctypes.c_void_p] * 12 + [ctypes.c_int64, ctypes.c_double, ctypes.c_int,
+                                                               ctypes.c_void_p])
+    _check(f(vb.batch, vb.kind.data_ptr(), vb.n.data_ptr(), vb.nrhs.data_ptr(), vb.A.data_ptr(),
+             vb.lda.data_ptr(), vb.ipiv.data_ptr(), vb.B.data_ptr(), vb.ldb.data_ptr(), vb.X.data_ptr(),
+             vb.ldx.data_ptr(), vb.iter.data_ptr(), vb.info.data_ptr(), int(o.max_iterations),
+             float(o.tolerance), int(bool(o.use_fallback)), _stream()))
+    return vb.info.cpu().numpy(), vb.iter.cpu().numpy()
 
 
 def ipiv_to_lapack(ipiv, nb):

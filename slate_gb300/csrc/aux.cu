@@ -244,16 +244,6 @@ sskinny_n_kernel(int64_t m, int64_t kk, int nrhs, float alpha, const float* __re
         }
 }
 
-template <typename S, typename D>
-__global__ void convert_kernel(int64_t m, int64_t n, const S* __restrict__ A, int64_t lda,
-                               D* __restrict__ B, int64_t ldb)
-{
-    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    int64_t j = blockIdx.y;
-    for (; j < n; j += gridDim.y)
-        if (i < m) B[i + j * ldb] = D(A[i + j * lda]);
-}
-
 __global__ void geadd_kernel(int64_t m, int64_t n, double alpha, const double* __restrict__ A, int64_t lda,
                              double beta, double* B, int64_t ldb)
 {
@@ -327,10 +317,21 @@ __global__ void generate_kernel(int dist, int64_t seed, int64_t m, int64_t n, in
     }
 }
 
-__global__ void shift_diag_kernel(int64_t n, double alpha, double* A, int64_t lda)
+template <typename T>
+__global__ void shift_diag_kernel(int64_t n, T alpha, T* A, int64_t lda)
 {
     int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n) A[i + i * lda] += alpha;
+}
+
+// D = S on one triangle (lower: i >= j, upper: i <= j), the rest of D untouched.
+__global__ void copy_tri_kernel(int lower, int64_t n, const double* __restrict__ S, int64_t lds, double* D,
+                                int64_t ldd)
+{
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int64_t j = blockIdx.y; j < n; j += gridDim.y)
+        if (lower ? (i >= j) : (i <= j)) D[i + j * ldd] = S[i + j * lds];
 }
 
 __global__ void symmetrize_lower_kernel(int64_t n, double* A, int64_t lda)
@@ -454,19 +455,13 @@ extern "C" int slt_sgemm_skinny(int64_t m, int64_t nrhs, int64_t k, float alpha,
 extern "C" int slt_convert_d2s(int64_t m, int64_t n, const double* A, int64_t lda, float* B, int64_t ldb,
                                cudaStream_t stream)
 {
-    if (m <= 0 || n <= 0) return SLT_OK;
-    dim3 grid(unsigned(ceildiv(m, 256)), unsigned(std::min<int64_t>(n, 65535)));
-    convert_kernel<double, float><<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb); slt::count_launch();
-    return slt_from_cuda(cudaGetLastError());
+    return slt_convert_d2s_scaled(m, n, A, lda, nullptr, nullptr, B, ldb, stream);
 }
 
 extern "C" int slt_convert_s2d(int64_t m, int64_t n, const float* A, int64_t lda, double* B, int64_t ldb,
                                cudaStream_t stream)
 {
-    if (m <= 0 || n <= 0) return SLT_OK;
-    dim3 grid(unsigned(ceildiv(m, 256)), unsigned(std::min<int64_t>(n, 65535)));
-    convert_kernel<float, double><<<grid, 256, 0, stream>>>(m, n, A, lda, B, ldb); slt::count_launch();
-    return slt_from_cuda(cudaGetLastError());
+    return slt_convert_s2d_scaled(m, n, A, lda, nullptr, B, ldb, stream);
 }
 
 extern "C" int slt_dcopy2d(int64_t m, int64_t n, const double* A, int64_t lda, double* B, int64_t ldb,
@@ -507,7 +502,23 @@ extern "C" int slt_dgenerate(int dist, int64_t seed, int64_t m, int64_t n, int64
 extern "C" int slt_dshift_diag(int64_t n, double alpha, double* A, int64_t lda, cudaStream_t stream)
 {
     if (n <= 0) return SLT_OK;
-    shift_diag_kernel<<<unsigned(ceildiv(n, 256)), 256, 0, stream>>>(n, alpha, A, lda); slt::count_launch();
+    shift_diag_kernel<double><<<unsigned(ceildiv(n, 256)), 256, 0, stream>>>(n, alpha, A, lda); slt::count_launch();
+    return slt_from_cuda(cudaGetLastError());
+}
+
+extern "C" int slt_sshift_diag(int64_t n, float alpha, float* A, int64_t lda, cudaStream_t stream)
+{
+    if (n <= 0) return SLT_OK;
+    shift_diag_kernel<float><<<unsigned(ceildiv(n, 256)), 256, 0, stream>>>(n, alpha, A, lda); slt::count_launch();
+    return slt_from_cuda(cudaGetLastError());
+}
+
+extern "C" int slt_dcopy_tri(int lower, int64_t n, const double* S, int64_t lds, double* D, int64_t ldd,
+                             cudaStream_t stream)
+{
+    if (n <= 0) return SLT_OK;
+    dim3 grid(unsigned(ceildiv(n, 256)), unsigned(std::min<int64_t>(n, 65535)));
+    copy_tri_kernel<<<grid, 256, 0, stream>>>(lower, n, S, lds, D, ldd); slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 

@@ -151,6 +151,9 @@ void slt_options_default(slt_options* o)
     o->pivot_threshold = 1.0;
     o->factor_precision = SLT_PREC_FP32;
     o->gemm_engine = 0;
+    o->refine = SLT_REFINE_IR;
+    o->equilibrate = -1;
+    o->lo_retry = -1;
 }
 
 const char* slt_status_string(int st)

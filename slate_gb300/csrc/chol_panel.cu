@@ -22,6 +22,62 @@ namespace slt {
 
 constexpr int kCpThreads = 256;
 constexpr int kCpIB = 64;
+constexpr int kCpSub = 16;
+
+// One warp: Cholesky of the bw x bw (bw <= 16) lower block S (row-major,
+// row stride lds) in registers, lane r holding row r; the factor is written
+// back to S and its inverse to Inv (16 x 17, Inv[k * 17 + c] = L^{-1}(k, c),
+// zero above the diagonal and outside bw).  Returns 0, or the 1-based column
+// of the first non-positive pivot.
+template <typename T>
+__device__ int factor_invert_16(T* S, int lds, int bw, T* Inv)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int r = threadIdx.x & 31;
+    T a[kCpSub];
+    #pragma unroll
+    for (int c = 0; c < kCpSub; ++c) a[c] = (r < bw && c <= r) ? S[r * lds + c] : T(0);
+    int fail = 0;
+    #pragma unroll
+    for (int j = 0; j < kCpSub; ++j) {
+        if (j < bw && !fail) {
+            const T d = __shfl_sync(FULL, a[j], j);
+            if (!(d > T(0))) {
+                fail = j + 1;
+            }
+            else {
+                const T sd = sqrt(d);
+                if (r == j) a[j] = sd;
+                else if (r > j) a[j] = a[j] / sd;
+                #pragma unroll
+                for (int c = j + 1; c < kCpSub; ++c) {
+                    const T lcj = __shfl_sync(FULL, a[j], c);
+                    if (r >= c) a[c] = fma(-a[j], lcj, a[c]);
+                }
+            }
+        }
+    }
+    if (fail) return fail;
+    // lane c: column c of L^{-1} by forward substitution
+    const int c = r;
+    T x[kCpSub];
+    #pragma unroll
+    for (int k = 0; k < kCpSub; ++k) {
+        T acc = (k == c) ? T(1) : T(0);
+        #pragma unroll
+        for (int p = 0; p < k; ++p) acc = fma(-__shfl_sync(FULL, a[p], k), x[p], acc);
+        const T lkk = __shfl_sync(FULL, a[k], k);
+        x[k] = (k < bw && c < bw && k >= c) ? acc / lkk : T(0);
+    }
+    if (r < kCpSub) {
+        #pragma unroll
+        for (int k = 0; k < kCpSub; ++k) Inv[k * (kCpSub + 1) + r] = x[k];
+        #pragma unroll
+        for (int cc = 0; cc < kCpSub; ++cc)
+            if (r < bw && cc <= r) S[r * lds + cc] = a[cc];
+    }
+    return 0;
+}
 
 template <typename T>
 struct CholPanelArgs {
@@ -40,6 +96,7 @@ chol_panel_kernel(CholPanelArgs<T> a)
     T* D = reinterpret_cast<T*>(cp_smem_raw);             // [64][65] factor, D[i*65 + l] = L(i,l)
     T* Xs = D + kCpIB * (kCpIB + 1);                        // [64][68] solved rows staging
     T* Us = Xs + kCpIB * 68;                                // [64][68] update operand
+    T* Dinv = Us + kCpIB * 68;                              // [4][16][17] sub-block inverses
     __shared__ int s_fail;
     const int G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
     const int64_t ld = a.ld;
@@ -49,40 +106,66 @@ chol_panel_kernel(CholPanelArgs<T> a)
 
     for (int64_t c0 = 0; c0 < a.nbk; c0 += kCpIB) {
         const int kb = int(min64(kCpIB, a.nbk - c0));
-        // ---- 1. factor the diagonal block in shared memory (every block)
+        // ---- 1. factor the diagonal block in shared memory (every block), in
+        //      16-column steps: warp 0 factors the 16 x 16 diagonal sub-block in
+        //      registers and inverts it, then all threads solve the sub-block
+        //      rows below it and update the rest of the 64 x 64 block.
         for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
             int i = e % kCpIB, l = e / kCpIB;
             D[i * (kCpIB + 1) + l] = (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
         }
         if (t == 0) s_fail = 0;
         __syncthreads();
-        for (int j = 0; j < kb; ++j) {
-            const T d = D[j * (kCpIB + 1) + j];
-            if (!(d > T(0))) {
-                if (t == 0 && !s_fail) {
+        for (int jb = 0, jbi = 0; jb < kb; jb += kCpSub, ++jbi) {
+            const int bw = min(kCpSub, kb - jb);
+            if (t < 32) {
+                const int fail = factor_invert_16(D + jb * (kCpIB + 1) + jb, kCpIB + 1, bw,
+                                                  Dinv + jbi * kCpSub * (kCpSub + 1));
+                if (t == 0 && fail) {
                     s_fail = 1;
-                    if (c0 >= rb && c0 < re) atomicCAS(a.info, 0, int(a.info_offset + c0 + j + 1));
+                    if (c0 >= rb && c0 < re) atomicCAS(a.info, 0, int(a.info_offset + c0 + jb + fail));
                 }
-                break;
             }
-            const T sd = sqrt(d);
-            for (int i = j + 1 + t; i < kb; i += kCpThreads) D[i * (kCpIB + 1) + j] /= sd;
             __syncthreads();
-            if (t == 0) D[j * (kCpIB + 1) + j] = sd;
-            {
-                // rows i = j+1+(t&63), columns l = j+1+(t>>6), +4, ... up to i
-                const int i = j + 1 + (t & 63);
-                if (i < kb) {
-                    const T dij = D[i * (kCpIB + 1) + j];
-                    for (int l = j + 1 + (t >> 6); l <= i; l += 4)
-                        D[i * (kCpIB + 1) + l] -= dij * D[l * (kCpIB + 1) + j];
+            if (s_fail) break;
+            // rows i in [jb + bw, kb) of the sub-block column: X = B L_sub^{-T}
+            const int below = kb - jb - bw;
+            const T* Di = Dinv + jbi * kCpSub * (kCpSub + 1);
+            T xv[3];
+            #pragma unroll
+            for (int u = 0; u < 3; ++u) {
+                const int e = t + u * kCpThreads;
+                xv[u] = T(0);
+                if (e < below * bw) {
+                    const int i = jb + bw + e / bw, c = e % bw;
+                    T acc = T(0);
+                    for (int p = 0; p <= c; ++p) acc = fma(D[i * (kCpIB + 1) + jb + p], Di[c * (kCpSub + 1) + p], acc);
+                    xv[u] = acc;
                 }
+            }
+            __syncthreads();
+            #pragma unroll
+            for (int u = 0; u < 3; ++u) {
+                const int e = t + u * kCpThreads;
+                if (e < below * bw) D[(jb + bw + e / bw) * (kCpIB + 1) + jb + e % bw] = xv[u];
+            }
+            __syncthreads();
+            // trailing update inside the block: D[i][c] -= sum_p D[i][jb+p] D[c][jb+p], jb+bw <= c <= i < kb
+            for (int e = t; e < below * below; e += kCpThreads) {
+                const int i = jb + bw + e % below, c = jb + bw + e / below;
+                if (c > i) continue;
+                T acc = T(0);
+                for (int p = 0; p < bw; ++p)
+                    acc = fma(D[i * (kCpIB + 1) + jb + p], D[c * (kCpIB + 1) + jb + p], acc);
+                D[i * (kCpIB + 1) + c] -= acc;
             }
             __syncthreads();
         }
         __syncthreads();
         const bool failed = s_fail != 0;
-        // ---- 2. solve the owned rows below the block: X L^T = B, 64 rows at a time
+        // ---- 2. solve the owned rows below the block: X L^T = B, 64 rows at a
+        //      time, 4 lanes per row; per 16-column sub-block subtract the
+        //      solved sub-blocks, then multiply by the sub-block inverse.
         if (!failed) {
             const int64_t r0 = max64(rb, c0 + kb);
             for (int64_t rr = r0; rr < re; rr += kCpIB) {
@@ -93,14 +176,31 @@ chol_panel_kernel(CholPanelArgs<T> a)
                     Xs[i * (kCpIB + 1) + l] = (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
                 }
                 __syncthreads();
-                // 4 lanes per row, 64 rows: forward substitution over the kb columns
-                const int row = t >> 2, q = t & 3;
-                for (int j = 0; j < kb; ++j) {
-                    T part = T(0);
-                    for (int l = q; l < j; l += 4) part = fma(Xs[row * (kCpIB + 1) + l], D[j * (kCpIB + 1) + l], part);
-                    part += __shfl_xor_sync(0xffffffffu, part, 2);
-                    part += __shfl_xor_sync(0xffffffffu, part, 1);
-                    if (q == 0) Xs[row * (kCpIB + 1) + j] = (Xs[row * (kCpIB + 1) + j] - part) / D[j * (kCpIB + 1) + j];
+                const int row = t >> 2, q = t & 3, lane = t & 31;
+                T* xr = Xs + row * (kCpIB + 1);
+                for (int jb = 0, jbi = 0; jb < kb; jb += kCpSub, ++jbi) {
+                    const int bw = min(kCpSub, kb - jb);
+                    const T* Di = Dinv + jbi * kCpSub * (kCpSub + 1);
+                    T y[4];
+                    #pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int c = q + 4 * u;
+                        T acc = (c < bw) ? xr[jb + c] : T(0);
+                        if (c < bw)
+                            for (int p = 0; p < jb; ++p) acc = fma(-xr[p], D[(jb + c) * (kCpIB + 1) + p], acc);
+                        y[u] = acc;
+                    }
+                    T out[4] = {T(0), T(0), T(0), T(0)};
+                    #pragma unroll
+                    for (int p = 0; p < kCpSub; ++p) {
+                        const T zp = __shfl_sync(0xffffffffu, y[p / 4], (lane & ~3) | (p & 3));
+                        #pragma unroll
+                        for (int u = 0; u < 4; ++u) out[u] = fma(zp, Di[(q + 4 * u) * (kCpSub + 1) + p], out[u]);
+                    }
+                    __syncwarp();
+                    #pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (q + 4 * u < bw) xr[jb + q + 4 * u] = out[u];
                     __syncwarp();
                 }
                 __syncthreads();
@@ -193,7 +293,8 @@ static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) return SLT_ERR_NOT_SUPPORTED;
-    const size_t smem = (size_t(kCpIB) * (kCpIB + 1) + size_t(2) * kCpIB * 68) * sizeof(T);
+    const size_t smem = (size_t(kCpIB) * (kCpIB + 1) + size_t(2) * kCpIB * 68 +
+                         size_t(kCpIB / kCpSub) * kCpSub * (kCpSub + 1)) * sizeof(T);
     static bool cfg = false;
     if (!cfg) {
         SLT_CUDA_TRY(cudaFuncSetAttribute(chol_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));

@@ -47,7 +47,6 @@ double timer_value(const char* name)
 
 void timers_clear() { t_timers.clear(); }
 
-#define TRY(expr) do { int rc_ = (expr); if (rc_ != SLT_OK) return rc_; } while (0)
 
 // ---------------------------------------------------------------------------
 // Type dispatch onto the kernel layer.
@@ -268,6 +267,19 @@ template int potrs_dev<float>(int64_t, int64_t, const float*, int64_t, int64_t, 
 // Mixed precision.
 namespace {
 
+// Equilibration is on by default only for the 16-bit tiers, whose operand
+// range or mantissa a badly scaled matrix can exceed; FP32 and TF32 keep
+// SLATE's unscaled cast (src/gesv_mixed.cc:196-199).
+bool equilibrate_on(const slt_options& o)
+{
+    if (o.equilibrate >= 0) return o.equilibrate != 0;
+    return o.factor_precision == SLT_PREC_BF16 || o.factor_precision == SLT_PREC_FP16;
+}
+
+// The low-precision factorisation the mixed solvers refine with: FP32
+// storage of A_s = diag(r) A diag(c) (r = c = 1 without equilibration), the
+// O(n^3) update in the tier's arithmetic.  solve() applies
+// A^{-1} = diag(c) A_s^{-1} diag(r).
 struct LoFactor {
     int chol;
     int64_t n, nb;
@@ -277,22 +289,58 @@ struct LoFactor {
     int* ipiv;
     int64_t ld = 0;
     int* status = nullptr;
+    DevBuf scales;     // r (n), c (n), row-maximum words (n)
+    const double* r = nullptr;
+    const double* c = nullptr;
+    double sigma = 0.0;  // diagonal shift of a 16-bit Cholesky factor (0: none)
 
     int factor(const double* Ahi, int64_t lda, FactorCtx& fc, int64_t* info, cudaStream_t s) {
         ld = ((n + 31) / 32) * 32;
         TRY(A.alloc(sizeof(float) * size_t(ld) * size_t(n), s));
-        TRY(slt_convert_d2s(n, n, Ahi, lda, A.as<float>(), ld, s));
+        if (equilibrate_on(o)) {
+            TRY(scales.alloc(sizeof(double) * 3 * size_t(n), s));
+            double* rr = scales.as<double>();
+            if (chol) {
+                TRY(slt_dpoequ(n, Ahi, lda, rr, s));
+                r = c = rr;
+            }
+            else {
+                TRY(slt_dgeequ(n, n, Ahi, lda, rr, rr + n, rr + 2 * n, s));
+                r = rr;
+                c = rr + n;
+            }
+        }
         status = fc.d_status;
-        if (chol) TRY(potrf_dev<float>(n, A.as<float>(), ld, o, fc, s));
-        else TRY(getrf_dev<float>(n, n, A.as<float>(), ld, ipiv, o, fc, s));
-        return finish_factor(fc, info, s);
+        if (!chol) {
+            TRY(slt_convert_d2s_scaled(n, n, Ahi, lda, r, c, A.as<float>(), ld, s));
+            TRY(getrf_dev<float>(n, n, A.as<float>(), ld, ipiv, o, fc, s));
+            return finish_factor(fc, info, s);
+        }
+        // Cholesky in a 16-bit tier: a matrix with lambda_min below the
+        // tier's rounding error breaks down in low precision although it is
+        // SPD in FP64.  Factor A_s + sigma I instead, sigma = c u_tier with
+        // c = 1, 8, 64 (A_s has diagonal in [0.25, 1) after equilibration),
+        // and let the FP64 refinement correct for the shift.
+        const bool shift = o.factor_precision == SLT_PREC_BF16 || o.factor_precision == SLT_PREC_FP16;
+        const double u = o.factor_precision == SLT_PREC_BF16 ? 0x1p-8 : 0x1p-11;
+        for (int attempt = 0;; ++attempt) {
+            TRY(slt_convert_d2s_scaled(n, n, Ahi, lda, r, c, A.as<float>(), ld, s));
+            if (attempt > 0) {
+                sigma = u * double(int64_t(1) << (3 * (attempt - 1)));
+                TRY(slt_sshift_diag(n, float(sigma), A.as<float>(), ld, s));
+                SLT_CUDA_TRY(cudaMemsetAsync(fc.d_info, 0, sizeof(int), s));
+            }
+            TRY(potrf_dev<float>(n, A.as<float>(), ld, o, fc, s));
+            TRY(finish_factor(fc, info, s));
+            if (*info == 0 || !shift || attempt == 3) return SLT_OK;
+        }
     }
-    // X (double) <- M^{-1} R (double), through FP32.
+    // X (double) <- A^{-1} R (double), through FP32.  R and X may alias.
     int solve(int64_t nrhs, const double* R, int64_t ldr, double* X, int64_t ldx, float* wlo, cudaStream_t s) {
-        TRY(slt_convert_d2s(n, nrhs, R, ldr, wlo, n, s));
+        TRY(slt_convert_d2s_scaled(n, nrhs, R, ldr, r, nullptr, wlo, n, s));
         if (chol) TRY(potrs_dev<float>(n, nrhs, A.as<float>(), ld, nb, wlo, n, status, s));
         else TRY(getrs_dev<float>(n, nrhs, A.as<float>(), ld, ipiv, nb, wlo, n, status, s));
-        return slt_convert_s2d(n, nrhs, wlo, n, X, ldx, s);
+        return slt_convert_s2d_scaled(n, nrhs, wlo, n, c, X, ldx, s);
     }
 };
 
@@ -309,6 +357,122 @@ bool converged(const double* cr, const double* cx, int64_t k, double cte)
         if (!(cr[i] <= cx[i] * cte)) return false;
     return true;
 }
+
+// Right-preconditioned FGMRES(restart) for one right-hand side
+// (src/gesv_mixed_gmres.cc:225-395): CGS2 Arnoldi in FP64 on the GPU, the
+// preconditioner the low-precision factors, Givens rotations and the small
+// triangular solve on the host.  Starts from the x it is given.
+struct Fgmres {
+    int chol;
+    int64_t n;
+    const double* A;
+    int64_t lda;
+    LoFactor& lo;
+    double cte;
+    int64_t restart = 0, R1 = 1;
+    DevBuf nws, scal, V, W, Wlo;
+
+    Fgmres(int chol_, int64_t n_, const double* A_, int64_t lda_, LoFactor& lo_, double cte_)
+        : chol(chol_), n(n_), A(A_), lda(lda_), lo(lo_), cte(cte_) {}
+
+    int init(int64_t itermax, int64_t nb, cudaStream_t s) {
+        restart = std::max<int64_t>(0, std::min<int64_t>(std::min<int64_t>(30, itermax), std::min(nb, n) - 1));
+        R1 = restart + 1;
+        TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, 1)), s));
+        TRY(scal.alloc(sizeof(double) * (4 + 4 * R1), s));
+        TRY(V.alloc(sizeof(double) * size_t(n) * size_t(R1), s));
+        TRY(W.alloc(sizeof(double) * size_t(n) * size_t(R1), s));
+        return Wlo.alloc(sizeof(float) * size_t(n), s);
+    }
+
+    // Runs until the stopping test holds or itermax Arnoldi steps are spent.
+    // *used: the steps taken; *conv: whether the test held.
+    int run(const double* b, int64_t ldb, double* x, int64_t ldx, int64_t itermax, int* used, bool* conv,
+            cudaStream_t s) {
+        double* Vd = V.as<double>();
+        double* Wd = W.as<double>();
+        float* wlo = Wlo.as<float>();
+        double* dsc = scal.as<double>();
+        double* dh = dsc + 4;
+        double* dz = dh + R1;
+        double* dy = dz + R1;
+        std::vector<double> H(size_t(R1) * size_t(R1)), S(R1), gc(R1), gs(R1), hh(2 * R1);
+        *conv = false;
+        int64_t iiter = 0;
+        int citer = 0;
+        bool stopped = false;
+        while (iiter < itermax) {
+            // residual and stopping test
+            TRY(slt_dresidual(n, 1, A, lda, chol, b, ldb, x, ldx, Vd, n, nws.p, s));
+            TRY(slt_dcolmax(n, 1, x, ldx, dsc, s));
+            TRY(slt_dcolmax(n, 1, Vd, n, dsc + 1, s));
+            TRY(slt_dnrm2(n, Vd, dsc + 2, s));
+            double hv[3];
+            TRY(read_doubles(dsc, hv, 3, s));
+            const double cx = hv[0], cr = hv[1];
+            if (cr <= cx * cte) { citer = int(iiter); *conv = true; stopped = true; break; }
+            double ares = hv[2];
+            if (ares == 0) { citer = int(iiter); stopped = true; break; }
+            TRY(slt_dgeadd(n, 1, 1.0 / ares, Vd, n, 0.0, Vd, n, s));
+            S.assign(R1, 0.0);
+            S[0] = ares;
+            int64_t j = 0;
+            for (; j < restart && iiter < itermax && !(ares <= cx * cte); ++j, ++iiter) {
+                double* vj1 = Vd + (j + 1) * n;
+                double* wj1 = Wd + (j + 1) * n;
+                TRY(lo.solve(1, Vd + j * n, n, wj1, n, wlo, s));
+                TRY(slt_dgemm_skinny(n, 1, n, 1.0, A, lda, chol, wj1, n, 0.0, vj1, n, nws.p, s));
+                // CGS2
+                TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dh, R1, s));
+                TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dh, R1, 1.0, vj1, n, nws.p, s));
+                TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dz, R1, s));
+                TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dz, R1, 1.0, vj1, n, nws.p, s));
+                TRY(slt_dnrm2(n, vj1, dsc + 3, s));
+                TRY(read_doubles(dh, hh.data(), 2 * R1, s));
+                double nrm = 0;
+                TRY(read_doubles(dsc + 3, &nrm, 1, s));
+                TRY(slt_dgeadd(n, 1, 1.0 / nrm, vj1, n, 0.0, vj1, n, s));
+                double* hj = H.data() + j * R1;
+                for (int64_t i = 0; i <= j; ++i) hj[i] = hh[i] + hh[R1 + i];
+                hj[j + 1] = nrm;
+                auto rot = [](double* xx, double* yy, double cc, double ss) {
+                    double tx = cc * *xx + ss * *yy;
+                    double ty = cc * *yy - ss * *xx;
+                    *xx = tx; *yy = ty;
+                };
+                for (int64_t i = 0; i < j; ++i) rot(&hj[i], &hj[i + 1], gc[i], gs[i]);
+                {
+                    double a = hj[j], bb = hj[j + 1];
+                    double roe = std::fabs(a) > std::fabs(bb) ? a : bb;
+                    double scale = std::fabs(a) + std::fabs(bb);
+                    if (scale == 0) { gc[j] = 1; gs[j] = 0; }
+                    else {
+                        double rr = scale * std::sqrt((a / scale) * (a / scale) + (bb / scale) * (bb / scale));
+                        rr = std::copysign(1.0, roe) * rr;
+                        gc[j] = a / rr; gs[j] = bb / rr;
+                    }
+                }
+                rot(&hj[j], &hj[j + 1], gc[j], gs[j]);
+                rot(&S[j], &S[j + 1], gc[j], gs[j]);
+                ares = std::fabs(S[j + 1]);
+            }
+            // x += W(:, 1:j) H(0:j-1, 0:j-1)^{-1} S(0:j-1)
+            if (j > 0) {
+                std::vector<double> y(S.begin(), S.begin() + j);
+                for (int64_t rr = j - 1; rr >= 0; --rr) {
+                    double sum = y[rr];
+                    for (int64_t cc = rr + 1; cc < j; ++cc) sum -= H[rr + cc * R1] * y[cc];
+                    y[rr] = sum / H[rr + rr * R1];
+                }
+                SLT_CUDA_TRY(cudaMemcpyAsync(dy, y.data(), sizeof(double) * size_t(j), cudaMemcpyHostToDevice, s));
+                TRY(slt_dgemm_skinny(n, 1, j, 1.0, Wd + n, n, 0, dy, R1, 1.0, x, ldx, nws.p, s));
+                SLT_CUDA_TRY(cudaStreamSynchronize(s));
+            }
+        }
+        *used = stopped ? citer : int(iiter);
+        return SLT_OK;
+    }
+};
 
 int fallback_fp64(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
                   const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,
@@ -338,9 +502,14 @@ int fallback_fp64(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int
 } // namespace
 
 // gesv_mixed / posv_mixed (src/gesv_mixed.cc:105-289, src/posv_mixed.cc:105-320).
-int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
-                   const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,
-                   int* iter, int64_t* info, cudaStream_t s)
+// With o.refine == SLT_REFINE_IR_GMRES the IR loop stops early once a
+// column's residual max-norm falls by less than half in one step, and every
+// column still unconverged continues with FGMRES-IR from its current x on the
+// remaining iteration budget; *iter then counts IR steps plus the largest
+// number of Arnoldi steps any column took.
+static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                           const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,
+                           int* iter, int64_t* info, cudaStream_t s)
 {
     if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
     *iter = 0;
@@ -353,6 +522,7 @@ int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, in
     const double tol = o.tolerance > 0 ? o.tolerance : eps * std::sqrt(double(n));
     const int64_t itermax = o.max_iterations;
     const int64_t nb = eff_nb(o);
+    const bool chain = o.refine == SLT_REFINE_IR_GMRES;
 
     DevBuf nws, scal, R, Wlo, st, col;
     TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, std::min<int64_t>(nrhs, 16))), s));
@@ -392,6 +562,8 @@ int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, in
         TRY(slt_dcolmax(n, nrhs, R.as<double>(), n, dcr, s));
         return read_doubles(dcx, h.data(), 2 * nrhs, s);
     };
+    int64_t ir_steps = 0;
+    bool stalled = false;
     if (linfo != 0) {
         *iter = -3;
     }
@@ -401,11 +573,37 @@ int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, in
         tm.stop(std::string(pfx) + (chol ? "::potrs_lo" : "::getrs_lo"));
         TRY(residual());
         if (converged(h.data() + nrhs, h.data(), nrhs, cte)) { *iter = 0; conv = true; }
-        for (int64_t it = 0; it < itermax && !conv; ++it) {
+        std::vector<double> prev(nrhs);
+        for (int64_t it = 0; it < itermax && !conv && !stalled; ++it) {
+            std::copy(h.begin() + nrhs, h.end(), prev.begin());
             TRY(lo.solve(nrhs, R.as<double>(), n, R.as<double>(), n, Wlo.as<float>(), s));
             TRY(slt_dgeadd(n, nrhs, 1.0, R.as<double>(), n, 1.0, X, ldx, s));
             TRY(residual());
+            ir_steps = it + 1;
             if (converged(h.data() + nrhs, h.data(), nrhs, cte)) { *iter = int(it + 1); conv = true; }
+            else if (chain) {
+                for (int64_t c = 0; c < nrhs; ++c)
+                    if (!(h[nrhs + c] <= h[c] * cte) && !(h[nrhs + c] <= 0.5 * prev[c])) stalled = true;
+            }
+        }
+        if (!conv && chain && itermax - ir_steps > 0) {
+            // GMRES-IR on the stalled columns, preconditioned by the same factors
+            tm.start(std::string(pfx) + "::gmres");
+            Fgmres g(chol, n, A, lda, lo, cte);
+            TRY(g.init(itermax - ir_steps, nb, s));
+            std::vector<double> hx(h.begin(), h.begin() + nrhs), hr(h.begin() + nrhs, h.end());
+            bool all = true;
+            int worst = 0;
+            for (int64_t c = 0; c < nrhs; ++c) {
+                if (hr[c] <= hx[c] * cte) continue;
+                int used = 0;
+                bool cc = false;
+                TRY(g.run(B + c * ldb, ldb, X + c * ldx, ldx, itermax - ir_steps, &used, &cc, s));
+                all = all && cc;
+                worst = std::max(worst, used);
+            }
+            tm.stop(std::string(pfx) + "::gmres");
+            if (all) { conv = true; *iter = int(ir_steps + worst); }
         }
     }
     *info = linfo;
@@ -423,9 +621,9 @@ int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, in
 // low-precision factors, CGS2 Arnoldi in FP64, Givens rotations on the
 // host.  Each right-hand side is an independent instance sharing the
 // factorisation.
-int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
-                         const double* B, int64_t ldb, double* X, int64_t ldx,
-                         const slt_options& o, int* iter, int64_t* info, cudaStream_t s)
+static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                                 const double* B, int64_t ldb, double* X, int64_t ldx,
+                                 const slt_options& o, int* iter, int64_t* info, cudaStream_t s)
 {
     if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
     *iter = 0;
@@ -438,28 +636,18 @@ int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t l
     const double tol = o.tolerance > 0 ? o.tolerance : eps * std::sqrt(double(n));
     const int64_t itermax = o.max_iterations;
     const int64_t nb = eff_nb(o);
-    const int64_t restart = std::max<int64_t>(
-        0, std::min<int64_t>(std::min<int64_t>(30, itermax), std::min(nb, n) - 1));
-    const int64_t R1 = restart + 1;
 
-    DevBuf nws, scal, st, V, W, vec, Wlo;
-    TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, 1)), s));
-    TRY(scal.alloc(sizeof(double) * (4 + 4 * R1), s));
+    DevBuf nws, scal, st, Wlo;
+    TRY(nws.alloc(slt_norm_ws_bytes(n), s));
+    TRY(scal.alloc(sizeof(double) * 4, s));
     TRY(st.alloc(2 * sizeof(int), s));
-    TRY(V.alloc(sizeof(double) * size_t(n) * size_t(R1), s));
-    TRY(W.alloc(sizeof(double) * size_t(n) * size_t(R1), s));
-    TRY(vec.alloc(sizeof(double) * size_t(n), s));
-    TRY(Wlo.alloc(sizeof(float) * size_t(n) * size_t(std::max<int64_t>(nrhs, 1)), s));
+    TRY(Wlo.alloc(sizeof(float) * size_t(n), s));
     SLT_CUDA_TRY(cudaMemsetAsync(st.p, 0, 2 * sizeof(int), s));
     FactorCtx fc{st.as<int>(), st.as<int>() + 1};
-    double* dsc = scal.as<double>();
-    double* dh = dsc + 4;
-    double* dz = dh + R1;
-    double* dy = dz + R1;
 
     double Anorm = 0;
-    TRY(slt_dnorm_inf(n, n, A, lda, chol, dsc, nws.p, s));
-    TRY(read_doubles(dsc, &Anorm, 1, s));
+    TRY(slt_dnorm_inf(n, n, A, lda, chol, scal.as<double>(), nws.p, s));
+    TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
     const double cte = Anorm * tol;
 
     LoFactor lo{chol, n, nb, o, {}, ipiv};
@@ -471,92 +659,20 @@ int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t l
     *info = linfo;
     bool all_conv = true;
     int worst_iter = 0;
-    double* Vd = V.as<double>();
-    double* Wd = W.as<double>();
-    float* wlo = Wlo.as<float>();
     if (linfo != 0) {
         *iter = -3;
         all_conv = false;
     }
     else {
-        std::vector<double> H(size_t(R1) * size_t(R1)), S(R1), gc(R1), gs(R1), hh(2 * R1);
+        Fgmres g(chol, n, A, lda, lo, cte);
+        TRY(g.init(itermax, nb, s));
         for (int64_t c = 0; c < nrhs; ++c) {
             const double* b = B + c * ldb;
             double* x = X + c * ldx;
-            bool conv = false;
+            TRY(lo.solve(1, b, ldb, x, ldx, Wlo.as<float>(), s));
             int citer = 0;
-            TRY(lo.solve(1, b, ldb, x, ldx, wlo, s));
-            int64_t iiter = 0;
-            double cx = 0, cr = 0;
-            while (iiter < itermax) {
-                // residual and stopping test
-                TRY(slt_dresidual(n, 1, A, lda, chol, b, ldb, x, ldx, Vd, n, nws.p, s));
-                TRY(slt_dcolmax(n, 1, x, ldx, dsc, s));
-                TRY(slt_dcolmax(n, 1, Vd, n, dsc + 1, s));
-                TRY(slt_dnrm2(n, Vd, dsc + 2, s));
-                double hv[3];
-                TRY(read_doubles(dsc, hv, 3, s));
-                cx = hv[0]; cr = hv[1];
-                if (cr <= cx * cte) { citer = int(iiter); conv = true; break; }
-                double ares = hv[2];
-                if (ares == 0) { citer = int(iiter); conv = false; break; }
-                TRY(slt_dgeadd(n, 1, 1.0 / ares, Vd, n, 0.0, Vd, n, s));
-                S.assign(R1, 0.0);
-                S[0] = ares;
-                int64_t j = 0;
-                for (; j < restart && iiter < itermax && !(ares <= cx * cte); ++j, ++iiter) {
-                    double* vj1 = Vd + (j + 1) * n;
-                    double* wj1 = Wd + (j + 1) * n;
-                    TRY(lo.solve(1, Vd + j * n, n, wj1, n, wlo, s));
-                    TRY(slt_dgemm_skinny(n, 1, n, 1.0, A, lda, chol, wj1, n, 0.0, vj1, n, nws.p, s));
-                    // CGS2
-                    TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dh, R1, s));
-                    TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dh, R1, 1.0, vj1, n, nws.p, s));
-                    TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dz, R1, s));
-                    TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dz, R1, 1.0, vj1, n, nws.p, s));
-                    TRY(slt_dnrm2(n, vj1, dsc + 3, s));
-                    TRY(read_doubles(dh, hh.data(), 2 * R1, s));
-                    double nrm = 0;
-                    TRY(read_doubles(dsc + 3, &nrm, 1, s));
-                    TRY(slt_dgeadd(n, 1, 1.0 / nrm, vj1, n, 0.0, vj1, n, s));
-                    double* hj = H.data() + j * R1;
-                    for (int64_t i = 0; i <= j; ++i) hj[i] = hh[i] + hh[R1 + i];
-                    hj[j + 1] = nrm;
-                    auto rot = [](double* xx, double* yy, double cc, double ss) {
-                        double tx = cc * *xx + ss * *yy;
-                        double ty = cc * *yy - ss * *xx;
-                        *xx = tx; *yy = ty;
-                    };
-                    for (int64_t i = 0; i < j; ++i) rot(&hj[i], &hj[i + 1], gc[i], gs[i]);
-                    {
-                        double a = hj[j], bb = hj[j + 1];
-                        double roe = std::fabs(a) > std::fabs(bb) ? a : bb;
-                        double scale = std::fabs(a) + std::fabs(bb);
-                        if (scale == 0) { gc[j] = 1; gs[j] = 0; }
-                        else {
-                            double r = scale * std::sqrt((a / scale) * (a / scale) + (bb / scale) * (bb / scale));
-                            r = std::copysign(1.0, roe) * r;
-                            gc[j] = a / r; gs[j] = bb / r;
-                        }
-                    }
-                    rot(&hj[j], &hj[j + 1], gc[j], gs[j]);
-                    rot(&S[j], &S[j + 1], gc[j], gs[j]);
-                    ares = std::fabs(S[j + 1]);
-                }
-                // X += W(:, 1:j) H(0:j-1, 0:j-1)^{-1} S(0:j-1)
-                if (j > 0) {
-                    std::vector<double> y(S.begin(), S.begin() + j);
-                    for (int64_t r = j - 1; r >= 0; --r) {
-                        double sum = y[r];
-                        for (int64_t cc = r + 1; cc < j; ++cc) sum -= H[r + cc * R1] * y[cc];
-                        y[r] = sum / H[r + r * R1];
-                    }
-                    SLT_CUDA_TRY(cudaMemcpyAsync(dy, y.data(), sizeof(double) * size_t(j),
-                                                 cudaMemcpyHostToDevice, s));
-                    TRY(slt_dgemm_skinny(n, 1, j, 1.0, Wd + n, n, 0, dy, R1, 1.0, x, ldx, nws.p, s));
-                    SLT_CUDA_TRY(cudaStreamSynchronize(s));
-                }
-            }
+            bool conv = false;
+            TRY(g.run(b, ldb, x, ldx, itermax, &citer, &conv, s));
             if (!conv) { all_conv = false; citer = int(-itermax - 1); }
             worst_iter = (c == 0) ? citer : (citer < 0 || worst_iter < 0 ? std::min(worst_iter, citer)
                                                                         : std::max(worst_iter, citer));
@@ -570,6 +686,55 @@ int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t l
     }
     tm.stop(pfx);
     return finish_factor(fc, nullptr, s);   // bounded-wait status of every launch above
+}
+
+// A 16-bit factorisation that breaks down (info > 0 even after the diagonal
+// shifts) or whose refinement does not converge is retried once with an
+// FP32 factorisation before SLATE's FP64 fallback: the retry costs one FP32
+// factorisation, the FP64 fallback an FP64 one, an order of magnitude more
+// on this part.  A is unchanged between the two attempts (the first runs
+// without the fallback).  o.lo_retry: -1 auto (on for BF16 / FP16), 0, 1.
+static bool ladder_on(const slt_options& o)
+{
+    const bool low = o.factor_precision == SLT_PREC_BF16 || o.factor_precision == SLT_PREC_FP16 ||
+                     o.factor_precision == SLT_PREC_TF32;
+    return low && (o.lo_retry < 0 ? (o.factor_precision != SLT_PREC_TF32) : o.lo_retry != 0);
+}
+
+template <typename F>
+static int with_ladder(F once, const slt_options& o, const char* key, int* iter, int64_t* info)
+{
+    if (!ladder_on(o)) return once(o);
+    slt_options o1 = o;
+    o1.use_fallback = 0;
+    TRY(once(o1));
+    if (*iter >= 0) return SLT_OK;
+    slt_options o2 = o;
+    o2.factor_precision = SLT_PREC_FP32;
+    const int rc = once(o2);
+    t_timers[key] = 1.0;          // marks that the FP32 retry ran
+    (void) info;
+    return rc;
+}
+
+int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                   const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,
+                   int* iter, int64_t* info, cudaStream_t s)
+{
+    t_timers.erase(chol ? "posv_mixed::retry_fp32" : "gesv_mixed::retry_fp32");
+    return with_ladder([&](const slt_options& oo) {
+        return gesv_mixed_once(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, oo, iter, info, s);
+    }, o, chol ? "posv_mixed::retry_fp32" : "gesv_mixed::retry_fp32", iter, info);
+}
+
+int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
+                         const double* B, int64_t ldb, double* X, int64_t ldx,
+                         const slt_options& o, int* iter, int64_t* info, cudaStream_t s)
+{
+    t_timers.erase(chol ? "posv_mixed_gmres::retry_fp32" : "gesv_mixed_gmres::retry_fp32");
+    return with_ladder([&](const slt_options& oo) {
+        return gesv_mixed_gmres_once(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, oo, iter, info, s);
+    }, o, chol ? "posv_mixed_gmres::retry_fp32" : "gesv_mixed_gmres::retry_fp32", iter, info);
 }
 
 } // namespace slt

@@ -31,6 +31,7 @@ namespace slt {
 constexpr int kPanelThreads = 256;
 constexpr int kMaxPanelBlocks = 1024;
 constexpr int kMaxIb = 64;
+constexpr size_t kPanelStagedMax = 96 * 1024;   // dynamic shared memory of the staged panel
 
 template <typename T>
 struct PanelExchange {
@@ -68,6 +69,78 @@ __device__ __forceinline__ void warp_argmax(T& av, T& v, int& row)
         int orow = __shfl_down_sync(0xffffffffu, row, off);
         if (better(oav, orow, av, row)) { av = oav; v = ov; row = orow; }
     }
+}
+
+// End of an ib-wide stripe (all its columns final): the interchanges of the
+// stripe applied to the panel columns outside it, the unit-lower solve of the
+// top block right of the stripe, and the rank-kb update of the owned rows
+// below it.  Returns false when the kernel must stop (bounded wait failed).
+template <typename T>
+__device__ bool stripe_end(const PanelArgs<T>& a, int G, int b, int t, int64_t k0, int kb, int64_t rb,
+                           int64_t re, const int* s_piv, T (*s_L)[kMaxIb + 1], T (*s_U)[32 + 1])
+{
+    const int64_t ld = a.ld;
+    T* P = a.P;
+    if (!grid_sync(a.bar, unsigned(G), a.status)) return false;
+    {
+        const int64_t nout = a.nbk - kb;
+        for (int64_t q = int64_t(b) * kPanelThreads + t; q < nout; q += int64_t(G) * kPanelThreads) {
+            const int64_t cc = (q < k0) ? q : q + kb;
+            T* col = P + cc * ld;
+            for (int jj = 0; jj < kb; ++jj) {
+                int64_t r = k0 + jj, pr = s_piv[jj];
+                if (pr != r) { T tmp = __ldcg(&col[r]); col[r] = __ldcg(&col[pr]); col[pr] = tmp; }
+            }
+            if (cc >= k0 + kb) {
+                for (int r = 1; r < kb; ++r) {
+                    T s = __ldcg(&col[k0 + r]);
+                    for (int l = 0; l < r; ++l) s -= __ldcg(&P[k0 + r + (k0 + l) * ld]) * __ldcg(&col[k0 + l]);
+                    col[k0 + r] = s;
+                }
+            }
+        }
+    }
+    if (k0 + kb < a.nbk) {
+        if (!grid_sync(a.bar, unsigned(G), a.status)) return false;
+        // ---- rank-kb update of owned rows below the stripe
+        const int64_t c0 = k0 + kb;
+        const int64_t r0 = max(rb, k0 + kb);
+        for (int64_t rr = r0; rr < re; rr += 32) {
+            const int nr = int(min64(32, re - rr));
+            __syncthreads();
+            for (int e = t; e < 32 * kb; e += kPanelThreads) {
+                int i = e % 32, l = e / 32;
+                s_L[i][l] = (i < nr) ? __ldcg(&P[rr + i + (k0 + l) * ld]) : T(0);
+            }
+            for (int64_t cb = c0; cb < a.nbk; cb += 32) {
+                const int nc = int(min64(32, a.nbk - cb));
+                __syncthreads();
+                for (int e = t; e < kb * 32; e += kPanelThreads) {
+                    int l = e % kb, c = e / kb;
+                    s_U[l][c] = (c < nc) ? __ldcg(&P[k0 + l + (cb + c) * ld]) : T(0);
+                }
+                __syncthreads();
+                // 32 x 32 outputs, 4 per thread
+                const int i = t % 32;
+                const int cg = t / 32;   // 0..7 -> columns cg, cg+8, cg+16, cg+24
+                if (i < nr) {
+                    #pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        int c = cg + 8 * q;
+                        if (c < nc) {
+                            T s = T(0);
+                            for (int l = 0; l < kb; ++l) s = fma(s_L[i][l], s_U[l][c], s);
+                            T* q2 = &P[rr + i + (cb + c) * ld];
+                            *q2 = __ldcg(q2) - s;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if (!grid_sync(a.bar, unsigned(G), a.status)) return false;
+    }
+    return true;
 }
 
 template <typename T>
@@ -204,67 +277,189 @@ getrf_panel_kernel(PanelArgs<T> a)
             __syncthreads();
         }
 
-        // ---- all stripe columns final: interchanges outside the stripe, and
-        //      the unit-lower solve of the top block right of the stripe
-        if (!grid_sync(a.bar, unsigned(G), a.status)) return;
-        {
-            const int64_t nout = a.nbk - kb;
-            for (int64_t q = int64_t(b) * kPanelThreads + t; q < nout; q += int64_t(G) * kPanelThreads) {
-                const int64_t cc = (q < k0) ? q : q + kb;
-                T* col = P + cc * ld;
-                for (int jj = 0; jj < kb; ++jj) {
-                    int64_t r = k0 + jj, pr = s_piv[jj];
-                    if (pr != r) { T tmp = __ldcg(&col[r]); col[r] = __ldcg(&col[pr]); col[pr] = tmp; }
-                }
-                if (cc >= k0 + kb) {
-                    for (int r = 1; r < kb; ++r) {
-                        T s = __ldcg(&col[k0 + r]);
-                        for (int l = 0; l < r; ++l) s -= __ldcg(&P[k0 + r + (k0 + l) * ld]) * __ldcg(&col[k0 + l]);
-                        col[k0 + r] = s;
-                    }
-                }
-            }
+        if (!stripe_end(a, G, b, t, k0, kb, rb, re, s_piv, s_L, s_U)) return;
+    }
+}
+
+// Staged variant, used when a block's rows of one stripe fit in shared memory
+// (rows_per_block x ib elements).  Same arithmetic and the same choices as
+// getrf_panel_kernel, with two changes on the per-column critical path:
+//  * the block's rows of the current stripe live in shared memory for the
+//    whole stripe (loaded once, written back at its end), so the search, the
+//    scaling and the rank-1 update never wait on L2;
+//  * the per-column grid barrier is replaced by a per-block sequence flag
+//    published (release) with the block's candidate: every block waits
+//    (acquire, bounded) until all flags reach the column's sequence number,
+//    then reads the candidates -- one L2 round trip fewer than a
+//    counter barrier followed by the reads.  Candidates stay double
+//    buffered: a block can run at most one column ahead of the slowest.
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads)
+getrf_panel2_kernel(PanelArgs<T> a, int* flags)
+{
+    constexpr int NW = kPanelThreads / 32;
+    const int G = gridDim.x;
+    const int b = blockIdx.x;
+    const int t = threadIdx.x;
+    const int lane = t & 31, warp = t >> 5;
+    const int64_t ld = a.ld;
+    T* P = a.P;
+    const int64_t rb = int64_t(b) * a.rows_per_block;
+    const int64_t re = min(a.prows, rb + a.rows_per_block);
+    const int nrow = int(max64(0, re - rb));
+    const int RP = int(a.rows_per_block);
+    const int64_t diag_len = min(a.prows, a.nbk);
+    PanelExchange<T>* ex = a.ex;
+
+    extern __shared__ unsigned char p2_smem_raw[];
+    T* S = reinterpret_cast<T*>(p2_smem_raw);          // S[c * RP + r]: owned row rb + r, stripe column c
+    __shared__ T s_av[NW], s_v[NW];
+    __shared__ int s_row[NW];
+    __shared__ int s_piv[kMaxIb];
+    __shared__ T s_u[kMaxIb];
+    __shared__ T s_pval;
+    __shared__ int s_p, s_wb, s_fail;
+    __shared__ T s_L[32][kMaxIb + 1];
+    __shared__ T s_U[kMaxIb][32 + 1];
+    if (t == 0) s_fail = 0;
+    int seq = 0;
+
+    for (int64_t k0 = 0; k0 < diag_len; k0 += a.ib) {
+        const int kb = int(min64(a.ib, diag_len - k0));
+        __syncthreads();
+        for (int e = t; e < nrow * kb; e += kPanelThreads) {
+            const int r = e % nrow, c = e / nrow;
+            S[c * RP + r] = __ldcg(&P[rb + r + (k0 + c) * ld]);
         }
-        if (k0 + kb < a.nbk) {
-            if (!grid_sync(a.bar, unsigned(G), a.status)) return;
-            // ---- rank-kb update of owned rows below the stripe
-            const int64_t c0 = k0 + kb;
-            const int64_t r0 = max(rb, k0 + kb);
-            for (int64_t rr = r0; rr < re; rr += 32) {
-                const int nr = int(min64(32, re - rr));
-                __syncthreads();
-                for (int e = t; e < 32 * kb; e += kPanelThreads) {
-                    int i = e % 32, l = e / 32;
-                    s_L[i][l] = (i < nr) ? __ldcg(&P[rr + i + (k0 + l) * ld]) : T(0);
-                }
-                for (int64_t cb = c0; cb < a.nbk; cb += 32) {
-                    const int nc = int(min64(32, a.nbk - cb));
-                    __syncthreads();
-                    for (int e = t; e < kb * 32; e += kPanelThreads) {
-                        int l = e % kb, c = e / kb;
-                        s_U[l][c] = (c < nc) ? __ldcg(&P[k0 + l + (cb + c) * ld]) : T(0);
-                    }
-                    __syncthreads();
-                    // 32 x 32 outputs, 4 per thread
-                    const int i = t % 32;
-                    const int cg = t / 32;   // 0..7 -> columns cg, cg+8, cg+16, cg+24
-                    if (i < nr) {
-                        #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            int c = cg + 8 * q;
-                            if (c < nc) {
-                                T s = T(0);
-                                for (int l = 0; l < kb; ++l) s = fma(s_L[i][l], s_U[l][c], s);
-                                T* q2 = &P[rr + i + (cb + c) * ld];
-                                *q2 = __ldcg(q2) - s;
-                            }
+        __syncthreads();
+        for (int64_t j = k0; j < k0 + kb; ++j) {
+            ++seq;
+            const int par = seq & 1;
+            const int jc = int(j - k0);
+            // ---- local candidate from shared memory
+            T bav = T(-1), bv = T(0);
+            int brow = INT_MAX;
+            for (int64_t i = max(rb, j) + t; i < re; i += kPanelThreads) {
+                const T v = S[jc * RP + int(i - rb)];
+                const T av = fabs(v);
+                if (better(av, int(i), bav, brow)) { bav = av; bv = v; brow = int(i); }
+            }
+            warp_argmax(bav, bv, brow);
+            if (lane == 0) { s_av[warp] = bav; s_v[warp] = bv; s_row[warp] = brow; }
+            __syncthreads();
+            if (warp == 0) {
+                bav = lane < NW ? s_av[lane] : T(-1);
+                bv = lane < NW ? s_v[lane] : T(0);
+                brow = lane < NW ? s_row[lane] : INT_MAX;
+                warp_argmax(bav, bv, brow);
+                if (lane == 0) { s_av[0] = bav; s_v[0] = bv; s_row[0] = brow; }
+            }
+            __syncthreads();
+            brow = s_row[0];
+            const bool has = brow != INT_MAX && s_av[0] >= T(0);
+            if (t == 0) {
+                ex->cand_val[par][b] = s_v[0];
+                ex->cand_row[par][b] = has ? brow : INT_MAX;
+            }
+            if (has)
+                for (int c = t; c < kb; c += kPanelThreads)
+                    ex->cand_rowvals[par][b][c] = S[c * RP + int(brow - rb)];
+            if (j >= rb && j < re)
+                for (int c = t; c < kb; c += kPanelThreads)
+                    ex->diag_rowvals[par][c] = S[c * RP + int(j - rb)];
+            __threadfence();
+            __syncthreads();
+            if (t == 0) st_release_u32(reinterpret_cast<unsigned*>(&flags[b]), unsigned(seq));
+
+            // ---- wait for every block's candidate, then reduce them (warp 0)
+            if (warp == 0) {
+                bool ok = true;
+                const unsigned long long t0 = globaltimer();
+                for (int q = lane; q < G && ok; q += 32) {
+                    for (unsigned it = 1; ld_acquire_u32(reinterpret_cast<const unsigned*>(&flags[q])) <
+                                          unsigned(seq); ++it) {
+                        if ((it & 63u) == 0 && (ld_volatile_i32(a.status) != 0 || globaltimer() - t0 > kWaitNs)) {
+                            atomicCAS(a.status, 0, SLT_ERR_TIMEOUT);
+                            ok = false;
+                            break;
                         }
                     }
                 }
-                __syncthreads();
+                ok = __all_sync(0xffffffffu, ok);
+                T gav = T(-1), gv = T(0);
+                int grow = INT_MAX, gwb = -1;
+                if (ok) {
+                    for (int q = lane; q < G; q += 32) {
+                        int r = ((volatile int*) ex->cand_row[par])[q];
+                        T v = ((volatile T*) ex->cand_val[par])[q];
+                        T av = (r == INT_MAX) ? T(-1) : fabs(v);
+                        if (r != INT_MAX && better(av, r, gav, grow)) { gav = av; gv = v; grow = r; gwb = q; }
+                    }
+                }
+                #pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    T oav = __shfl_down_sync(0xffffffffu, gav, off);
+                    T ov = __shfl_down_sync(0xffffffffu, gv, off);
+                    int orow = __shfl_down_sync(0xffffffffu, grow, off);
+                    int owb = __shfl_down_sync(0xffffffffu, gwb, off);
+                    if (better(oav, orow, gav, grow)) { gav = oav; gv = ov; grow = orow; gwb = owb; }
+                }
+                if (lane == 0) {
+                    if (!ok) s_fail = 1;
+                    if (grow == INT_MAX) {
+                        // whole column NaN: keep the diagonal (SLATE's scan
+                        // starts from it and '>' never accepts a NaN)
+                        grow = int(j);
+                        gwb = -1;
+                        gv = ((volatile T*) ex->diag_rowvals[par])[jc];
+                    }
+                    s_p = grow;
+                    s_wb = gwb;
+                    s_pval = gv;
+                    s_piv[jc] = grow;
+                    if (b == 0 && ok) {
+                        a.ipiv[j] = grow;
+                        if (gv == T(0)) atomicCAS(a.info, 0, int(a.info_offset + j + 1));
+                    }
+                }
             }
-            if (!grid_sync(a.bar, unsigned(G), a.status)) return;
+            __syncthreads();
+            if (s_fail) return;
+            const int64_t p = s_p;
+            const int wb = s_wb;
+            const T pval = s_pval;
+            for (int c = t; c < kb; c += kPanelThreads)
+                s_u[c] = (wb >= 0) ? ((volatile T*) ex->cand_rowvals[par][wb])[c]
+                                   : ((volatile T*) ex->diag_rowvals[par])[c];
+            __syncthreads();
+            if (p != j) {
+                if (j >= rb && j < re)
+                    for (int c = t; c < kb; c += kPanelThreads) S[c * RP + int(j - rb)] = s_u[c];
+                if (p >= rb && p < re)
+                    for (int c = t; c < kb; c += kPanelThreads)
+                        S[c * RP + int(p - rb)] = ((volatile T*) ex->diag_rowvals[par])[c];
+            }
+            __syncthreads();
+            // ---- scale and rank-1 update of the owned rows below j
+            const bool recip = fabs(pval) >= Real<T>::safe_min();
+            const T rinv = T(1) / pval;
+            for (int64_t i = max(rb, j + 1) + t; i < re; i += kPanelThreads) {
+                const int r = int(i - rb);
+                T l = S[jc * RP + r];
+                if (recip) l *= rinv;
+                else if (pval != T(0)) l /= pval;
+                S[jc * RP + r] = l;
+                for (int c = jc + 1; c < kb; ++c) S[c * RP + r] -= l * s_u[c];
+            }
+            __syncthreads();
         }
+        // stripe final in shared memory: write it back
+        for (int e = t; e < nrow * kb; e += kPanelThreads) {
+            const int r = e % nrow, c = e / nrow;
+            P[rb + r + (k0 + c) * ld] = S[c * RP + r];
+        }
+        __threadfence();
+        if (!stripe_end(a, G, b, t, k0, kb, rb, re, s_piv, s_L, s_U)) return;
     }
 }
 
@@ -415,8 +610,32 @@ static int launch_panel(int64_t prows, int64_t nbk, int64_t ib, T* P, int64_t ld
     args.rows_per_block = R; args.info_offset = info_offset;
     args.P = P; args.ipiv = ipiv; args.info = info; args.status = status;
     args.bar = bar; args.ex = ex;
-    void* kargs[] = { &args };
+    // staged variant when the block's stripe rows fit in shared memory
+    const size_t staged = sizeof(T) * size_t(R) * size_t(ib);
+    int* flags = reinterpret_cast<int*>(base + 256 + ((sizeof(PanelExchange<double>) + 255) & ~size_t(255)));
     const int pidx = prof_begin(SLT_PROF_PANEL, stream);
+    if (staged <= kPanelStagedMax) {
+        static bool cfg2 = false;
+        if (!cfg2) {
+            SLT_CUDA_TRY(cudaFuncSetAttribute(getrf_panel2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              int(kPanelStagedMax)));
+            cfg2 = true;
+        }
+        int per2 = 0;
+        SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, getrf_panel2_kernel<T>, kPanelThreads,
+                                                                   staged));
+        if (per2 >= 1 && int64_t(sms) * per2 >= G) {
+            SLT_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * size_t(kMaxPanelBlocks), stream));
+            void* kargs2[] = { &args, &flags };
+            SLT_CUDA_TRY(cudaLaunchCooperativeKernel((const void*) getrf_panel2_kernel<T>, dim3(unsigned(G)),
+                                                     dim3(kPanelThreads), kargs2, staged, stream));
+            count_launch();
+            const double nb_ = double(nbk), m_ = double(prows);
+            prof_end(pidx, stream, m_ * nb_ * nb_ - nb_ * nb_ * nb_ / 3.0, 2.0 * m_ * nb_ * sizeof(T));
+            return SLT_OK;
+        }
+    }
+    void* kargs[] = { &args };
     SLT_CUDA_TRY(cudaLaunchCooperativeKernel((const void*) getrf_panel_kernel<T>, dim3(unsigned(G)),
                                              dim3(kPanelThreads), kargs, 0, stream));
     count_launch();
@@ -449,10 +668,11 @@ static int launch_laswp(const int* plan, int64_t maxcount, T* A, int64_t lda, in
 
 using namespace slt;
 
+// Panel scratch: grid barrier (256 B), candidate exchange, per-block flags.
 extern "C" size_t slt_getrf_panel_ws_bytes(int64_t prows, int64_t ib)
 {
     (void) prows; (void) ib;
-    return 256 + sizeof(PanelExchange<double>);
+    return 256 + ((sizeof(PanelExchange<double>) + 255) & ~size_t(255)) + sizeof(int) * size_t(kMaxPanelBlocks);
 }
 
 extern "C" int slt_dgetrf_panel(int64_t prows, int64_t nbk, int64_t ib, double* P, int64_t ld,

@@ -121,6 +121,16 @@ int slt_convert_d2s(int64_t m, int64_t n, const double* A, int64_t lda, float* B
                     cudaStream_t stream);
 int slt_convert_s2d(int64_t m, int64_t n, const float* A, int64_t lda, double* B, int64_t ldb,
                     cudaStream_t stream);
+/* B = diag(r) A diag(c) cast to float (r, c may be null), and X = diag(r) B */
+int slt_convert_d2s_scaled(int64_t m, int64_t n, const double* A, int64_t lda, const double* r,
+                           const double* c, float* B, int64_t ldb, cudaStream_t stream);
+int slt_convert_s2d_scaled(int64_t m, int64_t n, const float* B, int64_t ldb, const double* r,
+                           double* X, int64_t ldx, cudaStream_t stream);
+/* power-of-two equilibration scales: general (row r, column c; ws m words),
+ * SPD (d from the diagonal) */
+int slt_dgeequ(int64_t m, int64_t n, const double* A, int64_t lda, double* r, double* c, void* ws,
+               cudaStream_t stream);
+int slt_dpoequ(int64_t n, const double* A, int64_t lda, double* d, cudaStream_t stream);
 int slt_dcopy2d(int64_t m, int64_t n, const double* A, int64_t lda, double* B, int64_t ldb,
                 cudaStream_t stream);
 /* B = alpha A + beta B */
@@ -151,8 +161,12 @@ int slt_dgenerate_sigma(int64_t n, double cond, int dist, int spd, int64_t seed,
                         cudaStream_t stream);
 /* A(i,i) += alpha for i < n */
 int slt_dshift_diag(int64_t n, double alpha, double* A, int64_t lda, cudaStream_t stream);
+int slt_sshift_diag(int64_t n, float alpha, float* A, int64_t lda, cudaStream_t stream);
 /* Symmetrise from the lower triangle: A(j,i) = A(i,j) for i > j. */
 int slt_dsymmetrize_lower(int64_t n, double* A, int64_t lda, cudaStream_t stream);
+/* D = S on the lower (lower = 1) or upper triangle, diagonal included */
+int slt_dcopy_tri(int lower, int64_t n, const double* S, int64_t lds, double* D, int64_t ldd, cudaStream_t stream);
+int slt_dtranspose(int64_t m, int64_t n, const double* A, int64_t lda, double* B, int64_t ldb, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -13,3 +13,6 @@ static inline int slt_from_cuda(cudaError_t e)
         cudaError_t e_ = (expr);                                  \
         if (e_ != cudaSuccess) return slt_from_cuda(e_);          \
     } while (0)
+
+// Propagates a non-zero slt status.
+#define TRY(expr) do { int rc_ = (expr); if (rc_ != SLT_OK) return rc_; } while (0)

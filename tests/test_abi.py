@@ -46,3 +46,39 @@ def test_options_mirror():
     import slate_gb300 as s
     o = s.Options(nb=256, factor_precision="bf16")._c()
     assert o.nb == 256 and o.factor_precision == s.PREC_BF16
+
+
+def test_c_api_handles_host_only(slt):
+    """SLATE's C API handles: options round trip, grid and tile checks."""
+    L = slt.lib()
+    vp, i64 = ctypes.c_void_p, ctypes.c_int64
+    L.slate_Options_create.restype = vp
+    o = L.slate_Options_create()
+    L.slate_Options_set_BlockSize.argtypes = [vp, i64]
+    L.slate_Options_get_BlockSize.argtypes = [vp, i64]
+    L.slate_Options_get_BlockSize.restype = i64
+    L.slate_Options_set_BlockSize(o, 256)
+    assert L.slate_Options_get_BlockSize(o, 1) == 256
+    L.slate_Options_get_BlockSize.argtypes = [vp, i64]
+    assert L.slate_Options_get_BlockSize(None, 7) == 7
+    L.slate_Options_set_Tolerance.argtypes = [vp, ctypes.c_double]
+    L.slate_Options_get_Tolerance.argtypes = [vp, ctypes.c_double]
+    L.slate_Options_get_Tolerance.restype = ctypes.c_double
+    L.slate_Options_set_Tolerance(o, 1e-9)
+    assert L.slate_Options_get_Tolerance(o, 0.0) == 1e-9
+    L.slate_Options_destroy.argtypes = [vp]
+    L.slate_Options_destroy(o)
+    mk = L.slate_Matrix_create_fromScaLAPACK_r64
+    mk.restype = vp
+    mk.argtypes = [i64, i64, vp, i64, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_ssize_t]
+    import numpy as np
+    a = np.zeros((8, 8), order="F")
+    assert mk(8, 8, a.ctypes.data, 8, 4, 4, 2, 1, 0) is None        # 2 x 1 grid rejected
+    assert mk(8, 8, a.ctypes.data, 8, 4, 2, 1, 1, 0) is None        # mb != nb rejected
+    h = mk(8, 8, a.ctypes.data, 8, 4, 4, 1, 1, 0)
+    assert h
+    L.slate_Matrix_m_r64.argtypes = [vp]
+    L.slate_Matrix_m_r64.restype = i64
+    assert L.slate_Matrix_m_r64(h) == 8
+    L.slate_Matrix_destroy_r64.argtypes = [vp]
+    L.slate_Matrix_destroy_r64(h)

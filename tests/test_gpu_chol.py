@@ -7,7 +7,8 @@ from gpu_util import EPS, berr, spd, to_dev, to_host
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("n,nb", [(1, 4), (5, 4), (64, 16), (100, 32), (300, 64), (1000, 256), (1300, 512)])
+@pytest.mark.parametrize("n,nb", [(1, 4), (5, 4), (64, 16), (100, 32), (300, 64), (1000, 256), (1300, 512),
+                                  (45, 7), (77, 40), (530, 100)])
 def test_potrf_parity(orc, slt, n, nb):
     import torch
     A = spd(orc, n, 40 + n)
@@ -36,16 +37,17 @@ def test_posv_backward_error(orc, slt, n, nb, nrhs):
     assert berr(orc, A, to_host(dB), B, sym=True) <= 3 * EPS
 
 
-def test_potrf_not_spd(orc, slt):
+@pytest.mark.parametrize("bad", [0, 130, 150, 199])
+def test_potrf_not_spd(orc, slt, bad):
     import torch
     n = 200
     A = spd(orc, n, 3)
-    A[130, 130] = -5.0
+    A[bad, bad] = -5.0
     dA = to_dev(A)
     info = slt.potrf(dA, slt.Options(nb=64))
     torch.cuda.synchronize()
     Ao = A.copy(order="F")
-    assert info == orc.potrf(Ao, 64) == 131
+    assert info == orc.potrf(Ao, 64) == bad + 1
 
 
 def test_potrf_known_answer_minij(orc, slt):

@@ -136,3 +136,59 @@ def test_generate_sigma_matches_restatement(orc, slt, dist, spd):
     if spd:
         np.testing.assert_allclose(A, A.T, atol=1e-14)
         assert np.linalg.eigvalsh(A).min() > 0
+
+
+@pytest.mark.parametrize("fn", ["gesv_mixed", "posv_mixed"])
+def test_fp16_equilibration_of_badly_scaled_matrix(orc, slt, fn):
+    """Rows and columns scaled by 2^-20 .. 2^20: the FP16 operands of the
+    trailing update overflow without scaling; the power-of-two
+    equilibration keeps them in range, and the FP64 refinement on the
+    unscaled matrix still reaches FP64 backward error."""
+    chol = fn.startswith("posv")
+    n, nb = 1024, 256
+    rng = np.random.default_rng(5)
+    d = 2.0 ** rng.integers(-20, 21, n)
+    if chol:
+        A = np.asfortranarray(d[:, None] * spd(orc, n, 51) * d[None, :])
+    else:
+        e = 2.0 ** rng.integers(-20, 21, n)
+        A = np.asfortranarray(d[:, None] * orc.generate(2, 52, n, n) * e[None, :])
+    B = orc.generate(2, 53, n, 2)
+    info, it, X, Aout = _run(slt, fn, A, B, slt.Options(nb=nb, factor_precision="fp16", equilibrate=1))
+    assert info == 0 and it >= 0
+    assert berr(orc, A, X, B, sym=chol) <= 3 * n * EPS
+    assert np.array_equal(Aout, A)
+
+
+def _sigma_system(slt, n, cond, seed, spd):
+    import torch
+    dA = slt.colmajor(torch.zeros(n, n, dtype=torch.float64, device="cuda"))
+    slt.generate_sigma(dA, cond, "logrand" if spd else "geo", spd, seed=seed)
+    torch.cuda.synchronize()
+    return to_host(dA)
+
+
+@pytest.mark.parametrize("kappa", [1e4, 1e6])
+@pytest.mark.parametrize("fn", ["gesv_mixed", "posv_mixed"])
+def test_ill_conditioned_16bit_without_fp64_fallback(orc, slt, fn, kappa):
+    """FP16 factors at kappa = 1e4, 1e6: plain IR contracts by about
+    kappa * u_fp16 per step and may diverge.  The ir+gmres chain continues
+    stalled columns with FGMRES-IR on the same factors; if that fails too,
+    the FP32 retry refactors in FP32 -- in every case the answer reaches FP64
+    backward error without SLATE's FP64 fallback (A left untouched)."""
+    chol = fn.startswith("posv")
+    n, nb = 2048, 256
+    A = _sigma_system(slt, n, kappa, 61, chol)
+    xt = orc.generate(2, 62, n, 1)
+    B = np.asfortranarray(A @ xt)
+    _, it_ir, _, _ = _run(slt, fn, A, B, slt.Options(nb=nb, factor_precision="fp16", lo_retry=0))
+    _, it_ch, _, _ = _run(slt, fn, A, B, slt.Options(nb=nb, factor_precision="fp16", refine="ir+gmres",
+                                                     lo_retry=0))
+    info, it, X, Aout = _run(slt, fn, A, B, slt.Options(nb=nb, factor_precision="fp16", refine="ir+gmres"))
+    retried = slt.timer(fn + "::retry_fp32") > 0
+    print(fn, kappa, "ir:", it_ir, "ir+gmres:", it_ch, "with fp32 retry:", it, retried)
+    assert info == 0 and it >= 0
+    assert np.array_equal(Aout, A)          # no FP64 fallback
+    assert retried == (it_ch < 0)
+    assert berr(orc, A, X, B, sym=chol) <= 3 * n * EPS
+    assert np.abs(X - xt).max() / np.abs(xt).max() <= kappa * 3 * n * EPS
