@@ -65,6 +65,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
     p.add_argument("--batch", type=int, default=20000, help="config 5: number of systems")
+    p.add_argument("--no-loop", action="store_true", help="config 5: skip the per-system loop")
     p.add_argument("--kappas", default=None, help="comma list (configs 3, 4)")
     p.add_argument("--precs", default=None, help="comma list (configs 3, 4)")
     p.add_argument("--refine", default="ir+gmres", help="configs 3: ir | ir+gmres")
@@ -420,8 +421,12 @@ def run_config5(args, slt, torch, dev):
         ts.append(t)
     rec["batched_mixed_ms"] = ts[-1] * 1e3
     rec["batched_mixed_effective_tflops"] = flops / ts[-1] / 1e12
+    rec["batched_mixed_phase_ms"] = {k: slt.timer("vbatched_mixed::" + k) * 1e3 for k in ("factor_lo", "refine", "fallback")}
     rec["batched_mixed_iter_hist"] = {str(int(v)): int(c) for v, c in zip(*np.unique(iters, return_counts=True))}
     rec["batched_mixed_berr_max"] = berr_max(X)
+    if args.no_loop:
+        print(json.dumps(rec))
+        return
     # per-system loop of the library's own gesv / posv (FP64), A, B restored first
     A.copy_(A0)
     B.copy_(B0)

@@ -86,7 +86,68 @@ struct CholPanelArgs {
     int* info;
     int* status;
     GridBarrier* bar;
+    int* next_fail;     // set when the lookahead factor of the next diagonal block fails
+    T* dinv_ws;         // its 16 x 16 sub-block inverses, [4][16][17]
 };
+
+// The 64 x 64 (kb x kb) diagonal block D (row-major in shared memory, row
+// stride 65, lower triangle) factored in place by the whole CTA, in 16-column
+// steps: warp 0 factors the 16 x 16 diagonal sub-block and inverts it into
+// Dinv, then all threads solve the sub-block rows below it and update the
+// rest of the block.  Returns 0, or the 1-based column (within the block) of
+// the first non-positive pivot; the same value in every thread.
+template <typename T>
+__device__ int factor_diag_block(T* D, T* Dinv, int kb)
+{
+    __shared__ int s_f;
+    const int t = threadIdx.x;
+    if (t == 0) s_f = 0;
+    __syncthreads();
+    for (int jb = 0, jbi = 0; jb < kb; jb += kCpSub, ++jbi) {
+        const int bw = min(kCpSub, kb - jb);
+        if (t < 32) {
+            const int fail = factor_invert_16(D + jb * (kCpIB + 1) + jb, kCpIB + 1, bw,
+                                              Dinv + jbi * kCpSub * (kCpSub + 1));
+            if (t == 0 && fail) s_f = jb + fail;
+        }
+        __syncthreads();
+        if (s_f) break;
+        // rows i in [jb + bw, kb) of the sub-block column: X = B L_sub^{-T}
+        const int below = kb - jb - bw;
+        const T* Di = Dinv + jbi * kCpSub * (kCpSub + 1);
+        T xv[3];
+        #pragma unroll
+        for (int u = 0; u < 3; ++u) {
+            const int e = t + u * kCpThreads;
+            xv[u] = T(0);
+            if (e < below * bw) {
+                const int i = jb + bw + e / bw, c = e % bw;
+                T acc = T(0);
+                for (int p = 0; p <= c; ++p) acc = fma(D[i * (kCpIB + 1) + jb + p], Di[c * (kCpSub + 1) + p], acc);
+                xv[u] = acc;
+            }
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int u = 0; u < 3; ++u) {
+            const int e = t + u * kCpThreads;
+            if (e < below * bw) D[(jb + bw + e / bw) * (kCpIB + 1) + jb + e % bw] = xv[u];
+        }
+        __syncthreads();
+        // trailing update inside the block: D[i][c] -= sum_p D[i][jb+p] D[c][jb+p], jb+bw <= c <= i < kb
+        for (int e = t; e < below * below; e += kCpThreads) {
+            const int i = jb + bw + e % below, c = jb + bw + e / below;
+            if (c > i) continue;
+            T acc = T(0);
+            for (int p = 0; p < bw; ++p)
+                acc = fma(D[i * (kCpIB + 1) + jb + p], D[c * (kCpIB + 1) + jb + p], acc);
+            D[i * (kCpIB + 1) + c] -= acc;
+        }
+        __syncthreads();
+        }
+    __syncthreads();
+    return s_f;
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kCpThreads)
@@ -106,60 +167,26 @@ chol_panel_kernel(CholPanelArgs<T> a)
 
     for (int64_t c0 = 0; c0 < a.nbk; c0 += kCpIB) {
         const int kb = int(min64(kCpIB, a.nbk - c0));
-        // ---- 1. factor the diagonal block in shared memory (every block), in
-        //      16-column steps: warp 0 factors the 16 x 16 diagonal sub-block in
-        //      registers and inverts it, then all threads solve the sub-block
-        //      rows below it and update the rest of the 64 x 64 block.
+        // ---- 1. the factored diagonal block in shared memory.  First step:
+        //      every block factors it (no earlier step could).  Later steps:
+        //      its owner factored it during the previous step's update phase
+        //      (below) and published L11 in P, the sub-block inverses and a
+        //      failure word in the workspace; every block loads them.
         for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
             int i = e % kCpIB, l = e / kCpIB;
             D[i * (kCpIB + 1) + l] = (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
         }
-        if (t == 0) s_fail = 0;
+        if (c0 > 0)
+            for (int e = t; e < (kCpIB / kCpSub) * kCpSub * (kCpSub + 1); e += kCpThreads)
+                Dinv[e] = __ldcg(&a.dinv_ws[e]);
+        if (t == 0) s_fail = (c0 > 0) ? ld_volatile_i32(a.next_fail) : 0;
         __syncthreads();
-        for (int jb = 0, jbi = 0; jb < kb; jb += kCpSub, ++jbi) {
-            const int bw = min(kCpSub, kb - jb);
-            if (t < 32) {
-                const int fail = factor_invert_16(D + jb * (kCpIB + 1) + jb, kCpIB + 1, bw,
-                                                  Dinv + jbi * kCpSub * (kCpSub + 1));
-                if (t == 0 && fail) {
-                    s_fail = 1;
-                    if (c0 >= rb && c0 < re) atomicCAS(a.info, 0, int(a.info_offset + c0 + jb + fail));
-                }
+        if (c0 == 0) {
+            const int f = factor_diag_block(D, Dinv, kb);
+            if (t == 0 && f) {
+                s_fail = 1;
+                if (c0 >= rb && c0 < re) atomicCAS(a.info, 0, int(a.info_offset + c0 + f));
             }
-            __syncthreads();
-            if (s_fail) break;
-            // rows i in [jb + bw, kb) of the sub-block column: X = B L_sub^{-T}
-            const int below = kb - jb - bw;
-            const T* Di = Dinv + jbi * kCpSub * (kCpSub + 1);
-            T xv[3];
-            #pragma unroll
-            for (int u = 0; u < 3; ++u) {
-                const int e = t + u * kCpThreads;
-                xv[u] = T(0);
-                if (e < below * bw) {
-                    const int i = jb + bw + e / bw, c = e % bw;
-                    T acc = T(0);
-                    for (int p = 0; p <= c; ++p) acc = fma(D[i * (kCpIB + 1) + jb + p], Di[c * (kCpSub + 1) + p], acc);
-                    xv[u] = acc;
-                }
-            }
-            __syncthreads();
-            #pragma unroll
-            for (int u = 0; u < 3; ++u) {
-                const int e = t + u * kCpThreads;
-                if (e < below * bw) D[(jb + bw + e / bw) * (kCpIB + 1) + jb + e % bw] = xv[u];
-            }
-            __syncthreads();
-            // trailing update inside the block: D[i][c] -= sum_p D[i][jb+p] D[c][jb+p], jb+bw <= c <= i < kb
-            for (int e = t; e < below * below; e += kCpThreads) {
-                const int i = jb + bw + e % below, c = jb + bw + e / below;
-                if (c > i) continue;
-                T acc = T(0);
-                for (int p = 0; p < bw; ++p)
-                    acc = fma(D[i * (kCpIB + 1) + jb + p], D[c * (kCpIB + 1) + jb + p], acc);
-                D[i * (kCpIB + 1) + c] -= acc;
-            }
-            __syncthreads();
         }
         __syncthreads();
         const bool failed = s_fail != 0;
@@ -212,17 +239,18 @@ chol_panel_kernel(CholPanelArgs<T> a)
         }
         __threadfence();
         if (!grid_sync(a.bar, unsigned(G), a.status)) return;
-        // every block has read the diagonal block: its owner writes the factor back
-        if (c0 >= rb && c0 < re)
+        // every block has read the diagonal block: its owner writes the factor
+        // back (later diagonal blocks were written by the lookahead below)
+        if (c0 == 0 && c0 >= rb && c0 < re)
             for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
                 int i = e % kCpIB, l = e / kCpIB;
                 if (i < kb && l < kb && i >= l) P[c0 + i + (c0 + l) * ld] = D[i * (kCpIB + 1) + l];
             }
+        const int64_t cbeg = c0 + kb;
         // ---- 3. rank-kb update of the owned rows in panel columns [c0+kb, nbk):
         //      64 x 64 output tiles, 4 x 4 per thread, operands staged [l][row]
         //      and [l][col] (row stride 68) so each thread reads two 4-vectors
         //      per k step for 16 FMAs.
-        const int64_t cbeg = c0 + kb;
         if (cbeg < a.nbk && !failed) {
             T* X3 = Xs;                                  // [64][68]
             T* U3 = Us;                                  // [64][68]
@@ -277,6 +305,29 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 }
             }
         }
+        // ---- 4. lookahead: the owner of the next diagonal block (its rows
+        //      updated just above, and it has no other work in lower-
+        //      triangular column tiles) factors it now, while the other
+        //      blocks are still updating.
+        if (!failed && cbeg < a.nbk && cbeg >= rb && cbeg < re) {
+            const int kbn = int(min64(kCpIB, a.nbk - cbeg));
+            __syncthreads();
+            for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+                int i = e % kCpIB, l = e / kCpIB;
+                D[i * (kCpIB + 1) + l] = (i < kbn && l < kbn && i >= l) ? __ldcg(&P[cbeg + i + (cbeg + l) * ld]) : T(0);
+            }
+            __syncthreads();
+            const int f = factor_diag_block(D, Dinv, kbn);
+            for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+                int i = e % kCpIB, l = e / kCpIB;
+                if (i < kbn && l < kbn && i >= l) P[cbeg + i + (cbeg + l) * ld] = D[i * (kCpIB + 1) + l];
+            }
+            for (int e = t; e < (kCpIB / kCpSub) * kCpSub * (kCpSub + 1); e += kCpThreads) a.dinv_ws[e] = Dinv[e];
+            if (t == 0 && f) {
+                atomicCAS(a.info, 0, int(a.info_offset + cbeg + f));
+                *reinterpret_cast<volatile int*>(a.next_fail) = 1;
+            }
+        }
         __threadfence();
         if (!grid_sync(a.bar, unsigned(G), a.status)) return;
         if (failed) return;       // every block saw the same failing diagonal block
@@ -306,9 +357,12 @@ static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info
     const int64_t maxg = int64_t(sms) * per_sm;             // all blocks co-resident
     int64_t R = ceildiv(ceildiv(m, maxg), kCpIB) * kCpIB;     // multiple of 64
     int64_t G = ceildiv(m, R);
+    // ws: barrier at 0, failure word at 256, sub-block inverses at 512
     GridBarrier* bar = static_cast<GridBarrier*>(ws);
-    SLT_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), stream));
-    CholPanelArgs<T> args{m, nbk, ld, R, info_offset, P, info, status, bar};
+    int* next_fail = reinterpret_cast<int*>(static_cast<char*>(ws) + 256);
+    T* dinv_ws = reinterpret_cast<T*>(static_cast<char*>(ws) + 512);
+    SLT_CUDA_TRY(cudaMemsetAsync(ws, 0, 512, stream));
+    CholPanelArgs<T> args{m, nbk, ld, R, info_offset, P, info, status, bar, next_fail, dinv_ws};
     void* kargs[] = { &args };
     const int pidx = prof_begin(SLT_PROF_POTRF, stream);
     SLT_CUDA_TRY(cudaLaunchCooperativeKernel((const void*) chol_panel_kernel<T>, dim3(unsigned(G)),
@@ -322,9 +376,16 @@ static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info
 
 using namespace slt;
 
+// Device scratch of one panel launch: grid barrier, lookahead failure word
+// and the next diagonal block's sub-block inverses.
+extern "C" size_t slt_chol_panel_ws_bytes(void)
+{
+    return 512 + size_t(kCpIB / kCpSub) * kCpSub * (kCpSub + 1) * sizeof(double);
+}
+
 // Factor the Cholesky column panel with top-left P (the diagonal element),
-// m rows (to the bottom of the matrix), nbk columns.  ws: >= 256 bytes of
-// device scratch for the grid barrier.
+// m rows (to the bottom of the matrix), nbk columns.  ws: slt_chol_panel_ws_bytes()
+// bytes of device scratch.
 extern "C" int slt_dchol_panel(int64_t m, int64_t nbk, double* P, int64_t ld, int* info, int64_t info_offset,
                                void* ws, int* status, cudaStream_t stream)
 { return launch_chol_panel<double>(m, nbk, P, ld, info, info_offset, ws, status, stream); }

@@ -222,7 +222,7 @@ int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc,
     if (n < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
     const int64_t nb = eff_nb(o);
     DevBuf bar;
-    TRY(bar.alloc(256, s));
+    TRY(bar.alloc(slt_chol_panel_ws_bytes(), s));
     for (int64_t r0 = 0; r0 < n; r0 += nb) {
         const int64_t kb = std::min(nb, n - r0);
         // the whole column panel (diagonal block and everything below) in one launch
@@ -386,9 +386,12 @@ struct Fgmres {
     }
 
     // Runs until the stopping test holds or itermax Arnoldi steps are spent.
-    // *used: the steps taken; *conv: whether the test held.
+    // *used: the steps taken; *conv: whether the test held.  SLATE's loop
+    // tests the true residual only at the top of a restart cycle, so a cycle
+    // that ends on the budget is never tested; final_check (used by the
+    // IR -> GMRES-IR chain, which is not SLATE's driver) tests it once more.
     int run(const double* b, int64_t ldb, double* x, int64_t ldx, int64_t itermax, int* used, bool* conv,
-            cudaStream_t s) {
+            cudaStream_t s, bool final_check = false) {
         double* Vd = V.as<double>();
         double* Wd = W.as<double>();
         float* wlo = Wlo.as<float>();
@@ -468,6 +471,14 @@ struct Fgmres {
                 TRY(slt_dgemm_skinny(n, 1, j, 1.0, Wd + n, n, 0, dy, R1, 1.0, x, ldx, nws.p, s));
                 SLT_CUDA_TRY(cudaStreamSynchronize(s));
             }
+        }
+        if (!stopped && final_check) {
+            TRY(slt_dresidual(n, 1, A, lda, chol, b, ldb, x, ldx, Vd, n, nws.p, s));
+            TRY(slt_dcolmax(n, 1, x, ldx, dsc, s));
+            TRY(slt_dcolmax(n, 1, Vd, n, dsc + 1, s));
+            double hv[2];
+            TRY(read_doubles(dsc, hv, 2, s));
+            if (hv[1] <= hv[0] * cte) *conv = true;
         }
         *used = stopped ? citer : int(iiter);
         return SLT_OK;
@@ -598,7 +609,7 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
                 if (hr[c] <= hx[c] * cte) continue;
                 int used = 0;
                 bool cc = false;
-                TRY(g.run(B + c * ldb, ldb, X + c * ldx, ldx, itermax - ir_steps, &used, &cc, s));
+                TRY(g.run(B + c * ldb, ldb, X + c * ldx, ldx, itermax - ir_steps, &used, &cc, s, true));
                 all = all && cc;
                 worst = std::max(worst, used);
             }

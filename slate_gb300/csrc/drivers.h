@@ -29,6 +29,7 @@ int slt_dsweep(int kind, int64_t n, int64_t nrhs, const double* M, int64_t ldm, 
 int slt_ssweep(int kind, int64_t n, int64_t nrhs, const float* M, int64_t ldm, float* X, int64_t ldx,
                int* flags, int* status, cudaStream_t s);
 size_t slt_sweep_flags_bytes(int64_t n);
+size_t slt_chol_panel_ws_bytes(void);
 int slt_dchol_panel(int64_t m, int64_t nbk, double* P, int64_t ld, int* info, int64_t info_offset, void* ws,
                     int* status, cudaStream_t stream);
 int slt_schol_panel(int64_t m, int64_t nbk, float* P, int64_t ld, int* info, int64_t info_offset, void* ws,

@@ -206,156 +206,6 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
     }
 }
 
-// Wide variant: 128-row blocks (two 64-row sub-blocks solved inside the CTA
-// with the same 64 x 64 inverses), so the chain of cross-CTA hand-offs that
-// bounds a sweep is half as long.  Used for FP32, whose 128 x 128 staging tile
-// fits in shared memory next to the rest (about 99 KB).
-constexpr int kSw2 = 128;
-
-template <typename T>
-struct Sweep2Smem {
-    T Ts[kSw2][kSw2 + 1];      // off-diagonal tile, [col][row]
-    T Ds[kSwBS][kSwBS + 1];    // one 64 x 64 diagonal inverse, [row][col]
-    T xs[kSw2][kSwRhs];        // solved block x_j
-    T xi[kSw2][kSwRhs];        // this block's right-hand side / solution
-};
-
-template <typename T, bool FORWARD, bool UNIT, bool TRANS>
-__global__ void __launch_bounds__(256)
-sweep2_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T* __restrict__ Dinv,
-              T* X, int64_t ldx, int* ticket, int* ready, int* status)
-{
-    extern __shared__ unsigned char sw_smem_raw[];
-    Sweep2Smem<T>& sm = *reinterpret_cast<Sweep2Smem<T>*>(sw_smem_raw);
-    __shared__ int s_p, s_ok;
-    const int t = threadIdx.x;
-    const int nblk = int(ceildiv(n, kSw2));
-
-    auto opM = [&](int64_t r, int64_t c) -> T {
-        return TRANS ? __ldg(&M[c + r * ldm]) : __ldg(&M[r + c * ldm]);
-    };
-
-    for (;;) {
-        if (t == 0) s_p = atomicAdd(ticket, 1);
-        __syncthreads();
-        const int p = s_p;
-        if (p >= nblk) break;
-        const int bi = FORWARD ? p : nblk - 1 - p;
-        const int64_t i0 = int64_t(bi) * kSw2;
-        const int ni = int(min64(kSw2, n - i0));
-        for (int e = t; e < kSw2 * kSwRhs; e += 256) {
-            int r = e % kSw2, q = e / kSw2;
-            sm.xi[r][q] = (r < ni && q < nrhs) ? X[i0 + r + q * ldx] : T(0);
-        }
-
-        // accumulate op(M)(i, j) x_j over the solved blocks: row r, 8 right-hand sides per thread
-        const int r = t % kSw2, g = t / kSw2;
-        T acc[8];
-        #pragma unroll
-        for (int u = 0; u < 8; ++u) acc[u] = T(0);
-        for (int pq = 0; pq < p; ++pq) {
-            const int bj = FORWARD ? pq : nblk - 1 - pq;
-            const int64_t j0 = int64_t(bj) * kSw2;
-            const int nj = int(min64(kSw2, n - j0));
-            __syncthreads();
-            for (int e = t; e < kSw2 * kSw2; e += 256) {
-                int rr, c;
-                if (TRANS) { c = e % kSw2; rr = e / kSw2; }
-                else       { rr = e % kSw2; c = e / kSw2; }
-                sm.Ts[c][rr] = (rr < ni && c < nj) ? opM(i0 + rr, j0 + c) : T(0);
-            }
-            if (t == 0) {
-                int ok = 1;
-                if (ld_acquire_i32(&ready[pq]) == 0) {
-                    const uint64_t t0 = sw_globaltimer();
-                    for (unsigned it = 1; ld_acquire_i32(&ready[pq]) == 0; ++it) {
-                        if ((it & 255u) == 0 &&
-                            (ld_volatile_i32(status) != 0 || sw_globaltimer() - t0 > 2000000000ull)) {
-                            atomicCAS(status, 0, SLT_ERR_TIMEOUT);
-                            ok = 0;
-                            break;
-                        }
-                    }
-                }
-                s_ok = ok;
-            }
-            __syncthreads();
-            if (!s_ok) return;
-            for (int e = t; e < kSw2 * kSwRhs; e += 256) {
-                int rr = e % kSw2, q = e / kSw2;
-                sm.xs[rr][q] = (rr < nj && q < nrhs) ? __ldcg(&X[j0 + rr + q * ldx]) : T(0);
-            }
-            __syncthreads();
-            #pragma unroll 4
-            for (int c = 0; c < kSw2; ++c) {
-                const T a = sm.Ts[c][r];
-                #pragma unroll
-                for (int u = 0; u < 8; ++u) acc[u] = fma(a, sm.xs[c][g * 8 + u], acc[u]);
-            }
-        }
-        __syncthreads();
-        #pragma unroll
-        for (int u = 0; u < 8; ++u) sm.xi[r][g * 8 + u] -= acc[u];
-        __syncthreads();
-
-        // the diagonal 128 x 128 block: solve the first 64-row sub-block (in
-        // solve order) with its inverse, update the second with the tile
-        // between them, then solve the second
-        const int n0 = min(kSwBS, ni), n1 = ni - n0;
-        const int first = FORWARD ? 0 : 1;
-        const int r6 = t % kSwBS, g6 = t / kSwBS;     // 4 groups x 4 right-hand sides
-        for (int step = 0; step < 2; ++step) {
-            const int sb = (step == 0) ? first : 1 - first;
-            const int nsb = (sb == 0) ? n0 : n1;
-            if (nsb <= 0) continue;
-            const int roff = sb * kSwBS;
-            if (step == 1) {
-                const int ooff = (1 - sb) * kSwBS;
-                const int no = (sb == 0) ? n1 : n0;
-                for (int e = t; e < kSwBS * kSwBS; e += 256) {
-                    int rr, c;
-                    if (TRANS) { c = e % kSwBS; rr = e / kSwBS; }
-                    else       { rr = e % kSwBS; c = e / kSwBS; }
-                    sm.Ts[c][rr] = (rr < nsb && c < no) ? opM(i0 + roff + rr, i0 + ooff + c) : T(0);
-                }
-                __syncthreads();
-                T a4[4] = {T(0), T(0), T(0), T(0)};
-                #pragma unroll 8
-                for (int c = 0; c < kSwBS; ++c) {
-                    const T a = sm.Ts[c][r6];
-                    #pragma unroll
-                    for (int u = 0; u < 4; ++u) a4[u] = fma(a, sm.xi[ooff + c][g6 * 4 + u], a4[u]);
-                }
-                #pragma unroll
-                for (int u = 0; u < 4; ++u) sm.xi[roff + r6][g6 * 4 + u] -= a4[u];
-            }
-            {
-                const T* dinv = Dinv + size_t(i0 / kSwBS + sb) * kSwBS * kSwBS;
-                for (int e = t; e < kSwBS * kSwBS; e += 256) sm.Ds[e / kSwBS][e % kSwBS] = dinv[e];
-            }
-            __syncthreads();
-            T y[4] = {T(0), T(0), T(0), T(0)};
-            #pragma unroll 8
-            for (int c = 0; c < kSwBS; ++c) {
-                const T d = sm.Ds[r6][c];
-                #pragma unroll
-                for (int u = 0; u < 4; ++u) y[u] = fma(d, sm.xi[roff + c][g6 * 4 + u], y[u]);
-            }
-            __syncthreads();
-            #pragma unroll
-            for (int u = 0; u < 4; ++u) sm.xi[roff + r6][g6 * 4 + u] = y[u];
-            __syncthreads();
-        }
-        for (int e = t; e < kSw2 * kSwRhs; e += 256) {
-            int rr = e % kSw2, q = e / kSw2;
-            if (rr < ni && q < nrhs) X[i0 + rr + q * ldx] = sm.xi[rr][q];
-        }
-        __threadfence();
-        __syncthreads();
-        if (t == 0) st_release_i32(&ready[p], 1);
-    }
-}
-
 template <typename T, bool FORWARD, bool UNIT, bool TRANS>
 static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, int64_t ldx, int* flags,
                         int* status, cudaStream_t s)
@@ -376,12 +226,8 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     count_launch();
     SLT_CUDA_TRY(cudaGetLastError());
     SLT_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * size_t(nblk + 1), s));
-    // FP32: the 128-row variant; FP64 keeps 64-row blocks (its 128 x 128
-    // staging tile would not leave room for a second CTA per SM)
-    constexpr bool wide = sizeof(T) == 4;
-    auto fn = wide ? sweep2_kernel<T, FORWARD, UNIT, TRANS> : sweep_kernel<T, FORWARD, UNIT, TRANS>;
-    const size_t smem = wide ? sizeof(Sweep2Smem<T>) : sizeof(SweepSmem<T>);
-    const int64_t nchain = ceildiv(n, wide ? kSw2 : kSwBS);
+    auto fn = sweep_kernel<T, FORWARD, UNIT, TRANS>;
+    const size_t smem = sizeof(SweepSmem<T>);
     static bool cfg = false;
     if (!cfg) {
         SLT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
@@ -391,7 +237,7 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     SLT_CUDA_TRY(cudaGetDevice(&dev));
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, smem));
-    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(nchain, int64_t(sms) * std::max(per, 1)));
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(nblk, int64_t(sms) * std::max(per, 1)));
     const int pidx = prof_begin(SLT_PROF_SWEEP, s);
     fn<<<unsigned(grid), 256, smem, s>>>(n, int(nrhs), M, ldm, Dinv, X, ldx, flags, flags + 1, status);
     count_launch();

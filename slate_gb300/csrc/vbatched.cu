@@ -736,6 +736,8 @@ extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const
     SLT_CUDA_TRY(cudaMemcpyAsync(dsys.p, list.data(), sizeof(Sys) * list.size(), cudaMemcpyHostToDevice, stream));
     SLT_CUDA_TRY(cudaMemsetAsync(ctr.p, 0, sizeof(int) * size_t(itermax + 2), stream));
 
+    TimerSet tm(stream);
+    tm.start("vbatched_mixed::factor_lo");
     // phase 1: norm + cast + FP32 factor + first solve
     const size_t smem_f = std::max(factor_smem(false), sizeof(float) * size_t(std::max(1, maxn)) * size_t(maxr));
     const void* kf = reinterpret_cast<const void*>(&vb_mixed_factor_kernel);
@@ -746,6 +748,8 @@ extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const
     count_launch();
     SLT_CUDA_TRY(cudaGetLastError());
 
+    tm.stop("vbatched_mixed::factor_lo");
+    tm.start("vbatched_mixed::refine");
     // phase 2: itermax + 1 refinement steps, captured once as a CUDA graph
     const size_t smem_r = sizeof(double) * size_t(std::max(1, maxn)) * size_t(maxr);
     const void* kr = reinterpret_cast<const void*>(&vb_refine_kernel);
@@ -768,6 +772,7 @@ extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const
     }
     if (rc == SLT_OK) rc = slt_from_cuda(cudaGraphInstantiate(&exec, graph, 0));
     if (rc == SLT_OK) rc = slt_from_cuda(cudaGraphLaunch(exec, stream));
+    tm.stop("vbatched_mixed::refine");
     if (rc == SLT_OK) rc = slt_from_cuda(cudaStreamSynchronize(stream));
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -787,6 +792,8 @@ extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const
             fb.push_back(s);
         }
     if (fb.empty()) return SLT_OK;
+    tm.start("vbatched_mixed::fallback");
+    struct StopAtExit { TimerSet& t; ~StopAtExit() { t.stop("vbatched_mixed::fallback"); } } stop_fb{tm};
     const size_t smem_p = std::max(factor_smem(true), sizeof(double) * size_t(std::max(1, maxn)) * size_t(maxr));
     return run_plain(fb, d_info, stream, smem_p);
 }
