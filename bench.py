@@ -587,8 +587,17 @@ def main():
             peak, bound, unit = peaks.get("hbm_gbs", 6800.0), "hbm", "GB/s"
             src = "MEASURED_PEAKS.json hbm_gbs"
             achieved = d["bytes"] / d["seconds"] / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+        if os.path.exists(tp):
+            t = json.load(open(tp)).get(dom[0])
+            if t and d["launches"]:
+                # the captured launch's DRAM bytes, scaled by algorithmic bytes per launch
+                traffic = t["dram_bytes"] * (d["bytes"] / d["launches"]) / t["algorithmic_bytes"]
         roof = {"kernel": dom[0], "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-                "frac": achieved / peak, "traffic": None, "peak_source": src,
+                "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch",
+                "algorithmic_bytes_per_launch": d["bytes"] / d["launches"] if d["launches"] else None,
+                "peak_source": src,
                 "launches_per_step": d["launches"] / args.steps,
                 "share_of_step": d["seconds"] / (t_step * args.steps)}
     cpu = cpu_baseline_sample(args) if (ws == 1 and rank == 0 and not args.no_cpu) else None

@@ -35,7 +35,7 @@ typedef intptr_t slate_mpi_comm_t;   /* MPI_Comm placeholder, ignored */
 
 typedef char slate_Uplo;             /* 'U', 'L' (include/slate/c_api/types.h) */
 typedef char slate_Target;           /* 'H', 'T', 'N', 'B', 'D' */
-typedef char slate_MethodLU;         /* '*', 'P' supported; 'C', 'N', 'R', 'B' rejected */
+typedef char slate_MethodLU;         /* '*', 'P', 'N' (NoPiv) supported; 'C', 'R', 'B' rejected */
 
 typedef void* slate_Options;
 typedef struct slate_Pivots_struct* slate_Pivots;

@@ -90,6 +90,25 @@ int slt_dgetrs_device(int64_t n, int64_t nrhs, const double* dLU, int64_t lda, c
                       double* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream);
 int slt_sgetrs_device(int64_t n, int64_t nrhs, const float* dLU, int64_t lda, const int* d_ipiv,
                       float* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream);
+/* slate::getrs with Op::Trans / ConjTrans (real: the same), src/getrs.cc:66-117;
+ * trans = 'N' is slt_dgetrs_device. */
+int slt_dgetrs_trans_device(char trans, int64_t n, int64_t nrhs, const double* dLU, int64_t lda,
+                            const int* d_ipiv, double* dB, int64_t ldb, const slt_options* opts,
+                            slt_stream_t stream);
+/* slate::gecondest (src/gecondest.cc) from getrf's factors and slate::pocondest
+ * (src/pocondest.cc) from potrf's: reciprocal condition number estimate in
+ * the 1-norm ('1') or infinity norm ('I'); anorm = ||A|| in that norm. */
+int slt_dgecondest_device(char norm, int64_t n, const double* dLU, int64_t lda, const int* d_ipiv,
+                          double anorm, double* rcond, const slt_options* opts, slt_stream_t stream);
+int slt_dpocondest_device(char norm, int64_t n, const double* dL, int64_t lda, double anorm,
+                          double* rcond, const slt_options* opts, slt_stream_t stream);
+/* slate::getri (src/getri.cc): dA (getrf's factors) <- A^{-1}; slate::potri
+ * (src/potri.cc): dA (potrf's lower factor) <- lower triangle of A^{-1}.
+ * *info = i > 0 when the i-th diagonal entry of the factor is exactly zero. */
+int slt_dgetri_device(int64_t n, double* dA, int64_t lda, const int* d_ipiv, const slt_options* opts,
+                      slt_stream_t stream, int64_t* info);
+int slt_dpotri_device(int64_t n, double* dA, int64_t lda, const slt_options* opts, slt_stream_t stream,
+                      int64_t* info);
 /* slate::gesv, src/gesv.cc:85-109 */
 int slt_dgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv,
                      double* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream,
@@ -237,6 +256,21 @@ void slate_dsposv_(const char* uplo, const int* n, const int* nrhs, double* a, c
 void slate_dposv_(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda,
                   double* b, const int* ldb, int* info);
 void slate_dpotrf_(const char* uplo, const int* n, double* a, const int* lda, int* info);
+/* lapack_api/lapack_getri.cc, lapack_potri.cc, lapack_gecon.cc, lapack_pocon.cc
+ * (gecon / pocon take the factors without pivots, as LAPACK's do; work and
+ * iwork are not used) */
+void slate_dgetri(const int* n, double* a, const int* lda, int* ipiv, double* work, const int* lwork, int* info);
+void slate_dgetri_(const int* n, double* a, const int* lda, int* ipiv, double* work, const int* lwork, int* info);
+void slate_dpotri(const char* uplo, const int* n, double* a, const int* lda, int* info);
+void slate_dpotri_(const char* uplo, const int* n, double* a, const int* lda, int* info);
+void slate_dgecon(const char* norm, const int* n, double* a, const int* lda, double* anorm, double* rcond,
+                  double* work, int* iwork, int* info);
+void slate_dgecon_(const char* norm, const int* n, double* a, const int* lda, double* anorm, double* rcond,
+                   double* work, int* iwork, int* info);
+void slate_dpocon(const char* uplo, const int* n, double* a, const int* lda, double* anorm, double* rcond,
+                  double* work, int* iwork, int* info);
+void slate_dpocon_(const char* uplo, const int* n, double* a, const int* lda, double* anorm, double* rcond,
+                   double* work, int* iwork, int* info);
 
 #ifdef __cplusplus
 }

@@ -175,14 +175,52 @@ def getrf(A, opts=None):
     return int(info.value), ipiv[:min(m, n)]
 
 
-def getrs(A, ipiv, B, opts=None):
-    """Solve A X = B with the factors of getrf; B is overwritten (slate::getrs)."""
+def getrs(A, ipiv, B, opts=None, trans="N"):
+    """Solve op(A) X = B with the factors of getrf, op = trans ('N', 'T' or
+    'C'); B is overwritten (slate::getrs)."""
     import torch
     po, o = _opts(opts)
     n = A.shape[0]
+    if trans.upper() != "N":
+        if A.dtype != torch.float64:
+            raise TypeError("transposed getrs is FP64")
+        f = lib().slt_dgetrs_trans_device
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_char, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(_Options), ctypes.c_void_p]
+        _check(f(trans.upper().encode(), n, B.shape[1], _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), _dev(B),
+                 _ld(B), po, _stream()))
+        return
     f = lib().slt_dgetrs_device if A.dtype == torch.float64 else lib().slt_sgetrs_device
     _check(f(n, B.shape[1], _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), _dev(B), _ld(B), po,
              _stream()))
+
+
+def gecondest(LU, ipiv, anorm, norm="1", opts=None):
+    """slate::gecondest: reciprocal condition number estimate from getrf's
+    factors; anorm = ||A|| in `norm` ('1' or 'I')."""
+    po, o = _opts(opts)
+    f = lib().slt_dgecondest_device
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_double,
+                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_Options), ctypes.c_void_p]
+    r = ctypes.c_double(0.0)
+    _check(f(norm.encode(), LU.shape[0], _dev(LU), _ld(LU), ctypes.c_void_p(ipiv.data_ptr()), float(anorm),
+             ctypes.byref(r), po, _stream()))
+    return r.value
+
+
+def pocondest(L, anorm, norm="1", opts=None):
+    """slate::pocondest: reciprocal condition number estimate from potrf's
+    lower factor; anorm = ||A||."""
+    po, o = _opts(opts)
+    f = lib().slt_dpocondest_device
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_char, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_double,
+                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_Options), ctypes.c_void_p]
+    r = ctypes.c_double(0.0)
+    _check(f(norm.encode(), L.shape[0], _dev(L), _ld(L), float(anorm), ctypes.byref(r), po, _stream()))
+    return r.value
 
 
 def gesv(A, B, opts=None):

@@ -72,14 +72,18 @@ slt_options opts_for(slate_Options h, int64_t nb)
     if (h) o = static_cast<COpts*>(h)->o;
     else slt_options_default(&o);
     o.nb = nb;        // the matrix's tile size, as in SLATE
+    // MethodLU::NoPiv: keep every diagonal pivot (src/getrf_nopiv.cc), which
+    // the panel's threshold rule gives with threshold 0
+    if (h && static_cast<COpts*>(h)->method_lu == 'N') o.pivot_threshold = 0.0;
     return o;
 }
 
+// MethodLU::PartialPiv (and Auto) and NoPiv are served; CALU, RBT and BEAM are not.
 bool lu_method_ok(slate_Options h)
 {
     if (!h) return true;
     const char m = static_cast<COpts*>(h)->method_lu;
-    return m == '*' || m == 'P';
+    return m == '*' || m == 'P' || m == 'N';
 }
 
 void finish(int status, int64_t info)

@@ -197,6 +197,22 @@ int slt_dgetrs_device(int64_t n, int64_t nrhs, const double* dLU, int64_t lda, c
     return finish_factor(st.fc, nullptr, s);
 }
 
+int slt_dgetrs_trans_device(char trans, int64_t n, int64_t nrhs, const double* dLU, int64_t lda,
+                            const int* d_ipiv, double* dB, int64_t ldb, const slt_options* opts,
+                            slt_stream_t stream)
+{
+    if (trans == 'N' || trans == 'n') return slt_dgetrs_device(n, nrhs, dLU, lda, d_ipiv, dB, ldb, opts, stream);
+    if (trans != 'T' && trans != 't' && trans != 'C' && trans != 'c') return SLT_ERR_ARG;
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    Status st;
+    int rc = st.init(s);
+    if (rc) return rc;
+    rc = getrs_trans_dev<double>(n, nrhs, dLU, lda, d_ipiv, o.nb, dB, ldb, st.fc.d_status, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, nullptr, s);
+}
+
 int slt_sgetrs_device(int64_t n, int64_t nrhs, const float* dLU, int64_t lda, const int* d_ipiv,
                       float* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream)
 {
@@ -454,7 +470,7 @@ static void lapack_getrs_impl(char trans, int n, int nrhs, double* a, int lda, i
                               int* info)
 {
     *info = 0;
-    if (trans != 'N' && trans != 'n') { *info = -1; return; }
+    if (std::strchr("NnTtCc", trans) == nullptr || trans == 0) { *info = -1; return; }
     if (n < 0) { *info = -2; return; }
     if (nrhs < 0) { *info = -3; return; }
     if (lda < std::max(1, n)) { *info = -5; return; }
@@ -467,7 +483,7 @@ static void lapack_getrs_impl(char trans, int n, int nrhs, double* a, int lda, i
     DevBuf dA, dB, dP;
     if (to_device(a, n, n, lda, dA, s) || to_device(b, n, nrhs, ldb, dB, s) ||
         to_device(rel.data(), n, 1, n, dP, s)) { *info = -100; return; }
-    int rc = slt_dgetrs_device(n, nrhs, dA.as<double>(), n, dP.as<int>(), dB.as<double>(), n, &o, s);
+    int rc = slt_dgetrs_trans_device(trans, n, nrhs, dA.as<double>(), n, dP.as<int>(), dB.as<double>(), n, &o, s);
     if (rc) { *info = -1000 + rc; return; }
     if (to_host(dB, b, n, nrhs, ldb, s) || cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
 }

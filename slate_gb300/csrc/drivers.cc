@@ -66,12 +66,12 @@ static int k_gemm(char tb, int64_t m, int64_t n, int64_t k, float alpha, const f
     return slt_sgemm(tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower, s);
 }
 
-static int k_panel(int64_t prows, int64_t nbk, int64_t ib, double* P, int64_t ld, int* ipiv, int* info,
+static int k_panel(int64_t prows, int64_t nbk, int64_t ib, double thr, double* P, int64_t ld, int* ipiv, int* info,
                    int64_t off, void* ws, int* status, cudaStream_t s)
-{ return slt_dgetrf_panel(prows, nbk, ib, P, ld, ipiv, info, off, ws, status, s); }
-static int k_panel(int64_t prows, int64_t nbk, int64_t ib, float* P, int64_t ld, int* ipiv, int* info,
+{ return slt_dgetrf_panel(prows, nbk, ib, P, ld, ipiv, info, off, thr, ws, status, s); }
+static int k_panel(int64_t prows, int64_t nbk, int64_t ib, double thr, float* P, int64_t ld, int* ipiv, int* info,
                    int64_t off, void* ws, int* status, cudaStream_t s)
-{ return slt_sgetrf_panel(prows, nbk, ib, P, ld, ipiv, info, off, ws, status, s); }
+{ return slt_sgetrf_panel(prows, nbk, ib, P, ld, ipiv, info, off, thr, ws, status, s); }
 
 static int k_laswp(const int* plan, int64_t maxc, double* A, int64_t lda, int64_t nc, cudaStream_t s)
 { return slt_dlaswp_plan(plan, maxc, A, lda, nc, s); }
@@ -157,7 +157,8 @@ int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_opti
         const int64_t prows = m - r0;
         const int64_t diag = std::min(prows, nbk);
         T* P = A + r0 + r0 * lda;
-        TRY(k_panel(prows, nbk, ib, P, lda, ipiv + r0, fc.d_info, r0, pws.p, fc.d_status, s));
+        const double thr = (o.pivot_threshold >= 0.0 && o.pivot_threshold <= 1.0) ? o.pivot_threshold : 1.0;
+        TRY(k_panel(prows, nbk, ib, thr, P, lda, ipiv + r0, fc.d_info, r0, pws.p, fc.d_status, s));
         TRY(slt_swap_plan(ipiv + r0, diag, r0, plan.as<int>(), s));
         const int64_t c1 = r0 + nbk;
         TRY(k_laswp(plan.as<int>(), 2 * diag, A + c1 * lda, lda, n - c1, s));
@@ -201,6 +202,32 @@ int getrs_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv
         TRY(k_sweep(1, n, nc, LU, lda, w, n, flags.as<int>(), d_status, s));
         SLT_CUDA_TRY(cudaMemcpy2DAsync(B + c0 * ldb, size_t(ldb) * sizeof(T), w, size_t(n) * sizeof(T),
                                        size_t(n) * sizeof(T), size_t(nc), cudaMemcpyDeviceToDevice, s));
+    }
+    return SLT_OK;
+}
+
+// getrs Trans (src/getrs.cc:66-117 with Op::Trans): A^T X = B with
+// P A = L U is U^T L^T P X = B: a forward sweep with U^T, a backward sweep
+// with L^T, then the inverse row permutation.
+template <typename T>
+int getrs_trans_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv, int64_t nb,
+                    T* B, int64_t ldb, int* d_status, cudaStream_t s)
+{
+    if (n < 0 || nrhs < 0) return SLT_ERR_ARG;
+    if (n == 0 || nrhs == 0) return SLT_OK;
+    DevBuf perm, W, flags;
+    TRY(perm.alloc(sizeof(int) * size_t(n), s));
+    TRY(W.alloc(sizeof(T) * size_t(n) * size_t(std::min<int64_t>(nrhs, 16)), s));
+    TRY(flags.alloc(slt_sweep_flags_bytes(n), s));
+    TRY(slt_perm_from_ipiv(ipiv, n, nb, perm.as<int>(), s));
+    T* w = W.as<T>();
+    for (int64_t c0 = 0; c0 < nrhs; c0 += 16) {
+        const int64_t nc = std::min<int64_t>(16, nrhs - c0);
+        SLT_CUDA_TRY(cudaMemcpy2DAsync(w, size_t(n) * sizeof(T), B + c0 * ldb, size_t(ldb) * sizeof(T),
+                                       size_t(n) * sizeof(T), size_t(nc), cudaMemcpyDeviceToDevice, s));
+        TRY(k_sweep(4, n, nc, LU, lda, w, n, flags.as<int>(), d_status, s));
+        TRY(k_sweep(5, n, nc, LU, lda, w, n, flags.as<int>(), d_status, s));
+        TRY(k_permute(0, perm.as<int>(), n, nc, w, n, B + c0 * ldb, ldb, s));
     }
     return SLT_OK;
 }
@@ -258,6 +285,8 @@ template int getrf_dev<double>(int64_t, int64_t, double*, int64_t, int*, const s
 template int getrf_dev<float>(int64_t, int64_t, float*, int64_t, int*, const slt_options&, FactorCtx&, cudaStream_t);
 template int getrs_dev<double>(int64_t, int64_t, const double*, int64_t, const int*, int64_t, double*, int64_t, int*, cudaStream_t);
 template int getrs_dev<float>(int64_t, int64_t, const float*, int64_t, const int*, int64_t, float*, int64_t, int*, cudaStream_t);
+template int getrs_trans_dev<double>(int64_t, int64_t, const double*, int64_t, const int*, int64_t, double*, int64_t, int*, cudaStream_t);
+template int getrs_trans_dev<float>(int64_t, int64_t, const float*, int64_t, const int*, int64_t, float*, int64_t, int*, cudaStream_t);
 template int potrf_dev<double>(int64_t, double*, int64_t, const slt_options&, FactorCtx&, cudaStream_t);
 template int potrf_dev<float>(int64_t, float*, int64_t, const slt_options&, FactorCtx&, cudaStream_t);
 template int potrs_dev<double>(int64_t, int64_t, const double*, int64_t, int64_t, double*, int64_t, int*, cudaStream_t);

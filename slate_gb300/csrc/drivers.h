@@ -97,6 +97,9 @@ template <typename T>
 int getrs_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv, int64_t nb,
               T* B, int64_t ldb, int* d_status, cudaStream_t s);
 template <typename T>
+int getrs_trans_dev(int64_t n, int64_t nrhs, const T* LU, int64_t lda, const int* ipiv, int64_t nb,
+              T* B, int64_t ldb, int* d_status, cudaStream_t s);
+template <typename T>
 int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc, cudaStream_t s);
 template <typename T>
 int potrs_dev(int64_t n, int64_t nrhs, const T* L, int64_t lda, int64_t nb, T* B, int64_t ldb,

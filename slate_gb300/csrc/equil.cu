@@ -90,17 +90,35 @@ __global__ void sym_scale_kernel(int64_t n, const double* __restrict__ A, int64_
     d[i] = s;
 }
 
-// B = D(r_i * A_ij * c_j) with r or c null meaning 1.  Each thread handles
-// four rows of one column (1024 rows per block), so that every warp keeps
-// four coalesced loads in flight.
-template <typename S, typename D>
+// x 2^k without a floating-point multiply (the FP64 pipe is the slow one on
+// this part): add k to the exponent field when x and the result are normal
+// numbers; zeros, subnormals, Inf/NaN and out-of-range results take the
+// multiply.
+__device__ __forceinline__ double scale_pow2(double x, int k)
+{
+    const long long b = __double_as_longlong(x);
+    const int e = int((b >> 52) & 0x7ff);
+    if (e == 0 || e == 0x7ff || e + k <= 0 || e + k >= 0x7ff) return x * ldexp(1.0, k);
+    return __longlong_as_double(b + (static_cast<long long>(k) << 52));
+}
+
+// k of a power-of-two scale 2^k (the scales above are exact powers of two)
+__device__ __forceinline__ int pow2_exponent(double s)
+{
+    return int((__double_as_longlong(s) >> 52) & 0x7ff) - 1023;
+}
+
+// B = D(r_i * A_ij * c_j); SCALED = false: B = D(A) (r, c unused).  Each
+// thread handles four rows of one column (1024 rows per block), so that every
+// warp keeps four coalesced loads in flight.
+template <typename S, typename D, bool SCALED>
 __global__ void convert_scaled_kernel(int64_t m, int64_t n, const S* __restrict__ A, int64_t lda,
                                       const double* __restrict__ r, const double* __restrict__ c,
                                       D* __restrict__ B, int64_t ldb)
 {
     const int64_t i0 = int64_t(blockIdx.x) * 1024 + threadIdx.x;
     for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
-        const double cj = c ? c[j] : 1.0;
+        const int kc = (SCALED && c) ? pow2_exponent(c[j]) : 0;
         S v[4];
         #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -110,7 +128,10 @@ __global__ void convert_scaled_kernel(int64_t m, int64_t n, const S* __restrict_
         #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int64_t i = i0 + 256 * k;
-            if (i < m) B[i + j * ldb] = D(double(v[k]) * (r ? r[i] : 1.0) * cj);
+            if (i < m) {
+                if (SCALED) B[i + j * ldb] = D(scale_pow2(double(v[k]), (r ? pow2_exponent(r[i]) : 0) + kc));
+                else B[i + j * ldb] = D(v[k]);
+            }
         }
     }
 }
@@ -154,7 +175,8 @@ extern "C" int slt_convert_d2s_scaled(int64_t m, int64_t n, const double* A, int
 {
     if (m <= 0 || n <= 0) return SLT_OK;
     dim3 g(unsigned(ceildiv(m, 1024)), unsigned(std::min<int64_t>(n, 65535)));
-    convert_scaled_kernel<double, float><<<g, 256, 0, stream>>>(m, n, A, lda, r, c, B, ldb);
+    if (r || c) convert_scaled_kernel<double, float, true><<<g, 256, 0, stream>>>(m, n, A, lda, r, c, B, ldb);
+    else convert_scaled_kernel<double, float, false><<<g, 256, 0, stream>>>(m, n, A, lda, r, c, B, ldb);
     count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
@@ -165,7 +187,8 @@ extern "C" int slt_convert_s2d_scaled(int64_t m, int64_t n, const float* B, int6
 {
     if (m <= 0 || n <= 0) return SLT_OK;
     dim3 g(unsigned(ceildiv(m, 1024)), unsigned(std::min<int64_t>(n, 65535)));
-    convert_scaled_kernel<float, double><<<g, 256, 0, stream>>>(m, n, B, ldb, r, nullptr, X, ldx);
+    if (r) convert_scaled_kernel<float, double, true><<<g, 256, 0, stream>>>(m, n, B, ldb, r, nullptr, X, ldx);
+    else convert_scaled_kernel<float, double, false><<<g, 256, 0, stream>>>(m, n, B, ldb, r, nullptr, X, ldx);
     count_launch();
     return slt_from_cuda(cudaGetLastError());
 }

@@ -44,6 +44,7 @@ struct PanelExchange {
 template <typename T>
 struct PanelArgs {
     int64_t prows, nbk, ib, ld, rows_per_block, info_offset;
+    double threshold;   // SLATE's PivotThreshold: keep the diagonal when |a_jj| >= threshold * max
     T* P;
     int* ipiv;
     int* info;
@@ -232,6 +233,11 @@ getrf_panel_kernel(PanelArgs<T> a)
                         gwb = -1;
                         gv = __ldcg(&P[j + j * ld]);
                     }
+                    else if (a.threshold < 1.0 && grow != int(j)) {
+                        // threshold rule (Tile_getrf.hh:272-289): keep the diagonal
+                        const T dv = ((volatile T*) ex->diag_rowvals[par])[j - k0];
+                        if (fabs(dv) >= gav * T(a.threshold)) { grow = int(j); gwb = -1; gv = dv; }
+                    }
                     s_p = grow;
                     s_wb = gwb;
                     s_pval = gv;
@@ -413,6 +419,11 @@ getrf_panel2_kernel(PanelArgs<T> a, int* flags)
                         gwb = -1;
                         gv = ((volatile T*) ex->diag_rowvals[par])[jc];
                     }
+                    else if (a.threshold < 1.0 && grow != int(j)) {
+                        // threshold rule (Tile_getrf.hh:272-289): keep the diagonal
+                        const T dv = ((volatile T*) ex->diag_rowvals[par])[jc];
+                        if (fabs(dv) >= gav * T(a.threshold)) { grow = int(j); gwb = -1; gv = dv; }
+                    }
                     s_p = grow;
                     s_wb = gwb;
                     s_pval = gv;
@@ -581,7 +592,8 @@ __global__ void permute_rows_kernel(int forward, const int* __restrict__ perm, i
 
 template <typename T>
 static int launch_panel(int64_t prows, int64_t nbk, int64_t ib, T* P, int64_t ld, int* ipiv,
-                        int* info, int64_t info_offset, void* ws, int* status, cudaStream_t stream)
+                        int* info, int64_t info_offset, double threshold, void* ws, int* status,
+                        cudaStream_t stream)
 {
     if (prows <= 0 || nbk <= 0) return SLT_OK;
     if (ib <= 0 || ib > kMaxIb) return SLT_ERR_ARG;
@@ -608,6 +620,7 @@ static int launch_panel(int64_t prows, int64_t nbk, int64_t ib, T* P, int64_t ld
     PanelArgs<T> args;
     args.prows = prows; args.nbk = nbk; args.ib = ib; args.ld = ld;
     args.rows_per_block = R; args.info_offset = info_offset;
+    args.threshold = threshold;
     args.P = P; args.ipiv = ipiv; args.info = info; args.status = status;
     args.bar = bar; args.ex = ex;
     // staged variant when the block's stripe rows fit in shared memory
@@ -676,17 +689,17 @@ extern "C" size_t slt_getrf_panel_ws_bytes(int64_t prows, int64_t ib)
 }
 
 extern "C" int slt_dgetrf_panel(int64_t prows, int64_t nbk, int64_t ib, double* P, int64_t ld,
-                                int* ipiv, int* info, int64_t info_offset, void* ws, int* status,
-                                cudaStream_t stream)
+                                int* ipiv, int* info, int64_t info_offset, double threshold, void* ws,
+                                int* status, cudaStream_t stream)
 {
-    return launch_panel<double>(prows, nbk, ib, P, ld, ipiv, info, info_offset, ws, status, stream);
+    return launch_panel<double>(prows, nbk, ib, P, ld, ipiv, info, info_offset, threshold, ws, status, stream);
 }
 
 extern "C" int slt_sgetrf_panel(int64_t prows, int64_t nbk, int64_t ib, float* P, int64_t ld,
-                                int* ipiv, int* info, int64_t info_offset, void* ws, int* status,
-                                cudaStream_t stream)
+                                int* ipiv, int* info, int64_t info_offset, double threshold, void* ws,
+                                int* status, cudaStream_t stream)
 {
-    return launch_panel<float>(prows, nbk, ib, P, ld, ipiv, info, info_offset, ws, status, stream);
+    return launch_panel<float>(prows, nbk, ib, P, ld, ipiv, info, info_offset, threshold, ws, status, stream);
 }
 
 extern "C" int slt_swap_plan(const int* ipiv, int64_t len, int64_t r0, int* plan, cudaStream_t stream)

@@ -55,13 +55,14 @@ int slt_tc_status(void);
  * panel's first row; *info (device) receives info_offset + j + 1 for the
  * first exactly-zero pivot (if *info is still 0).  ws: device workspace of
  * slt_getrf_panel_ws_bytes() bytes.  *status (device) receives
- * SLT_ERR_TIMEOUT if a grid barrier ever times out. */
+ * SLT_ERR_TIMEOUT if a grid barrier ever times out.  threshold: SLATE's
+ * PivotThreshold (1 = partial pivoting, 0 = keep the diagonal: no pivoting). */
 size_t slt_getrf_panel_ws_bytes(int64_t prows, int64_t ib);
 int slt_dgetrf_panel(int64_t prows, int64_t nbk, int64_t ib, double* P, int64_t ld,
-                     int* ipiv, int* info, int64_t info_offset, void* ws,
+                     int* ipiv, int* info, int64_t info_offset, double threshold, void* ws,
                      int* status, cudaStream_t stream);
 int slt_sgetrf_panel(int64_t prows, int64_t nbk, int64_t ib, float* P, int64_t ld,
-                     int* ipiv, int* info, int64_t info_offset, void* ws,
+                     int* ipiv, int* info, int64_t info_offset, double threshold, void* ws,
                      int* status, cudaStream_t stream);
 
 /* ---- row interchanges -----------------------------------------------------

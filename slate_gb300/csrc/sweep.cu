@@ -251,7 +251,8 @@ using namespace slt;
 
 // flags: device int[ceil(n/64) + 1] scratch; status: device int (timeouts).
 // kind: 0 unit lower (L of LU), 1 upper non-unit (U of LU), 2 lower
-// non-unit (L of Cholesky), 3 lower^T non-unit (L^T of Cholesky).
+// non-unit (L of Cholesky), 3 lower^T non-unit (L^T of Cholesky), 4 upper^T
+// non-unit (U^T of LU), 5 unit lower^T (L^T of LU).
 extern "C" int slt_dsweep(int kind, int64_t n, int64_t nrhs, const double* M, int64_t ldm, double* X,
                           int64_t ldx, int* flags, int* status, cudaStream_t s)
 {
@@ -260,6 +261,8 @@ extern "C" int slt_dsweep(int kind, int64_t n, int64_t nrhs, const double* M, in
         case 1: return launch_sweep<double, false, false, false>(n, nrhs, M, ldm, X, ldx, flags, status, s);
         case 2: return launch_sweep<double, true, false, false>(n, nrhs, M, ldm, X, ldx, flags, status, s);
         case 3: return launch_sweep<double, false, false, true>(n, nrhs, M, ldm, X, ldx, flags, status, s);
+        case 4: return launch_sweep<double, true, false, true>(n, nrhs, M, ldm, X, ldx, flags, status, s);
+        case 5: return launch_sweep<double, false, true, true>(n, nrhs, M, ldm, X, ldx, flags, status, s);
         default: return SLT_ERR_ARG;
     }
 }
@@ -272,6 +275,8 @@ extern "C" int slt_ssweep(int kind, int64_t n, int64_t nrhs, const float* M, int
         case 1: return launch_sweep<float, false, false, false>(n, nrhs, M, ldm, X, ldx, flags, status, s);
         case 2: return launch_sweep<float, true, false, false>(n, nrhs, M, ldm, X, ldx, flags, status, s);
         case 3: return launch_sweep<float, false, false, true>(n, nrhs, M, ldm, X, ldx, flags, status, s);
+        case 4: return launch_sweep<float, true, false, true>(n, nrhs, M, ldm, X, ldx, flags, status, s);
+        case 5: return launch_sweep<float, false, true, true>(n, nrhs, M, ldm, X, ldx, flags, status, s);
         default: return SLT_ERR_ARG;
     }
 }

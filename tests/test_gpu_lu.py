@@ -146,3 +146,38 @@ def test_float32_getrf(orc, slt):
     robust = mg > 1 + 1e3 * n * np.finfo(np.float32).eps
     gip = slt.ipiv_to_lapack(ipiv, nb)
     assert np.array_equal(gip[robust], oipiv[robust])
+
+
+@pytest.mark.parametrize("thr", [0.5, 0.1])
+def test_getrf_pivot_threshold(orc, slt, thr):
+    """SLATE's PivotThreshold rule (Tile_getrf.hh:272-289): the diagonal is
+    kept when |a_jj| >= threshold * max |a_ij|; pivots equal the oracle's."""
+    import torch
+    n, nb, ib = 500, 128, 32
+    A = orc.generate(2, 81, n, n)
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=nb, ib=ib, pivot_threshold=thr))
+    torch.cuda.synchronize()
+    oinfo, pt, po, oipiv, mg = orc.getrf(A.copy(order="F"), nb, ib, threshold=thr, margins=True)
+    assert info == oinfo == 0
+    gip = slt.ipiv_to_lapack(ipiv, nb)
+    robust = mg > 1 + 1e3 * n * EPS
+    assert np.array_equal(gip[robust], oipiv[robust])
+    full = np.arange(1, n + 1)
+    assert (gip != full).sum() < (slt.ipiv_to_lapack(slt.getrf(to_dev(A), slt.Options(nb=nb, ib=ib))[1], nb) != full).sum()
+
+
+def test_getrf_nopiv_via_threshold_zero(orc, slt):
+    """Threshold 0 keeps every diagonal pivot (MethodLU::NoPiv)."""
+    import torch
+    n, nb = 300, 64
+    A = np.asfortranarray(orc.generate(2, 82, n, n) + n * np.eye(n))
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=nb, pivot_threshold=0.0))
+    torch.cuda.synchronize()
+    assert info == 0
+    assert np.array_equal(slt.ipiv_to_lapack(ipiv, nb), np.arange(1, n + 1))
+    LU = to_host(dA)
+    L = np.tril(LU, -1) + np.eye(n)
+    U = np.triu(LU)
+    assert np.abs(L @ U - A).max() <= 1e-12 * np.abs(A).max()
