@@ -351,13 +351,22 @@ def run_mixed_sweep(args, slt, torch, dev, cfg):
         del B
 
 
-def run_config5(args, slt, torch, dev):
-    """Variable-size batch: batched FP64, batched mixed, per-system loop."""
+def run_config5(args, slt, torch, dev, ws=1, rank=0):
+    """Variable-size batch: batched FP64, batched mixed, per-system loop.
+    Under torchrun the systems are split across ranks (longest processing
+    time first, slate_gb300.partition); each rank solves its share with one
+    batched launch and the slowest rank's time is reported."""
     rng = np.random.default_rng(12345)
-    cnt = args.batch
-    ns = np.exp(rng.uniform(np.log(32), np.log(1024), cnt)).astype(np.int64)
-    rs = rng.integers(1, 9, cnt)
-    kinds = (np.arange(cnt) % 2).astype(np.int64)        # even: general, odd: SPD
+    cnt_all = args.batch
+    ns_all = np.exp(rng.uniform(np.log(32), np.log(1024), cnt_all)).astype(np.int64)
+    rs_all = rng.integers(1, 9, cnt_all)
+    kinds_all = (np.arange(cnt_all) % 2).astype(np.int64)        # even: general, odd: SPD
+    sel = np.arange(cnt_all)
+    if ws > 1:
+        from slate_gb300.partition import partition_systems, system_costs
+        sel = partition_systems(system_costs(ns_all, rs_all, kinds_all), ws)[0][rank]
+    ns, rs, kinds = ns_all[sel], rs_all[sel], kinds_all[sel]
+    cnt = len(sel)
     offA = np.concatenate([[0], np.cumsum(ns * ns)])
     offB = np.concatenate([[0], np.cumsum(ns * rs)])
     A0 = torch.empty(int(offA[-1]), dtype=torch.float64, device=dev)
@@ -365,13 +374,14 @@ def run_config5(args, slt, torch, dev):
     for i in range(cnt):
         n, r = int(ns[i]), int(rs[i])
         a = A0[offA[i]:offA[i + 1]].view(n, n).t()
+        gi = int(sel[i])                                  # seeds follow the global system index
         if kinds[i] == 0:
-            slt.generate(2, 10 * i + 1, slt.colmajor(a))
+            slt.generate(2, 10 * gi + 1, slt.colmajor(a))
         else:
             g = slt.colmajor(torch.empty(n, n, dtype=torch.float64, device=dev))
-            slt.generate(3, 10 * i + 1, g)
+            slt.generate(3, 10 * gi + 1, g)
             a.copy_((g @ g.t()) / n + torch.eye(n, dtype=torch.float64, device=dev))
-        slt.generate(2, 10 * i + 2, slt.colmajor(B0[offB[i]:offB[i + 1]].view(r, n).t()))
+        slt.generate(2, 10 * gi + 2, slt.colmajor(B0[offB[i]:offB[i + 1]].view(r, n).t()))
     A = A0.clone()
     B = B0.clone()
     X = torch.zeros_like(B0)
@@ -383,7 +393,7 @@ def run_config5(args, slt, torch, dev):
     sysv = views(A, B)
     Xv = [X[offB[i]:offB[i + 1]].view(int(rs[i]), int(ns[i])).t() for i in range(cnt)]
     vb = slt.VBatch(sysv, X=Xv)
-    flops = float(np.sum(np.where(kinds == 0, 2.0 * ns**3 / 3, ns**3 / 3.0) + 2.0 * ns * ns * rs))
+    flops = float(np.sum(np.where(kinds_all == 0, 2.0 * ns_all**3 / 3, ns_all**3 / 3.0) + 2.0 * ns_all * ns_all * rs_all))
 
     def berr_max(Xbuf):
         worst = 0.0
@@ -407,6 +417,14 @@ def run_config5(args, slt, torch, dev):
         B.copy_(B0)
         t, info = _event_time(torch, lambda: slt.solve_vbatched(vb))
         ts.append(t)
+    def tmax(t):
+        if ws > 1:
+            tt = torch.tensor([t], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            return float(tt.item())
+        return t
+    ts[-1] = tmax(ts[-1])
+    rec["n_gpus"] = ws
     rec["batched_fp64_ms"] = ts[-1] * 1e3
     rec["batched_fp64_tflops"] = flops / ts[-1] / 1e12
     rec["batched_fp64_info_nonzero"] = int((info != 0).sum())
@@ -419,13 +437,17 @@ def run_config5(args, slt, torch, dev):
         X.zero_()
         t, (info, iters) = _event_time(torch, lambda: slt.solve_mixed_vbatched(vb, slt.Options()))
         ts.append(t)
+    ts[-1] = tmax(ts[-1])
     rec["batched_mixed_ms"] = ts[-1] * 1e3
     rec["batched_mixed_effective_tflops"] = flops / ts[-1] / 1e12
     rec["batched_mixed_phase_ms"] = {k: slt.timer("vbatched_mixed::" + k) * 1e3 for k in ("factor_lo", "refine", "fallback")}
     rec["batched_mixed_iter_hist"] = {str(int(v)): int(c) for v, c in zip(*np.unique(iters, return_counts=True))}
     rec["batched_mixed_berr_max"] = berr_max(X)
-    if args.no_loop:
-        print(json.dumps(rec))
+    if args.no_loop or ws > 1:
+        if rank == 0:
+            print(json.dumps(rec))
+        if ws > 1:
+            torch.distributed.destroy_process_group()
         return
     # per-system loop of the library's own gesv / posv (FP64), A, B restored first
     A.copy_(A0)
@@ -454,12 +476,18 @@ def main():
     import torch
     import slate_gb300 as slt
     if args.config != 2:
-        torch.cuda.set_device(0)
-        dev = torch.device("cuda", 0)
+        ws, rank, local = dist_env()
+        if args.config == 5 and ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl")
+        elif ws > 1 and rank != 0:
+            return                      # configs 1, 3, 4: one replica on rank 0
+        torch.cuda.set_device(local)
+        dev = torch.device("cuda", local)
         if args.config == 1:
             return run_config1(args, slt, torch, dev)
         if args.config == 5:
-            return run_config5(args, slt, torch, dev)
+            return run_config5(args, slt, torch, dev, ws, rank)
         return run_mixed_sweep(args, slt, torch, dev, args.config)
     ws, rank, local = dist_env()
     if ws > 1:
