@@ -69,7 +69,18 @@ enum slt_refine {
 
 void slt_options_default(slt_options* opts);
 
-/* Status codes returned by the device layer (0 = success). */
+/* Status codes returned by the device layer (0 = success; CUDA errors are
+ * SLT_ERR_CUDA_BASE + the cudaError_t value). */
+#ifndef SLT_OK
+#define SLT_OK                 0
+#define SLT_ERR_ARG           -1
+#define SLT_ERR_TIMEOUT       -2
+#define SLT_ERR_NOMEM         -3
+#define SLT_ERR_NOT_SUPPORTED -4
+#define SLT_ERR_NO_DEVICE     -5
+#define SLT_ERR_LIMIT         -6
+#define SLT_ERR_CUDA_BASE   1000
+#endif
 const char* slt_status_string(int status);
 
 /* Library version string. */

@@ -381,3 +381,27 @@ int64_t slate_gb300_last_info(void) { return g_info; }
 int slate_gb300_last_status(void) { return g_status; }
 
 } // extern "C"
+
+// ---- small helpers for the header-only C++ API (include/slate_gb300.hh): the
+// per-panel pivot arrays live in device memory and the header stays free of
+// CUDA includes.
+extern "C" {
+
+int slt_ipiv_alloc(int64_t n, int** d)
+{
+    if (!d || n < 0) return SLT_ERR_ARG;
+    return slt_from_cuda(cudaMalloc(reinterpret_cast<void**>(d), sizeof(int) * size_t(n > 0 ? n : 1)));
+}
+int slt_ipiv_free(int* d) { return d ? slt_from_cuda(cudaFree(d)) : SLT_OK; }
+int slt_ipiv_download(const int* d, int64_t n, int* h)
+{
+    if (n <= 0) return SLT_OK;
+    return slt_from_cuda(cudaMemcpy(h, d, sizeof(int) * size_t(n), cudaMemcpyDeviceToHost));
+}
+int slt_ipiv_upload(const int* h, int64_t n, int* d)
+{
+    if (n <= 0) return SLT_OK;
+    return slt_from_cuda(cudaMemcpy(d, h, sizeof(int) * size_t(n), cudaMemcpyHostToDevice));
+}
+
+}  // extern "C"

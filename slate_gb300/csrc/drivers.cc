@@ -549,7 +549,7 @@ int fallback_fp64(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int
 // number of Arnoldi steps any column took.
 static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
                            const double* B, int64_t ldb, double* X, int64_t ldx, const slt_options& o,
-                           int* iter, int64_t* info, cudaStream_t s)
+                           int* iter, int64_t* info, cudaStream_t s, bool stop_early = false)
 {
     if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
     *iter = 0;
@@ -641,6 +641,7 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
                 TRY(g.run(B + c * ldb, ldb, X + c * ldx, ldx, itermax - ir_steps, &used, &cc, s, true));
                 all = all && cc;
                 worst = std::max(worst, used);
+                if (!cc && stop_early) break;
             }
             tm.stop(std::string(pfx) + "::gmres");
             if (all) { conv = true; *iter = int(ir_steps + worst); }
@@ -663,7 +664,8 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
 // factorisation.
 static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int* ipiv,
                                  const double* B, int64_t ldb, double* X, int64_t ldx,
-                                 const slt_options& o, int* iter, int64_t* info, cudaStream_t s)
+                                 const slt_options& o, int* iter, int64_t* info, cudaStream_t s,
+                                 bool stop_early = false)
 {
     if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(1, n)) return SLT_ERR_ARG;
     *iter = 0;
@@ -714,6 +716,8 @@ static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, i
             bool conv = false;
             TRY(g.run(b, ldb, x, ldx, itermax, &citer, &conv, s));
             if (!conv) { all_conv = false; citer = int(-itermax - 1); }
+            // a first attempt that the FP32 retry will redo: one failed column decides it
+            if (!conv && stop_early) { worst_iter = citer; break; }
             worst_iter = (c == 0) ? citer : (citer < 0 || worst_iter < 0 ? std::min(worst_iter, citer)
                                                                         : std::max(worst_iter, citer));
         }
@@ -744,14 +748,14 @@ static bool ladder_on(const slt_options& o)
 template <typename F>
 static int with_ladder(F once, const slt_options& o, const char* key, int* iter, int64_t* info)
 {
-    if (!ladder_on(o)) return once(o);
+    if (!ladder_on(o)) return once(o, false);
     slt_options o1 = o;
     o1.use_fallback = 0;
-    TRY(once(o1));
+    TRY(once(o1, true));
     if (*iter >= 0) return SLT_OK;
     slt_options o2 = o;
     o2.factor_precision = SLT_PREC_FP32;
-    const int rc = once(o2);
+    const int rc = once(o2, false);
     t_timers[key] = 1.0;          // marks that the FP32 retry ran
     (void) info;
     return rc;
@@ -762,8 +766,8 @@ int gesv_mixed_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t lda, in
                    int* iter, int64_t* info, cudaStream_t s)
 {
     t_timers.erase(chol ? "posv_mixed::retry_fp32" : "gesv_mixed::retry_fp32");
-    return with_ladder([&](const slt_options& oo) {
-        return gesv_mixed_once(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, oo, iter, info, s);
+    return with_ladder([&](const slt_options& oo, bool first) {
+        return gesv_mixed_once(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, oo, iter, info, s, first);
     }, o, chol ? "posv_mixed::retry_fp32" : "gesv_mixed::retry_fp32", iter, info);
 }
 
@@ -772,8 +776,8 @@ int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t l
                          const slt_options& o, int* iter, int64_t* info, cudaStream_t s)
 {
     t_timers.erase(chol ? "posv_mixed_gmres::retry_fp32" : "gesv_mixed_gmres::retry_fp32");
-    return with_ladder([&](const slt_options& oo) {
-        return gesv_mixed_gmres_once(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, oo, iter, info, s);
+    return with_ladder([&](const slt_options& oo, bool first) {
+        return gesv_mixed_gmres_once(chol, n, nrhs, A, lda, ipiv, B, ldb, X, ldx, oo, iter, info, s, first);
     }, o, chol ? "posv_mixed_gmres::retry_fp32" : "gesv_mixed_gmres::retry_fp32", iter, info);
 }
 

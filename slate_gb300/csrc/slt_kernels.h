@@ -16,6 +16,7 @@ extern "C" {
 #endif
 
 /* status codes */
+#ifndef SLT_OK
 #define SLT_OK                 0
 #define SLT_ERR_ARG           -1
 #define SLT_ERR_TIMEOUT       -2
@@ -24,6 +25,7 @@ extern "C" {
 #define SLT_ERR_NO_DEVICE     -5
 #define SLT_ERR_LIMIT         -6
 #define SLT_ERR_CUDA_BASE   1000
+#endif
 
 /* ---- trailing-matrix update GEMM:  C = alpha A op(B) + beta C --------------
  * transb 'N': B is k x n;  'T': B is n x k (C -= A B^T, the Cholesky update).

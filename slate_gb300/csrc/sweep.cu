@@ -206,126 +206,6 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
     }
 }
 
-// FP32 variant of sweep_kernel with self-validating hand-offs: a solved
-// block is published as 64-bit words (tag << 32 | float bits), tag = the
-// block's ticket + 1, in a buffer zeroed before the sweep.  A 64-bit store is
-// single-copy atomic, so a consumer that reads a word with the expected tag
-// has the value: it polls the data itself (one L2 round trip per hand-off)
-// instead of a release flag, a fence and a second load.  Each wait is bounded.
-__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
-{
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-template <bool FORWARD, bool UNIT, bool TRANS>
-__global__ void __launch_bounds__(256)
-sweep_tagged_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, const float* __restrict__ Dinv,
-                    float* X, int64_t ldx, int* ticket, unsigned long long* tagged, int* status)
-{
-    extern __shared__ unsigned char sw_smem_raw[];
-    SweepSmem<float>& sm = *reinterpret_cast<SweepSmem<float>*>(sw_smem_raw);
-    __shared__ int s_p, s_ok;
-    const int t = threadIdx.x;
-    const int nblk = int(ceildiv(n, kSwBS));
-
-    auto opM = [&](int64_t r, int64_t c) -> float {
-        return TRANS ? __ldg(&M[c + r * ldm]) : __ldg(&M[r + c * ldm]);
-    };
-
-    for (;;) {
-        if (t == 0) { s_p = atomicAdd(ticket, 1); s_ok = 1; }
-        __syncthreads();
-        const int p = s_p;
-        if (p >= nblk) break;
-        const int bi = FORWARD ? p : nblk - 1 - p;
-        const int64_t i0 = int64_t(bi) * kSwBS;
-        const int ni = int(min64(kSwBS, n - i0));
-        {
-            const float* dinv = Dinv + size_t(bi) * kSwBS * kSwBS;
-            for (int e = t; e < kSwBS * kSwBS; e += 256) sm.Ds[e / kSwBS][e % kSwBS] = dinv[e];
-        }
-        for (int e = t; e < kSwBS * kSwRhs; e += 256) {
-            int r = e % kSwBS, q = e / kSwBS;
-            sm.xi[r][q] = (r < ni && q < nrhs) ? X[i0 + r + q * ldx] : 0.f;
-        }
-        const int r = t % kSwBS, g = t / kSwBS;
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int pq = 0; pq < p; ++pq) {
-            const int bj = FORWARD ? pq : nblk - 1 - pq;
-            const int64_t j0 = int64_t(bj) * kSwBS;
-            const int nj = int(min64(kSwBS, n - j0));
-            __syncthreads();
-            for (int e = t; e < kSwBS * kSwBS; e += 256) {
-                int rr, c;
-                if (TRANS) { c = e % kSwBS; rr = e / kSwBS; }
-                else       { rr = e % kSwBS; c = e / kSwBS; }
-                sm.Ts[c][rr] = (rr < ni && c < nj) ? opM(i0 + rr, j0 + c) : 0.f;
-            }
-            // x_j from the tagged words of ticket pq (rows j0.., right-hand side q)
-            const unsigned tag = unsigned(pq + 1);
-            bool ok = true;
-            for (int e = t; e < kSwBS * kSwRhs; e += 256) {
-                const int rr = e % kSwBS, q = e / kSwBS;
-                float v = 0.f;
-                if (rr < nj && q < nrhs) {
-                    const unsigned long long* w = &tagged[size_t(q) * size_t(n) + size_t(j0 + rr)];
-                    unsigned long long word = ld_relaxed_u64(w);
-                    if (unsigned(word >> 32) != tag) {
-                        const uint64_t t0 = sw_globaltimer();
-                        for (unsigned it = 1; unsigned((word = ld_relaxed_u64(w)) >> 32) != tag; ++it) {
-                            if ((it & 255u) == 0 &&
-                                (ld_volatile_i32(status) != 0 || sw_globaltimer() - t0 > 2000000000ull)) {
-                                atomicCAS(status, 0, SLT_ERR_TIMEOUT);
-                                ok = false;
-                                break;
-                            }
-                        }
-                    }
-                    v = __uint_as_float(unsigned(word));
-                }
-                sm.xs[rr][q] = v;
-            }
-            if (!ok) s_ok = 0;
-            __syncthreads();
-            if (!s_ok) return;
-            #pragma unroll 4
-            for (int c = 0; c < kSwBS; ++c) {
-                const float a = sm.Ts[c][r];
-                #pragma unroll
-                for (int u = 0; u < 4; ++u) acc[u] = fmaf(a, sm.xs[c][g * 4 + u], acc[u]);
-            }
-        }
-        __syncthreads();
-        #pragma unroll
-        for (int u = 0; u < 4; ++u) sm.xi[r][g * 4 + u] -= acc[u];
-        __syncthreads();
-        {
-            float y[4] = {0.f, 0.f, 0.f, 0.f};
-            #pragma unroll 8
-            for (int c = 0; c < kSwBS; ++c) {
-                const float d = sm.Ds[r][c];
-                #pragma unroll
-                for (int u = 0; u < 4; ++u) y[u] = fmaf(d, sm.xi[c][g * 4 + u], y[u]);
-            }
-            __syncthreads();
-            #pragma unroll
-            for (int u = 0; u < 4; ++u) sm.xi[r][g * 4 + u] = y[u];
-        }
-        __syncthreads();
-        const unsigned long long tagp = static_cast<unsigned long long>(p + 1) << 32;
-        for (int e = t; e < kSwBS * kSwRhs; e += 256) {
-            int rr = e % kSwBS, q = e / kSwBS;
-            if (rr < ni && q < nrhs) {
-                const float v = sm.xi[rr][q];
-                X[i0 + rr + q * ldx] = v;
-                tagged[size_t(q) * size_t(n) + size_t(i0 + rr)] = tagp | __float_as_uint(v);
-            }
-        }
-    }
-}
-
 template <typename T, bool FORWARD, bool UNIT, bool TRANS>
 static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, int64_t ldx, int* flags,
                         int* status, cudaStream_t s)
@@ -346,31 +226,6 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     count_launch();
     SLT_CUDA_TRY(cudaGetLastError());
     SLT_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * size_t(nblk + 1), s));
-    if constexpr (sizeof(T) == 4) {
-        // FP32: tagged hand-offs; the tagged words follow the inverses
-        unsigned long long* tagged = reinterpret_cast<unsigned long long*>(
-            reinterpret_cast<char*>(Dinv) + size_t(nblk) * kSwBS * kSwBS * sizeof(double));
-        SLT_CUDA_TRY(cudaMemsetAsync(tagged, 0, sizeof(unsigned long long) * size_t(n) * size_t(nrhs), s));
-        auto fn = sweep_tagged_kernel<FORWARD, UNIT, TRANS>;
-        const size_t smem = sizeof(SweepSmem<float>);
-        static bool cfg = false;
-        if (!cfg) {
-            SLT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-            cfg = true;
-        }
-        int dev = 0, sms = 0, per = 0;
-        SLT_CUDA_TRY(cudaGetDevice(&dev));
-        SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, smem));
-        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(nblk, int64_t(sms) * std::max(per, 1)));
-        const int pidx = prof_begin(SLT_PROF_SWEEP, s);
-        fn<<<unsigned(grid), 256, smem, s>>>(n, int(nrhs), reinterpret_cast<const float*>(M), ldm,
-                                             reinterpret_cast<const float*>(Dinv), reinterpret_cast<float*>(X),
-                                             ldx, flags, tagged, status);
-        count_launch();
-        prof_end(pidx, s, double(n) * double(n) * double(nrhs), sizeof(T) * (double(n) * double(n) / 2 + 2.0 * n * nrhs));
-        return slt_from_cuda(cudaGetLastError());
-    }
     auto fn = sweep_kernel<T, FORWARD, UNIT, TRANS>;
     const size_t smem = sizeof(SweepSmem<T>);
     static bool cfg = false;
@@ -426,11 +281,10 @@ extern "C" int slt_ssweep(int kind, int64_t n, int64_t nrhs, const float* M, int
     }
 }
 
-// Scratch of one sweep: ticket + ready flags, the diagonal-block inverses
-// (sized for double), then the FP32 tagged hand-off words (n x 16).
+// Scratch of one sweep: ticket + ready flags, then the diagonal-block
+// inverses (sized for double).
 extern "C" size_t slt_sweep_flags_bytes(int64_t n)
 {
     const int64_t nblk = ceildiv(n, kSwBS);
-    return ((sizeof(int) * size_t(nblk + 1) + 255) & ~size_t(255)) + size_t(nblk) * kSwBS * kSwBS * sizeof(double) +
-           sizeof(unsigned long long) * size_t(n) * kSwRhs;
+    return ((sizeof(int) * size_t(nblk + 1) + 255) & ~size_t(255)) + size_t(nblk) * kSwBS * kSwBS * sizeof(double);
 }
