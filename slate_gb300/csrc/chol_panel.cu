@@ -5,15 +5,22 @@
 // 56-81) followed by a batched trsm of the tiles below (src/potrf.cc:109-120).
 // Here the whole nb-wide panel (rows r0..n-1, columns r0..r0+nb-1) is one
 // cooperative persistent launch.  Block b owns a band of R rows (R a
-// multiple of 64).  For each 64-column step:
-//   1. every block loads the 64 x 64 diagonal block and factors it in shared
-//      memory (the owner of those rows records info, and writes the factor
-//      back after the next barrier, once every block has read the block);
-//   2. every block solves its own rows below it, X = B L^{-T};
-//   3. grid barrier; every block updates its rows in the remaining panel
-//      columns with the freshly solved rows (rank-64 update);
-//   4. grid barrier.
-// Barriers are the bounded grid barriers of common.cuh.
+// multiple of 64).  For each 64-column step k:
+//   1. every block loads the factored 64 x 64 diagonal block and its 16 x 16
+//      sub-block inverses (step 0: every block factors it itself);
+//   2. every block solves its own rows below it, X = B L^{-T}; the blocks
+//      owning rows of the remaining panel columns ("head" rows, the update
+//      operand of everyone) count themselves done in a per-step counter;
+//   3. every block waits for that counter (a grid barrier at step 0 only) and
+//      updates its rows in the remaining panel columns (rank-64 update);
+//   4. the owner of the next diagonal block -- its only update tile is that
+//      block -- factors it at once and publishes it (L11 in P, the inverses
+//      and a failure word in the workspace, then a release of the step
+//      number); the next step's blocks wait for exactly that.
+// No grid-wide barrier separates the steps: the critical path is the owner
+// chain solve -> diagonal tile update -> factor.  Every wait is a bounded
+// acquire spin (common.cuh), and the cooperative launch keeps all blocks
+// resident, so every awaited block is running.
 
 #include "common.cuh"
 #include "prof.h"
@@ -87,8 +94,28 @@ struct CholPanelArgs {
     int* status;
     GridBarrier* bar;
     int* next_fail;     // set when the lookahead factor of the next diagonal block fails
-    T* dinv_ws;         // its 16 x 16 sub-block inverses, [4][16][17]
+    unsigned* diag_ready;  // index of the last diagonal block published by the lookahead
+    unsigned* head_done;   // per step: blocks that solved rows needed by the others' update
+    T* dinv_ws;         // per step: the diagonal block's 16 x 16 sub-block inverses, [16][4][16][17]
 };
+
+constexpr int kCpDinv = (kCpIB / kCpSub) * kCpSub * (kCpSub + 1);   // inverses of one diagonal block
+
+// Bounded acquire spin of thread 0 until *p >= target; false on timeout or
+// when another block has already failed (status set).
+__device__ __forceinline__ bool wait_at_least(const unsigned* p, unsigned target, int* status)
+{
+    if (ld_acquire_u32(p) >= target) return true;
+    const unsigned long long t0 = globaltimer();
+    for (unsigned it = 1; ld_acquire_u32(p) < target; ++it) {
+        if ((it & 63u) == 0 && (ld_volatile_i32(status) != 0 || globaltimer() - t0 > kWaitNs)) {
+            atomicCAS(status, 0, SLT_ERR_TIMEOUT);
+            return false;
+        }
+        __nanosleep(32);
+    }
+    return true;
+}
 
 // The 64 x 64 (kb x kb) diagonal block D (row-major in shared memory, row
 // stride 65, lower triangle) factored in place by the whole CTA, in 16-column
@@ -158,7 +185,7 @@ chol_panel_kernel(CholPanelArgs<T> a)
     T* Xs = D + kCpIB * (kCpIB + 1);                        // [64][68] solved rows staging
     T* Us = Xs + kCpIB * 68;                                // [64][68] update operand
     T* Dinv = Us + kCpIB * 68;                              // [4][16][17] sub-block inverses
-    __shared__ int s_fail;
+    __shared__ int s_fail, s_abort;
     const int G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
     const int64_t ld = a.ld;
     T* P = a.P;
@@ -172,13 +199,18 @@ chol_panel_kernel(CholPanelArgs<T> a)
         //      its owner factored it during the previous step's update phase
         //      (below) and published L11 in P, the sub-block inverses and a
         //      failure word in the workspace; every block loads them.
+        const int k = int(c0 / kCpIB);
+        if (c0 > 0) {
+            if (t == 0) s_abort = wait_at_least(a.diag_ready, unsigned(k), a.status) ? 0 : 1;
+            __syncthreads();
+            if (s_abort) return;
+        }
         for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
             int i = e % kCpIB, l = e / kCpIB;
             D[i * (kCpIB + 1) + l] = (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
         }
         if (c0 > 0)
-            for (int e = t; e < (kCpIB / kCpSub) * kCpSub * (kCpSub + 1); e += kCpThreads)
-                Dinv[e] = __ldcg(&a.dinv_ws[e]);
+            for (int e = t; e < kCpDinv; e += kCpThreads) Dinv[e] = __ldcg(&a.dinv_ws[size_t(k) * kCpDinv + e]);
         if (t == 0) s_fail = (c0 > 0) ? ld_volatile_i32(a.next_fail) : 0;
         __syncthreads();
         if (c0 == 0) {
@@ -237,8 +269,26 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 }
             }
         }
+        // ---- rows [c0 + kb, nbk) are the update operand of every block: their
+        //      owners announce them solved; the others wait for exactly those
+        //      blocks (a grid barrier only at the first step, whose diagonal
+        //      block every block read from P before its owner overwrites it).
+        const int64_t cbeg = c0 + kb;
+        const int64_t hend = min64(a.nbk, a.m);
+        const int first_head = int(cbeg / a.rows_per_block);
+        const int n_head = (cbeg < hend) ? int((hend - 1) / a.rows_per_block) - first_head + 1 : 0;
+        const bool head = !failed && cbeg < hend && rb < hend && re > cbeg;
         __threadfence();
-        if (!grid_sync(a.bar, unsigned(G), a.status)) return;
+        __syncthreads();
+        if (head && t == 0) atomicAdd(&a.head_done[k], 1u);
+        if (c0 == 0) {
+            if (!grid_sync(a.bar, unsigned(G), a.status)) return;
+        }
+        if (!failed && n_head > 0) {
+            if (t == 0) s_abort = wait_at_least(&a.head_done[k], unsigned(n_head), a.status) ? 0 : 1;
+            __syncthreads();
+            if (s_abort) return;
+        }
         // every block has read the diagonal block: its owner writes the factor
         // back (later diagonal blocks were written by the lookahead below)
         if (c0 == 0 && c0 >= rb && c0 < re)
@@ -246,7 +296,6 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 int i = e % kCpIB, l = e / kCpIB;
                 if (i < kb && l < kb && i >= l) P[c0 + i + (c0 + l) * ld] = D[i * (kCpIB + 1) + l];
             }
-        const int64_t cbeg = c0 + kb;
         // ---- 3. rank-kb update of the owned rows in panel columns [c0+kb, nbk):
         //      64 x 64 output tiles, 4 x 4 per thread, operands staged [l][row]
         //      and [l][col] (row stride 68) so each thread reads two 4-vectors
@@ -322,14 +371,15 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 int i = e % kCpIB, l = e / kCpIB;
                 if (i < kbn && l < kbn && i >= l) P[cbeg + i + (cbeg + l) * ld] = D[i * (kCpIB + 1) + l];
             }
-            for (int e = t; e < (kCpIB / kCpSub) * kCpSub * (kCpSub + 1); e += kCpThreads) a.dinv_ws[e] = Dinv[e];
+            for (int e = t; e < kCpDinv; e += kCpThreads) a.dinv_ws[size_t(k + 1) * kCpDinv + e] = Dinv[e];
             if (t == 0 && f) {
                 atomicCAS(a.info, 0, int(a.info_offset + cbeg + f));
                 *reinterpret_cast<volatile int*>(a.next_fail) = 1;
             }
+            __threadfence();
+            __syncthreads();
+            if (t == 0) st_release_u32(a.diag_ready, unsigned(k + 1));
         }
-        __threadfence();
-        if (!grid_sync(a.bar, unsigned(G), a.status)) return;
         if (failed) return;       // every block saw the same failing diagonal block
     }
 }
@@ -357,12 +407,18 @@ static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info
     const int64_t maxg = int64_t(sms) * per_sm;             // all blocks co-resident
     int64_t R = ceildiv(ceildiv(m, maxg), kCpIB) * kCpIB;     // multiple of 64
     int64_t G = ceildiv(m, R);
-    // ws: barrier at 0, failure word at 256, sub-block inverses at 512
-    GridBarrier* bar = static_cast<GridBarrier*>(ws);
-    int* next_fail = reinterpret_cast<int*>(static_cast<char*>(ws) + 256);
-    T* dinv_ws = reinterpret_cast<T*>(static_cast<char*>(ws) + 512);
+    if (nbk > 16 * kCpIB) return SLT_ERR_ARG;                // per-step words below
+    // ws: barrier at 0, failure word at 256, diagonal-ready word at 260,
+    // per-step head counters at 264, per-step sub-block inverses at 512
+    char* w = static_cast<char*>(ws);
+    GridBarrier* bar = reinterpret_cast<GridBarrier*>(w);
+    int* next_fail = reinterpret_cast<int*>(w + 256);
+    unsigned* diag_ready = reinterpret_cast<unsigned*>(w + 260);
+    unsigned* head_done = reinterpret_cast<unsigned*>(w + 264);
+    T* dinv_ws = reinterpret_cast<T*>(w + 512);
     SLT_CUDA_TRY(cudaMemsetAsync(ws, 0, 512, stream));
-    CholPanelArgs<T> args{m, nbk, ld, R, info_offset, P, info, status, bar, next_fail, dinv_ws};
+    CholPanelArgs<T> args{m, nbk, ld, R, info_offset, P, info, status, bar, next_fail, diag_ready, head_done,
+                          dinv_ws};
     void* kargs[] = { &args };
     const int pidx = prof_begin(SLT_PROF_POTRF, stream);
     SLT_CUDA_TRY(cudaLaunchCooperativeKernel((const void*) chol_panel_kernel<T>, dim3(unsigned(G)),
@@ -380,7 +436,7 @@ using namespace slt;
 // and the next diagonal block's sub-block inverses.
 extern "C" size_t slt_chol_panel_ws_bytes(void)
 {
-    return 512 + size_t(kCpIB / kCpSub) * kCpSub * (kCpSub + 1) * sizeof(double);
+    return 512 + size_t(16) * kCpDinv * sizeof(double);
 }
 
 // Factor the Cholesky column panel with top-left P (the diagonal element),
