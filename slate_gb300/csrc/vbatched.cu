@@ -24,19 +24,28 @@
 #include "common.cuh"
 #include "drivers.h"
 #include "prof.h"
+#include "vbatched_table.h"
 
 #include <algorithm>
+#include <cstdlib>
+#include <string>
 #include <vector>
 
 namespace slt {
 namespace vb {
 
 constexpr int NT = 256;       // threads per CTA
-constexpr int PB = 32;        // panel width
+constexpr int PBMAX = 32;     // widest panel (the tuning table picks 16 or 32 per system)
 constexpr int TS = 64;        // trailing-update tile
-constexpr int TSP = TS + 1;   // padded smem row
+constexpr int TSV = TS + 4;   // smem row of a trailing-update operand: 16-byte aligned rows
 constexpr int MAXR = 8;       // right-hand sides per solve pass
 constexpr int MAXN = 2048;
+// In-panel updates: rows processed RG at a time and panel columns CH at a
+// time, so that each batch of loads is issued before any of it is used.
+template <typename T> struct PanelBatch;
+template <> struct PanelBatch<float> { static constexpr int RG = 4, CH = 8; };
+template <> struct PanelBatch<double> { static constexpr int RG = 2, CH = 8; };
+constexpr int SWP = 4;           // row-swap elements per thread and batch
 constexpr unsigned FULL = 0xffffffffu;
 
 struct Sys {
@@ -45,7 +54,7 @@ struct Sys {
     double* X;      // solution (written; may equal B)
     int* ipiv;      // LU: 1-based pivots
     float* lo;      // mixed: FP32 factor, leading dimension n
-    int n, nrhs, kind, lda, ldb, ldx, id, pad;
+    int n, nrhs, kind, lda, ldb, ldx, id, pb;   // pb: panel width (16 or 32)
 };
 
 __device__ __forceinline__ double tabs(double x) { return fabs(x); }
@@ -89,34 +98,106 @@ __device__ double block_max(double v, double* sv)
     return v;
 }
 
+// st(e, ld(e)) for e in [0, cnt), NB loads per thread issued before any of
+// their results is stored (a load followed at once by a dependent store would
+// otherwise wait out the full memory latency per element).
+template <int NB, typename Load, typename Store>
+__device__ __forceinline__ void batched_copy(int cnt, Load ld, Store st)
+{
+    for (int e0 = threadIdx.x; e0 < cnt; e0 += NB * NT) {
+        decltype(ld(0)) v[NB];
+        #pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            const int e = e0 + u * NT;
+            if (e < cnt) v[u] = ld(e);
+        }
+        #pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            const int e = e0 + u * NT;
+            if (e < cnt) st(e, v[u]);
+        }
+    }
+}
+
+// v = p[0 .. 3] from shared memory in one (float) or two (double) 16-byte loads;
+// p is 16-byte aligned.
+__device__ __forceinline__ void lds4(const float* p, float (&v)[4])
+{
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double (&v)[4])
+{
+    const double2 t0 = *reinterpret_cast<const double2*>(p), t1 = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = t0.x; v[1] = t0.y; v[2] = t1.x; v[3] = t1.y;
+}
+
 // C (m x nn) -= A (m x kk) * op(B), kk <= PB.  op(B)(q, c) = B[q + c ldb]
 // (TRANS = false: the U12 row block) or B[c + q ldb] (TRANS = true: L21^T).
 // LOWER: C starts on the diagonal and only its lower triangle is updated.
-// Thread (tx, ty) of a 16 x 16 grid owns rows tx + 16 i and columns ty + 16 j
-// of each 64 x 64 tile, so that C accesses are coalesced along rows.
-template <typename T, bool TRANS, bool LOWER>
+// Thread (tx, ty) of a 16 x 16 grid owns rows 4 tx .. 4 tx + 3 and columns
+// 4 ty .. 4 ty + 3 of each 64 x 64 tile and reads its four A and four B
+// values per k-step with one vector load each from shared memory.
+// FP32 (PIPE) is software-pipelined: the next tile's operands are fetched
+// into registers and this tile's C is loaded before the FMAs, so that no
+// global load is waited on right after it is issued.  FP64 is bound by its
+// FMA pipe and keeps registers for a second CTA per SM instead: operands are
+// fetched just before use, and C is read in one batch after the FMAs.
+template <typename T, bool TRANS, bool LOWER, int PB>
 __device__ void tile_update(T* C, int ldc, const T* A, int lda, const T* B, int ldb, int m, int nn, int kk,
                             T* sA, T* sB)
 {
+    constexpr int EPT = TS * PB / NT;      // operand elements per thread and tile
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int mt = (m + TS - 1) / TS, nt = (nn + TS - 1) / TS;
-    for (int t = 0; t < mt * nt; ++t) {
-        const int bi = t % mt, bj = t / mt;
-        if (LOWER && bi < bj) continue;
-        const int r0 = bi * TS, c0 = bj * TS;
-        for (int e = threadIdx.x; e < TS * PB; e += NT) {
+    const int ntiles = mt * nt;
+    auto valid = [&](int t) { return !LOWER || (t % mt) >= (t / mt); };
+    auto next = [&](int t) {
+        do { ++t; } while (t < ntiles && !valid(t));
+        return t;
+    };
+    T ra[EPT], rb[EPT];
+    auto fetch = [&](int t) {
+        const int r0 = (t % mt) * TS, c0 = (t / mt) * TS;
+        #pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+            const int e = threadIdx.x + u * NT;
             const int r = e % TS, q = e / TS;
-            sA[q * TSP + r] = (r0 + r < m && q < kk) ? A[(r0 + r) + size_t(q) * lda] : T(0);
+            ra[u] = (r0 + r < m && q < kk) ? A[(r0 + r) + size_t(q) * lda] : T(0);
+            int qb, c;
+            if (TRANS) { c = e % TS; qb = e / TS; }
+            else { qb = e % PB; c = e / PB; }
+            rb[u] = (c0 + c < nn && qb < kk) ? (TRANS ? B[(c0 + c) + size_t(qb) * ldb] : B[qb + size_t(c0 + c) * ldb])
+                                             : T(0);
         }
-        for (int e = threadIdx.x; e < TS * PB; e += NT) {
-            int q, c;
-            if (TRANS) { c = e % TS; q = e / TS; }
-            else { q = e % PB; c = e / PB; }
-            T v = T(0);
-            if (c0 + c < nn && q < kk) v = TRANS ? B[(c0 + c) + size_t(q) * ldb] : B[q + size_t(c0 + c) * ldb];
-            sB[q * TSP + c] = v;
+    };
+    constexpr bool PIPE = sizeof(T) == 4;
+    int t = 0;                               // tile (0, 0) is always valid
+    if (PIPE && ntiles > 0) fetch(t);
+    while (t < ntiles) {
+        if (!PIPE) fetch(t);
+        #pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+            const int e = threadIdx.x + u * NT;
+            sA[(e / TS) * TSV + e % TS] = ra[u];
+            if (TRANS) sB[(e / TS) * TSV + e % TS] = rb[u];
+            else sB[(e % PB) * TSV + e / PB] = rb[u];
         }
         __syncthreads();
+        const int r0 = (t % mt) * TS, c0 = (t / mt) * TS;
+        T cv[4][4];
+        auto load_c = [&]() {
+            #pragma unroll
+            for (int i = 0; i < 4; ++i)
+                #pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int r = r0 + 4 * tx + i, c = c0 + 4 * ty + j;
+                    cv[i][j] = (r < m && c < nn && (!LOWER || r >= c)) ? C[r + size_t(c) * ldc] : T(0);
+                }
+        };
+        if (PIPE) load_c();
+        const int tn = next(t);
+        if (PIPE && tn < ntiles) fetch(tn);
         T acc[4][4];
         #pragma unroll
         for (int i = 0; i < 4; ++i)
@@ -124,80 +205,154 @@ __device__ void tile_update(T* C, int ldc, const T* A, int lda, const T* B, int 
             for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
         for (int q = 0; q < kk; ++q) {
             T a[4], b[4];
-            #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = sA[q * TSP + tx + 16 * i];
-            #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = sB[q * TSP + ty + 16 * j];
+            lds4(sA + q * TSV + 4 * tx, a);
+            lds4(sB + q * TSV + 4 * ty, b);
             #pragma unroll
             for (int i = 0; i < 4; ++i)
                 #pragma unroll
                 for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
         }
+        if (!PIPE) load_c();
         #pragma unroll
         for (int i = 0; i < 4; ++i)
             #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const int r = r0 + tx + 16 * i, c = c0 + ty + 16 * j;
-                if (r < m && c < nn && (!LOWER || r >= c)) C[r + size_t(c) * ldc] -= acc[i][j];
+                const int r = r0 + 4 * tx + i, c = c0 + 4 * ty + j;
+                if (r < m && c < nn && (!LOWER || r >= c)) C[r + size_t(c) * ldc] = cv[i][j] - acc[i][j];
             }
         __syncthreads();
+        t = tn;
     }
 }
 
 template <typename T>
-struct FactorSmem {
-    T sA[PB * TSP];
-    T sB[PB * TSP];
-    T sL[PB * PB];
+struct alignas(16) FactorSmem {
+    T sA[PBMAX * TSV];
+    T sB[PBMAX * TSV];
+    T sL[PBMAX * PBMAX];
+    T sU[PBMAX];          // LU: panel part of the pivot row; Cholesky: panel part of column j
     T sv[NT / 32];
     int si[NT / 32];
 };
 
+// Column-by-column LU of the panel rows k .. n - 1, columns k .. k + kb - 1,
+// held at Pn (element (i, c) of the panel at Pn[i + c pld]: in place in M, or
+// a shared-memory copy).  Row interchanges reach the columns outside the
+// panel in M, each column swapped by the one thread that owns it, so that they
+// need no barrier; inside the panel threads 0 .. kb - 1 swap and stage the new
+// pivot row in sm.sU.  Rows are updated RG at a time from batched loads, and
+// the update of column j + 1 feeds the next pivot search.  Returns info.
+template <typename T>
+__device__ int lu_panel(T* M, int n, int ld, int k, int kb, int* ipiv, int info, FactorSmem<T>& sm, T* Pn, int pld)
+{
+    const int m = n - k;
+    T best = T(-1);
+    int bi = n;
+    for (int ii = threadIdx.x; ii < m; ii += NT) {
+        const T v = tabs(Pn[ii]);
+        if (v > best) { best = v; bi = k + ii; }
+    }
+    constexpr int RG = PanelBatch<T>::RG, CH = PanelBatch<T>::CH;
+    for (int jj = 0; jj < kb; ++jj) {
+        const int j = k + jj;
+        block_argmax(best, bi, sm.sv, sm.si);
+        const int p = (bi < n) ? bi : j, pp = p - k;
+        if (threadIdx.x == 0) ipiv[j] = p + 1;
+        if (p != j)
+            for (int t0 = threadIdx.x; t0 < n - kb; t0 += SWP * NT) {
+                T av[SWP], bv[SWP];
+                #pragma unroll
+                for (int u = 0; u < SWP; ++u) {
+                    const int t = min(t0 + u * NT, n - kb - 1);
+                    const int c = t < k ? t : t + kb;
+                    av[u] = M[j + size_t(c) * ld];
+                    bv[u] = M[p + size_t(c) * ld];
+                }
+                #pragma unroll
+                for (int u = 0; u < SWP; ++u) {
+                    const int t = t0 + u * NT;
+                    if (t < n - kb) {
+                        const int c = t < k ? t : t + kb;
+                        M[j + size_t(c) * ld] = bv[u];
+                        M[p + size_t(c) * ld] = av[u];
+                    }
+                }
+            }
+        if (threadIdx.x < kb) {
+            T* col = Pn + size_t(threadIdx.x) * pld;
+            const T a = col[jj], b = col[pp];
+            if (p != j) { col[jj] = b; col[pp] = a; }
+            sm.sU[threadIdx.x] = b;
+        }
+        __syncthreads();
+        const T piv = sm.sU[jj];
+        if (piv == T(0) && info == 0) info = j + 1;
+        const bool recip = tabs(piv) >= Real<T>::safe_min();
+        const T r = recip ? T(1) / piv : T(0);
+        // rows below: l = a_ij / piv, then a_ic -= l u_jc for the panel's columns c > j
+        best = T(-1);
+        bi = n;
+        for (int i0 = jj + 1 + threadIdx.x; i0 < m; i0 += RG * NT) {
+            T seg[RG][CH];
+            T l[RG];
+            #pragma unroll
+            for (int g = 0; g < RG; ++g) {
+                const int ii = min(i0 + g * NT, m - 1);
+                #pragma unroll
+                for (int q = 0; q < CH; ++q) seg[g][q] = Pn[ii + size_t(min(jj + q, kb - 1)) * pld];
+            }
+            #pragma unroll
+            for (int g = 0; g < RG; ++g) {
+                const int ii = i0 + g * NT;
+                if (ii >= m) continue;
+                l[g] = piv == T(0) ? seg[g][0] : (recip ? seg[g][0] * r : seg[g][0] / piv);
+                Pn[ii + size_t(jj) * pld] = l[g];
+                #pragma unroll
+                for (int q = 1; q < CH; ++q)
+                    if (jj + q < kb) {
+                        seg[g][q] -= l[g] * sm.sU[jj + q];
+                        Pn[ii + size_t(jj + q) * pld] = seg[g][q];
+                    }
+                if (jj + 1 < kb) {
+                    const T v = tabs(seg[g][1]);
+                    if (v > best) { best = v; bi = k + ii; }
+                }
+            }
+            for (int c0 = jj + CH; c0 < kb; c0 += CH) {
+                #pragma unroll
+                for (int g = 0; g < RG; ++g) {
+                    const int ii = min(i0 + g * NT, m - 1);
+                    #pragma unroll
+                    for (int q = 0; q < CH; ++q) seg[g][q] = Pn[ii + size_t(min(c0 + q, kb - 1)) * pld];
+                }
+                #pragma unroll
+                for (int g = 0; g < RG; ++g) {
+                    const int ii = i0 + g * NT;
+                    #pragma unroll
+                    for (int q = 0; q < CH; ++q)
+                        if (ii < m && c0 + q < kb) {
+                            seg[g][q] -= l[g] * sm.sU[c0 + q];
+                            Pn[ii + size_t(c0 + q) * pld] = seg[g][q];
+                        }
+                }
+            }
+        }
+        // the next block_argmax's barrier orders these updates before the
+        // next interchange and before sU is rewritten
+    }
+    __syncthreads();
+    return info;
+}
+
 // LU with partial pivoting of the n x n matrix M (leading dimension ld), in
 // place; ipiv 1-based.  Returns SLATE's info (first exactly-zero pivot).
-template <typename T>
+template <typename T, int PB>
 __device__ int lu_factor(T* M, int n, int ld, int* ipiv, FactorSmem<T>& sm)
 {
     int info = 0;
     for (int k = 0; k < n; k += PB) {
         const int kb = min(PB, n - k);
-        for (int j = k; j < k + kb; ++j) {
-            T best = T(-1);
-            int bi = n;
-            for (int i = j + threadIdx.x; i < n; i += NT) {
-                const T v = tabs(M[i + size_t(j) * ld]);
-                if (v > best) { best = v; bi = i; }
-            }
-            block_argmax(best, bi, sm.sv, sm.si);
-            const int p = (bi < n) ? bi : j;
-            if (threadIdx.x == 0) ipiv[j] = p + 1;
-            if (p != j)
-                for (int c = threadIdx.x; c < n; c += NT) {
-                    const T t = M[j + size_t(c) * ld];
-                    M[j + size_t(c) * ld] = M[p + size_t(c) * ld];
-                    M[p + size_t(c) * ld] = t;
-                }
-            __syncthreads();
-            const T piv = M[j + size_t(j) * ld];
-            if (piv != T(0)) {
-                if (tabs(piv) >= Real<T>::safe_min()) {
-                    const T r = T(1) / piv;
-                    for (int i = j + 1 + threadIdx.x; i < n; i += NT) M[i + size_t(j) * ld] *= r;
-                }
-                else {
-                    for (int i = j + 1 + threadIdx.x; i < n; i += NT) M[i + size_t(j) * ld] /= piv;
-                }
-            }
-            else if (info == 0) {
-                info = j + 1;
-            }
-            __syncthreads();
-            for (int i = j + 1 + threadIdx.x; i < n; i += NT) {
-                const T l = M[i + size_t(j) * ld];
-                for (int c = j + 1; c < k + kb; ++c) M[i + size_t(c) * ld] -= l * M[j + size_t(c) * ld];
-            }
-            __syncthreads();
-        }
+        info = lu_panel<T>(M, n, ld, k, kb, ipiv, info, sm, M + k + size_t(k) * ld, ld);
         const int rest = n - k - kb;
         if (rest > 0) {
             // U12 = L11^{-1} A12: L11 (unit lower) to smem, one column per thread
@@ -222,99 +377,246 @@ __device__ int lu_factor(T* M, int n, int ld, int* ipiv, FactorSmem<T>& sm)
                     if (q < kb) M[(k + q) + size_t(c) * ld] = x[q];
             }
             __syncthreads();
-            tile_update<T, false, false>(M + (k + kb) + size_t(k + kb) * ld, ld, M + (k + kb) + size_t(k) * ld, ld,
-                                         M + k + size_t(k + kb) * ld, ld, rest, rest, kb, sm.sA, sm.sB);
+            tile_update<T, false, false, PB>(M + (k + kb) + size_t(k + kb) * ld, ld, M + (k + kb) + size_t(k) * ld, ld,
+                                             M + k + size_t(k + kb) * ld, ld, rest, rest, kb, sm.sA, sm.sB);
         }
     }
     return info;
 }
 
-// Lower Cholesky of M in place.  Returns SLATE's info (first non-positive
-// leading minor); the factorisation stops there.
+// Column-by-column Cholesky of the panel rows k .. n - 1, columns k .. k +
+// kb - 1 at Pn (as for lu_panel); column j's panel rows are staged in sm.sU
+// before it is scaled.  Returns 0 or the failing leading minor.
 template <typename T>
-__device__ int chol_factor(T* M, int n, int ld, FactorSmem<T>& sm)
+__device__ int chol_panel(int n, int k, int kb, FactorSmem<T>& sm, T* Pn, int pld)
 {
-    for (int k = 0; k < n; k += PB) {
-        const int kb = min(PB, n - k);
-        for (int j = k; j < k + kb; ++j) {
-            const T d = M[j + size_t(j) * ld];
-            if (!(d > T(0))) return j + 1;
-            const T s = sqrt(d);
-            __syncthreads();
-            if (threadIdx.x == 0) M[j + size_t(j) * ld] = s;
-            const T r = T(1) / s;
-            for (int i = j + 1 + threadIdx.x; i < n; i += NT) M[i + size_t(j) * ld] *= r;
-            __syncthreads();
-            for (int i = j + 1 + threadIdx.x; i < n; i += NT) {
-                const T l = M[i + size_t(j) * ld];
-                const int ce = min(k + kb - 1, i);
-                for (int c = j + 1; c <= ce; ++c) M[i + size_t(c) * ld] -= l * M[c + size_t(j) * ld];
+    const int m = n - k;
+    constexpr int RG = PanelBatch<T>::RG, CH = PanelBatch<T>::CH;
+    for (int jj = 0; jj < kb; ++jj) {
+        if (threadIdx.x < kb - jj) sm.sU[threadIdx.x] = Pn[(jj + threadIdx.x) + size_t(jj) * pld];
+        __syncthreads();
+        const T d = sm.sU[0];
+        if (!(d > T(0))) return k + jj + 1;
+        const T sd = sqrt(d);
+        const T r = T(1) / sd;
+        if (threadIdx.x == 0) Pn[jj + size_t(jj) * pld] = sd;
+        // rows below: l = a_ij / sqrt(d), then a_ic -= l l_cj for the panel's
+        // columns j < c <= min(i, k + kb - 1)
+        for (int i0 = jj + 1 + threadIdx.x; i0 < m; i0 += RG * NT) {
+            T seg[RG][CH];
+            T l[RG];
+            #pragma unroll
+            for (int g = 0; g < RG; ++g) {
+                const int ii = min(i0 + g * NT, m - 1);
+                #pragma unroll
+                for (int q = 0; q < CH; ++q) seg[g][q] = Pn[ii + size_t(min(jj + q, kb - 1)) * pld];
             }
-            __syncthreads();
+            #pragma unroll
+            for (int g = 0; g < RG; ++g) {
+                const int ii = i0 + g * NT;
+                if (ii >= m) continue;
+                const int ce = min(kb - 1, ii);      // last panel column of this row
+                l[g] = seg[g][0] * r;
+                Pn[ii + size_t(jj) * pld] = l[g];
+                #pragma unroll
+                for (int q = 1; q < CH; ++q)
+                    if (jj + q <= ce) {
+                        seg[g][q] -= l[g] * (sm.sU[q] * r);
+                        Pn[ii + size_t(jj + q) * pld] = seg[g][q];
+                    }
+            }
+            for (int c0 = jj + CH; c0 < kb; c0 += CH) {
+                #pragma unroll
+                for (int g = 0; g < RG; ++g) {
+                    const int ii = min(i0 + g * NT, m - 1);
+                    #pragma unroll
+                    for (int q = 0; q < CH; ++q) seg[g][q] = Pn[ii + size_t(min(c0 + q, kb - 1)) * pld];
+                }
+                #pragma unroll
+                for (int g = 0; g < RG; ++g) {
+                    const int ii = i0 + g * NT;
+                    const int ce = min(kb - 1, ii);
+                    #pragma unroll
+                    for (int q = 0; q < CH; ++q)
+                        if (ii < m && c0 + q <= ce) {
+                            seg[g][q] -= l[g] * (sm.sU[c0 + q - jj] * r);
+                            Pn[ii + size_t(c0 + q) * pld] = seg[g][q];
+                        }
+                }
+            }
         }
-        const int rest = n - k - kb;
-        if (rest > 0) {
-            tile_update<T, true, true>(M + (k + kb) + size_t(k + kb) * ld, ld, M + (k + kb) + size_t(k) * ld, ld,
-                                       M + (k + kb) + size_t(k) * ld, ld, rest, rest, kb, sm.sA, sm.sB);
-        }
+        __syncthreads();
     }
     return 0;
 }
 
-// Y (n x nr, column-major, leading dimension n, shared memory) <- A^{-1} Y
-// with the factors in M.
-template <typename T>
-__device__ void lu_solve(const T* M, int n, int ld, const int* ipiv, T* Y, int nr)
+// Lower Cholesky of M in place.  Returns SLATE's info (first non-positive
+// leading minor); the factorisation stops there.
+template <typename T, int PB>
+__device__ int chol_factor(T* M, int n, int ld, FactorSmem<T>& sm)
 {
-    if (threadIdx.x < nr) {
-        T* y = Y + threadIdx.x * n;
-        for (int j = 0; j < n; ++j) {
-            const int p = ipiv[j] - 1;
-            if (p > j && p < n) { const T t = y[j]; y[j] = y[p]; y[p] = t; }
-        }
+    for (int k = 0; k < n; k += PB) {
+        const int kb = min(PB, n - k);
+        const int f = chol_panel<T>(n, k, kb, sm, M + k + size_t(k) * ld, ld);
+        if (f) return f;
+        const int rest = n - k - kb;
+        if (rest > 0)
+            tile_update<T, true, true, PB>(M + (k + kb) + size_t(k + kb) * ld, ld, M + (k + kb) + size_t(k) * ld, ld,
+                                           M + (k + kb) + size_t(k) * ld, ld, rest, rest, kb, sm.sA, sm.sB);
     }
+    return 0;
+}
+
+// Factor with the panel width the tuning table chose for this system.
+template <typename T>
+__device__ int factor_sys(int kind, int pb, T* M, int n, int ld, int* ipiv, FactorSmem<T>& sm)
+{
+    if (kind == 0) return pb == 16 ? lu_factor<T, 16>(M, n, ld, ipiv, sm) : lu_factor<T, 32>(M, n, ld, ipiv, sm);
+    return pb == 16 ? chol_factor<T, 16>(M, n, ld, sm) : chol_factor<T, 32>(M, n, ld, sm);
+}
+
+// Blocked triangular solves on Y (n x nr, column-major, leading dimension
+// n, shared memory; nr <= MAXR).  Per block of SB rows, warp q solves the
+// diagonal block for right-hand side q (lane r owns row r; shuffles, no
+// barrier) from a shared tile, then every thread applies the block to the
+// rows not yet solved, one row per thread, while the next diagonal block is
+// staged: two barriers per block.
+constexpr int SB = 32;
+constexpr int SBP = SB + 1;
+constexpr size_t kTileBytes = sizeof(double) * SB * SBP;   // solve tile at the start of shared memory
+
+// op(T)(r, c) of the triangle stored in M: TRANS reads M(c, r).
+template <typename T, bool TRANS>
+__device__ __forceinline__ T tri_at(const T* M, int ld, int r, int c)
+{
+    return TRANS ? M[c + size_t(r) * ld] : M[r + size_t(c) * ld];
+}
+
+// tile(r, c) = op(M)(jb + r, jb + c) on the LOWER or upper triangle of the
+// bs x bs diagonal block, zero elsewhere; reads are coalesced along memory.
+template <typename T, bool TRANS, bool LOWER>
+__device__ __forceinline__ void stage_tile(const T* M, int ld, int jb, int bs, T* tile)
+{
+    // element (lane, warp + 8u) of the tile in memory order: all loads first
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    constexpr int U = SB * SB / NT;
+    T v[U];
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int slow = w + (NT / 32) * u;
+        const int r = TRANS ? slow : lane, c = TRANS ? lane : slow;
+        const bool in = r < bs && c < bs && (LOWER ? c <= r : c >= r);
+        v[u] = in ? tri_at<T, TRANS>(M, ld, jb + r, jb + c) : T(0);
+    }
+    #pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int slow = w + (NT / 32) * u;
+        const int r = TRANS ? slow : lane, c = TRANS ? lane : slow;
+        tile[r * SBP + c] = v[u];
+    }
+}
+
+// Y rows [i0, i1) -= op(M)(rows, jb .. jb + bs) * Y(jb .. jb + bs, :)
+template <typename T, bool TRANS>
+__device__ __forceinline__ void block_gemv(const T* M, int ld, T* Y, int n, int nr, int i0, int i1, int jb, int bs)
+{
+    for (int i = i0 + threadIdx.x; i < i1; i += NT) {
+        T acc[MAXR];
+        #pragma unroll
+        for (int q = 0; q < MAXR; ++q) acc[q] = T(0);
+        for (int c = 0; c < bs; ++c) {
+            const T m = tri_at<T, TRANS>(M, ld, i, jb + c);
+            #pragma unroll
+            for (int q = 0; q < MAXR; ++q)
+                if (q < nr) acc[q] = fma(m, Y[q * n + jb + c], acc[q]);
+        }
+        #pragma unroll
+        for (int q = 0; q < MAXR; ++q)
+            if (q < nr) Y[q * n + i] -= acc[q];
+    }
+}
+
+// Y <- L^{-1} Y, L = lower triangle of M; UNIT: unit diagonal.
+template <typename T, bool UNIT>
+__device__ void solve_lower(const T* M, int n, int ld, T* Y, int nr, T* tile)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    stage_tile<T, false, true>(M, ld, 0, min(SB, n), tile);
     __syncthreads();
-    for (int j = 0; j < n - 1; ++j) {
-        const int len = n - j - 1;
-        for (int e = threadIdx.x; e < len * nr; e += NT) {
-            const int i = j + 1 + e % len, q = e / len;
-            Y[q * n + i] -= M[i + size_t(j) * ld] * Y[q * n + j];
+    for (int jb = 0; jb < n; jb += SB) {
+        const int bs = min(SB, n - jb);
+        if (warp < nr) {
+            T y = lane < bs ? Y[warp * n + jb + lane] : T(0);
+            #pragma unroll
+            for (int c = 0; c < SB; ++c) {
+                if (!UNIT && lane == c && c < bs) y /= tile[lane * SBP + c];
+                const T yc = __shfl_sync(FULL, y, c);
+                if (lane > c) y -= tile[lane * SBP + c] * yc;
+            }
+            if (lane < bs) Y[warp * n + jb + lane] = y;
         }
         __syncthreads();
-    }
-    for (int j = n - 1; j >= 0; --j) {
-        if (threadIdx.x < nr) Y[threadIdx.x * n + j] /= M[j + size_t(j) * ld];
-        __syncthreads();
-        for (int e = threadIdx.x; e < j * nr; e += NT) {
-            const int i = e % j, q = e / j;
-            Y[q * n + i] -= M[i + size_t(j) * ld] * Y[q * n + j];
-        }
+        block_gemv<T, false>(M, ld, Y, n, nr, jb + bs, n, jb, bs);
+        if (jb + SB < n) stage_tile<T, false, true>(M, ld, jb + SB, min(SB, n - jb - SB), tile);
         __syncthreads();
     }
 }
 
-template <typename T>
-__device__ void chol_solve(const T* M, int n, int ld, T* Y, int nr)
+// Y <- U^{-1} Y with non-unit U = upper triangle of M (TRANS = false) or
+// U = L^T for the lower triangle L of M (TRANS = true).
+template <typename T, bool TRANS>
+__device__ void solve_upper(const T* M, int n, int ld, T* Y, int nr, T* tile)
 {
-    for (int j = 0; j < n; ++j) {
-        if (threadIdx.x < nr) Y[threadIdx.x * n + j] /= M[j + size_t(j) * ld];
-        __syncthreads();
-        const int len = n - j - 1;
-        for (int e = threadIdx.x; e < len * nr; e += NT) {
-            const int i = j + 1 + e % len, q = e / len;
-            Y[q * n + i] -= M[i + size_t(j) * ld] * Y[q * n + j];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int jlast = ((n - 1) / SB) * SB;
+    stage_tile<T, TRANS, false>(M, ld, jlast, n - jlast, tile);
+    __syncthreads();
+    for (int jb = jlast; jb >= 0; jb -= SB) {
+        const int bs = min(SB, n - jb);
+        if (warp < nr) {
+            T y = lane < bs ? Y[warp * n + jb + lane] : T(0);
+            #pragma unroll
+            for (int c = SB - 1; c >= 0; --c) {
+                if (lane == c && c < bs) y /= tile[lane * SBP + c];
+                const T yc = __shfl_sync(FULL, y, c);
+                if (lane < c) y -= tile[lane * SBP + c] * yc;
+            }
+            if (lane < bs) Y[warp * n + jb + lane] = y;
         }
         __syncthreads();
-    }
-    for (int j = n - 1; j >= 0; --j) {
-        if (threadIdx.x < nr) Y[threadIdx.x * n + j] /= M[j + size_t(j) * ld];
+        block_gemv<T, TRANS>(M, ld, Y, n, nr, 0, jb, jb, bs);
+        if (jb > 0) stage_tile<T, TRANS, false>(M, ld, jb - SB, SB, tile);
         __syncthreads();
-        for (int e = threadIdx.x; e < j * nr; e += NT) {
-            const int i = e % j, q = e / j;
-            Y[q * n + i] -= M[j + size_t(i) * ld] * Y[q * n + j];
+    }
+}
+
+// Y <- A^{-1} Y with the LU factors in M (row interchanges ipiv, 1-based).
+template <typename T>
+__device__ void lu_solve(const T* M, int n, int ld, const int* ipiv, T* Y, int nr, T* tile)
+{
+    // row interchanges staged in the tile area (n <= MAXN ints fit), then
+    // applied in order by one thread per right-hand side
+    int* sp = reinterpret_cast<int*>(tile);
+    batched_copy<MAXN / NT>(n, [&](int j) { return ipiv[j]; }, [&](int j, int v) { sp[j] = v; });
+    __syncthreads();
+    if (threadIdx.x < nr) {
+        T* y = Y + threadIdx.x * n;
+        for (int j = 0; j < n; ++j) {
+            const int p = sp[j] - 1;
+            if (p > j && p < n) { const T t = y[j]; y[j] = y[p]; y[p] = t; }
         }
-        __syncthreads();
     }
+    __syncthreads();
+    solve_lower<T, true>(M, n, ld, Y, nr, tile);
+    solve_upper<T, false>(M, n, ld, Y, nr, tile);
+}
+
+// Y <- A^{-1} Y with the lower Cholesky factor in M.
+template <typename T>
+__device__ void chol_solve(const T* M, int n, int ld, T* Y, int nr, T* tile)
+{
+    solve_lower<T, false>(M, n, ld, Y, nr, tile);
+    solve_upper<T, true>(M, n, ld, Y, nr, tile);
 }
 
 __device__ __forceinline__ int next_system(int* counter, int* s_w)
@@ -326,40 +628,47 @@ __device__ __forceinline__ int next_system(int* counter, int* s_w)
     return w;
 }
 
-// Plain FP64: factor in place, then X = A^{-1} B (X may be B).
-__global__ void __launch_bounds__(NT) vb_plain_kernel(const Sys* __restrict__ sys, int count, int* counter,
-                                                      int* info)
+// Plain FP64: factor in place, then X = A^{-1} B (X may be B).  s.lo non-null: factor a copy placed
+// there (as doubles) and leave A untouched.  iter non-null: iter[id] = 0
+// (the mixed API's systems assigned to the FP64 tier).
+__global__ void __launch_bounds__(NT, 2) vb_plain_kernel(const Sys* __restrict__ sys, int count, int* counter,
+                                                      int* info, int* iter)
 {
     extern __shared__ __align__(16) unsigned char vb_smem[];
     __shared__ int s_w;
     auto& fs = *reinterpret_cast<FactorSmem<double>*>(vb_smem);
-    double* Y = reinterpret_cast<double*>(vb_smem);
+    double* tile = reinterpret_cast<double*>(vb_smem);
+    double* Y = reinterpret_cast<double*>(vb_smem + kTileBytes);
     for (;;) {
         const int w = next_system(counter, &s_w);
         if (w >= count) return;
-        const Sys s = sys[w];
+        Sys s = sys[w];
+        if (threadIdx.x == 0 && iter) iter[s.id] = 0;
         if (s.n <= 0) {
             if (threadIdx.x == 0) info[s.id] = 0;
             continue;
         }
-        const int inf = (s.kind == 0) ? lu_factor<double>(s.A, s.n, s.lda, s.ipiv, fs)
-                                      : chol_factor<double>(s.A, s.n, s.lda, fs);
+        if (s.lo) {
+            double* Wk = reinterpret_cast<double*>(s.lo);
+            for (int64_t e = threadIdx.x; e < int64_t(s.n) * s.n; e += NT)
+                Wk[e] = s.A[(e % s.n) + size_t(e / s.n) * s.lda];
+            __syncthreads();
+            s.A = Wk;
+            s.lda = s.n;
+        }
+        const int inf = factor_sys<double>(s.kind, s.pb, s.A, s.n, s.lda, s.ipiv, fs);
         __syncthreads();
         if (threadIdx.x == 0) info[s.id] = inf;
         if (inf != 0) continue;
         for (int c0 = 0; c0 < s.nrhs; c0 += MAXR) {
             const int nr = min(MAXR, s.nrhs - c0);
-            for (int e = threadIdx.x; e < s.n * nr; e += NT) {
-                const int i = e % s.n, q = e / s.n;
-                Y[e] = s.B[i + size_t(c0 + q) * s.ldb];
-            }
+            batched_copy<4>(s.n * nr, [&](int e) { return s.B[e % s.n + size_t(c0 + e / s.n) * s.ldb]; },
+                            [&](int e, double v) { Y[e] = v; });
             __syncthreads();
-            if (s.kind == 0) lu_solve<double>(s.A, s.n, s.lda, s.ipiv, Y, nr);
-            else chol_solve<double>(s.A, s.n, s.lda, Y, nr);
-            for (int e = threadIdx.x; e < s.n * nr; e += NT) {
-                const int i = e % s.n, q = e / s.n;
-                s.X[i + size_t(c0 + q) * s.ldx] = Y[e];
-            }
+            if (s.kind == 0) lu_solve<double>(s.A, s.n, s.lda, s.ipiv, Y, nr, tile);
+            else chol_solve<double>(s.A, s.n, s.lda, Y, nr, tile);
+            for (int e = threadIdx.x; e < s.n * nr; e += NT)
+                s.X[e % s.n + size_t(c0 + e / s.n) * s.ldx] = Y[e];
             __syncthreads();
         }
     }
@@ -369,25 +678,26 @@ __global__ void __launch_bounds__(NT) vb_plain_kernel(const Sys* __restrict__ sy
 // the FP32 copy lo = float(A) (SPD: lower triangle only).
 __device__ double norm_and_cast(const Sys& s, double* sv)
 {
+    constexpr int NB = 8;       // elements loaded per batch and thread
     const int n = s.n;
     double mx = 0.0;
     for (int i = threadIdx.x; i < n; i += NT) {
         double acc = 0.0;
-        if (s.kind == 0) {
-            for (int j = 0; j < n; ++j) {
-                const double a = s.A[i + size_t(j) * s.lda];
-                s.lo[i + size_t(j) * n] = float(a);
-                acc += fabs(a);
-            }
+        const int jl = s.kind == 0 ? n : i + 1;     // SPD: the lower triangle is cast
+        for (int j0 = 0; j0 < jl; j0 += NB) {
+            double a[NB];
+            #pragma unroll
+            for (int u = 0; u < NB; ++u)
+                if (j0 + u < jl) a[u] = s.A[i + size_t(j0 + u) * s.lda];
+            #pragma unroll
+            for (int u = 0; u < NB; ++u)
+                if (j0 + u < jl) {
+                    s.lo[i + size_t(j0 + u) * n] = float(a[u]);
+                    acc += fabs(a[u]);
+                }
         }
-        else {
-            for (int j = 0; j <= i; ++j) {
-                const double a = s.A[i + size_t(j) * s.lda];
-                s.lo[i + size_t(j) * n] = float(a);
-                acc += fabs(a);
-            }
+        if (s.kind != 0)
             for (int j = i + 1; j < n; ++j) acc += fabs(s.A[j + size_t(i) * s.lda]);
-        }
         mx = (acc > mx || acc != acc) ? acc : mx;
     }
     return block_max(mx, sv);
@@ -395,14 +705,15 @@ __device__ double norm_and_cast(const Sys& s, double* sv)
 
 // Mixed, phase 1: norm + FP32 copy, FP32 factorisation, x0 = A_lo^{-1} b.
 // iter[id] = 0 (refinement pending) or -3 (low-precision factor failed).
-__global__ void __launch_bounds__(NT) vb_mixed_factor_kernel(const Sys* __restrict__ sys, int count, int* counter,
+__global__ void __launch_bounds__(NT, 2) vb_mixed_factor_kernel(const Sys* __restrict__ sys, int count, int* counter,
                                                              int* info, int* iter, int* state, double* anorm)
 {
     extern __shared__ __align__(16) unsigned char vb_smem[];
     __shared__ int s_w;
     __shared__ double s_red[NT / 32];
     auto& fs = *reinterpret_cast<FactorSmem<float>*>(vb_smem);
-    float* Y = reinterpret_cast<float*>(vb_smem);
+    float* tile = reinterpret_cast<float*>(vb_smem);
+    float* Y = reinterpret_cast<float*>(vb_smem + kTileBytes);
     for (;;) {
         const int w = next_system(counter, &s_w);
         if (w >= count) return;
@@ -413,8 +724,7 @@ __global__ void __launch_bounds__(NT) vb_mixed_factor_kernel(const Sys* __restri
         }
         const double an = norm_and_cast(s, s_red);
         __syncthreads();
-        const int inf = (s.kind == 0) ? lu_factor<float>(s.lo, s.n, s.n, s.ipiv, fs)
-                                      : chol_factor<float>(s.lo, s.n, s.n, fs);
+        const int inf = factor_sys<float>(s.kind, s.pb, s.lo, s.n, s.n, s.ipiv, fs);
         __syncthreads();
         if (threadIdx.x == 0) {
             info[s.id] = inf;
@@ -424,13 +734,11 @@ __global__ void __launch_bounds__(NT) vb_mixed_factor_kernel(const Sys* __restri
         }
         if (inf != 0) continue;
         const int nr = s.nrhs;     // <= MAXR (checked on the host)
-        for (int e = threadIdx.x; e < s.n * nr; e += NT) {
-            const int i = e % s.n, q = e / s.n;
-            Y[e] = float(s.B[i + size_t(q) * s.ldb]);
-        }
+        batched_copy<4>(s.n * nr, [&](int e) { return float(s.B[e % s.n + size_t(e / s.n) * s.ldb]); },
+                        [&](int e, float v) { Y[e] = v; });
         __syncthreads();
-        if (s.kind == 0) lu_solve<float>(s.lo, s.n, s.n, s.ipiv, Y, nr);
-        else chol_solve<float>(s.lo, s.n, s.n, Y, nr);
+        if (s.kind == 0) lu_solve<float>(s.lo, s.n, s.n, s.ipiv, Y, nr, tile);
+        else chol_solve<float>(s.lo, s.n, s.n, Y, nr, tile);
         for (int e = threadIdx.x; e < s.n * nr; e += NT) {
             const int i = e % s.n, q = e / s.n;
             s.X[i + size_t(q) * s.ldx] = double(Y[e]);
@@ -478,7 +786,8 @@ __global__ void __launch_bounds__(NT) vb_refine_kernel(const Sys* __restrict__ s
     __shared__ int s_w;
     __shared__ double s_red[NT / 32];
     __shared__ int s_bad;
-    double* R = reinterpret_cast<double*>(vb_smem);
+    float* tile = reinterpret_cast<float*>(vb_smem);
+    double* R = reinterpret_cast<double*>(vb_smem + kTileBytes);
     for (;;) {
         const int w = next_system(counters + step, &s_w);
         if (w >= count) return;
@@ -496,6 +805,7 @@ __global__ void __launch_bounds__(NT) vb_refine_kernel(const Sys* __restrict__ s
             case 7: residual_rows<7>(s, R); break;
             default: residual_rows<8>(s, R); break;
         }
+        __syncthreads();
         if (threadIdx.x == 0) s_bad = 0;
         __syncthreads();
         const double tol = tolerance > 0 ? tolerance : 2.220446049250313e-16 * sqrt(double(n));
@@ -524,7 +834,7 @@ __global__ void __launch_bounds__(NT) vb_refine_kernel(const Sys* __restrict__ s
         // correction in FP32.  R (double) -> Y (float) in place, 8 NT elements
         // at a time: the floats of chunk k land on the doubles of chunk k / 2,
         // which were read before the barrier.
-        float* Y = reinterpret_cast<float*>(vb_smem);
+        float* Y = reinterpret_cast<float*>(vb_smem + kTileBytes);
         for (int base = 0; base < n * nr; base += 8 * NT) {
             double v[8];
             #pragma unroll
@@ -540,17 +850,23 @@ __global__ void __launch_bounds__(NT) vb_refine_kernel(const Sys* __restrict__ s
             }
             __syncthreads();
         }
-        if (s.kind == 0) lu_solve<float>(s.lo, n, n, s.ipiv, Y, nr);
-        else chol_solve<float>(s.lo, n, n, Y, nr);
-        for (int e = threadIdx.x; e < n * nr; e += NT) {
-            const int i = e % n, q = e / n;
-            s.X[i + size_t(q) * s.ldx] += double(Y[e]);
-        }
+        if (s.kind == 0) lu_solve<float>(s.lo, n, n, s.ipiv, Y, nr, tile);
+        else chol_solve<float>(s.lo, n, n, Y, nr, tile);
+        batched_copy<4>(n * nr, [&](int e) { return s.X[e % n + size_t(e / n) * s.ldx] + double(Y[e]); },
+                        [&](int e, double v) { s.X[e % n + size_t(e / n) * s.ldx] = v; });
         __syncthreads();
     }
 }
 
-size_t factor_smem(bool dbl) { return dbl ? sizeof(FactorSmem<double>) : sizeof(FactorSmem<float>); }
+// Dynamic shared memory of the factor + solve kernels: the factorisation's
+// staging, or the solve tile followed by the n x nr right-hand sides.
+size_t solve_smem(bool dbl, int maxn, int maxr)
+{
+    const size_t es = dbl ? sizeof(double) : sizeof(float);
+    const size_t f = dbl ? sizeof(FactorSmem<double>) : sizeof(FactorSmem<float>);
+    const size_t y = kTileBytes + es * size_t(std::max(1, maxn)) * size_t(maxr);
+    return std::max(f, y);
+}
 
 } // namespace vb
 } // namespace slt
@@ -575,6 +891,24 @@ int fetch(std::vector<P>& h, const P* d, int64_t batch, cudaStream_t s)
     if (!d) return SLT_OK;
     SLT_CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(P) * size_t(batch), cudaMemcpyDeviceToHost, s));
     return SLT_OK;
+}
+
+// The tuning table's entry for a system of size n, with overrides used by
+// the tuner itself: SLT_VBATCHED_PB = 16 | 32, SLT_VBATCHED_TIER = fp32 | fp64.
+VbTune tune_for(int n)
+{
+    VbTune t = kVbTable[sizeof(kVbTable) / sizeof(kVbTable[0]) - 1];
+    for (const VbTune& e : kVbTable)
+        if (n <= e.max_n) { t = e; break; }
+    if (const char* v = std::getenv("SLT_VBATCHED_PB")) {
+        const int pb = std::atoi(v);
+        if (pb == 16 || pb == 32) { t.pb_fp64 = pb; t.pb_mixed = pb; }
+    }
+    if (const char* v = std::getenv("SLT_VBATCHED_TIER")) {
+        if (std::string(v) == "fp64") t.mixed_tier = 0;
+        if (std::string(v) == "fp32") t.mixed_tier = 1;
+    }
+    return t;
 }
 
 // Largest-first work list (cost ~ n^3 for the factorisation + n^2 nrhs).
@@ -626,20 +960,30 @@ int set_smem(const void* kernel, size_t smem)
     return slt_from_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
 }
 
-int run_plain(const std::vector<Sys>& list, int* d_info, cudaStream_t s, size_t smem)
+// Launches vb_plain_kernel over `list`; dsys and ctr receive the device
+// copies and must outlive the launch.
+int launch_plain(const std::vector<Sys>& list, int* d_info, int* d_iter, cudaStream_t s, size_t smem,
+                 DevBuf& dsys, DevBuf& ctr)
 {
     if (list.empty()) return SLT_OK;
     const int count = int(list.size());
-    DevBuf dsys, ctr;
     TRY(dsys.alloc(sizeof(Sys) * list.size(), s));
     TRY(ctr.alloc(sizeof(int), s));
     SLT_CUDA_TRY(cudaMemcpyAsync(dsys.p, list.data(), sizeof(Sys) * list.size(), cudaMemcpyHostToDevice, s));
     SLT_CUDA_TRY(cudaMemsetAsync(ctr.p, 0, sizeof(int), s));
     const void* k = reinterpret_cast<const void*>(&vb_plain_kernel);
     TRY(set_smem(k, smem));
-    vb_plain_kernel<<<grid_for(k, smem, count), NT, smem, s>>>(dsys.as<Sys>(), count, ctr.as<int>(), d_info);
+    vb_plain_kernel<<<grid_for(k, smem, count), NT, smem, s>>>(dsys.as<Sys>(), count, ctr.as<int>(), d_info,
+                                                              d_iter);
     count_launch();
     SLT_CUDA_TRY(cudaGetLastError());
+    return SLT_OK;
+}
+
+int run_plain(const std::vector<Sys>& list, int* d_info, cudaStream_t s, size_t smem)
+{
+    DevBuf dsys, ctr;
+    TRY(launch_plain(list, d_info, nullptr, s, smem, dsys, ctr));
     SLT_CUDA_TRY(cudaStreamSynchronize(s));   // list and buffers are released on return
     return SLT_OK;
 }
@@ -690,8 +1034,9 @@ extern "C" int slt_dsolve_vbatched(int64_t batch, const int* d_kind, const int* 
     list.reserve(size_t(batch));
     for (int i : work_order(h))
         list.push_back(Sys{h.A[i], h.B[i], h.B[i], h.ipiv[i], nullptr, h.n[i], h.nrhs[i], h.kind[i],
-                           std::max(1, h.lda[i]), std::max(1, h.ldb[i]), std::max(1, h.ldb[i]), i, 0});
-    const size_t smem = std::max(factor_smem(true), sizeof(double) * size_t(std::max(1, maxn)) * size_t(maxr));
+                           std::max(1, h.lda[i]), std::max(1, h.ldb[i]), std::max(1, h.ldb[i]), i,
+                           tune_for(h.n[i]).pb_fp64});
+    const size_t smem = solve_smem(true, maxn, maxr);
     return run_plain(list, d_info, stream, smem);
 }
 
@@ -700,6 +1045,8 @@ extern "C" int slt_dsolve_vbatched(int64_t batch, const int* d_kind, const int* 
 // systems that fail (their A[i] then holds the FP64 factors).  A[i], B[i] are
 // left unchanged otherwise; X[i] receives the solution; iter[i] and info[i]
 // follow slate::gesv_mixed (0 .. itermax, -3, -(itermax + 1)).  nrhs[i] <= 8.
+// Sizes whose tuning-table tier is FP64 skip the FP32 attempt: a copy of A[i]
+// is factored in FP64 and solved into X[i] (iter[i] = 0; A[i], B[i] kept).
 extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const int* d_n, const int* d_nrhs,
                                          double* const* d_A, const int* d_lda, int* const* d_ipiv,
                                          double* const* d_B, const int* d_ldb, double* const* d_X,
@@ -715,20 +1062,42 @@ extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const
     int maxn = 0, maxr = 1;
     TRY(validate(h, true, &maxn, &maxr));
     const std::vector<int> ord = work_order(h);
+    // Per system, the table's tier: FP32 factor + FP64 refinement (n^2 floats
+    // of workspace for the factor) or a direct FP64 solve of a copy (n^2
+    // doubles), whichever measured faster for its size.
     size_t lo_words = 0;
     std::vector<size_t> off(static_cast<size_t>(batch));
+    std::vector<VbTune> tune(static_cast<size_t>(batch));
     for (int i : ord) {
+        tune[size_t(i)] = tune_for(h.n[i]);
         off[size_t(i)] = lo_words;
-        lo_words += (size_t(h.n[i]) * size_t(h.n[i]) + 3) & ~size_t(3);
+        const size_t words = size_t(h.n[i]) * size_t(h.n[i]) * (tune[size_t(i)].mixed_tier ? 1 : 2);
+        lo_words += (words + 3) & ~size_t(3);
     }
-    DevBuf lo, dsys, ctr, st, an;
-    const int count = int(batch);
+    DevBuf lo, dsys, ctr, st, an, dsys64, ctr64;
     TRY(lo.alloc(sizeof(float) * std::max<size_t>(lo_words, 4), stream));
-    std::vector<Sys> list;
+    std::vector<Sys> list, direct;
     list.reserve(size_t(batch));
-    for (int i : ord)
-        list.push_back(Sys{h.A[i], h.B[i], h.X[i], h.ipiv[i], lo.as<float>() + off[size_t(i)], h.n[i], h.nrhs[i],
-                           h.kind[i], std::max(1, h.lda[i]), std::max(1, h.ldb[i]), std::max(1, h.ldx[i]), i, 0});
+    for (int i : ord) {
+        const VbTune& t = tune[size_t(i)];
+        const Sys sy{h.A[i], h.B[i], h.X[i], h.ipiv[i], lo.as<float>() + off[size_t(i)], h.n[i], h.nrhs[i],
+                     h.kind[i], std::max(1, h.lda[i]), std::max(1, h.ldb[i]), std::max(1, h.ldx[i]), i,
+                     t.mixed_tier ? t.pb_mixed : t.pb_fp64};
+        (t.mixed_tier ? list : direct).push_back(sy);
+    }
+    const int count = int(list.size());
+
+    TimerSet tm(stream);
+    if (!direct.empty()) {
+        tm.start("vbatched_mixed::direct_fp64");
+        const size_t smem_p = solve_smem(true, maxn, maxr);
+        TRY(launch_plain(direct, d_info, d_iter, stream, smem_p, dsys64, ctr64));
+        tm.stop("vbatched_mixed::direct_fp64");
+    }
+    if (count == 0) {
+        SLT_CUDA_TRY(cudaStreamSynchronize(stream));
+        return SLT_OK;
+    }
     TRY(dsys.alloc(sizeof(Sys) * list.size(), stream));
     TRY(ctr.alloc(sizeof(int) * size_t(itermax + 2), stream));
     TRY(st.alloc(sizeof(int) * size_t(count), stream));
@@ -736,10 +1105,9 @@ extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const
     SLT_CUDA_TRY(cudaMemcpyAsync(dsys.p, list.data(), sizeof(Sys) * list.size(), cudaMemcpyHostToDevice, stream));
     SLT_CUDA_TRY(cudaMemsetAsync(ctr.p, 0, sizeof(int) * size_t(itermax + 2), stream));
 
-    TimerSet tm(stream);
     tm.start("vbatched_mixed::factor_lo");
     // phase 1: norm + cast + FP32 factor + first solve
-    const size_t smem_f = std::max(factor_smem(false), sizeof(float) * size_t(std::max(1, maxn)) * size_t(maxr));
+    const size_t smem_f = solve_smem(false, maxn, maxr);
     const void* kf = reinterpret_cast<const void*>(&vb_mixed_factor_kernel);
     TRY(set_smem(kf, smem_f));
     int* counters = ctr.as<int>();
@@ -751,7 +1119,7 @@ extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const
     tm.stop("vbatched_mixed::factor_lo");
     tm.start("vbatched_mixed::refine");
     // phase 2: itermax + 1 refinement steps, captured once as a CUDA graph
-    const size_t smem_r = sizeof(double) * size_t(std::max(1, maxn)) * size_t(maxr);
+    const size_t smem_r = kTileBytes + sizeof(double) * size_t(std::max(1, maxn)) * size_t(maxr);
     const void* kr = reinterpret_cast<const void*>(&vb_refine_kernel);
     TRY(set_smem(kr, smem_r));
     const int gr = grid_for(kr, smem_r, count);
@@ -789,11 +1157,12 @@ extern "C" int slt_dsolve_mixed_vbatched(int64_t batch, const int* d_kind, const
         if (hst[size_t(w)] == 2) {
             Sys s = list[size_t(w)];
             s.lo = nullptr;
+            s.pb = tune[size_t(s.id)].pb_fp64;
             fb.push_back(s);
         }
     if (fb.empty()) return SLT_OK;
     tm.start("vbatched_mixed::fallback");
     struct StopAtExit { TimerSet& t; ~StopAtExit() { t.stop("vbatched_mixed::fallback"); } } stop_fb{tm};
-    const size_t smem_p = std::max(factor_smem(true), sizeof(double) * size_t(std::max(1, maxn)) * size_t(maxr));
+    const size_t smem_p = solve_smem(true, maxn, maxr);
     return run_plain(fb, d_info, stream, smem_p);
 }

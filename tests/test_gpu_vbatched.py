@@ -122,3 +122,49 @@ def test_vbatched_rejects_oversize(slt):
     b = slt.colmajor(torch.zeros(2049, 1, dtype=torch.float64, device="cuda"))
     with pytest.raises(slt.SlateError):
         slt.solve_vbatched(slt.VBatch([(0, a, b)]))
+
+
+@pytest.mark.parametrize("pb", [16, 32])
+def test_vbatched_plain_panel_width(orc, slt, monkeypatch, pb):
+    """Both panel widths the tuning table can pick: same backward error bar,
+    and the pivots of either width equal the oracle's (partial pivoting does
+    not depend on the blocking) on rows with a clear pivot margin."""
+    import torch
+    monkeypatch.setenv("SLT_VBATCHED_PB", str(pb))
+    systems = _systems(orc, [15, 16, 17, 33, 100, 161, 250], 7, nrhs_max=9)
+    dsys = _to_dev_systems(slt, systems)
+    vb = slt.VBatch(dsys)
+    info = slt.solve_vbatched(vb)
+    torch.cuda.synchronize()
+    assert (info == 0).all()
+    for t, ((k, A, B), (_, dA, dB)) in enumerate(zip(systems, dsys)):
+        n = A.shape[0]
+        assert berr(orc, A, to_host(dB), B, sym=(k == 1)) <= 3 * EPS, (t, n, k, pb)
+        if k == 0:
+            oinfo, pt, po, oipiv, mg = orc.getrf(A.copy(order="F"), 32, 32, margins=True)
+            gip = vb.ipiv_t[t][:n].cpu().numpy().astype(np.int64)
+            robust = mg > 1 + 1e3 * n * EPS
+            assert np.array_equal(gip[robust], oipiv[robust]), (t, n, pb)
+
+
+@pytest.mark.parametrize("tier,pb", [("fp32", 16), ("fp32", 32), ("fp64", 32)])
+def test_vbatched_mixed_tiers(orc, slt, monkeypatch, tier, pb):
+    """The mixed API in each tier the table can pick: FP32 factor + FP64
+    refinement (iter >= 0) or the direct FP64 solve of a copy (iter 0);
+    A and B untouched either way."""
+    import torch
+    monkeypatch.setenv("SLT_VBATCHED_TIER", tier)
+    monkeypatch.setenv("SLT_VBATCHED_PB", str(pb))
+    systems = _systems(orc, [1, 16, 31, 64, 97, 200], 8)
+    dsys = _to_dev_systems(slt, systems)
+    X = [slt.colmajor(torch.zeros_like(b)) for _, _, b in dsys]
+    vb = slt.VBatch(dsys, X=X)
+    info, it = slt.solve_mixed_vbatched(vb, slt.Options())
+    torch.cuda.synchronize()
+    assert (info == 0).all()
+    assert ((it == 0).all() if tier == "fp64" else (it >= 0).all()), it
+    for t, ((k, A, B), (_, dA, dB), x) in enumerate(zip(systems, dsys, X)):
+        n = A.shape[0]
+        bar = 3 * EPS if tier == "fp64" else 3 * n * EPS
+        assert berr(orc, A, to_host(x), B, sym=(k == 1)) <= bar, (t, n, k)
+        assert np.array_equal(to_host(dA), A) and np.array_equal(to_host(dB), B)
