@@ -7,6 +7,7 @@
 // ipiv (lapack_api/lapack_gesv.cc:90-100).
 
 #include "drivers.h"
+#include "lapack_opts.h"
 
 #include <algorithm>
 #include <cstdlib>
@@ -60,21 +61,7 @@ int64_t env_int(const char* name, int64_t dflt)
     return x != 0 ? x : dflt;
 }
 
-slt_options lapack_opts()
-{
-    slt_options o;
-    slt_options_default(&o);
-    o.nb = env_int("SLATE_LAPACK_NB", 512);
-    o.ib = std::min<int64_t>(env_int("SLATE_LAPACK_IB", 32), o.nb);
-    if (const char* p = std::getenv("SLATE_LAPACK_FACTOR_PRECISION")) {
-        std::string v(p);
-        if (v == "fp32") o.factor_precision = SLT_PREC_FP32;
-        else if (v == "tf32") o.factor_precision = SLT_PREC_TF32;
-        else if (v == "bf16") o.factor_precision = SLT_PREC_BF16;
-        else if (v == "fp16") o.factor_precision = SLT_PREC_FP16;
-    }
-    return o;
-}
+thread_local const slt_options* t_opts_override = nullptr;
 
 // Host <-> device helpers for the LAPACK entry points.
 template <typename T>
@@ -136,6 +123,30 @@ int getrf_device_impl(int64_t m, int64_t n, T* dA, int64_t lda, int* d_ipiv, con
 }
 
 } // namespace
+
+namespace slt {
+
+slt_options lapack_opts()
+{
+    if (t_opts_override) return *t_opts_override;
+    slt_options o;
+    slt_options_default(&o);
+    o.nb = env_int("SLATE_LAPACK_NB", 512);
+    o.ib = std::min<int64_t>(env_int("SLATE_LAPACK_IB", 32), o.nb);
+    if (const char* p = std::getenv("SLATE_LAPACK_FACTOR_PRECISION")) {
+        std::string v(p);
+        if (v == "fp32") o.factor_precision = SLT_PREC_FP32;
+        else if (v == "tf32") o.factor_precision = SLT_PREC_TF32;
+        else if (v == "bf16") o.factor_precision = SLT_PREC_BF16;
+        else if (v == "fp16") o.factor_precision = SLT_PREC_FP16;
+    }
+    return o;
+}
+
+LapackOptsScope::LapackOptsScope(const slt_options& o) : prev_(t_opts_override) { t_opts_override = &o; }
+LapackOptsScope::~LapackOptsScope() { t_opts_override = prev_; }
+
+} // namespace slt
 
 extern "C" {
 

@@ -12,6 +12,7 @@
 // pivots.
 
 #include "drivers.h"
+#include "lapack_opts.h"
 
 #include <algorithm>
 #include <cstring>
@@ -97,12 +98,6 @@ cudaStream_t stream_()
     return st.s;
 }
 
-int64_t env_nb()
-{
-    const char* v = std::getenv("SLATE_LAPACK_NB");
-    const int64_t x = v ? std::strtoll(v, nullptr, 0) : 0;
-    return x > 0 ? x : 512;
-}
 
 int upload(const double* a, int64_t n, int64_t lda, DevBuf& d, cudaStream_t s)
 {
@@ -129,9 +124,7 @@ void getri_impl(int n, double* a, int lda, const int* ipiv, int* info)
     if (lda < std::max(1, n)) { *info = -3; return; }
     if (n == 0) return;
     cudaStream_t s = stream_();
-    slt_options o;
-    slt_options_default(&o);
-    o.nb = env_nb();
+    const slt_options o = lapack_opts();
     std::vector<int> rel(static_cast<size_t>(n));
     for (int r = 0; r < n; ++r) rel[size_t(r)] = int(ipiv[r] - 1 - (r / o.nb) * o.nb);
     DevBuf dA, dP;
@@ -175,9 +168,7 @@ void potri_impl(char uplo, int n, double* a, int lda, int* info)
     if (lda < std::max(1, n)) { *info = -4; return; }
     if (n == 0) return;
     cudaStream_t s = stream_();
-    slt_options o;
-    slt_options_default(&o);
-    o.nb = env_nb();
+    const slt_options o = lapack_opts();
     DevBuf dL;
     if (lower_factor(uplo, n, a, lda, dL, s)) { *info = -100; return; }
     int64_t inf = 0;
@@ -206,9 +197,7 @@ void gecon_impl(char norm, int n, const double* a, int lda, double anorm, double
     if (lda < std::max(1, n)) { *info = -4; return; }
     if (anorm < 0) { *info = -5; return; }
     cudaStream_t s = stream_();
-    slt_options o;
-    slt_options_default(&o);
-    o.nb = env_nb();
+    const slt_options o = lapack_opts();
     if (n == 0) { *rcond = 1.0; return; }
     DevBuf dA, dP;
     if (upload(a, n, lda, dA, s) || identity_pivots(n, o.nb, dP, s)) { *info = -100; return; }
@@ -226,9 +215,7 @@ void pocon_impl(char uplo, int n, const double* a, int lda, double anorm, double
     if (anorm < 0) { *info = -5; return; }
     if (n == 0) { *rcond = 1.0; return; }
     cudaStream_t s = stream_();
-    slt_options o;
-    slt_options_default(&o);
-    o.nb = env_nb();
+    const slt_options o = lapack_opts();
     DevBuf dL;
     if (lower_factor(uplo, n, a, lda, dL, s)) { *info = -100; return; }
     const int rc = slt_dpocondest_device('1', n, dL.as<double>(), n, anorm, rcond, &o, s);
