@@ -54,6 +54,7 @@ typedef struct slt_options {
     int     lo_retry;         /* 16-bit factor failed or did not converge: retry
                                  with an FP32 factor before the FP64 fallback;
                                  -1 auto (on for BF16/FP16), 0, 1               */
+    int64_t depth;            /* Option::Depth of gesv_rbt's butterflies, default 2 */
 } slt_options;
 
 /* Refinement of the mixed solvers.  SLT_REFINE_IR is SLATE's gesv_mixed loop
@@ -146,6 +147,25 @@ int slt_dsgesv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, in
                             const double* dB, int64_t ldb, double* dX, int64_t ldx,
                             const slt_options* opts, slt_stream_t stream, int* iter,
                             int64_t* info);
+/* slate::gesv_rbt, src/gesv_rbt.cc:100-230: random butterfly transform of
+ * depth opts->depth, LU without pivoting of the transformed matrix, FP64
+ * refinement against A (iter 0..itermax, or -(itermax+1) and the
+ * partial-pivoting fallback).  dA receives the factors of the transformed
+ * matrix (after the fallback: A itself, as SLATE leaves it). */
+int slt_dgesv_rbt_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, const double* dB, int64_t ldb,
+                         double* dX, int64_t ldx, const slt_options* opts, slt_stream_t stream, int* iter,
+                         int64_t* info);
+/* slate::gerbt(U, A, V) and gerbt(U, B) (src/gerbt.cc, Tile_gerbt.hh): one
+ * random diagonal of n entries per side (SLATE's packed n x depth storage
+ * uses its first column at every level), levels of tiles of nb.
+ *   gerbt2: A <- W_U^T A W_V;  gerbt1: B <- W^T B (trans 'T') or W B ('N').
+ * rbt_diag: w = exp(r / 20), r uniform(-1, 1) from the Philox stream of seed
+ * (internal_rbt_generate.cc:36-50). */
+int slt_dgerbt2_device(int64_t n, double* dA, int64_t lda, const double* u, const double* v, int64_t depth,
+                       int64_t nb, slt_stream_t stream);
+int slt_dgerbt1_device(char trans, int64_t n, int64_t nrhs, double* dB, int64_t ldb, const double* w,
+                       int64_t depth, int64_t nb, slt_stream_t stream);
+int slt_drbt_diag_device(int64_t n, int64_t seed, double* w, slt_stream_t stream);
 /* slate::posv_mixed, src/posv_mixed.cc:105-320 (A lower) */
 int slt_dsposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, const double* dB,
                       int64_t ldb, double* dX, int64_t ldx, const slt_options* opts,

@@ -41,7 +41,7 @@ inline void check(int status) { if (status != 0) throw Exception(status); }
 
 enum class Option {
     Lookahead, BlockSize, InnerBlocking, MaxPanelThreads, Tolerance, Target, MaxIterations,
-    UseFallbackSolver, PivotThreshold, MethodLU,
+    UseFallbackSolver, PivotThreshold, MethodLU, Depth,
     FactorPrecision, Refine, Equilibrate          // this library's additions
 };
 enum class Target : char { Host = 'H', HostTask = 'T', HostNest = 'N', HostBatch = 'B', Devices = 'D' };
@@ -142,6 +142,7 @@ inline slt_options to_c(const Options& opts, int64_t nb)
             case Option::Tolerance:         o.tolerance = kv.second.d(); break;
             case Option::UseFallbackSolver: o.use_fallback = int(kv.second.i() != 0); break;
             case Option::PivotThreshold:    o.pivot_threshold = kv.second.d(); break;
+            case Option::Depth:             o.depth = kv.second.i(); break;
             case Option::MethodLU:
                 if (kv.second.i() == int64_t(MethodLU::NoPiv)) o.pivot_threshold = 0.0;
                 break;
@@ -229,6 +230,19 @@ inline int64_t gesv_mixed(Matrix<double>& A, Pivots& pivots, Matrix<double>& B, 
     check(slt_dsgesv_device(A.n(), B.n(), A.data(), A.stride(), piv.p, B.data(), B.stride(), X.data(), X.stride(),
                             &o, nullptr, &iter, &info));
     pivots_from_device(piv.p, A.n(), A.tileNb(0), pivots);
+    return info;
+}
+
+// slate::gesv_rbt (src/gesv_rbt.cc): random butterfly transform (Option::Depth,
+// default 2), LU without pivoting, FP64 refinement; A receives the factors of
+// the transformed matrix.  Returns info.
+inline int64_t gesv_rbt(Matrix<double>& A, Matrix<double>& B, Matrix<double>& X, int& iter,
+                        const Options& opts = Options())
+{
+    slt_options o = detail::to_c(opts, A.tileNb(0));
+    int64_t info = 0;
+    check(slt_dgesv_rbt_device(A.n(), B.n(), A.data(), A.stride(), B.data(), B.stride(), X.data(), X.stride(), &o,
+                               nullptr, &iter, &info));
     return info;
 }
 

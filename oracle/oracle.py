@@ -243,6 +243,126 @@ def posv_mixed_gmres(A, b, nb, itermax=30, tol=0.0, use_fallback=True):
     return int(info), X, int(it.value)
 
 
+# ---------------------------------------------------------------------------
+# Random butterfly transforms (src/gerbt.cc, src/internal/Tile_gerbt.hh) and
+# gesv_rbt (src/gesv_rbt.cc:100-230), restated with numpy: every product and
+# sum is one numpy operation, rounded once, in the order Tile_gerbt.hh writes
+# it, so the results are bit-comparable with a kernel that does not fuse.
+
+def rbt_half(n, nb, depth, k):
+    """Half length of level k (0 = largest) in elements (gerbt_iterate_1d/_2d:
+    half_len = 2^(d-k-1) * ceil(nt / 2^d) tiles of nb)."""
+    nt = -(-n // nb)
+    inner = -(-nt // (1 << depth))
+    return (1 << (depth - k - 1)) * inner * nb
+
+
+def _halves(n, H):
+    x = np.concatenate([np.arange(b, min(b + H, n)) for b in range(0, n, 2 * H)]).astype(np.int64)
+    return x[x + H < n], x[x + H >= n]          # paired, unpaired first-half indices
+
+
+def gerbt2(A, u, v, depth, nb):
+    """A <- W_U^T A W_V, levels smallest first (gerbt(U, A, V),
+    src/gerbt.cc:160-200; Tile_gerbt.hh:22-80)."""
+    A = np.array(A, dtype=np.float64, order="F")
+    n = A.shape[0]
+    h, r2 = 0.5, 1.0 / np.sqrt(2.0)
+    for k in range(depth - 1, -1, -1):
+        H = rbt_half(n, nb, depth, k)
+        xp, xu = _halves(n, H)
+        ix = np.ix_
+        a11 = A[ix(xp, xp)].copy(); a12 = A[ix(xp, xp + H)].copy()
+        a21 = A[ix(xp + H, xp)].copy(); a22 = A[ix(xp + H, xp + H)].copy()
+        s1, s2, d1, d2 = a11 + a12, a21 + a22, a11 - a12, a21 - a22
+        u1, u2 = u[xp][:, None], u[xp + H][:, None]
+        v1, v2 = v[xp][None, :], v[xp + H][None, :]
+        A[ix(xp, xp)] = ((h * u1) * (s1 + s2)) * v1
+        A[ix(xp, xp + H)] = ((h * u1) * (d1 + d2)) * v2
+        A[ix(xp + H, xp)] = ((h * u2) * (s1 - s2)) * v1
+        A[ix(xp + H, xp + H)] = ((h * u2) * (d1 - d2)) * v2
+        if len(xu):
+            # row unpaired, column paired
+            b11 = A[ix(xu, xp)].copy(); b12 = A[ix(xu, xp + H)].copy()
+            uu = u[xu][:, None]
+            A[ix(xu, xp)] = ((r2 * uu) * (b11 + b12)) * v1
+            A[ix(xu, xp + H)] = ((r2 * uu) * (b11 - b12)) * v2
+            # row paired, column unpaired
+            c11 = A[ix(xp, xu)].copy(); c21 = A[ix(xp + H, xu)].copy()
+            vu = v[xu][None, :]
+            A[ix(xp, xu)] = ((r2 * u1) * (c11 + c21)) * vu
+            A[ix(xp + H, xu)] = ((r2 * u2) * (c11 - c21)) * vu
+            # both unpaired
+            A[ix(xu, xu)] = (uu * A[ix(xu, xu)]) * vu
+    return A
+
+
+def gerbt1(trans, B, w, depth, nb):
+    """B <- W^T B ('T', smallest first) or W B ('N', largest first)
+    (gerbt(U, B), src/gerbt.cc:230-280; Tile_gerbt.hh:84-230)."""
+    B = np.array(B, dtype=np.float64, order="F")
+    n = B.shape[0]
+    r2 = 1.0 / np.sqrt(2.0)
+    levels = range(depth - 1, -1, -1) if trans == "T" else range(depth)
+    for k in levels:
+        H = rbt_half(n, nb, depth, k)
+        xp, xu = _halves(n, H)
+        b1, b2 = B[xp, :].copy(), B[xp + H, :].copy()
+        w1, w2 = w[xp][:, None], w[xp + H][:, None]
+        if trans == "T":
+            B[xp, :] = (r2 * w1) * (b1 + b2)
+            B[xp + H, :] = (r2 * w2) * (b1 - b2)
+        else:
+            B[xp, :] = r2 * ((w1 * b1) + (w2 * b2))
+            B[xp + H, :] = r2 * ((w1 * b1) - (w2 * b2))
+        if len(xu):
+            B[xu, :] = w[xu][:, None] * B[xu, :]
+    return B
+
+
+def gesv_rbt(A, B, nb, u, v, depth=2, ib=16, itermax=30, tol=0.0, use_fallback=True):
+    """slate::gesv_rbt with the given diagonals: returns (X, iter, info)
+    (src/gesv_rbt.cc:100-230; stopping test internal_util.hh:121-138)."""
+    n, nrhs = B.shape
+    eps = np.finfo(np.float64).eps
+    tol = tol if tol > 0 else eps * np.sqrt(n)
+    cte = np.abs(A).sum(1).max() * tol
+    Ap = gerbt2(A, u, v, depth, nb)
+    info, pt, po, _, _ = getrf(Ap, nb, ib, threshold=0.0)
+
+    def solve(Y):
+        Y = gerbt1("T", Y, u, depth, nb)
+        getrs(Ap, pt, po, Y, nb)
+        return gerbt1("N", Y, v, depth, nb)
+
+    X = np.array(B, order="F")
+    if info == 0:
+        X = solve(X)
+    if itermax == 0:
+        return X, 0, info
+
+    def conv(X):
+        R = np.asfortranarray(B - A @ X)
+        return R, bool(np.all(np.abs(R).max(0) <= np.abs(X).max(0) * cte))
+
+    it = 0
+    done = False
+    if info == 0:
+        R, done = conv(X)
+        while not done and it < itermax:
+            X = X + solve(R)
+            it += 1
+            R, done = conv(X)
+    if done:
+        return X, it, 0
+    if use_fallback:
+        A2 = np.array(A, order="F")
+        X = np.array(B, order="F")
+        finfo, _, _ = gesv(A2, X, nb, ib)
+        return X, -itermax - 1, finfo
+    return X, -itermax - 1, info
+
+
 def backward_error(A, X, B, sym_lower=False):
     """||B - A X||_1 / (n ||A||_1 ||X||_1), the SLATE tester's check."""
     n, nrhs = X.shape

@@ -34,7 +34,8 @@ class _Options(ctypes.Structure):
                 ("max_iterations", ctypes.c_int64), ("tolerance", ctypes.c_double),
                 ("use_fallback", ctypes.c_int), ("pivot_threshold", ctypes.c_double),
                 ("factor_precision", ctypes.c_int), ("gemm_engine", ctypes.c_int),
-                ("refine", ctypes.c_int), ("equilibrate", ctypes.c_int), ("lo_retry", ctypes.c_int)]
+                ("refine", ctypes.c_int), ("equilibrate", ctypes.c_int), ("lo_retry", ctypes.c_int),
+                ("depth", ctypes.c_int64)]
 
 
 @dataclass
@@ -52,6 +53,7 @@ class Options:
     refine: object = "ir"          # "ir" (SLATE) or "ir+gmres" (GMRES-IR once IR stalls)
     equilibrate: int = -1          # -1 auto (on for bf16/fp16), 0 off, 1 on
     lo_retry: int = -1             # -1 auto (on for bf16/fp16): FP32 retry before the FP64 fallback
+    depth: int = 2                 # Option::Depth of gesv_rbt's butterflies
 
     def _c(self):
         p = self.factor_precision
@@ -60,7 +62,7 @@ class Options:
                         float(self.tolerance), int(bool(self.use_fallback)),
                         float(self.pivot_threshold), p, int(self.gemm_engine),
                         _REFINE_NAMES[self.refine] if isinstance(self.refine, str) else int(self.refine),
-                        int(self.equilibrate), int(self.lo_retry))
+                        int(self.equilibrate), int(self.lo_retry), int(self.depth))
 
 
 _lib = None
@@ -87,6 +89,7 @@ def lib():
             "slt_dpotrs_device": [i64, i64, vp, i64, vp, i64, optp, vp],
             "slt_dposv_device": [i64, i64, vp, i64, vp, i64, optp, vp, dp],
             "slt_dsgesv_device": [i64, i64, vp, i64, ip, vp, i64, vp, i64, optp, vp, iptr, dp],
+            "slt_dgesv_rbt_device": [i64, i64, vp, i64, vp, i64, vp, i64, optp, vp, iptr, dp],
             "slt_dsgesv_gmres_device": [i64, i64, vp, i64, ip, vp, i64, vp, i64, optp, vp, iptr, dp],
             "slt_dsposv_device": [i64, i64, vp, i64, vp, i64, vp, i64, optp, vp, iptr, dp],
             "slt_dsposv_gmres_device": [i64, i64, vp, i64, vp, i64, vp, i64, optp, vp, iptr, dp],
@@ -288,6 +291,60 @@ def gesv_mixed(A, B, X, opts=None):
 def gesv_mixed_gmres(A, B, X, opts=None):
     """slate::gesv_mixed_gmres: low-precision LU + FP64 FGMRES-IR."""
     return _mixed(lib().slt_dsgesv_gmres_device, False, A, B, X, opts)
+
+
+def gesv_rbt(A, B, X, opts=None):
+    """slate::gesv_rbt: random butterfly transform, LU without pivoting, FP64
+    refinement (src/gesv_rbt.cc).  A receives the factors of the transformed
+    matrix.  Returns (info, iter)."""
+    import torch
+    po, o = _opts(opts)
+    info = ctypes.c_int64(0)
+    it = ctypes.c_int(0)
+    _check(lib().slt_dgesv_rbt_device(A.shape[0], B.shape[1], _dev(A, torch.float64), _ld(A),
+                                      _dev(B, torch.float64), _ld(B), _dev(X, torch.float64), _ld(X), po,
+                                      _stream(), ctypes.byref(it), ctypes.byref(info)))
+    return int(info.value), int(it.value)
+
+
+def _vec(w, n):
+    import torch
+    if not (isinstance(w, torch.Tensor) and w.is_cuda and w.dtype == torch.float64 and w.is_contiguous()
+            and w.numel() >= n):
+        raise TypeError("expected a contiguous float64 CUDA vector of at least %d entries" % n)
+    return ctypes.c_void_p(w.data_ptr())
+
+
+def gerbt2(A, u, v, depth, nb):
+    """slate::gerbt(U, A, V): A <- W_U^T A W_V with diagonals u, v (n)."""
+    import torch
+    L = lib()
+    L.slt_dgerbt2_device.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]
+    _check(L.slt_dgerbt2_device(A.shape[0], _dev(A, torch.float64), _ld(A), _vec(u, A.shape[0]),
+                                _vec(v, A.shape[0]), int(depth), int(nb), _stream()))
+
+
+def gerbt1(trans, B, w, depth, nb):
+    """slate::gerbt(U, B): B <- W^T B (trans 'T') or W B ('N')."""
+    import torch
+    L = lib()
+    L.slt_dgerbt1_device.argtypes = [ctypes.c_char, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                     ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                     ctypes.c_void_p]
+    _check(L.slt_dgerbt1_device(trans.encode() if isinstance(trans, str) else trans, B.shape[0], B.shape[1],
+                                _dev(B, torch.float64), _ld(B), _vec(w, B.shape[0]), int(depth), int(nb),
+                                _stream()))
+
+
+def rbt_diag(n, seed, device="cuda"):
+    """The random butterfly diagonal exp(r / 20), r uniform(-1, 1) (Philox)."""
+    import torch
+    w = torch.empty(n, dtype=torch.float64, device=device)
+    L = lib()
+    L.slt_drbt_diag_device.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+    _check(L.slt_drbt_diag_device(int(n), int(seed), ctypes.c_void_p(w.data_ptr()), _stream()))
+    return w
 
 
 def posv_mixed(A, B, X, opts=None):

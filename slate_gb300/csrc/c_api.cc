@@ -30,7 +30,7 @@ thread_local int g_status = 0;
 
 struct COpts {
     slt_options o;
-    int64_t chunk = 0, panel_threads = 1, depth = 2;
+    int64_t chunk = 0, panel_threads = 1;
     char target = 'D', method_lu = '*';
     bool hold = false;
     COpts() { slt_options_default(&o); }
@@ -276,7 +276,7 @@ SLT_OPT(InnerBlocking, int64_t, o.ib)
 SLT_OPT(MaxPanelThreads, int64_t, panel_threads)
 SLT_OPT(Tolerance, double, o.tolerance)
 SLT_OPT(Target, slate_Target, target)
-SLT_OPT(Depth, int64_t, depth)
+SLT_OPT(Depth, int64_t, o.depth)
 SLT_OPT(MaxIterations, int64_t, o.max_iterations)
 SLT_OPT(PivotThreshold, double, o.pivot_threshold)
 SLT_OPT(MethodLU, slate_MethodLU, method_lu)

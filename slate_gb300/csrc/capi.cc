@@ -165,6 +165,7 @@ void slt_options_default(slt_options* o)
     o->refine = SLT_REFINE_IR;
     o->equilibrate = -1;
     o->lo_retry = -1;
+    o->depth = 2;
 }
 
 const char* slt_status_string(int st)
@@ -326,6 +327,19 @@ int slt_dposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, double* d
     tm.stop("posv::potrs");
     tm.stop("posv");
     return finish_factor(st.fc, nullptr, s);
+}
+
+int slt_dgesv_rbt_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, const double* dB, int64_t ldb,
+                         double* dX, int64_t ldx, const slt_options* opts, slt_stream_t stream, int* iter,
+                         int64_t* info)
+{
+    slt_options o = resolve(opts);
+    int it = 0;
+    int64_t inf = 0;
+    const int rc = gesv_rbt_dev(n, nrhs, dA, lda, dB, ldb, dX, ldx, o, &it, &inf, as_stream(stream));
+    if (iter) *iter = it;
+    if (info) *info = inf;
+    return rc;
 }
 
 int slt_dsgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_ipiv, const double* dB,

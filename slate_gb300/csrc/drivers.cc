@@ -657,6 +657,131 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
     return finish_factor(fc, nullptr, s);   // bounded-wait status of every launch above
 }
 
+// gesv_rbt (src/gesv_rbt.cc:100-230): A' = W_U^T A W_V with depth-d random
+// butterflies (rbt.cu), LU of A' without pivoting, X = W_V A'^{-1} W_U^T B,
+// then FP64 iterative refinement against the original A to SLATE's stopping
+// test; not converged after itermax steps -> iter = -(itermax + 1) and, with
+// use_fallback, X from partial-pivoting gesv of A.  On return A holds the
+// factors of A' (or, after the fallback, A itself, as SLATE restores it).
+// The random diagonals come from the Philox stream (seeds 42 and 42 + mt,
+// SLATE's rbt_seed and seed + mt).
+int gesv_rbt_dev(int64_t n, int64_t nrhs, double* A, int64_t lda, const double* B, int64_t ldb, double* X,
+                 int64_t ldx, const slt_options& o, int* iter, int64_t* info, cudaStream_t s)
+{
+    if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(1, n) || ldb < std::max<int64_t>(1, n) ||
+        ldx < std::max<int64_t>(1, n))
+        return SLT_ERR_ARG;
+    *iter = 0;
+    *info = 0;
+    if (n == 0 || nrhs == 0) return SLT_OK;
+    TimerSet tm(s);
+    tm.start("gesv_rbt");
+    const double eps = std::numeric_limits<double>::epsilon();
+    const double tol = o.tolerance > 0 ? o.tolerance : eps * std::sqrt(double(n));
+    const int64_t itermax = o.max_iterations;
+    const int64_t nb = eff_nb(o);
+    const int64_t d = o.depth >= 0 ? o.depth : 2;
+    const int64_t mt = (n + nb - 1) / nb;
+
+    DevBuf uv, Acp, R, nws, scal, col, st, piv;
+    TRY(uv.alloc(sizeof(double) * 2 * size_t(n), s));
+    double* u = uv.as<double>();
+    double* v = u + n;
+    TRY(slt_drbt_diag_device(n, 42, u, s));
+    TRY(slt_drbt_diag_device(n, 42 + mt, v, s));
+    TRY(st.alloc(2 * sizeof(int), s));
+    SLT_CUDA_TRY(cudaMemsetAsync(st.p, 0, 2 * sizeof(int), s));
+    FactorCtx fc{st.as<int>(), st.as<int>() + 1};
+    TRY(piv.alloc(sizeof(int) * size_t(n), s));
+
+    double cte = 0;
+    if (itermax > 0) {
+        TRY(Acp.alloc(sizeof(double) * size_t(n) * size_t(n), s));
+        TRY(R.alloc(sizeof(double) * size_t(n) * size_t(nrhs), s));
+        TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, std::min<int64_t>(nrhs, 16))), s));
+        TRY(scal.alloc(sizeof(double) * 4, s));
+        TRY(col.alloc(sizeof(double) * 2 * size_t(nrhs), s));
+        TRY(slt_dcopy2d(n, n, A, lda, Acp.as<double>(), n, s));
+        double Anorm = 0;
+        TRY(slt_dnorm_inf(n, n, A, lda, 0, scal.as<double>(), nws.p, s));
+        TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
+        cte = Anorm * tol;
+    }
+    TRY(slt_dcopy2d(n, nrhs, B, ldb, X, ldx, s));
+
+    // factor A' without pivoting (the panel's threshold rule with threshold 0)
+    slt_options onp = o;
+    onp.pivot_threshold = 0.0;
+    onp.factor_precision = SLT_PREC_FP64;
+    tm.start("gesv_rbt::gerbt");
+    TRY(slt_dgerbt2_device(n, A, lda, u, v, d, nb, s));
+    tm.stop("gesv_rbt::gerbt");
+    tm.start("gesv_rbt::getrf_nopiv");
+    TRY(getrf_dev<double>(n, n, A, lda, piv.as<int>(), onp, fc, s));
+    tm.stop("gesv_rbt::getrf_nopiv");
+    int64_t finfo = 0;
+    TRY(finish_factor(fc, &finfo, s));
+    // X = W_V A'^{-1} W_U^T X, one right-hand-side block
+    auto rbt_solve = [&](double* Y, int64_t ldy) -> int {
+        TRY(slt_dgerbt1_device('T', n, nrhs, Y, ldy, u, d, nb, s));
+        TRY(getrs_dev<double>(n, nrhs, A, lda, piv.as<int>(), nb, Y, ldy, fc.d_status, s));
+        return slt_dgerbt1_device('N', n, nrhs, Y, ldy, v, d, nb, s);
+    };
+    bool conv = false;
+    if (finfo == 0) {
+        tm.start("gesv_rbt::getrs_nopiv");
+        TRY(rbt_solve(X, ldx));
+        tm.stop("gesv_rbt::getrs_nopiv");
+    }
+    if (itermax == 0) {
+        *info = finfo;
+        tm.stop("gesv_rbt");
+        return finish_factor(fc, nullptr, s);
+    }
+    std::vector<double> h(2 * size_t(nrhs));
+    double* dcx = col.as<double>();
+    double* dcr = dcx + nrhs;
+    auto residual = [&]() -> int {
+        for (int64_t c0 = 0; c0 < nrhs; c0 += 16) {
+            const int64_t nc = std::min<int64_t>(16, nrhs - c0);
+            TRY(slt_dresidual(n, nc, Acp.as<double>(), n, 0, B + c0 * ldb, ldb, X + c0 * ldx, ldx,
+                              R.as<double>() + c0 * n, n, nws.p, s));
+        }
+        TRY(slt_dcolmax(n, nrhs, X, ldx, dcx, s));
+        TRY(slt_dcolmax(n, nrhs, R.as<double>(), n, dcr, s));
+        return read_doubles(dcx, h.data(), 2 * nrhs, s);
+    };
+    if (finfo == 0) {
+        tm.start("gesv_rbt::refine");
+        TRY(residual());
+        if (converged(h.data() + nrhs, h.data(), nrhs, cte)) { *iter = 0; conv = true; }
+        for (int64_t it = 0; it < itermax && !conv; ++it) {
+            TRY(rbt_solve(R.as<double>(), n));
+            TRY(slt_dgeadd(n, nrhs, 1.0, R.as<double>(), n, 1.0, X, ldx, s));
+            TRY(residual());
+            if (converged(h.data() + nrhs, h.data(), nrhs, cte)) { *iter = int(it + 1); conv = true; }
+        }
+        tm.stop("gesv_rbt::refine");
+    }
+    *info = 0;
+    if (!conv) {
+        *iter = int(-itermax - 1);
+        if (o.use_fallback) {
+            // A <- original; X from partial-pivoting gesv of the copy
+            TRY(slt_dcopy2d(n, n, Acp.as<double>(), n, A, lda, s));
+            slt_options o64 = o;
+            o64.factor_precision = SLT_PREC_FP64;
+            TRY(fallback_fp64(0, n, nrhs, Acp.as<double>(), n, piv.as<int>(), B, ldb, X, ldx, o64, info, tm,
+                              "gesv_rbt", s));
+        }
+        else {
+            *info = finfo;
+        }
+    }
+    tm.stop("gesv_rbt");
+    return finish_factor(fc, nullptr, s);
+}
+
 // gesv_mixed_gmres / posv_mixed_gmres (src/gesv_mixed_gmres.cc:110-410,
 // src/posv_mixed_gmres.cc:109-436): FGMRES(restart) preconditioned by the
 // low-precision factors, CGS2 Arnoldi in FP64, Givens rotations on the

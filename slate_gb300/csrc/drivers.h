@@ -112,6 +112,9 @@ int gesv_mixed_gmres_dev(int chol, int64_t n, int64_t nrhs, double* A, int64_t l
                          const double* B, int64_t ldb, double* X, int64_t ldx,
                          const slt_options& o, int* iter, int64_t* info, cudaStream_t s);
 
+int gesv_rbt_dev(int64_t n, int64_t nrhs, double* A, int64_t lda, const double* B, int64_t ldb, double* X,
+                 int64_t ldx, const slt_options& o, int* iter, int64_t* info, cudaStream_t s);
+
 // Read the factorisation status words; returns an slt status (timeout wins).
 int finish_factor(FactorCtx& fc, int64_t* info, cudaStream_t s);
 
