@@ -35,7 +35,8 @@ typedef intptr_t slate_mpi_comm_t;   /* MPI_Comm placeholder, ignored */
 
 typedef char slate_Uplo;             /* 'U', 'L' (include/slate/c_api/types.h) */
 typedef char slate_Target;           /* 'H', 'T', 'N', 'B', 'D' */
-typedef char slate_MethodLU;         /* '*', 'P', 'N' (NoPiv) supported; 'C', 'R', 'B' rejected */
+typedef char slate_MethodLU;         /* '*', 'P', 'N' (NoPiv), 'C' (CALU) supported; 'R', 'B' rejected */
+typedef char slate_Norm;             /* '1' / 'O' (one norm), 'I' (infinity norm) */
 
 typedef void* slate_Options;
 typedef struct slate_Pivots_struct* slate_Pivots;
@@ -101,10 +102,32 @@ void slate_lu_factor_r32(slate_Matrix_r32 A, slate_Pivots pivots, slate_Options 
 void slate_lu_solve_using_factor_r32(slate_Matrix_r32 A, slate_Pivots pivots, slate_Matrix_r32 B,
                                      slate_Options opts);
 
+/* MethodLU::NoPiv forms (src/c_api/wrappers.cc:715-880): getrf_nopiv has no
+ * pivots; solve_using_factor_nopiv applies none. */
+void slate_lu_solve_nopiv_r64(slate_Matrix_r64 A, slate_Matrix_r64 B, slate_Options opts);
+void slate_lu_factor_nopiv_r64(slate_Matrix_r64 A, slate_Options opts);
+void slate_lu_solve_using_factor_nopiv_r64(slate_Matrix_r64 A, slate_Matrix_r64 B, slate_Options opts);
+void slate_lu_solve_nopiv_r32(slate_Matrix_r32 A, slate_Matrix_r32 B, slate_Options opts);
+void slate_lu_factor_nopiv_r32(slate_Matrix_r32 A, slate_Options opts);
+void slate_lu_solve_using_factor_nopiv_r32(slate_Matrix_r32 A, slate_Matrix_r32 B, slate_Options opts);
+
+/* slate::lu_inverse_using_factor (getri) in place and out of place, and
+ * lu_rcondest_using_factor (gecondest: the pivots do not change the 1- or
+ * infinity-norm of A^{-1}) (src/c_api/wrappers.cc:882-945). */
+void slate_lu_inverse_using_factor_r64(slate_Matrix_r64 A, slate_Pivots pivots, slate_Options opts);
+void slate_lu_inverse_using_factor_out_of_place_r64(slate_Matrix_r64 A, slate_Pivots pivots,
+                                                    slate_Matrix_r64 A_inverse, slate_Options opts);
+double slate_lu_rcondest_using_factor_r64(slate_Norm norm, slate_Matrix_r64 A, double Anorm, slate_Options opts);
+
 /* slate::chol_solve = posv, chol_factor = potrf, chol_solve_using_factor = potrs */
 void slate_chol_solve_r64(slate_HermitianMatrix_r64 A, slate_Matrix_r64 B, slate_Options opts);
 void slate_chol_factor_r64(slate_HermitianMatrix_r64 A, slate_Options opts);
 void slate_chol_solve_using_factor_r64(slate_HermitianMatrix_r64 A, slate_Matrix_r64 B, slate_Options opts);
+/* slate::chol_inverse_using_factor (potri) and chol_rcondest_using_factor
+ * (pocondest) (src/c_api/wrappers.cc:1083-1130) */
+void slate_chol_inverse_using_factor_r64(slate_HermitianMatrix_r64 A, slate_Options opts);
+double slate_chol_rcondest_using_factor_r64(slate_Norm norm, slate_HermitianMatrix_r64 A, double Anorm,
+                                            slate_Options opts);
 
 /* Outcome of the last C-API call on this thread (no counterpart in SLATE,
  * whose C wrappers throw). */

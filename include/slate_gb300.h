@@ -55,6 +55,8 @@ typedef struct slt_options {
                                  with an FP32 factor before the FP64 fallback;
                                  -1 auto (on for BF16/FP16), 0, 1               */
     int64_t depth;            /* Option::Depth of gesv_rbt's butterflies, default 2 */
+    int     method_lu;        /* Option::MethodLU: 'P' partial pivoting (default,
+                                 also '*'), 'N' no pivoting, 'C' CALU      */
 } slt_options;
 
 /* Refinement of the mixed solvers.  SLT_REFINE_IR is SLATE's gesv_mixed loop

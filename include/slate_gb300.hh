@@ -45,7 +45,7 @@ enum class Option {
     FactorPrecision, Refine, Equilibrate          // this library's additions
 };
 enum class Target : char { Host = 'H', HostTask = 'T', HostNest = 'N', HostBatch = 'B', Devices = 'D' };
-enum class MethodLU : char { Auto = '*', PartialPiv = 'P', NoPiv = 'N' };
+enum class MethodLU : char { Auto = '*', PartialPiv = 'P', CALU = 'C', NoPiv = 'N' };
 enum class Uplo : char { Lower = 'L', Upper = 'U' };
 enum class Norm : char { One = '1', Inf = 'I' };
 
@@ -144,7 +144,8 @@ inline slt_options to_c(const Options& opts, int64_t nb)
             case Option::PivotThreshold:    o.pivot_threshold = kv.second.d(); break;
             case Option::Depth:             o.depth = kv.second.i(); break;
             case Option::MethodLU:
-                if (kv.second.i() == int64_t(MethodLU::NoPiv)) o.pivot_threshold = 0.0;
+                if (kv.second.i() == int64_t(MethodLU::NoPiv)) o.method_lu = 'N';
+                if (kv.second.i() == int64_t(MethodLU::CALU)) o.method_lu = 'C';
                 break;
             case Option::FactorPrecision:   o.factor_precision = int(kv.second.i()); break;
             case Option::Refine:            o.refine = int(kv.second.i()); break;

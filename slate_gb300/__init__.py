@@ -35,7 +35,7 @@ class _Options(ctypes.Structure):
                 ("use_fallback", ctypes.c_int), ("pivot_threshold", ctypes.c_double),
                 ("factor_precision", ctypes.c_int), ("gemm_engine", ctypes.c_int),
                 ("refine", ctypes.c_int), ("equilibrate", ctypes.c_int), ("lo_retry", ctypes.c_int),
-                ("depth", ctypes.c_int64)]
+                ("depth", ctypes.c_int64), ("method_lu", ctypes.c_int)]
 
 
 @dataclass
@@ -54,6 +54,7 @@ class Options:
     equilibrate: int = -1          # -1 auto (on for bf16/fp16), 0 off, 1 on
     lo_retry: int = -1             # -1 auto (on for bf16/fp16): FP32 retry before the FP64 fallback
     depth: int = 2                 # Option::Depth of gesv_rbt's butterflies
+    method_lu: str = "P"           # Option::MethodLU: "P" partial pivoting, "N" none, "C" CALU
 
     def _c(self):
         p = self.factor_precision
@@ -62,7 +63,8 @@ class Options:
                         float(self.tolerance), int(bool(self.use_fallback)),
                         float(self.pivot_threshold), p, int(self.gemm_engine),
                         _REFINE_NAMES[self.refine] if isinstance(self.refine, str) else int(self.refine),
-                        int(self.equilibrate), int(self.lo_retry), int(self.depth))
+                        int(self.equilibrate), int(self.lo_retry), int(self.depth),
+                        ord(self.method_lu[0]) if isinstance(self.method_lu, str) else int(self.method_lu))
 
 
 _lib = None

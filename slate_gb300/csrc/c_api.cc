@@ -72,18 +72,19 @@ slt_options opts_for(slate_Options h, int64_t nb)
     if (h) o = static_cast<COpts*>(h)->o;
     else slt_options_default(&o);
     o.nb = nb;        // the matrix's tile size, as in SLATE
-    // MethodLU::NoPiv: keep every diagonal pivot (src/getrf_nopiv.cc), which
-    // the panel's threshold rule gives with threshold 0
-    if (h && static_cast<COpts*>(h)->method_lu == 'N') o.pivot_threshold = 0.0;
+    // MethodLU::NoPiv (src/getrf_nopiv.cc) and CALU (src/getrf_tntpiv.cc)
+    if (h && static_cast<COpts*>(h)->method_lu == 'N') o.method_lu = 'N';
+    if (h && static_cast<COpts*>(h)->method_lu == 'C') o.method_lu = 'C';
     return o;
 }
 
-// MethodLU::PartialPiv (and Auto) and NoPiv are served; CALU, RBT and BEAM are not.
+// MethodLU::PartialPiv (and Auto), NoPiv and CALU are served; RBT is
+// gesv_rbt's own driver and BEAM is not built.
 bool lu_method_ok(slate_Options h)
 {
     if (!h) return true;
     const char m = static_cast<COpts*>(h)->method_lu;
-    return m == '*' || m == 'P' || m == 'N';
+    return m == '*' || m == 'P' || m == 'N' || m == 'C';
 }
 
 void finish(int status, int64_t info)
@@ -143,16 +144,17 @@ int getrs_dev_any<float>(int64_t n, int64_t nrhs, const float* A, int64_t lda, c
 // lu_factor (+ lu_solve_using_factor when B is given): A <- LU, pivots
 // recorded in P, B <- X.  SLATE skips the solve when info != 0.
 template <typename T>
-int lu_run(CMat<T>* A, slate_Pivots P, CMat<T>* B, slate_Options h, int64_t* info)
+int lu_run(CMat<T>* A, slate_Pivots P, CMat<T>* B, slate_Options h, int64_t* info, char method = 0)
 {
     *info = 0;
     if (!A || A->m != A->n) return SLT_ERR_ARG;
     if (B && B->m != A->n) return SLT_ERR_ARG;
-    if (!lu_method_ok(h)) return SLT_ERR_NOT_SUPPORTED;
+    if (!method && !lu_method_ok(h)) return SLT_ERR_NOT_SUPPORTED;
     const int64_t n = A->n;
     cudaStream_t s = cstream();
     if (!s) return SLT_ERR_NO_DEVICE;
     slt_options o = opts_for(h, A->nb);
+    if (method) o.method_lu = method;
     View<T> va, vb;
     DevBuf piv;
     TRY(va.open(*A, s));
@@ -170,6 +172,15 @@ int lu_run(CMat<T>* A, slate_Pivots P, CMat<T>* B, slate_Options h, int64_t* inf
         P->n = n;
     }
     return SLT_OK;
+}
+
+// Identity pivots in the per-panel form (row r of panel k stays: r - k nb).
+void identity_pivots(slate_Pivots_struct& P, int64_t n, int64_t nb)
+{
+    P.rel.resize(size_t(n));
+    for (int64_t r = 0; r < n; ++r) P.rel[size_t(r)] = int(r % nb);
+    P.n = n;
+    P.nb = nb;
 }
 
 template <typename T>
@@ -191,15 +202,69 @@ int lu_solve_factored(CMat<T>* A, slate_Pivots P, CMat<T>* B, slate_Options h)
     return SLT_OK;
 }
 
+// getri on the factors of A (in place, or into Ainv) with the recorded pivots.
+int lu_inverse(CMat<double>* A, slate_Pivots P, CMat<double>* Ainv, slate_Options h, int64_t* info)
+{
+    *info = 0;
+    if (!A || !P || A->m != A->n || P->n != A->n || P->nb != A->nb) return SLT_ERR_ARG;
+    if (Ainv && (Ainv->m != A->n || Ainv->n != A->n)) return SLT_ERR_ARG;
+    const int64_t n = A->n;
+    if (n == 0) return SLT_OK;
+    cudaStream_t s = cstream();
+    if (!s) return SLT_ERR_NO_DEVICE;
+    slt_options o = opts_for(h, A->nb);
+    CMat<double>* dst = Ainv ? Ainv : A;
+    View<double> v;
+    DevBuf piv;
+    if (Ainv) {
+        // the factors into the output's device view
+        TRY(v.open(*Ainv, s));
+        SLT_CUDA_TRY(cudaMemcpy2DAsync(v.p, size_t(v.ld) * sizeof(double), A->data, size_t(A->ld) * sizeof(double),
+                                       size_t(n) * sizeof(double), size_t(n),
+                                       A->dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    }
+    else {
+        TRY(v.open(*A, s));
+    }
+    TRY(piv.alloc(sizeof(int) * size_t(n), s));
+    SLT_CUDA_TRY(cudaMemcpyAsync(piv.p, P->rel.data(), sizeof(int) * size_t(n), cudaMemcpyHostToDevice, s));
+    TRY(slt_dgetri_device(n, v.p, v.ld, piv.as<int>(), &o, s, info));
+    return v.close(*dst, s);
+}
+
+double lu_rcond(slate_Norm norm, CMat<double>* A, double anorm, slate_Options h, int* st)
+{
+    *st = SLT_ERR_ARG;
+    const char nm = (norm == 'O' || norm == 'o' || norm == '1') ? '1' : (norm == 'I' || norm == 'i') ? 'I' : 0;
+    if (!A || A->m != A->n || !nm) return 0.0;
+    if (A->n == 0) { *st = SLT_OK; return 1.0; }
+    cudaStream_t s = cstream();
+    if (!s) { *st = SLT_ERR_NO_DEVICE; return 0.0; }
+    slt_options o = opts_for(h, A->nb);
+    slate_Pivots_struct P;
+    identity_pivots(P, A->n, A->nb);
+    View<double> v;
+    DevBuf piv;
+    double rc = 0.0;
+    int r = v.open(*A, s);
+    if (!r) r = piv.alloc(sizeof(int) * size_t(A->n), s);
+    if (!r) r = slt_from_cuda(cudaMemcpyAsync(piv.p, P.rel.data(), sizeof(int) * size_t(A->n), cudaMemcpyHostToDevice, s));
+    if (!r) r = slt_dgecondest_device(nm, A->n, v.p, v.ld, piv.as<int>(), anorm, &rc, &o, s);
+    if (!r) r = slt_from_cuda(cudaStreamSynchronize(s));
+    *st = r;
+    return rc;
+}
+
 // Cholesky on a Hermitian handle: the referenced triangle is brought to a
 // lower-triangular device array (transposed when uplo = 'U'), the driver
 // runs on it, and only the referenced triangle is written back.
-enum CholOp { kFactor, kSolve, kSolveFactored };
+enum CholOp { kFactor, kSolve, kSolveFactored, kInverse };
 
 int chol_run(CMat<double>* A, CMat<double>* B, slate_Options h, CholOp op, int64_t* info)
 {
     *info = 0;
-    if (!A || A->m != A->n || (op != kFactor && (!B || B->m != A->n))) return SLT_ERR_ARG;
+    const bool needs_b = op == kSolve || op == kSolveFactored;
+    if (!A || A->m != A->n || (needs_b && (!B || B->m != A->n))) return SLT_ERR_ARG;
     const int64_t n = A->n;
     if (n == 0) return SLT_OK;
     cudaStream_t s = cstream();
@@ -219,6 +284,7 @@ int chol_run(CMat<double>* A, CMat<double>* B, slate_Options h, CholOp op, int64
     View<double> vb;
     if (B) TRY(vb.open(*B, s));
     if (op == kFactor) TRY(slt_dpotrf_device(n, L.as<double>(), n, &o, s, info));
+    else if (op == kInverse) TRY(slt_dpotri_device(n, L.as<double>(), n, &o, s, info));
     else if (op == kSolve) TRY(slt_dposv_device(n, B->n, L.as<double>(), n, vb.p, vb.ld, &o, s, info));
     else TRY(slt_dpotrs_device(n, B->n, L.as<double>(), n, vb.p, vb.ld, &o, s));
     if (op != kSolveFactored) {
@@ -242,6 +308,33 @@ int chol_run(CMat<double>* A, CMat<double>* B, slate_Options h, CholOp op, int64
     if (B) TRY(vb.close(*B, s));
     SLT_CUDA_TRY(cudaStreamSynchronize(s));
     return SLT_OK;
+}
+
+double chol_rcond(slate_Norm norm, CMat<double>* A, double anorm, slate_Options h, int* st)
+{
+    *st = SLT_ERR_ARG;
+    const char nm = (norm == 'O' || norm == 'o' || norm == '1' || norm == 'I' || norm == 'i') ? '1' : 0;
+    if (!A || A->m != A->n || !nm) return 0.0;       // A symmetric: one and infinity norms agree
+    const int64_t n = A->n;
+    if (n == 0) { *st = SLT_OK; return 1.0; }
+    cudaStream_t s = cstream();
+    if (!s) { *st = SLT_ERR_NO_DEVICE; return 0.0; }
+    slt_options o = opts_for(h, A->nb);
+    DevBuf L, T2;
+    double rc = 0.0;
+    int r = L.alloc(sizeof(double) * size_t(n) * size_t(n), s);
+    if (!r) r = slt_from_cuda(cudaMemcpy2DAsync(L.p, size_t(n) * sizeof(double), A->data, size_t(A->ld) * sizeof(double),
+                                                size_t(n) * sizeof(double), size_t(n),
+                                                A->dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    if (!r && A->uplo == 'U') {
+        r = T2.alloc(sizeof(double) * size_t(n) * size_t(n), s);
+        if (!r) r = slt_dtranspose(n, n, L.as<double>(), n, T2.as<double>(), n, s);
+        if (!r) std::swap(L.p, T2.p);
+    }
+    if (!r) r = slt_dpocondest_device('1', n, L.as<double>(), n, anorm, &rc, &o, s);
+    if (!r) r = slt_from_cuda(cudaStreamSynchronize(s));
+    *st = r;
+    return rc;
 }
 
 template <typename T>
@@ -375,6 +468,68 @@ void slate_chol_solve_using_factor_r64(slate_HermitianMatrix_r64 A, slate_Matrix
     const int rc = chol_run(reinterpret_cast<CMat<double>*>(A), reinterpret_cast<CMat<double>*>(B), opts,
                             kSolveFactored, &info);
     finish(rc, info);
+}
+void slate_chol_inverse_using_factor_r64(slate_HermitianMatrix_r64 A, slate_Options opts)
+{
+    int64_t info = 0;
+    const int rc = chol_run(reinterpret_cast<CMat<double>*>(A), nullptr, opts, kInverse, &info);
+    finish(rc, info);
+}
+double slate_chol_rcondest_using_factor_r64(slate_Norm norm, slate_HermitianMatrix_r64 A, double Anorm,
+                                            slate_Options opts)
+{
+    int st = 0;
+    const double r = chol_rcond(norm, reinterpret_cast<CMat<double>*>(A), Anorm, opts, &st);
+    finish(st, 0);
+    return r;
+}
+
+#define SLT_NOPIV(R, T)                                                                                         \
+void slate_lu_solve_nopiv_##R(slate_Matrix_##R A, slate_Matrix_##R B, slate_Options opts)                       \
+{                                                                                                                \
+    int64_t info = 0;                                                                                            \
+    slate_Pivots_struct P;                                                                                       \
+    const int rc = lu_run<T>(reinterpret_cast<CMat<T>*>(A), &P, reinterpret_cast<CMat<T>*>(B), opts, &info, 'N'); \
+    finish(rc, info);                                                                                            \
+}                                                                                                                \
+void slate_lu_factor_nopiv_##R(slate_Matrix_##R A, slate_Options opts)                                         \
+{                                                                                                                \
+    int64_t info = 0;                                                                                            \
+    const int rc = lu_run<T>(reinterpret_cast<CMat<T>*>(A), nullptr, nullptr, opts, &info, 'N');                \
+    finish(rc, info);                                                                                            \
+}                                                                                                                \
+void slate_lu_solve_using_factor_nopiv_##R(slate_Matrix_##R A, slate_Matrix_##R B, slate_Options opts)         \
+{                                                                                                                \
+    auto* a = reinterpret_cast<CMat<T>*>(A);                                                                     \
+    if (!a) { finish(SLT_ERR_ARG, 0); return; }                                                                  \
+    slate_Pivots_struct P;                                                                                       \
+    identity_pivots(P, a->n, a->nb);                                                                             \
+    finish(lu_solve_factored<T>(a, &P, reinterpret_cast<CMat<T>*>(B), opts), 0);                                \
+}
+SLT_NOPIV(r64, double)
+SLT_NOPIV(r32, float)
+#undef SLT_NOPIV
+
+void slate_lu_inverse_using_factor_r64(slate_Matrix_r64 A, slate_Pivots pivots, slate_Options opts)
+{
+    int64_t info = 0;
+    const int rc = lu_inverse(reinterpret_cast<CMat<double>*>(A), pivots, nullptr, opts, &info);
+    finish(rc, info);
+}
+void slate_lu_inverse_using_factor_out_of_place_r64(slate_Matrix_r64 A, slate_Pivots pivots,
+                                                    slate_Matrix_r64 A_inverse, slate_Options opts)
+{
+    int64_t info = 0;
+    const int rc = lu_inverse(reinterpret_cast<CMat<double>*>(A), pivots, reinterpret_cast<CMat<double>*>(A_inverse),
+                              opts, &info);
+    finish(rc, info);
+}
+double slate_lu_rcondest_using_factor_r64(slate_Norm norm, slate_Matrix_r64 A, double Anorm, slate_Options opts)
+{
+    int st = 0;
+    const double r = lu_rcond(norm, reinterpret_cast<CMat<double>*>(A), Anorm, opts, &st);
+    finish(st, 0);
+    return r;
 }
 
 int64_t slate_gb300_last_info(void) { return g_info; }

@@ -166,6 +166,7 @@ void slt_options_default(slt_options* o)
     o->equilibrate = -1;
     o->lo_retry = -1;
     o->depth = 2;
+    o->method_lu = 'P';
 }
 
 const char* slt_status_string(int st)

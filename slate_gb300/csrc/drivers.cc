@@ -90,6 +90,10 @@ static int k_trsm_llnn(char tr, int64_t kb, int64_t n, const double* L, int64_t 
 { return slt_dtrsm_llnn(tr, kb, n, L, ldl, B, ldb, s); }
 static int k_trsm_llnn(char tr, int64_t kb, int64_t n, const float* L, int64_t ldl, float* B, int64_t ldb, cudaStream_t s)
 { return slt_strsm_llnn(tr, kb, n, L, ldl, B, ldb, s); }
+static int k_trsm_runn(int64_t m, int64_t kb, const double* U, int64_t ldu, double* B, int64_t ldb, cudaStream_t s)
+{ return slt_dtrsm_runn(m, kb, U, ldu, B, ldb, s); }
+static int k_trsm_runn(int64_t m, int64_t kb, const float* U, int64_t ldu, float* B, int64_t ldb, cudaStream_t s)
+{ return slt_strsm_runn(m, kb, U, ldu, B, ldb, s); }
 static int k_trsm_rltn(int64_t m, int64_t kb, const double* L, int64_t ldl, double* B, int64_t ldb, cudaStream_t s)
 { return slt_dtrsm_rltn(m, kb, L, ldl, B, ldb, s); }
 static int k_trsm_rltn(int64_t m, int64_t kb, const float* L, int64_t ldl, float* B, int64_t ldb, cudaStream_t s)
@@ -138,7 +142,13 @@ int finish_factor(FactorCtx& fc, int64_t* info, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // LU: right-looking, one cooperative panel launch per block column, then the
 // panel's interchanges on both sides, the U12 solve and the trailing GEMM
-// (impl::getrf, src/getrf.cc:22-244).
+// (impl::getrf, src/getrf.cc:22-244).  MethodLU::NoPiv is the panel's
+// threshold rule with threshold 0.  MethodLU::CALU follows SLATE's device path
+// on a 1 x 1 grid (src/getrf_tntpiv.cc, internal_getrf_tntpiv.cc:120-172): the
+// tournament has one participant, which factors the whole local panel with
+// partial pivoting, so the pivots are the partial-pivoting panel's; the
+// diagonal block keeps that factorisation and L21 is recomputed from the
+// original panel rows, permuted by the pivots, as A21 U11^{-1}.
 template <typename T>
 int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_options& o,
               FactorCtx& fc, cudaStream_t s)
@@ -149,17 +159,37 @@ int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_opti
     const int64_t mn = std::min(m, n);
     if (mn == 0) return SLT_OK;
     if (nb > 1024) return SLT_ERR_ARG;
-    DevBuf pws, plan;
+    const bool calu = o.method_lu == 'C' || o.method_lu == 'c';
+    const bool nopiv = o.method_lu == 'N' || o.method_lu == 'n';
+    DevBuf pws, plan, W, plan0;
     TRY(pws.alloc(slt_getrf_panel_ws_bytes(m, ib), s));
     TRY(plan.alloc(sizeof(int) * size_t(1 + 4 * nb), s));
+    if (calu) {
+        TRY(W.alloc(sizeof(T) * size_t(m) * size_t(std::min(nb, n)), s));
+        TRY(plan0.alloc(sizeof(int) * size_t(1 + 4 * nb), s));
+    }
     for (int64_t r0 = 0; r0 < mn; r0 += nb) {
         const int64_t nbk = std::min(nb, n - r0);
         const int64_t prows = m - r0;
         const int64_t diag = std::min(prows, nbk);
         T* P = A + r0 + r0 * lda;
-        const double thr = (o.pivot_threshold >= 0.0 && o.pivot_threshold <= 1.0) ? o.pivot_threshold : 1.0;
+        double thr = (o.pivot_threshold >= 0.0 && o.pivot_threshold <= 1.0) ? o.pivot_threshold : 1.0;
+        if (nopiv) thr = 0.0;
+        if (calu)
+            SLT_CUDA_TRY(cudaMemcpy2DAsync(W.p, sizeof(T) * size_t(prows), P, sizeof(T) * size_t(lda),
+                                           sizeof(T) * size_t(prows), size_t(nbk), cudaMemcpyDeviceToDevice, s));
         TRY(k_panel(prows, nbk, ib, thr, P, lda, ipiv + r0, fc.d_info, r0, pws.p, fc.d_status, s));
         TRY(slt_swap_plan(ipiv + r0, diag, r0, plan.as<int>(), s));
+        if (calu && prows > diag) {
+            // W <- the panel's interchanges applied to the original panel;
+            // L21 = W21 U11^{-1}
+            TRY(slt_swap_plan(ipiv + r0, diag, 0, plan0.as<int>(), s));
+            TRY(k_laswp(plan0.as<int>(), 2 * diag, W.as<T>(), prows, diag, s));
+            SLT_CUDA_TRY(cudaMemcpy2DAsync(P + diag, sizeof(T) * size_t(lda), W.as<T>() + diag,
+                                           sizeof(T) * size_t(prows), sizeof(T) * size_t(prows - diag),
+                                           size_t(diag), cudaMemcpyDeviceToDevice, s));
+            TRY(k_trsm_runn(prows - diag, diag, P, lda, P + diag, lda, s));
+        }
         const int64_t c1 = r0 + nbk;
         TRY(k_laswp(plan.as<int>(), 2 * diag, A + c1 * lda, lda, n - c1, s));
         TRY(k_laswp(plan.as<int>(), 2 * diag, A, lda, r0, s));

@@ -106,6 +106,10 @@ int slt_dtrsm_llnn(char trans, int64_t kb, int64_t n, const double* L, int64_t l
 int slt_strsm_llnn(char trans, int64_t kb, int64_t n, const float* L, int64_t ldl,
                    float* B, int64_t ldb, cudaStream_t stream);
 /* Right, lower^T, non-unit: B(m x kb) <- B L^{-T} (Cholesky column panel). */
+int slt_dtrsm_runn(int64_t m, int64_t kb, const double* U, int64_t ldu, double* B, int64_t ldb,
+                   cudaStream_t stream);
+int slt_strsm_runn(int64_t m, int64_t kb, const float* U, int64_t ldu, float* B, int64_t ldb,
+                   cudaStream_t stream);
 int slt_dtrsm_rltn(int64_t m, int64_t kb, const double* L, int64_t ldl, double* B,
                    int64_t ldb, cudaStream_t stream);
 int slt_strsm_rltn(int64_t m, int64_t kb, const float* L, int64_t ldl, float* B,

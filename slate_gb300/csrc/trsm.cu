@@ -236,6 +236,16 @@ extern "C" int slt_strsm_rltn(int64_t m, int64_t kb, const float* L, int64_t ldl
                               int64_t ldb, cudaStream_t stream)
 { return launch_trsm<float, true, false, false, true>(kb, m, L, ldl, B, ldb, stream); }
 
+// B (m x kb) <- B U^{-1}, U upper non-unit (the CALU panel's L21 = A21 U11^{-1},
+// src/getrf_tntpiv.cc: internal::trsm Side::Right on the upper diagonal tile):
+// the rows of B solved against op(T) = U^T, lower.
+extern "C" int slt_dtrsm_runn(int64_t m, int64_t kb, const double* U, int64_t ldu, double* B,
+                              int64_t ldb, cudaStream_t stream)
+{ return launch_trsm<double, true, false, true, true>(kb, m, U, ldu, B, ldb, stream); }
+extern "C" int slt_strsm_runn(int64_t m, int64_t kb, const float* U, int64_t ldu, float* B,
+                              int64_t ldb, cudaStream_t stream)
+{ return launch_trsm<float, true, false, true, true>(kb, m, U, ldu, B, ldb, stream); }
+
 extern "C" int slt_dpotrf_small(int64_t kb, double* A, int64_t lda, int* info, int64_t info_offset,
                                 cudaStream_t stream)
 { return launch_potrf_small<double>(kb, A, lda, info, info_offset, stream); }

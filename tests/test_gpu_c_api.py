@@ -144,3 +144,103 @@ def test_c_api_info(orc, slt):
         L.slate_Matrix_destroy_r64(h)
     L.slate_HermitianMatrix_destroy_r64(hs)
     L.slate_Options_destroy(opts)
+
+
+def _api_more(slt):
+    L = _api(slt)
+    for name in ("slate_lu_solve_nopiv_r64", "slate_lu_solve_using_factor_nopiv_r64"):
+        getattr(L, name).argtypes = [vp, vp, vp]
+    L.slate_lu_factor_nopiv_r64.argtypes = [vp, vp]
+    L.slate_lu_inverse_using_factor_r64.argtypes = [vp, vp, vp]
+    L.slate_lu_inverse_using_factor_out_of_place_r64.argtypes = [vp, vp, vp, vp]
+    L.slate_lu_rcondest_using_factor_r64.argtypes = [ctypes.c_char, vp, ctypes.c_double, vp]
+    L.slate_lu_rcondest_using_factor_r64.restype = ctypes.c_double
+    L.slate_chol_inverse_using_factor_r64.argtypes = [vp, vp]
+    L.slate_chol_rcondest_using_factor_r64.argtypes = [ctypes.c_char, vp, ctypes.c_double, vp]
+    L.slate_chol_rcondest_using_factor_r64.restype = ctypes.c_double
+    L.slate_Options_set_MethodLU.argtypes = [vp, ctypes.c_char]
+    return L
+
+
+def test_c_api_calu_and_nopiv(orc, slt):
+    import torch
+    L = _api_more(slt)
+    n, nb = 256, 64
+    A = orc.generate(2, 75, n, n)
+    B = orc.generate(2, 76, n, 2)
+    # CALU through the option: the same factors as the driver with method_lu "C"
+    opts = L.slate_Options_create()
+    L.slate_Options_set_MethodLU(opts, b"C")
+    a = A.copy(order="F")
+    h = _mat(L, a.ctypes.data, n, n, n, nb)
+    piv = L.slate_Pivots_create()
+    L.slate_lu_factor_r64(h, piv, opts)
+    assert L.slate_gb300_last_status() == 0 and L.slate_gb300_last_info() == 0
+    dA = to_dev(A)
+    slt.getrf(dA, slt.Options(nb=nb, method_lu="C"))
+    torch.cuda.synchronize()
+    assert np.array_equal(a, to_host(dA))
+    # NoPiv forms on a diagonally dominant matrix
+    D = np.asfortranarray(A + n * np.eye(n))
+    d, b = D.copy(order="F"), B.copy(order="F")
+    hd, hb = _mat(L, d.ctypes.data, n, n, n, nb), _mat(L, b.ctypes.data, n, 2, n, nb)
+    L.slate_lu_solve_nopiv_r64(hd, hb, None)
+    assert L.slate_gb300_last_status() == 0 and L.slate_gb300_last_info() == 0
+    assert berr(orc, D, b, B) <= 3 * EPS
+    d2, b2 = D.copy(order="F"), B.copy(order="F")
+    hd2, hb2 = _mat(L, d2.ctypes.data, n, n, n, nb), _mat(L, b2.ctypes.data, n, 2, n, nb)
+    L.slate_lu_factor_nopiv_r64(hd2, None)
+    L.slate_lu_solve_using_factor_nopiv_r64(hd2, hb2, None)
+    assert L.slate_gb300_last_status() == 0
+    assert np.array_equal(b2, b)
+    Lf = np.tril(d2, -1) + np.eye(n)
+    assert np.abs(Lf @ np.triu(d2) - D).max() <= 1e-12 * np.abs(D).max()
+    for x in (h, hd, hb, hd2, hb2):
+        L.slate_Matrix_destroy_r64(x)
+    L.slate_Pivots_destroy(piv)
+    L.slate_Options_destroy(opts)
+
+
+def test_c_api_inverse_and_rcond(orc, slt):
+    import scipy.linalg.lapack as lp
+    L = _api_more(slt)
+    n, nb = 200, 64
+    A = orc.generate(2, 77, n, n)
+    a = A.copy(order="F")
+    h = _mat(L, a.ctypes.data, n, n, n, nb)
+    piv = L.slate_Pivots_create()
+    L.slate_lu_factor_r64(h, piv, None)
+    anorm = np.abs(A).sum(0).max()
+    rc = L.slate_lu_rcondest_using_factor_r64(b"1", h, anorm, None)
+    assert L.slate_gb300_last_status() == 0
+    lu, _, _ = lp.dgetrf(A)
+    ref, _ = lp.dgecon(lu, anorm, norm="1")
+    assert abs(rc - ref) <= 0.01 * ref
+    ai = np.zeros((n, n), order="F")
+    hi = _mat(L, ai.ctypes.data, n, n, n, nb)
+    f = a.copy(order="F")
+    L.slate_lu_inverse_using_factor_out_of_place_r64(h, piv, hi, None)
+    assert L.slate_gb300_last_status() == 0 and np.array_equal(a, f)       # factors kept
+    Ainv = np.linalg.inv(A)
+    assert np.abs(ai - Ainv).max() <= 1e-10 * np.abs(Ainv).max()
+    L.slate_lu_inverse_using_factor_r64(h, piv, None)
+    assert np.array_equal(a, ai)
+    S = spd(orc, n, 78)
+    snorm = np.abs(S).sum(0).max()
+    for uplo in (b"L", b"U"):
+        s = S.copy(order="F")
+        hs = L.slate_HermitianMatrix_create_fromScaLAPACK_r64(uplo, n, s.ctypes.data, n, nb, 1, 1, 0)
+        L.slate_chol_factor_r64(hs, None)
+        rc = L.slate_chol_rcondest_using_factor_r64(b"1", hs, snorm, None)
+        c, _ = lp.dpotrf(S, lower=1)
+        ref, _ = lp.dpocon(c, snorm, uplo="L")
+        assert abs(rc - ref) <= 0.01 * ref
+        L.slate_chol_inverse_using_factor_r64(hs, None)
+        assert L.slate_gb300_last_status() == 0 and L.slate_gb300_last_info() == 0
+        Si = np.linalg.inv(S)
+        tri = np.tril if uplo == b"L" else np.triu
+        assert np.abs(tri(s) - tri(Si)).max() <= 1e-10 * np.abs(Si).max()
+        L.slate_HermitianMatrix_destroy_r64(hs)
+    for x in (h, hi):
+        L.slate_Matrix_destroy_r64(x)
+    L.slate_Pivots_destroy(piv)

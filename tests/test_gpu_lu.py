@@ -181,3 +181,54 @@ def test_getrf_nopiv_via_threshold_zero(orc, slt):
     L = np.tril(LU, -1) + np.eye(n)
     U = np.triu(LU)
     assert np.abs(L @ U - A).max() <= 1e-12 * np.abs(A).max()
+
+
+def test_getrf_nopiv_method(orc, slt):
+    """Options.method_lu = "N" is MethodLU::NoPiv: identity pivots."""
+    import torch
+    n, nb = 200, 64
+    A = np.asfortranarray(orc.generate(2, 83, n, n) + n * np.eye(n))
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=nb, method_lu="N"))
+    torch.cuda.synchronize()
+    assert info == 0 and np.array_equal(slt.ipiv_to_lapack(ipiv, nb), np.arange(1, n + 1))
+
+
+@pytest.mark.parametrize("m,n,nb", [(600, 600, 128), (700, 450, 64), (333, 333, 96)])
+def test_getrf_calu(orc, slt, m, n, nb):
+    """MethodLU::CALU on one GPU (SLATE's device path with a one-participant
+    tournament): the partial-pivoting panel's pivots, U as partial pivoting
+    gives it, L21 recomputed as A21 U11^{-1} from the permuted original rows;
+    P A = L U to rounding and the solve reaches backward error <= 3 eps."""
+    import torch
+    A = orc.generate(2, 84, m, n)
+    dA = to_dev(A)
+    info, ipiv = slt.getrf(dA, slt.Options(nb=nb, ib=32, method_lu="C"))
+    torch.cuda.synchronize()
+    assert info == 0
+    oinfo, pt, po, oipiv, mg = orc.getrf(A.copy(order="F"), nb, 32, margins=True)
+    gip = slt.ipiv_to_lapack(ipiv, nb)
+    robust = mg > 1 + 1e3 * max(m, n) * EPS
+    assert np.array_equal(gip[robust], oipiv[robust])
+    LU = to_host(dA)
+    k = min(m, n)
+    L = np.tril(LU, -1)[:, :k] + np.eye(m, k)
+    U = np.triu(LU)[:k, :]
+    PA = A.copy()
+    for r in range(k):
+        p = gip[r] - 1
+        if p != r:
+            PA[[r, p], :] = PA[[p, r], :]
+    assert np.abs(L @ U - PA).max() <= 1e3 * max(m, n) * EPS * np.abs(A).max()
+    # partial pivoting's factors agree to rounding (the pivots are the same)
+    dG = to_dev(A)
+    slt.getrf(dG, slt.Options(nb=nb, ib=32))
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(LU, to_host(dG), rtol=0, atol=1e-9 * np.abs(to_host(dG)).max())
+    if m == n:
+        B = orc.generate(2, 85, n, 2)
+        dB = to_dev(B)
+        slt.getrs(dA, ipiv, dB, slt.Options(nb=nb))
+        torch.cuda.synchronize()
+        X = to_host(dB)
+        assert np.abs(B - A @ X).sum(0).max() / (n * np.abs(A).sum(0).max() * np.abs(X).sum(0).max()) <= 3 * EPS
