@@ -35,7 +35,10 @@ enum slt_precision {
     SLT_PREC_FP32 = 1,   /* FP32 factorisation, SLATE's gesv_mixed<double,float> */
     SLT_PREC_TF32 = 2,   /* FP32 storage, TF32 tensor-core trailing update   */
     SLT_PREC_BF16 = 3,   /* FP32 storage, BF16 tensor-core trailing update   */
-    SLT_PREC_FP16 = 4    /* FP32 storage, FP16 tensor-core trailing update   */
+    SLT_PREC_FP16 = 4,   /* FP32 storage, FP16 tensor-core trailing update   */
+    SLT_PREC_FP8  = 5    /* FP32 storage, FP8 E4M3 tensor-core trailing update
+                            with a power-of-two scale per 128-row tile
+                            (experimental)                                   */
 };
 
 /* Options (SLATE Option keys, include/slate/enums.hh:453-490). */

@@ -60,7 +60,8 @@ static int k_gemm(char tb, int64_t m, int64_t n, int64_t k, float alpha, const f
                   const slt_options& o, cudaStream_t s)
 {
     int tier = o.factor_precision;
-    if ((tier == SLT_PREC_TF32 || tier == SLT_PREC_BF16 || tier == SLT_PREC_FP16) && alpha == -1.f
+    if ((tier == SLT_PREC_TF32 || tier == SLT_PREC_BF16 || tier == SLT_PREC_FP16 || tier == SLT_PREC_FP8) &&
+        alpha == -1.f
         && beta == 1.f && k >= 16 && m >= 128 && n >= 128)
         return slt_tc_gemm_update(tier, tb, m, n, k, A, lda, B, ldb, C, ldc, lower, nullptr, 0, s);
     return slt_sgemm(tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower, s);
@@ -326,13 +327,15 @@ template int potrs_dev<float>(int64_t, int64_t, const float*, int64_t, int64_t, 
 // Mixed precision.
 namespace {
 
-// Equilibration is on by default only for the 16-bit tiers, whose operand
-// range or mantissa a badly scaled matrix can exceed; FP32 and TF32 keep
-// SLATE's unscaled cast (src/gesv_mixed.cc:196-199).
+// Equilibration is on by default only for the 16- and 8-bit tiers, whose
+// operand range or mantissa a badly scaled matrix can exceed; FP32 and TF32
+// keep SLATE's unscaled cast (src/gesv_mixed.cc:196-199).
+bool low_tier(int p) { return p == SLT_PREC_BF16 || p == SLT_PREC_FP16 || p == SLT_PREC_FP8; }
+
 bool equilibrate_on(const slt_options& o)
 {
     if (o.equilibrate >= 0) return o.equilibrate != 0;
-    return o.factor_precision == SLT_PREC_BF16 || o.factor_precision == SLT_PREC_FP16;
+    return low_tier(o.factor_precision);
 }
 
 // The low-precision factorisation the mixed solvers refine with: FP32
@@ -380,8 +383,9 @@ struct LoFactor {
         // SPD in FP64.  Factor A_s + sigma I instead, sigma = c u_tier with
         // c = 1, 8, 64 (A_s has diagonal in [0.25, 1) after equilibration),
         // and let the FP64 refinement correct for the shift.
-        const bool shift = o.factor_precision == SLT_PREC_BF16 || o.factor_precision == SLT_PREC_FP16;
-        const double u = o.factor_precision == SLT_PREC_BF16 ? 0x1p-8 : 0x1p-11;
+        const bool shift = low_tier(o.factor_precision);
+        const double u = o.factor_precision == SLT_PREC_BF16 ? 0x1p-8
+                       : o.factor_precision == SLT_PREC_FP8  ? 0x1p-4 : 0x1p-11;
         for (int attempt = 0;; ++attempt) {
             TRY(slt_convert_d2s_scaled(n, n, Ahi, lda, r, c, A.as<float>(), ld, s));
             if (attempt > 0) {
@@ -887,16 +891,15 @@ static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, i
     return finish_factor(fc, nullptr, s);   // bounded-wait status of every launch above
 }
 
-// A 16-bit factorisation that breaks down (info > 0 even after the diagonal
+// A 16- or 8-bit factorisation that breaks down (info > 0 even after the diagonal
 // shifts) or whose refinement does not converge is retried once with an
 // FP32 factorisation before SLATE's FP64 fallback: the retry costs one FP32
 // factorisation, the FP64 fallback an FP64 one, an order of magnitude more
 // on this part.  A is unchanged between the two attempts (the first runs
-// without the fallback).  o.lo_retry: -1 auto (on for BF16 / FP16), 0, 1.
+// without the fallback).  o.lo_retry: -1 auto (on for BF16 / FP16 / FP8), 0, 1.
 static bool ladder_on(const slt_options& o)
 {
-    const bool low = o.factor_precision == SLT_PREC_BF16 || o.factor_precision == SLT_PREC_FP16 ||
-                     o.factor_precision == SLT_PREC_TF32;
+    const bool low = low_tier(o.factor_precision) || o.factor_precision == SLT_PREC_TF32;
     return low && (o.lo_retry < 0 ? (o.factor_precision != SLT_PREC_TF32) : o.lo_retry != 0);
 }
 

@@ -18,6 +18,12 @@
 //    accumulator and frees stages with tcgen05.commit; then all four warps
 //    read the accumulator with tcgen05.ld (32 lanes x 32 columns per
 //    instruction) and update C with coalesced column segments.
+// FP8 (E4M3, kind::f8f6f4): each 128-row tile of A and of op(B)^T is scaled
+// by a power of two s = 2^(8 - e), max|x| = m 2^e with m in [0.5, 1), so that
+// its largest entry lands in [128, 256) below E4M3's 448; the epilogue
+// multiplies the accumulator by 1 / (s_A s_B), exactly.  A K-tile is 128
+// bytes of K in every tier (64 16-bit, 32 TF32 or 128 FP8 elements) and each
+// MMA consumes 32 bytes of it, so the pipeline is the same for all kinds.
 // Every mbarrier wait is bounded: on timeout the CTA records
 // SLT_ERR_TIMEOUT, drains its own TMA copies (bounded), frees its TMEM and
 // returns.
@@ -30,6 +36,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 
 #include <mutex>
 
@@ -111,12 +118,16 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(ncols) : "memory");
 }
 
-template <int KIND>   // 0: kind::f16 (BF16/FP16 operands), 1: kind::tf32
+template <int KIND>   // 0: kind::f16 (BF16/FP16 operands), 1: kind::tf32, 2: kind::f8f6f4 (E4M3)
 __device__ __forceinline__ void umma(uint32_t taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
 {
     if (KIND == 0)
         asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                     :: "r"(taddr), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
+    else if (KIND == 2)
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}"
                      :: "r"(taddr), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
     else
         asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -173,9 +184,20 @@ struct TcArgs {
     int64_t ldc;
     int lower;
     int* status;
+    const float* inv_a;     // FP8: 1 / s per 128-row tile of A and of op(B)^T, else null
+    const float* inv_b;
 };
 
-// KIND 0: 16-bit operands (BF16 or FP16 per fmt), KIND 1: TF32.
+// elements of K in one 128-byte K tile for each kind
+template <int KIND>
+__host__ __device__ constexpr int kt_elems() { return KIND == 0 ? 64 : KIND == 2 ? 128 : 32; }
+
+__device__ __forceinline__ float tile_factor(const TcArgs& a, int64_t row0, int64_t col0)
+{
+    return a.inv_a ? a.inv_a[row0 / kTcBM] * a.inv_b[col0 / kTcBN] : 1.f;
+}
+
+// KIND 0: 16-bit operands (BF16 or FP16 per fmt), KIND 1: TF32, KIND 2: FP8 E4M3.
 template <int KIND>
 __global__ void __launch_bounds__(kTcThreads, 1)
 tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
@@ -198,7 +220,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     const int64_t row0 = int64_t(blockIdx.x) * BM;
     const int64_t col0 = int64_t(blockIdx.y) * BN;
     if (a.lower && row0 + BM - 1 < col0) return;       // tile strictly above the diagonal
-    const int KT = int(a.kpad / (KIND == 0 ? 64 : 32));
+    const int KT = int(a.kpad / kt_elems<KIND>());
 
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S), accum = smem_u32(bars + 2 * S);
     if (threadIdx.x == 0) {
@@ -227,8 +249,8 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             if (*(volatile int*) &s_abort) break;
             const uint32_t sa = base + s * STAGE, sb = sa + A_BYTES;
             mbar_expect_tx(full0 + 8 * s, STAGE);
-            tma_load_2d(sa, &mapA, full0 + 8 * s, kt * (KIND == 0 ? 64 : 32), int(row0));
-            tma_load_2d(sb, &mapB, full0 + 8 * s, kt * (KIND == 0 ? 64 : 32), int(col0));
+            tma_load_2d(sa, &mapA, full0 + 8 * s, kt * kt_elems<KIND>(), int(row0));
+            tma_load_2d(sb, &mapB, full0 + 8 * s, kt * kt_elems<KIND>(), int(col0));
             issued = kt + 1;
         }
     }
@@ -244,7 +266,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
             const uint32_t sa = base + s * STAGE, sb = sa + A_BYTES;
             const uint64_t da = sw128_desc(sa), db = sw128_desc(sb);
             #pragma unroll
-            for (int k = 0; k < 4; ++k)   // 4 MMAs of K = 16 (16-bit) or 8 (tf32): 32 bytes each
+            for (int k = 0; k < 4; ++k)   // 4 MMAs of K = 16 (16-bit), 8 (tf32) or 32 (fp8): 32 bytes each
                 umma<KIND>(taddr, da + uint64_t(2 * k), db + uint64_t(2 * k), idesc, (kt | k) != 0 ? 1u : 0u);
             umma_commit(empty0 + 8 * s);
         }
@@ -260,6 +282,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     tc_fence_after();
     if (ready) {
         const int64_t r = row0 + warp * 32 + lane;
+        const float f = tile_factor(a, row0, col0);
         #pragma unroll 1
         for (int cc = 0; cc < BN; cc += 32) {
             float v[32];
@@ -270,7 +293,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
                     const int64_t c = col0 + cc + i;
                     if (c < a.n && !(a.lower && r < c)) {
                         float* p = a.C + r + c * a.ldc;
-                        *p = *p - v[i];
+                        *p = *p - v[i] * f;
                     }
                 }
             }
@@ -334,7 +357,7 @@ tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_cons
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t mt = ceildiv(a.m, BM), nt = ceildiv(a.n, BN);
     const int64_t ntiles = mt * nt;
-    const int KT = int(a.kpad / (KIND == 0 ? 64 : 32));
+    const int KT = int(a.kpad / kt_elems<KIND>());
 
     const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S);
     const uint32_t tfull0 = smem_u32(bars + 2 * S), tempty0 = smem_u32(bars + 2 * S + 2);
@@ -381,8 +404,8 @@ tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_cons
                     }
                     const uint32_t sa = base + s * STAGE, sb = sa + A_BYTES;
                     mbar_expect_tx(full0 + 8 * s, STAGE);
-                    tma_load_2d(sa, &mapA, full0 + 8 * s, kt * (KIND == 0 ? 64 : 32), row0);
-                    tma_load_2d(sb, &mapB, full0 + 8 * s, kt * (KIND == 0 ? 64 : 32), col0);
+                    tma_load_2d(sa, &mapA, full0 + 8 * s, kt * kt_elems<KIND>(), row0);
+                    tma_load_2d(sb, &mapB, full0 + 8 * s, kt * kt_elems<KIND>(), col0);
                 }
             }
             // drain: the last armed phase of every stage must land before exit
@@ -451,6 +474,7 @@ tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_cons
             tc_fence_after();
             const int64_t row0 = (t % mt) * BM, col0 = (t / mt) * BN;
             const int64_t r = row0 + q * 32 + lane;
+            const float f = tile_factor(a, row0, col0);
             #pragma unroll 1
             for (int cc = 0; cc < BN; cc += 32, ++chunk) {
                 float v[32];
@@ -467,7 +491,7 @@ tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_cons
                 #pragma unroll
                 for (int i = 0; i < 32; ++i) {
                     const int64_t c = col0 + cc + i;
-                    sb[i * 32 + lane] = (a.lower && r < c) ? 0.f : -v[i];
+                    sb[i * 32 + lane] = (a.lower && r < c) ? 0.f : -(v[i] * f);
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 __syncwarp();
@@ -534,6 +558,72 @@ pack_kernel(int64_t rows, int64_t k, const float* __restrict__ src, int64_t ld, 
                 else {
                     dst[r * kpad + c] = TO(v);
                 }
+            }
+        }
+    }
+}
+
+// FP8 scales: one block per 128-row tile of an operand (element (r, c) at
+// src[r + c ld] when TRANS, else src[c + r ld]); inv[t] = 1 / s[t].
+template <bool TRANS>
+__global__ void __launch_bounds__(256)
+fp8_scale_kernel(int64_t rows, int64_t k, const float* __restrict__ src, int64_t ld, float* __restrict__ scale,
+                 float* __restrict__ inv)
+{
+    __shared__ float red[8];
+    const int64_t r0 = int64_t(blockIdx.x) * kTcBM;
+    const int64_t nr = min64(kTcBM, rows - r0);
+    float mx = 0.f;
+    if (nr > 0)
+        for (int64_t e = threadIdx.x; e < nr * k; e += 256) {
+            const int64_t r = TRANS ? r0 + e % nr : r0 + e / k;
+            const int64_t c = TRANS ? e / nr : e % k;
+            const float v = fabsf(TRANS ? src[r + c * ld] : src[c + r * ld]);
+            mx = v > mx ? v : mx;
+        }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; ++w) mx = fmaxf(mx, red[w]);
+        int e = 0;
+        float sc = 1.f;
+        if (mx > 0.f && isfinite(mx)) {
+            frexpf(mx, &e);
+            sc = ldexpf(1.f, 8 - e);
+        }
+        scale[blockIdx.x] = sc;
+        inv[blockIdx.x] = 1.f / sc;
+    }
+}
+
+// E4M3 K-major packing of s_t x (the tile's scale), as pack_kernel.
+template <bool TRANS>
+__global__ void __launch_bounds__(256)
+pack_fp8_kernel(int64_t rows, int64_t k, const float* __restrict__ src, int64_t ld, uint8_t* __restrict__ dst,
+                int64_t rpad, int64_t kpad, const float* __restrict__ scale)
+{
+    __shared__ float t[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const int64_t r0 = int64_t(blockIdx.y) * 32, c0 = int64_t(blockIdx.x) * 32;
+    const float sc = scale[r0 / kTcBM];               // 32-row blocks never straddle a 128-row tile
+    if (TRANS) {
+        for (int q = ty; q < 32; q += 8) {
+            const int64_t r = r0 + tx, c = c0 + q;
+            t[q][tx] = (r < rows && c < k) ? src[r + c * ld] : 0.f;
+        }
+        __syncthreads();
+        for (int q = ty; q < 32; q += 8) {
+            const int64_t r = r0 + q, c = c0 + tx;
+            if (r < rpad && c < kpad) dst[r * kpad + c] = __nv_fp8_e4m3(t[tx][q] * sc).__x;
+        }
+    }
+    else {
+        for (int q = ty; q < 32; q += 8) {
+            const int64_t r = r0 + q, c = c0 + tx;
+            if (r < rpad && c < kpad) {
+                const float v = (r < rows && c < k) ? src[c + r * ld] : 0.f;
+                dst[r * kpad + c] = __nv_fp8_e4m3(v * sc).__x;
             }
         }
     }
@@ -629,7 +719,8 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
                                   void* ws, size_t ws_bytes, cudaStream_t stream)
 {
     if (m < 0 || n < 0 || k < 0 || (transb != 'N' && transb != 'T')) return SLT_ERR_ARG;
-    if (tier != SLT_PREC_TF32 && tier != SLT_PREC_BF16 && tier != SLT_PREC_FP16) return SLT_ERR_ARG;
+    if (tier != SLT_PREC_TF32 && tier != SLT_PREC_BF16 && tier != SLT_PREC_FP16 && tier != SLT_PREC_FP8)
+        return SLT_ERR_ARG;
     if (m == 0 || n == 0 || k == 0) return SLT_OK;
     int rc = get_encode();
     if (rc) return rc;
@@ -638,10 +729,14 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
         SLT_CUDA_TRY(cudaMemset(g_tc_status, 0, sizeof(int)));
     }
     const bool tf32 = tier == SLT_PREC_TF32;
-    const int esize = tf32 ? 4 : 2;
-    const int64_t kpad = ceildiv(k, tf32 ? 32 : 64) * (tf32 ? 32 : 64);
+    const bool fp8 = tier == SLT_PREC_FP8;
+    const int esize = tf32 ? 4 : fp8 ? 1 : 2;
+    const int64_t kq = 128 / esize;                  // elements per 128-byte K tile
+    const int64_t kpad = ceildiv(k, kq) * kq;
     const int64_t mp = ceildiv(m, kTcBM) * kTcBM, np = ceildiv(n, kTcBN) * kTcBN;
-    const size_t need = size_t(mp + np) * size_t(kpad) * esize + 2048;
+    const int64_t mtl = mp / kTcBM, ntl = np / kTcBN;
+    const size_t scale_bytes = fp8 ? sizeof(float) * 2 * size_t(mtl + ntl) + 256 : 0;
+    const size_t need = size_t(mp + np) * size_t(kpad) * esize + 2048 + scale_bytes;
     void* owned = nullptr;
     if (!ws || ws_bytes < need) {
         if (cudaMallocAsync(&owned, need, stream) != cudaSuccess) { cudaGetLastError(); return SLT_ERR_NOMEM; }
@@ -649,8 +744,29 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
     }
     char* pa = static_cast<char*>(ws);
     char* pb = pa + ((size_t(mp) * kpad * esize + 1023) & ~size_t(1023));
+    float* sA = reinterpret_cast<float*>(pb + ((size_t(np) * kpad * esize + 1023) & ~size_t(1023)));
+    float* iA = sA + mtl;
+    float* sB = iA + mtl;
+    float* iB = sB + ntl;
     // pack operands
-    if (tier == SLT_PREC_BF16) {
+    if (fp8) {
+        fp8_scale_kernel<true><<<unsigned(mtl), 256, 0, stream>>>(m, k, A, lda, sA, iA);
+        count_launch();
+        if (transb == 'N') fp8_scale_kernel<false><<<unsigned(ntl), 256, 0, stream>>>(n, k, B, ldb, sB, iB);
+        else fp8_scale_kernel<true><<<unsigned(ntl), 256, 0, stream>>>(n, k, B, ldb, sB, iB);
+        count_launch();
+        dim3 ga(unsigned(ceildiv(kpad, 32)), unsigned(ceildiv(mp, 32)));
+        dim3 gb(unsigned(ceildiv(kpad, 32)), unsigned(ceildiv(np, 32)));
+        pack_fp8_kernel<true><<<ga, 256, 0, stream>>>(m, k, A, lda, reinterpret_cast<uint8_t*>(pa), mp, kpad, sA);
+        count_launch();
+        if (transb == 'N')
+            pack_fp8_kernel<false><<<gb, 256, 0, stream>>>(n, k, B, ldb, reinterpret_cast<uint8_t*>(pb), np, kpad, sB);
+        else
+            pack_fp8_kernel<true><<<gb, 256, 0, stream>>>(n, k, B, ldb, reinterpret_cast<uint8_t*>(pb), np, kpad, sB);
+        count_launch();
+        rc = slt_from_cuda(cudaGetLastError());
+    }
+    else if (tier == SLT_PREC_BF16) {
         rc = launch_pack<__nv_bfloat16, true>(m, k, A, lda, reinterpret_cast<__nv_bfloat16*>(pa), mp, kpad, stream);
         if (!rc) rc = (transb == 'N')
             ? launch_pack<__nv_bfloat16, false>(n, k, B, ldb, reinterpret_cast<__nv_bfloat16*>(pb), np, kpad, stream)
@@ -672,11 +788,12 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
         CUtensorMap mapA, mapB;
         CUtensorMapDataType dt = tier == SLT_PREC_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
                                : tier == SLT_PREC_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                               : fp8                   ? CU_TENSOR_MAP_DATA_TYPE_UINT8
                                                        : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
         rc = make_map(&mapA, pa, dt, esize, kpad, mp, kTcBM);
         if (!rc) rc = make_map(&mapB, pb, dt, esize, kpad, np, kTcBN);
         if (!rc) {
-            TcArgs args{m, n, kpad, C, ldc, lower, g_tc_status};
+            TcArgs args{m, n, kpad, C, ldc, lower, g_tc_status, fp8 ? iA : nullptr, fp8 ? iB : nullptr};
             const int pidx = prof_begin(SLT_PROF_GEMM_TC, stream);
             const bool tma_c = (reinterpret_cast<uintptr_t>(C) % 16 == 0) && (ldc % 4 == 0);
             CUtensorMap mapC;
@@ -698,6 +815,11 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
                     if (!cfg) { cudaFuncSetAttribute(tc_update_persistent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psm)); cfg = true; }
                     tc_update_persistent<1><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(2, kTcBM, kTcBN));
                 }
+                else if (fp8) {
+                    static bool cfg = false;
+                    if (!cfg) { cudaFuncSetAttribute(tc_update_persistent<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psm)); cfg = true; }
+                    tc_update_persistent<2><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(0, kTcBM, kTcBN));
+                }
                 else {
                     static bool cfg = false;
                     if (!cfg) { cudaFuncSetAttribute(tc_update_persistent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psm)); cfg = true; }
@@ -712,6 +834,11 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
                 static bool cfg = false;
                 if (!cfg) { cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); cfg = true; }
                 tc_update_kernel<1><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(2, kTcBM, kTcBN));
+            }
+            else if (fp8) {
+                static bool cfg = false;
+                if (!cfg) { cudaFuncSetAttribute(tc_update_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); cfg = true; }
+                tc_update_kernel<2><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(0, kTcBM, kTcBN));
             }
             else {
                 static bool cfg = false;

@@ -192,3 +192,51 @@ def test_ill_conditioned_16bit_without_fp64_fallback(orc, slt, fn, kappa):
     assert retried == (it_ch < 0)
     assert berr(orc, A, X, B, sym=chol) <= 3 * n * EPS
     assert np.abs(X - xt).max() / np.abs(xt).max() <= kappa * 3 * n * EPS
+
+
+def _spd_kappa(n, kappa, seed):
+    """Q diag(s) Q^T, s geometric from 1 to 1/kappa (Haar Q from a seed)."""
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    return np.asfortranarray((Q * np.geomspace(1.0, 1.0 / kappa, n)) @ Q.T)
+
+
+@pytest.mark.parametrize("fn", ["posv_mixed", "posv_mixed_gmres"])
+def test_fp8_tier_converges_when_kappa_small(orc, slt, fn):
+    """FP8 E4M3 trailing updates (per-tile power-of-two scales): kappa = 10
+    converges in a handful of steps to the FP64 bar."""
+    n = 1024
+    A = _spd_kappa(n, 10.0, 31)
+    B = orc.generate(2, 32, n, 2)
+    info, it, X, Aout = _run(slt, fn, A, B, slt.Options(nb=256, factor_precision="fp8", lo_retry=0))
+    assert info == 0 and 0 <= it <= 12, it
+    assert berr(orc, A, X, B, sym=True) <= 3 * n * EPS
+    assert np.array_equal(Aout, A)
+
+
+def test_fp8_tier_falls_back_when_kappa_large(orc, slt):
+    """kappa = 1e4 is beyond E4M3's 3-bit mantissa: no convergence in itermax
+    steps, iter = -(itermax + 1) and the FP64 fallback's solution; with the
+    ladder on, the FP32 retry converges instead."""
+    n = 768
+    A = _spd_kappa(n, 1e4, 33)
+    B = orc.generate(2, 34, n, 1)
+    info, it, X, _ = _run(slt, "posv_mixed", A, B, slt.Options(nb=256, factor_precision="fp8", lo_retry=0,
+                                                                   max_iterations=10))
+    assert info == 0 and it == -11
+    assert berr(orc, A, X, B, sym=True) <= 3 * EPS
+    info, it, X, Aout = _run(slt, "posv_mixed", A, B, slt.Options(nb=256, factor_precision="fp8"))
+    assert info == 0 and it >= 0
+    assert berr(orc, A, X, B, sym=True) <= 3 * n * EPS
+    assert np.array_equal(Aout, A)
+
+
+def test_fp8_tier_lu(orc, slt):
+    """The LU form: a diagonally dominant general matrix converges with FP8
+    updates."""
+    n = 1024
+    A = np.asfortranarray(orc.generate(2, 35, n, n) + 0.25 * n * np.eye(n))
+    B = orc.generate(2, 36, n, 2)
+    info, it, X, _ = _run(slt, "gesv_mixed", A, B, slt.Options(nb=256, factor_precision="fp8", lo_retry=0))
+    assert info == 0 and it >= 0
+    assert berr(orc, A, X, B) <= 3 * n * EPS

@@ -12,7 +12,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TIERS = {"tf32": 2, "bf16": 3, "fp16": 4}
+TIERS = {"tf32": 2, "bf16": 3, "fp16": 4, "fp8": 5}
 
 
 def _round(torch, x, tier):
@@ -79,5 +79,60 @@ def test_tc_update_lower(slt, tier):
     _call(slt, tier, "T", L, L, C, 1)
     low = torch.tril(torch.ones(n, n, device="cuda", dtype=torch.bool))
     tol = 1e-5 * k * float(L.abs().max() ** 2)
+    assert float((C - ref)[low].abs().max()) <= tol
+    assert torch.equal(C[~low], C0[~low])
+
+
+def _fp8_tiles(torch, X):
+    """X (rows x k) with each 128-row tile scaled by 2^(8 - e), max|tile| =
+    m 2^e, rounded to E4M3 and scaled back: the FP8 tier's operand."""
+    out = torch.empty_like(X)
+    for t in range(0, X.shape[0], 128):
+        blk = X[t:t + 128]
+        mx = blk.abs().max()
+        s = 1.0
+        if float(mx) > 0:
+            _, e = torch.frexp(mx)
+            s = 2.0 ** (8 - int(e))
+        out[t:t + 128] = (blk * s).to(torch.float8_e4m3fn).float() / s
+    return out
+
+
+@pytest.mark.parametrize("m,n,k,transb", [(128, 128, 64, "N"), (300, 200, 100, "N"), (129, 257, 33, "N"),
+                                          (1024, 768, 512, "N"), (640, 384, 256, "T"), (77, 500, 512, "T"),
+                                          (20000, 328, 128, "T")])
+def test_tc_update_fp8(slt, m, n, k, transb):
+    """FP8 E4M3 tier: per-128-row-tile power-of-two scales, FP32 accumulation."""
+    import torch
+    torch.backends.cuda.matmul.allow_tf32 = False
+    g = torch.Generator(device="cuda").manual_seed(m * 3 + n + k)
+    A = slt.colmajor(torch.randn(m, k, device="cuda", generator=g) * 7.0)
+    B = slt.colmajor(torch.randn(k, n, device="cuda", generator=g) * 0.01 if transb == "N"
+                     else torch.randn(n, k, device="cuda", generator=g) * 0.01)
+    C0 = torch.randn(m, n, device="cuda", generator=g)
+    C = slt.colmajor(C0.clone())
+    Bt = B.t() if transb == "N" else B              # n x k, the operand's rows
+    A8, B8 = _fp8_tiles(torch, A.contiguous()), _fp8_tiles(torch, Bt.contiguous())
+    ref = C0 - A8 @ B8.t()
+    _call(slt, "fp8", transb, A, B, C, 0)
+    tol = 1e-5 * k * float(A8.abs().max() * B8.abs().max())
+    err = float((C - ref).abs().max())
+    assert err <= tol, (err, tol)
+    # the quantisation error itself is that of a 3-bit mantissa: far above the tol
+    assert float((ref - (C0 - A @ Bt.t())).abs().max()) > 10 * tol
+
+
+def test_tc_update_fp8_lower(slt):
+    import torch
+    n, k = 700, 192
+    g = torch.Generator(device="cuda").manual_seed(9)
+    L = slt.colmajor(torch.randn(n, k, device="cuda", generator=g))
+    C0 = torch.randn(n, n, device="cuda", generator=g)
+    C = slt.colmajor(C0.clone())
+    L8 = _fp8_tiles(torch, L.contiguous())
+    ref = C0 - L8 @ L8.t()
+    _call(slt, "fp8", "T", L, L, C, 1)
+    low = torch.tril(torch.ones(n, n, device="cuda", dtype=torch.bool))
+    tol = 1e-5 * k * float(L8.abs().max()) ** 2
     assert float((C - ref)[low].abs().max()) <= tol
     assert torch.equal(C[~low], C0[~low])
