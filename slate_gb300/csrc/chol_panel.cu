@@ -30,6 +30,7 @@ namespace slt {
 constexpr int kCpThreads = 256;
 constexpr int kCpIB = 64;
 constexpr int kCpSub = 16;
+constexpr int kStage = kCpIB * kCpIB / kCpThreads;   // 64 x 64 tile elements per thread, loaded in one batch
 
 // One warp: Cholesky of the bw x bw (bw <= 16) lower block S (row-major,
 // row stride lds) in registers, lane r holding row r; the factor is written
@@ -177,7 +178,7 @@ __device__ int factor_diag_block(T* D, T* Dinv, int kb)
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kCpThreads)
+__global__ void __launch_bounds__(kCpThreads, 2)
 chol_panel_kernel(CholPanelArgs<T> a)
 {
     extern __shared__ unsigned char cp_smem_raw[];
@@ -205,12 +206,14 @@ chol_panel_kernel(CholPanelArgs<T> a)
             __syncthreads();
             if (s_abort) return;
         }
-        for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
-            int i = e % kCpIB, l = e / kCpIB;
-            D[i * (kCpIB + 1) + l] = (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
-        }
+        staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+            const int i = e % kCpIB, l = e / kCpIB;
+            return (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
+        }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
         if (c0 > 0)
-            for (int e = t; e < kCpDinv; e += kCpThreads) Dinv[e] = __ldcg(&a.dinv_ws[size_t(k) * kCpDinv + e]);
+            staged_copy<(kCpDinv + kCpThreads - 1) / kCpThreads, kCpThreads>(kCpDinv, [&](int e) {
+                return __ldcg(&a.dinv_ws[size_t(k) * kCpDinv + e]);
+            }, [&](int e, T v) { Dinv[e] = v; });
         if (t == 0) s_fail = (c0 > 0) ? ld_volatile_i32(a.next_fail) : 0;
         __syncthreads();
         if (c0 == 0) {
@@ -230,10 +233,10 @@ chol_panel_kernel(CholPanelArgs<T> a)
             for (int64_t rr = r0; rr < re; rr += kCpIB) {
                 const int nr = int(min64(kCpIB, re - rr));
                 __syncthreads();
-                for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
-                    int i = e % kCpIB, l = e / kCpIB;
-                    Xs[i * (kCpIB + 1) + l] = (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
-                }
+                staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                    const int i = e % kCpIB, l = e / kCpIB;
+                    return (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
+                }, [&](int e, T v) { Xs[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
                 __syncthreads();
                 const int row = t >> 2, q = t & 3, lane = t & 31;
                 T* xr = Xs + row * (kCpIB + 1);
@@ -307,20 +310,22 @@ chol_panel_kernel(CholPanelArgs<T> a)
             // rows tr + 16 i and columns tc + 16 j: lanes run along rows, so
             // the final read-modify-write of P is two 64-byte segments per warp
             const int tr = t & 15, tc = t >> 4;
-            for (int64_t cb = cbeg; cb < a.nbk; cb += kCpIB) {
+            // a column tile starting at or below the block's last row has no
+            // lower-triangular rows here, nor have the tiles after it
+            for (int64_t cb = cbeg; cb < a.nbk && cb < re; cb += kCpIB) {
                 const int nc = int(min64(kCpIB, a.nbk - cb));
                 __syncthreads();
-                for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
-                    int c = e % kCpIB, l = e / kCpIB;
-                    U3[l * 68 + c] = (c < nc && l < kb) ? __ldcg(&P[cb + c + (c0 + l) * ld]) : T(0);
-                }
+                staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                    const int c = e % kCpIB, l = e / kCpIB;
+                    return (c < nc && l < kb) ? __ldcg(&P[cb + c + (c0 + l) * ld]) : T(0);
+                }, [&](int e, T v) { U3[(e / kCpIB) * 68 + e % kCpIB] = v; });
                 for (int64_t rr = max64(r0, cb); rr < re; rr += kCpIB) {
                     const int nr = int(min64(kCpIB, re - rr));
                     __syncthreads();
-                    for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
-                        int i = e % kCpIB, l = e / kCpIB;
-                        X3[l * 68 + i] = (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
-                    }
+                    staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                        const int i = e % kCpIB, l = e / kCpIB;
+                        return (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
+                    }, [&](int e, T v) { X3[(e / kCpIB) * 68 + e % kCpIB] = v; });
                     __syncthreads();
                     T acc[4][4];
                     #pragma unroll
@@ -337,20 +342,21 @@ chol_panel_kernel(CholPanelArgs<T> a)
                             #pragma unroll
                             for (int j = 0; j < 4; ++j) acc[i][j] = fma(xr[i], uc[j], acc[i][j]);
                     }
+                    T old[4][4];
                     #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const int c = tc + 16 * j;
-                        if (c >= nc) continue;
+                    for (int j = 0; j < 4; ++j)
                         #pragma unroll
                         for (int i = 0; i < 4; ++i) {
-                            const int ii = tr + 16 * i;
-                            const int64_t gi = rr + ii;
-                            if (ii < nr && gi >= cb + c) {
-                                T* p = &P[gi + (cb + c) * ld];
-                                *p = __ldcg(p) - acc[i][j];
-                            }
+                            const int c = tc + 16 * j, ii = tr + 16 * i;
+                            if (c < nc && ii < nr && rr + ii >= cb + c) old[i][j] = __ldcg(&P[rr + ii + (cb + c) * ld]);
                         }
-                    }
+                    #pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const int c = tc + 16 * j, ii = tr + 16 * i;
+                            if (c < nc && ii < nr && rr + ii >= cb + c) P[rr + ii + (cb + c) * ld] = old[i][j] - acc[i][j];
+                        }
                 }
             }
         }
@@ -361,10 +367,10 @@ chol_panel_kernel(CholPanelArgs<T> a)
         if (!failed && cbeg < a.nbk && cbeg >= rb && cbeg < re) {
             const int kbn = int(min64(kCpIB, a.nbk - cbeg));
             __syncthreads();
-            for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
-                int i = e % kCpIB, l = e / kCpIB;
-                D[i * (kCpIB + 1) + l] = (i < kbn && l < kbn && i >= l) ? __ldcg(&P[cbeg + i + (cbeg + l) * ld]) : T(0);
-            }
+            staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                const int i = e % kCpIB, l = e / kCpIB;
+                return (i < kbn && l < kbn && i >= l) ? __ldcg(&P[cbeg + i + (cbeg + l) * ld]) : T(0);
+            }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
             __syncthreads();
             const int f = factor_diag_block(D, Dinv, kbn);
             for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {

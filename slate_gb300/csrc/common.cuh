@@ -84,6 +84,28 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned nblocks, in
     return s_ok != 0;
 }
 
+// st(e, ld(e)) for e in [0, cnt) by NTHR threads, each issuing NB loads
+// before it stores any of their results: an SM issues in order, so a load
+// whose result is stored at once costs its full memory latency, and a loop
+// of such pairs pays it once per element.
+template <int NB, int NTHR, typename Load, typename Store>
+__device__ __forceinline__ void staged_copy(int cnt, Load ld, Store st)
+{
+    for (int e0 = threadIdx.x; e0 < cnt; e0 += NB * NTHR) {
+        decltype(ld(0)) v[NB];
+        #pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            const int e = e0 + u * NTHR;
+            if (e < cnt) v[u] = ld(e);
+        }
+        #pragma unroll
+        for (int u = 0; u < NB; ++u) {
+            const int e = e0 + u * NTHR;
+            if (e < cnt) st(e, v[u]);
+        }
+    }
+}
+
 template <typename T> struct Real;
 template <> struct Real<double> {
     static __device__ __forceinline__ double safe_min() { return 2.2250738585072014e-308; }

@@ -98,27 +98,6 @@ __device__ double block_max(double v, double* sv)
     return v;
 }
 
-// st(e, ld(e)) for e in [0, cnt), NB loads per thread issued before any of
-// their results is stored (a load followed at once by a dependent store would
-// otherwise wait out the full memory latency per element).
-template <int NB, typename Load, typename Store>
-__device__ __forceinline__ void batched_copy(int cnt, Load ld, Store st)
-{
-    for (int e0 = threadIdx.x; e0 < cnt; e0 += NB * NT) {
-        decltype(ld(0)) v[NB];
-        #pragma unroll
-        for (int u = 0; u < NB; ++u) {
-            const int e = e0 + u * NT;
-            if (e < cnt) v[u] = ld(e);
-        }
-        #pragma unroll
-        for (int u = 0; u < NB; ++u) {
-            const int e = e0 + u * NT;
-            if (e < cnt) st(e, v[u]);
-        }
-    }
-}
-
 // v = p[0 .. 3] from shared memory in one (float) or two (double) 16-byte loads;
 // p is 16-byte aligned.
 __device__ __forceinline__ void lds4(const float* p, float (&v)[4])
@@ -597,7 +576,7 @@ __device__ void lu_solve(const T* M, int n, int ld, const int* ipiv, T* Y, int n
     // row interchanges staged in the tile area (n <= MAXN ints fit), then
     // applied in order by one thread per right-hand side
     int* sp = reinterpret_cast<int*>(tile);
-    batched_copy<MAXN / NT>(n, [&](int j) { return ipiv[j]; }, [&](int j, int v) { sp[j] = v; });
+    staged_copy<MAXN / NT, NT>(n, [&](int j) { return ipiv[j]; }, [&](int j, int v) { sp[j] = v; });
     __syncthreads();
     if (threadIdx.x < nr) {
         T* y = Y + threadIdx.x * n;
@@ -662,7 +641,7 @@ __global__ void __launch_bounds__(NT, 2) vb_plain_kernel(const Sys* __restrict__
         if (inf != 0) continue;
         for (int c0 = 0; c0 < s.nrhs; c0 += MAXR) {
             const int nr = min(MAXR, s.nrhs - c0);
-            batched_copy<4>(s.n * nr, [&](int e) { return s.B[e % s.n + size_t(c0 + e / s.n) * s.ldb]; },
+            staged_copy<4, NT>(s.n * nr, [&](int e) { return s.B[e % s.n + size_t(c0 + e / s.n) * s.ldb]; },
                             [&](int e, double v) { Y[e] = v; });
             __syncthreads();
             if (s.kind == 0) lu_solve<double>(s.A, s.n, s.lda, s.ipiv, Y, nr, tile);
@@ -734,7 +713,7 @@ __global__ void __launch_bounds__(NT, 2) vb_mixed_factor_kernel(const Sys* __res
         }
         if (inf != 0) continue;
         const int nr = s.nrhs;     // <= MAXR (checked on the host)
-        batched_copy<4>(s.n * nr, [&](int e) { return float(s.B[e % s.n + size_t(e / s.n) * s.ldb]); },
+        staged_copy<4, NT>(s.n * nr, [&](int e) { return float(s.B[e % s.n + size_t(e / s.n) * s.ldb]); },
                         [&](int e, float v) { Y[e] = v; });
         __syncthreads();
         if (s.kind == 0) lu_solve<float>(s.lo, s.n, s.n, s.ipiv, Y, nr, tile);
@@ -852,7 +831,7 @@ __global__ void __launch_bounds__(NT) vb_refine_kernel(const Sys* __restrict__ s
         }
         if (s.kind == 0) lu_solve<float>(s.lo, n, n, s.ipiv, Y, nr, tile);
         else chol_solve<float>(s.lo, n, n, Y, nr, tile);
-        batched_copy<4>(n * nr, [&](int e) { return s.X[e % n + size_t(e / n) * s.ldx] + double(Y[e]); },
+        staged_copy<4, NT>(n * nr, [&](int e) { return s.X[e % n + size_t(e / n) * s.ldx] + double(Y[e]); },
                         [&](int e, double v) { s.X[e % n + size_t(e / n) * s.ldx] = v; });
         __syncthreads();
     }
