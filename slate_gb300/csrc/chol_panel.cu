@@ -34,11 +34,10 @@ constexpr int kStage = kCpIB * kCpIB / kCpThreads;   // 64 x 64 tile elements pe
 
 // One warp: Cholesky of the bw x bw (bw <= 16) lower block S (row-major,
 // row stride lds) in registers, lane r holding row r; the factor is written
-// back to S and its inverse to Inv (16 x 17, Inv[k * 17 + c] = L^{-1}(k, c),
-// zero above the diagonal and outside bw).  Returns 0, or the 1-based column
-// of the first non-positive pivot.
+// back to S and the reciprocals of its diagonal to Rd[0 .. bw).  Returns 0,
+// or the 1-based column of the first non-positive pivot.
 template <typename T>
-__device__ int factor_invert_16(T* S, int lds, int bw, T* Inv)
+__device__ int factor_16(T* S, int lds, int bw, T* Rd)
 {
     const unsigned FULL = 0xffffffffu;
     const int r = threadIdx.x & 31;
@@ -55,7 +54,7 @@ __device__ int factor_invert_16(T* S, int lds, int bw, T* Inv)
             }
             else {
                 const T sd = sqrt(d);
-                if (r == j) a[j] = sd;
+                if (r == j) { a[j] = sd; Rd[j] = T(1) / sd; }
                 else if (r > j) a[j] = a[j] / sd;
                 #pragma unroll
                 for (int c = j + 1; c < kCpSub; ++c) {
@@ -66,25 +65,33 @@ __device__ int factor_invert_16(T* S, int lds, int bw, T* Inv)
         }
     }
     if (fail) return fail;
-    // lane c: column c of L^{-1} by forward substitution
-    const int c = r;
+    if (r < bw) {
+        #pragma unroll
+        for (int cc = 0; cc < kCpSub; ++cc)
+            if (cc <= r) S[r * lds + cc] = a[cc];
+    }
+    return 0;
+}
+
+// One warp: Inv (16 x 17, Inv[k * 17 + c] = L^{-1}(k, c), zero above the
+// diagonal and outside bw) of the factor factor_16 left in S; lane c forms
+// column c by forward substitution.
+template <typename T>
+__device__ void invert_16(const T* S, int lds, int bw, const T* Rd, T* Inv)
+{
+    const int c = threadIdx.x & 31;
     T x[kCpSub];
     #pragma unroll
     for (int k = 0; k < kCpSub; ++k) {
         T acc = (k == c) ? T(1) : T(0);
         #pragma unroll
-        for (int p = 0; p < k; ++p) acc = fma(-__shfl_sync(FULL, a[p], k), x[p], acc);
-        const T lkk = __shfl_sync(FULL, a[k], k);
-        x[k] = (k < bw && c < bw && k >= c) ? acc / lkk : T(0);
+        for (int p = 0; p < k; ++p) acc = fma(-S[k * lds + p], x[p], acc);
+        x[k] = (k < bw && c < bw && k >= c) ? acc * Rd[k] : T(0);
     }
-    if (r < kCpSub) {
+    if (c < kCpSub) {
         #pragma unroll
-        for (int k = 0; k < kCpSub; ++k) Inv[k * (kCpSub + 1) + r] = x[k];
-        #pragma unroll
-        for (int cc = 0; cc < kCpSub; ++cc)
-            if (r < bw && cc <= r) S[r * lds + cc] = a[cc];
+        for (int k = 0; k < kCpSub; ++k) Inv[k * (kCpSub + 1) + c] = x[k];
     }
-    return 0;
 }
 
 template <typename T>
@@ -120,59 +127,66 @@ __device__ __forceinline__ bool wait_at_least(const unsigned* p, unsigned target
 
 // The 64 x 64 (kb x kb) diagonal block D (row-major in shared memory, row
 // stride 65, lower triangle) factored in place by the whole CTA, in 16-column
-// steps: warp 0 factors the 16 x 16 diagonal sub-block and inverts it into
-// Dinv, then all threads solve the sub-block rows below it and update the
-// rest of the block.  Returns 0, or the 1-based column (within the block) of
-// the first non-positive pivot; the same value in every thread.
+// steps: warp 0 factors the 16 x 16 diagonal sub-block; then warps 1-7 solve
+// the sub-block rows below it by forward substitution and update the rest of
+// the block (their own 224-thread barrier), while warp 0 inverts the
+// sub-block into Dinv for the panel's row solves -- the inversion stays off
+// the chain of sub-block steps.  Returns 0, or the 1-based column (within the
+// block) of the first non-positive pivot; the same value in every thread.
+__device__ __forceinline__ void bar_workers() { asm volatile("bar.sync 1, %0;" :: "n"(kCpThreads - 32) : "memory"); }
+
 template <typename T>
 __device__ int factor_diag_block(T* D, T* Dinv, int kb)
 {
     __shared__ int s_f;
+    __shared__ T s_rd[kCpIB / kCpSub][kCpSub];
     const int t = threadIdx.x;
     if (t == 0) s_f = 0;
     __syncthreads();
     for (int jb = 0, jbi = 0; jb < kb; jb += kCpSub, ++jbi) {
         const int bw = min(kCpSub, kb - jb);
+        T* S = D + jb * (kCpIB + 1) + jb;
         if (t < 32) {
-            const int fail = factor_invert_16(D + jb * (kCpIB + 1) + jb, kCpIB + 1, bw,
-                                              Dinv + jbi * kCpSub * (kCpSub + 1));
+            const int fail = factor_16(S, kCpIB + 1, bw, s_rd[jbi]);
             if (t == 0 && fail) s_f = jb + fail;
         }
         __syncthreads();
         if (s_f) break;
-        // rows i in [jb + bw, kb) of the sub-block column: X = B L_sub^{-T}
         const int below = kb - jb - bw;
-        const T* Di = Dinv + jbi * kCpSub * (kCpSub + 1);
-        T xv[3];
-        #pragma unroll
-        for (int u = 0; u < 3; ++u) {
-            const int e = t + u * kCpThreads;
-            xv[u] = T(0);
-            if (e < below * bw) {
-                const int i = jb + bw + e / bw, c = e % bw;
+        if (t < 32) {
+            invert_16(S, kCpIB + 1, bw, s_rd[jbi], Dinv + jbi * kCpSub * (kCpSub + 1));
+        }
+        else if (below > 0) {
+            const int w = t - 32;
+            // rows i in [jb + bw, kb) of the sub-block column: X L^T = B, row by row
+            if (w < below) {
+                const int i = jb + bw + w;
+                T* xi = D + i * (kCpIB + 1) + jb;
+                T x[kCpSub];
+                #pragma unroll
+                for (int c = 0; c < kCpSub; ++c) {
+                    T acc = (c < bw) ? xi[c] : T(0);
+                    #pragma unroll
+                    for (int p = 0; p < c; ++p) acc = fma(-x[p], S[c * (kCpIB + 1) + p], acc);
+                    x[c] = (c < bw) ? acc * s_rd[jbi][c] : T(0);
+                }
+                #pragma unroll
+                for (int c = 0; c < kCpSub; ++c)
+                    if (c < bw) xi[c] = x[c];
+            }
+            bar_workers();
+            // trailing update inside the block: D[i][c] -= sum_p D[i][jb+p] D[c][jb+p], jb+bw <= c <= i < kb
+            for (int e = w; e < below * below; e += kCpThreads - 32) {
+                const int i = jb + bw + e % below, c = jb + bw + e / below;
+                if (c > i) continue;
                 T acc = T(0);
-                for (int p = 0; p <= c; ++p) acc = fma(D[i * (kCpIB + 1) + jb + p], Di[c * (kCpSub + 1) + p], acc);
-                xv[u] = acc;
+                for (int p = 0; p < bw; ++p)
+                    acc = fma(D[i * (kCpIB + 1) + jb + p], D[c * (kCpIB + 1) + jb + p], acc);
+                D[i * (kCpIB + 1) + c] -= acc;
             }
         }
         __syncthreads();
-        #pragma unroll
-        for (int u = 0; u < 3; ++u) {
-            const int e = t + u * kCpThreads;
-            if (e < below * bw) D[(jb + bw + e / bw) * (kCpIB + 1) + jb + e % bw] = xv[u];
-        }
-        __syncthreads();
-        // trailing update inside the block: D[i][c] -= sum_p D[i][jb+p] D[c][jb+p], jb+bw <= c <= i < kb
-        for (int e = t; e < below * below; e += kCpThreads) {
-            const int i = jb + bw + e % below, c = jb + bw + e / below;
-            if (c > i) continue;
-            T acc = T(0);
-            for (int p = 0; p < bw; ++p)
-                acc = fma(D[i * (kCpIB + 1) + jb + p], D[c * (kCpIB + 1) + jb + p], acc);
-            D[i * (kCpIB + 1) + c] -= acc;
-        }
-        __syncthreads();
-        }
+    }
     __syncthreads();
     return s_f;
 }
