@@ -127,12 +127,13 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
         // inverse of the diagonal block (row-major), and this block's RHS
         {
             const T* dinv = Dinv + size_t(bi) * kSwBS * kSwBS;
-            for (int e = t; e < kSwBS * kSwBS; e += 256) sm.Ds[e / kSwBS][e % kSwBS] = dinv[e];
+            staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) { return dinv[e]; },
+                                                  [&](int e, T v) { sm.Ds[e / kSwBS][e % kSwBS] = v; });
         }
-        for (int e = t; e < kSwBS * kSwRhs; e += 256) {
-            int r = e % kSwBS, q = e / kSwBS;
-            sm.xi[r][q] = (r < ni && q < nrhs) ? X[i0 + r + q * ldx] : T(0);
-        }
+        staged_copy<kSwBS * kSwRhs / 256, 256>(kSwBS * kSwRhs, [&](int e) {
+            const int r = e % kSwBS, q = e / kSwBS;
+            return (r < ni && q < nrhs) ? X[i0 + r + q * ldx] : T(0);
+        }, [&](int e, T v) { sm.xi[e % kSwBS][e / kSwBS] = v; });
 
         // accumulate op(M)(i, j) x_j over the solved blocks
         const int r = t % kSwBS, g = t / kSwBS;           // 4 groups x 4 right-hand sides
@@ -142,12 +143,13 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
             const int64_t j0 = int64_t(bj) * kSwBS;
             const int nj = int(min64(kSwBS, n - j0));
             __syncthreads();
-            for (int e = t; e < kSwBS * kSwBS; e += 256) {
-                int rr, c;
-                if (TRANS) { c = e % kSwBS; rr = e / kSwBS; }
-                else       { rr = e % kSwBS; c = e / kSwBS; }
-                sm.Ts[c][rr] = (rr < ni && c < nj) ? opM(i0 + rr, j0 + c) : T(0);
-            }
+            staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) {
+                const int rr = TRANS ? e / kSwBS : e % kSwBS, c = TRANS ? e % kSwBS : e / kSwBS;
+                return (rr < ni && c < nj) ? opM(i0 + rr, j0 + c) : T(0);
+            }, [&](int e, T v) {
+                const int rr = TRANS ? e / kSwBS : e % kSwBS, c = TRANS ? e % kSwBS : e / kSwBS;
+                sm.Ts[c][rr] = v;
+            });
             if (t == 0) {
                 int ok = 1;
                 if (ld_acquire_i32(&ready[pq]) == 0) {
@@ -165,10 +167,10 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
             }
             __syncthreads();
             if (!s_ok) return;
-            for (int e = t; e < kSwBS * kSwRhs; e += 256) {
-                int rr = e % kSwBS, q = e / kSwBS;
-                sm.xs[rr][q] = (rr < nj && q < nrhs) ? __ldcg(&X[j0 + rr + q * ldx]) : T(0);
-            }
+            staged_copy<kSwBS * kSwRhs / 256, 256>(kSwBS * kSwRhs, [&](int e) {
+                const int rr = e % kSwBS, q = e / kSwBS;
+                return (rr < nj && q < nrhs) ? __ldcg(&X[j0 + rr + q * ldx]) : T(0);
+            }, [&](int e, T v) { sm.xs[e % kSwBS][e / kSwBS] = v; });
             __syncthreads();
             #pragma unroll 4
             for (int c = 0; c < kSwBS; ++c) {
