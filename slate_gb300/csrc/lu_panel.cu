@@ -109,17 +109,17 @@ __device__ bool stripe_end(const PanelArgs<T>& a, int G, int b, int t, int64_t k
         for (int64_t rr = r0; rr < re; rr += 32) {
             const int nr = int(min64(32, re - rr));
             __syncthreads();
-            for (int e = t; e < 32 * kb; e += kPanelThreads) {
-                int i = e % 32, l = e / 32;
-                s_L[i][l] = (i < nr) ? __ldcg(&P[rr + i + (k0 + l) * ld]) : T(0);
-            }
+            staged_copy<8, kPanelThreads>(32 * kb, [&](int e) {
+                const int i = e % 32, l = e / 32;
+                return (i < nr) ? __ldcg(&P[rr + i + (k0 + l) * ld]) : T(0);
+            }, [&](int e, T v) { s_L[e % 32][e / 32] = v; });
             for (int64_t cb = c0; cb < a.nbk; cb += 32) {
                 const int nc = int(min64(32, a.nbk - cb));
                 __syncthreads();
-                for (int e = t; e < kb * 32; e += kPanelThreads) {
-                    int l = e % kb, c = e / kb;
-                    s_U[l][c] = (c < nc) ? __ldcg(&P[k0 + l + (cb + c) * ld]) : T(0);
-                }
+                staged_copy<8, kPanelThreads>(kb * 32, [&](int e) {
+                    const int l = e % kb, c = e / kb;
+                    return (c < nc) ? __ldcg(&P[k0 + l + (cb + c) * ld]) : T(0);
+                }, [&](int e, T v) { s_U[e % kb][e / kb] = v; });
                 __syncthreads();
                 // 32 x 32 outputs, 4 per thread
                 const int i = t % 32;
@@ -333,10 +333,8 @@ getrf_panel2_kernel(PanelArgs<T> a, int* flags)
     for (int64_t k0 = 0; k0 < diag_len; k0 += a.ib) {
         const int kb = int(min64(a.ib, diag_len - k0));
         __syncthreads();
-        for (int e = t; e < nrow * kb; e += kPanelThreads) {
-            const int r = e % nrow, c = e / nrow;
-            S[c * RP + r] = __ldcg(&P[rb + r + (k0 + c) * ld]);
-        }
+        staged_copy<8, kPanelThreads>(nrow * kb, [&](int e) { return __ldcg(&P[rb + e % nrow + (k0 + e / nrow) * ld]); },
+                                      [&](int e, T v) { S[(e / nrow) * RP + e % nrow] = v; });
         __syncthreads();
         for (int64_t j = k0; j < k0 + kb; ++j) {
             ++seq;

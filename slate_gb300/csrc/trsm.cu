@@ -44,12 +44,13 @@ trsm_kernel(int kb, int64_t nvec, const T* __restrict__ Tm, int64_t ldt, T* B, i
         return RIGHT ? (v0 + c) + int64_t(r) * ldb : int64_t(r) + (v0 + c) * ldb;
     };
 
-    for (int e = t; e < kb * kTrsmCols; e += 256) {
-        int r, c;
-        if (RIGHT) { c = e % kTrsmCols; r = e / kTrsmCols; }
-        else       { r = e % kb; c = e / kb; }
-        X[r * kTrsmCols + c] = (c < nv) ? B[bidx(r, c)] : T(0);
-    }
+    staged_copy<16, 256>(kb * kTrsmCols, [&](int e) {
+        const int r = RIGHT ? e / kTrsmCols : e % kb, c = RIGHT ? e % kTrsmCols : e / kb;
+        return (c < nv) ? B[bidx(r, c)] : T(0);
+    }, [&](int e, T v) {
+        const int r = RIGHT ? e / kTrsmCols : e % kb, c = RIGHT ? e % kTrsmCols : e / kb;
+        X[r * kTrsmCols + c] = v;
+    });
     __syncthreads();
 
     const int nblk = (kb + kTrsmDB - 1) / kTrsmDB;
@@ -59,10 +60,10 @@ trsm_kernel(int kb, int64_t nvec, const T* __restrict__ Tm, int64_t ldt, T* B, i
         const int re = min(kb, rb + kTrsmDB);
         const int nr = re - rb;
         // stage the diagonal block of op(T)
-        for (int e = t; e < kTrsmDB * kTrsmDB; e += 256) {
-            int i = e % kTrsmDB, l = e / kTrsmDB;
-            D[i * (kTrsmDB + 1) + l] = (i < nr && l < nr) ? opT(rb + i, rb + l) : T(0);
-        }
+        staged_copy<kTrsmDB * kTrsmDB / 256, 256>(kTrsmDB * kTrsmDB, [&](int e) {
+            const int i = e % kTrsmDB, l = e / kTrsmDB;
+            return (i < nr && l < nr) ? opT(rb + i, rb + l) : T(0);
+        }, [&](int e, T v) { D[(e % kTrsmDB) * (kTrsmDB + 1) + e / kTrsmDB] = v; });
         // update rows [rb, re) from the solved rows
         {
             const int i = t % kTrsmDB;
