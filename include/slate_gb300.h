@@ -36,9 +36,11 @@ enum slt_precision {
     SLT_PREC_TF32 = 2,   /* FP32 storage, TF32 tensor-core trailing update   */
     SLT_PREC_BF16 = 3,   /* FP32 storage, BF16 tensor-core trailing update   */
     SLT_PREC_FP16 = 4,   /* FP32 storage, FP16 tensor-core trailing update   */
-    SLT_PREC_FP8  = 5    /* FP32 storage, FP8 E4M3 tensor-core trailing update
+    SLT_PREC_FP8  = 5,   /* FP32 storage, FP8 E4M3 tensor-core trailing update
                             with a power-of-two scale per 128-row tile
                             (experimental)                                   */
+    SLT_PREC_TF32X3 = 6  /* FP32 storage, split-precision 3xTF32 tensor-core
+                            trailing update (inputs to 22 bits, FP32 sums)   */
 };
 
 /* Options (SLATE Option keys, include/slate/enums.hh:453-490). */

@@ -21,7 +21,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libslate_gb300.so")
 
 PREC_FP64, PREC_FP32, PREC_TF32, PREC_BF16, PREC_FP16 = 0, 1, 2, 3, 4
-_PREC_NAMES = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "fp16": 4, "fp8": 5}
+_PREC_NAMES = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "fp16": 4, "fp8": 5, "tf32x3": 6}
 _REFINE_NAMES = {"ir": 0, "ir+gmres": 2}
 
 

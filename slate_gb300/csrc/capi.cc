@@ -140,6 +140,7 @@ slt_options lapack_opts()
         else if (v == "bf16") o.factor_precision = SLT_PREC_BF16;
         else if (v == "fp16") o.factor_precision = SLT_PREC_FP16;
         else if (v == "fp8") o.factor_precision = SLT_PREC_FP8;
+        else if (v == "tf32x3") o.factor_precision = SLT_PREC_TF32X3;
     }
     return o;
 }

@@ -60,7 +60,8 @@ static int k_gemm(char tb, int64_t m, int64_t n, int64_t k, float alpha, const f
                   const slt_options& o, cudaStream_t s)
 {
     int tier = o.factor_precision;
-    if ((tier == SLT_PREC_TF32 || tier == SLT_PREC_BF16 || tier == SLT_PREC_FP16 || tier == SLT_PREC_FP8) &&
+    if ((tier == SLT_PREC_TF32 || tier == SLT_PREC_BF16 || tier == SLT_PREC_FP16 || tier == SLT_PREC_FP8 ||
+         tier == SLT_PREC_TF32X3) &&
         alpha == -1.f
         && beta == 1.f && k >= 16 && m >= 128 && n >= 128)
         return slt_tc_gemm_update(tier, tb, m, n, k, A, lda, B, ldb, C, ldc, lower, nullptr, 0, s);

@@ -629,6 +629,53 @@ pack_fp8_kernel(int64_t rows, int64_t k, const float* __restrict__ src, int64_t 
     }
 }
 
+// 3xTF32 packing: each K-major row holds three TF32 segments of kseg
+// elements, [hi | hi | lo] for A (ROLE 0) and [hi | lo | hi] for op(B)^T
+// (ROLE 1), hi = rna_tf32(x), lo = rna_tf32(x - hi), so that one TF32 GEMM
+// over K' = 3 kseg accumulates A_hi B_hi + A_hi B_lo + A_lo B_hi: FP32 inputs
+// to 22 bits, products exact, FP32 accumulation.
+__device__ __forceinline__ float rna_tf32(float v)
+{
+    uint32_t u;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(v));
+    return __uint_as_float(u);
+}
+
+template <bool TRANS, int ROLE>
+__global__ void __launch_bounds__(256)
+pack3_kernel(int64_t rows, int64_t k, const float* __restrict__ src, int64_t ld, float* __restrict__ dst,
+             int64_t rpad, int64_t kseg)
+{
+    __shared__ float t[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const int64_t r0 = int64_t(blockIdx.y) * 32, c0 = int64_t(blockIdx.x) * 32;
+    const int64_t kp = 3 * kseg;
+    auto put = [&](int64_t r, int64_t c, float v) {
+        const float hi = rna_tf32(v), lo = rna_tf32(v - hi);
+        float* row = dst + r * kp;
+        row[c] = ROLE == 0 ? hi : hi;
+        row[kseg + c] = ROLE == 0 ? hi : lo;
+        row[2 * kseg + c] = ROLE == 0 ? lo : hi;
+    };
+    if (TRANS) {
+        for (int q = ty; q < 32; q += 8) {
+            const int64_t r = r0 + tx, c = c0 + q;
+            t[q][tx] = (r < rows && c < k) ? src[r + c * ld] : 0.f;
+        }
+        __syncthreads();
+        for (int q = ty; q < 32; q += 8) {
+            const int64_t r = r0 + q, c = c0 + tx;
+            if (r < rpad && c < kseg) put(r, c, t[tx][q]);
+        }
+    }
+    else {
+        for (int q = ty; q < 32; q += 8) {
+            const int64_t r = r0 + q, c = c0 + tx;
+            if (r < rpad && c < kseg) put(r, c, (r < rows && c < k) ? src[c + r * ld] : 0.f);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Host side
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
@@ -719,7 +766,8 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
                                   void* ws, size_t ws_bytes, cudaStream_t stream)
 {
     if (m < 0 || n < 0 || k < 0 || (transb != 'N' && transb != 'T')) return SLT_ERR_ARG;
-    if (tier != SLT_PREC_TF32 && tier != SLT_PREC_BF16 && tier != SLT_PREC_FP16 && tier != SLT_PREC_FP8)
+    if (tier != SLT_PREC_TF32 && tier != SLT_PREC_BF16 && tier != SLT_PREC_FP16 && tier != SLT_PREC_FP8 &&
+        tier != SLT_PREC_TF32X3)
         return SLT_ERR_ARG;
     if (m == 0 || n == 0 || k == 0) return SLT_OK;
     int rc = get_encode();
@@ -728,11 +776,13 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
         SLT_CUDA_TRY(cudaMalloc(&g_tc_status, sizeof(int)));
         SLT_CUDA_TRY(cudaMemset(g_tc_status, 0, sizeof(int)));
     }
-    const bool tf32 = tier == SLT_PREC_TF32;
+    const bool x3 = tier == SLT_PREC_TF32X3;
+    const bool tf32 = tier == SLT_PREC_TF32 || x3;
     const bool fp8 = tier == SLT_PREC_FP8;
     const int esize = tf32 ? 4 : fp8 ? 1 : 2;
     const int64_t kq = 128 / esize;                  // elements per 128-byte K tile
-    const int64_t kpad = ceildiv(k, kq) * kq;
+    const int64_t kseg = ceildiv(k, kq) * kq;        // one operand segment
+    const int64_t kpad = x3 ? 3 * kseg : kseg;
     const int64_t mp = ceildiv(m, kTcBM) * kTcBM, np = ceildiv(n, kTcBN) * kTcBN;
     const int64_t mtl = mp / kTcBM, ntl = np / kTcBN;
     const size_t scale_bytes = fp8 ? sizeof(float) * 2 * size_t(mtl + ntl) + 256 : 0;
@@ -749,7 +799,19 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
     float* sB = iA + mtl;
     float* iB = sB + ntl;
     // pack operands
-    if (fp8) {
+    if (x3) {
+        dim3 ga(unsigned(ceildiv(kseg, 32)), unsigned(ceildiv(mp, 32)));
+        dim3 gb(unsigned(ceildiv(kseg, 32)), unsigned(ceildiv(np, 32)));
+        pack3_kernel<true, 0><<<ga, 256, 0, stream>>>(m, k, A, lda, reinterpret_cast<float*>(pa), mp, kseg);
+        count_launch();
+        if (transb == 'N')
+            pack3_kernel<false, 1><<<gb, 256, 0, stream>>>(n, k, B, ldb, reinterpret_cast<float*>(pb), np, kseg);
+        else
+            pack3_kernel<true, 1><<<gb, 256, 0, stream>>>(n, k, B, ldb, reinterpret_cast<float*>(pb), np, kseg);
+        count_launch();
+        rc = slt_from_cuda(cudaGetLastError());
+    }
+    else if (fp8) {
         fp8_scale_kernel<true><<<unsigned(mtl), 256, 0, stream>>>(m, k, A, lda, sA, iA);
         count_launch();
         if (transb == 'N') fp8_scale_kernel<false><<<unsigned(ntl), 256, 0, stream>>>(n, k, B, ldb, sB, iB);
@@ -850,7 +912,7 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
             count_launch();
             rc = slt_from_cuda(cudaGetLastError());
             double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);
-            prof_end(pidx, stream, 2.0 * mn * double(k), 8.0 * mn + double(esize) * double(k) * double(m + n));
+            prof_end(pidx, stream, 2.0 * mn * double(k), 8.0 * mn + double(esize) * double(kpad) * double(m + n));
         }
     }
     if (owned) cudaFreeAsync(owned, stream);

@@ -240,3 +240,17 @@ def test_fp8_tier_lu(orc, slt):
     info, it, X, _ = _run(slt, "gesv_mixed", A, B, slt.Options(nb=256, factor_precision="fp8", lo_retry=0))
     assert info == 0 and it >= 0
     assert berr(orc, A, X, B) <= 3 * n * EPS
+
+
+@pytest.mark.parametrize("fn", ["gesv_mixed", "posv_mixed"])
+def test_tf32x3_tier_matches_fp32(orc, slt, fn):
+    """The split-precision 3xTF32 tier refines like the FP32 tier (iteration
+    count within one) to the same FP64 bar."""
+    n = 1500
+    chol = fn.startswith("posv")
+    A = spd(orc, n, 41) if chol else orc.generate(2, 42, n, n)
+    B = orc.generate(2, 43, n, 2)
+    info, it, X, _ = _run(slt, fn, A, B, slt.Options(nb=256, factor_precision="tf32x3"))
+    info32, it32, _, _ = _run(slt, fn, A, B, slt.Options(nb=256, factor_precision="fp32"))
+    assert info == 0 and it >= 0 and abs(it - it32) <= 1, (it, it32)
+    assert berr(orc, A, X, B, sym=chol) <= 3 * n * EPS

@@ -12,7 +12,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TIERS = {"tf32": 2, "bf16": 3, "fp16": 4, "fp8": 5}
+TIERS = {"tf32": 2, "bf16": 3, "fp16": 4, "fp8": 5, "tf32x3": 6}
 
 
 def _round(torch, x, tier):
@@ -136,3 +136,28 @@ def test_tc_update_fp8_lower(slt):
     tol = 1e-5 * k * float(L8.abs().max()) ** 2
     assert float((C - ref)[low].abs().max()) <= tol
     assert torch.equal(C[~low], C0[~low])
+
+
+@pytest.mark.parametrize("m,n,k,transb", [(128, 128, 64, "N"), (300, 200, 100, "N"), (1024, 768, 512, "N"),
+                                          (640, 384, 256, "T"), (77, 500, 512, "T"), (20000, 328, 128, "T")])
+def test_tc_update_tf32x3(slt, m, n, k, transb):
+    """Split-precision 3xTF32: C -= A op(B) to near-FP32 accuracy on the
+    tensor cores; compared with an FP64 product, the error stays at the
+    scale of FP32 rounding (far below a single TF32 product's)."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(m + 5 * n + k)
+    A = slt.colmajor(torch.randn(m, k, device="cuda", generator=g))
+    B = slt.colmajor(torch.randn(k, n, device="cuda", generator=g) if transb == "N"
+                     else torch.randn(n, k, device="cuda", generator=g))
+    C0 = torch.randn(m, n, device="cuda", generator=g)
+    C = slt.colmajor(C0.clone())
+    opB = B if transb == "N" else B.t()
+    ref = C0.double() - A.double() @ opB.double()
+    _call(slt, "tf32x3", transb, A, B, C, 0)
+    scale = float((A.abs().double() @ opB.abs().double()).max()) + float(C0.abs().max())
+    err = float((C.double() - ref).abs().max())
+    assert err <= 2e-6 * scale, (err, scale)
+    # a single TF32 product is ~100x further off
+    Ct = slt.colmajor(C0.clone())
+    _call(slt, "tf32", transb, A, B, Ct, 0)
+    assert float((Ct.double() - ref).abs().max()) > 10 * err
