@@ -25,7 +25,15 @@ constexpr int kMaxRhs = 16;
 
 // y_seg(i, r) = sum_{j in segment} op(A)(i, j) X(j, r)   (MODE 0)
 // y_seg(i, 0) = sum_{j in segment} |op(A)(i, j)|         (MODE 1)
-// Tiles of 64 x 64; SYM: A symmetric with lower storage.
+// Tiles of 64 x 64; SYM: A symmetric with lower storage.  The next tile (and
+// its slice of X) is fetched into registers while the current one is used,
+// so a block keeps a whole tile of loads in flight instead of waiting out one
+// load latency per element; the shared tile is reused for the final
+// reduction.  Every sum is formed in the same order as a plain loop over the
+// tiles (thread group g adds columns g, g + 4, ... of each tile in turn).
+constexpr int kRowopPer = 64 * 64 / 256;     // tile elements per thread
+constexpr int kRowopTile = 64 * 65;          // padded tile, doubles
+
 template <int MODE, bool SYM, int NR>
 __global__ void __launch_bounds__(256)
 rowop_kernel(int64_t m, int64_t k, int nrhs, const double* __restrict__ A, int64_t lda,
@@ -33,10 +41,10 @@ rowop_kernel(int64_t m, int64_t k, int nrhs, const double* __restrict__ A, int64
              double* __restrict__ part)
 {
     extern __shared__ double rowop_smem[];
-    double (*As)[65] = reinterpret_cast<double (*)[65]>(rowop_smem);                        // [64][65]
-    double (*xs)[kMaxRhs] = reinterpret_cast<double (*)[kMaxRhs]>(rowop_smem + 64 * 65);    // [64][16]
-    double (*red)[64][kMaxRhs + 1] =
-        reinterpret_cast<double (*)[64][kMaxRhs + 1]>(rowop_smem + 64 * 65 + 64 * kMaxRhs);  // [4][64][17]
+    double (*As)[65] = reinterpret_cast<double (*)[65]>(rowop_smem);                         // [64][65]
+    double (*xs)[NR] = reinterpret_cast<double (*)[NR]>(rowop_smem + kRowopTile);            // [64][NR]
+    double (*red)[64][NR + 1] = reinterpret_cast<double (*)[64][NR + 1]>(rowop_smem);        // [4][64][NR+1], after the loop
+    constexpr int XPER = (64 * NR + 255) / 256;
     const int t = threadIdx.x;
     const int r = t % 64, g = t / 64;
     const int64_t I = blockIdx.x;
@@ -48,42 +56,59 @@ rowop_kernel(int64_t m, int64_t k, int nrhs, const double* __restrict__ A, int64
     // NR: compile-time right-hand-side count (1, 2, 4, 8 or 16); MODE 1 uses 1.
     const int nr = (MODE == 0) ? nrhs : 1;
 
+    double pre[kRowopPer];
+    double xpre[XPER];
+    // element u of this thread: tile row i = t % 64, tile column c = t / 64 + 4 u;
+    // a tile above the diagonal is the transpose of the stored tile (J, I), read
+    // along its columns (i is then the stored row within tile J).
+    auto fetch = [&](int64_t J) {
+        const int64_t col0 = J * 64;
+        const bool transposed = SYM && (J > I);
+        #pragma unroll
+        for (int u = 0; u < kRowopPer; ++u) {
+            const int i = t % 64, c = t / 64 + 4 * u;
+            const int64_t gi = transposed ? col0 + i : row0 + i;     // stored row
+            const int64_t gc = transposed ? row0 + c : col0 + c;     // stored column
+            const bool in = transposed ? (gi < k && gc < m) : (gi < m && gc < k);
+            const bool mirror = SYM && J == I && gi < gc;            // upper half of a diagonal tile
+            pre[u] = in ? (mirror ? A[gc + gi * lda] : A[gi + gc * lda]) : 0.0;
+        }
+        if (MODE == 0) {
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u, c = e % 64, q = e / 64;
+                const int64_t gc = col0 + c;
+                xpre[u] = (q < nr && gc < k) ? X[gc + q * ldx] : 0.0;
+            }
+        }
+    };
+    auto put = [&](int64_t J) {
+        const bool transposed = SYM && (J > I);
+        #pragma unroll
+        for (int u = 0; u < kRowopPer; ++u) {
+            const int i = t % 64, c = t / 64 + 4 * u;
+            if (transposed) As[i][c] = pre[u];
+            else As[c][i] = pre[u];
+        }
+        if (MODE == 0) {
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u, c = e % 64, q = e / 64;
+                if (q < NR) xs[c][q] = xpre[u];
+            }
+        }
+    };
+
     double acc[NR];
     #pragma unroll
     for (int q = 0; q < NR; ++q) acc[q] = 0.0;
 
+    if (J0 < J1) fetch(J0);
     for (int64_t J = J0; J < J1; ++J) {
-        const int64_t col0 = J * 64;
-        const bool transposed = SYM && (J > I);
         __syncthreads();
-        // stage the tile: As[c][i] = op(A)(row0 + i, col0 + c)
-        for (int e = t; e < 64 * 64; e += 256) {
-            int i = e % 64, c = e / 64;
-            double v = 0.0;
-            if (!transposed) {
-                int64_t gi = row0 + i, gc = col0 + c;
-                if (gi < m && gc < k) {
-                    v = A[gi + gc * lda];
-                    if (SYM && gi < gc) v = 0.0;   // never happens off the diagonal tile
-                    if (SYM && J == I && gi < gc) v = A[gc + gi * lda];
-                }
-                As[c][i] = v;
-            }
-            else {
-                // stored tile (J, I): rows col0.., cols row0..; As[c][i] = A(col0+c, row0+i)
-                int64_t gr = col0 + i, gc = row0 + c;   // coalesced read along gr
-                if (gr < k && gc < m) v = A[gr + gc * lda];
-                As[i][c] = v;
-            }
-        }
-        if (MODE == 0) {
-            for (int e = t; e < 64 * nrhs; e += 256) {
-                int c = e % 64, q = e / 64;
-                int64_t gc = col0 + c;
-                xs[c][q] = (gc < k) ? X[gc + q * ldx] : 0.0;
-            }
-        }
+        put(J);
         __syncthreads();
+        if (J + 1 < J1) fetch(J + 1);
         // group g takes tile columns c = g, g+4, ...
         if (MODE == 0) {
             #pragma unroll 4
@@ -97,6 +122,7 @@ rowop_kernel(int64_t m, int64_t k, int nrhs, const double* __restrict__ A, int64
             for (int c = g; c < 64; c += 4) acc[0] += fabs(As[c][r]);
         }
     }
+    __syncthreads();
     #pragma unroll
     for (int q = 0; q < NR; ++q)
         if (q < nr) red[g][r][q] = acc[q];
@@ -142,19 +168,24 @@ __global__ void max_reduce_kernel(int64_t m, int64_t nseg, const double* __restr
     if (threadIdx.x == 0) *out = red[0];
 }
 
-constexpr size_t kRowopSmem = sizeof(double) * (64 * 65 + 64 * kMaxRhs + 4 * 64 * (kMaxRhs + 1));
+// padded tile + X slice; the reduction area [4][64][NR+1] reuses the same space
+constexpr size_t rowop_smem_bytes(int nr)
+{
+    return sizeof(double) * size_t(std::max(kRowopTile + 64 * nr, 4 * 64 * (nr + 1)));
+}
 
 template <int MODE, bool SYM, int NR>
 static int launch_rowop_nr(dim3 grid, cudaStream_t stream, int64_t m, int64_t k, int nrhs, const double* A,
                            int64_t lda, const double* X, int64_t ldx, int64_t tps, double* part)
 {
+    constexpr size_t smem = rowop_smem_bytes(NR);
     static bool configured = false;
     if (!configured) {
         SLT_CUDA_TRY(cudaFuncSetAttribute(rowop_kernel<MODE, SYM, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          int(kRowopSmem)));
+                                          int(smem)));
         configured = true;
     }
-    rowop_kernel<MODE, SYM, NR><<<grid, 256, kRowopSmem, stream>>>(m, k, nrhs, A, lda, X, ldx, tps, part);
+    rowop_kernel<MODE, SYM, NR><<<grid, 256, smem, stream>>>(m, k, nrhs, A, lda, X, ldx, tps, part);
     return SLT_OK;
 }
 

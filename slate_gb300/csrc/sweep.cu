@@ -8,13 +8,21 @@
 //   op(M) = M or M^T, X overwritten in place, nrhs <= 16.
 //
 // Row blocks of 64 are taken in solve order through an atomic ticket.  The
-// block with ticket p accumulates op(M)(i, j) x_j over the blocks already
-// solved (tickets < p), waiting on each block's ready flag with a bounded
-// acquire spin, then solves its 64 x 64 diagonal block in shared memory and
-// publishes x_i with a release flag.  Tickets are taken by running blocks
-// in order, so a block only ever waits for blocks that are already running.
-// The matrix is read once (HBM-bound); the critical path is one diagonal
-// solve per block.
+// block with ticket p accumulates op(M)(i, j) x_j over the blocks solved
+// two or more steps before it (tickets < p - 1), waiting on each block's
+// ready flag with a bounded acquire spin and fetching the next tile and its
+// x_j into registers while it multiplies the current one.  It then forms
+// y_i = inv(op(M)_ii) (b_i - acc) before its predecessor has finished, and
+// the only work left on the chain of dependent blocks is
+//     x_i = y_i - W_i x_{i-1},   W_i = inv(op(M)_ii) op(M)(i, i-1)
+// (i - 1: the predecessor in solve order), with W_i formed beside the
+// diagonal-block inverses before the sweep.  x_i is published with a
+// release flag.  Tickets are taken by running blocks in order, so a block
+// only ever waits for blocks that are already running.  The matrix is read
+// once (HBM-bound); the critical path is one 64 x 64 matrix-vector product
+// per block.  For up to 4 right-hand sides the four thread groups of a block
+// split the 64 columns of every product and add their partial sums in
+// shared memory; for more, each group owns 4 right-hand sides.
 
 #include "common.cuh"
 #include "prof.h"
@@ -26,11 +34,25 @@ constexpr int kSwRhs = 16;
 
 template <typename T>
 struct SweepSmem {
-    T Ts[kSwBS][kSwBS + 1];    // off-diagonal tile, [col][row]
-    T Ds[kSwBS][kSwBS + 1];    // diagonal tile, [row][col]
+    T Ts[kSwBS][kSwBS + 1];    // off-diagonal tile, [col][row]; then W_i, [row][col]
+    T Ds[kSwBS][kSwBS + 1];    // inverse of the diagonal block, [row][col]
     T xs[kSwBS][kSwRhs];       // solved block x_j
-    T xi[kSwBS][kSwRhs];       // this block's right-hand side / solution
+    T xi[kSwBS][kSwRhs];       // this block's right-hand side
+    T red[4][kSwBS][4];        // partial sums of the four column groups
 };
+
+// a[0..3] += v * s[0..3], s 16-byte aligned in shared memory
+__device__ __forceinline__ void axpy4(float v, const float* s, float* a)
+{
+    const float4 x = *reinterpret_cast<const float4*>(s);
+    a[0] = fmaf(v, x.x, a[0]); a[1] = fmaf(v, x.y, a[1]); a[2] = fmaf(v, x.z, a[2]); a[3] = fmaf(v, x.w, a[3]);
+}
+__device__ __forceinline__ void axpy4(double v, const double* s, double* a)
+{
+    const double2 x = *reinterpret_cast<const double2*>(s);
+    const double2 y = *reinterpret_cast<const double2*>(s + 2);
+    a[0] = fma(v, x.x, a[0]); a[1] = fma(v, x.y, a[1]); a[2] = fma(v, y.x, a[2]); a[3] = fma(v, y.y, a[3]);
+}
 
 __device__ __forceinline__ int ld_acquire_i32(const int* p)
 {
@@ -98,6 +120,32 @@ trinv_kernel(int64_t n, const T* __restrict__ M, int64_t ldm, T* __restrict__ Di
     __syncthreads();
     T* out = Dinv + size_t(blockIdx.x) * kSwBS * kSwBS;
     for (int e = t; e < kSwBS * kSwBS; e += 256) out[e] = Xv[e / kSwBS][e % kSwBS];
+
+    // W = inv(op(M)_ii) op(M)(i, j), j the block solved just before i
+    const int64_t bj = FORWARD ? int64_t(blockIdx.x) - 1 : int64_t(blockIdx.x) + 1;
+    if (bj < 0 || bj >= int64_t(gridDim.x)) return;
+    const int64_t j0 = bj * kSwBS;
+    const int nj = int(min64(kSwBS, n - j0));
+    staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) {
+        const int l = TRANS ? e / kSwBS : e % kSwBS, cc = TRANS ? e % kSwBS : e / kSwBS;
+        return (l < ni && cc < nj) ? (TRANS ? M[(j0 + cc) + (i0 + l) * ldm] : M[(i0 + l) + (j0 + cc) * ldm]) : T(0);
+    }, [&](int e, T v) {
+        const int l = TRANS ? e / kSwBS : e % kSwBS, cc = TRANS ? e % kSwBS : e / kSwBS;
+        Ds[l][cc] = v;
+    });
+    __syncthreads();
+    const int wc = t % kSwBS, wr = t / kSwBS;    // column wc, rows wr, wr + 4, ...
+    T w[kSwBS / 4];
+    #pragma unroll
+    for (int j = 0; j < kSwBS / 4; ++j) w[j] = T(0);
+    for (int l = 0; l < kSwBS; ++l) {
+        const T tl = Ds[l][wc];
+        #pragma unroll
+        for (int j = 0; j < kSwBS / 4; ++j) w[j] = fma(Xv[wr + 4 * j][l], tl, w[j]);
+    }
+    T* wout = Dinv + size_t(gridDim.x + blockIdx.x) * kSwBS * kSwBS;
+    #pragma unroll
+    for (int j = 0; j < kSwBS / 4; ++j) wout[(wr + 4 * j) * kSwBS + wc] = w[j];
 }
 
 template <typename T, bool FORWARD, bool UNIT, bool TRANS>
@@ -105,18 +153,38 @@ __global__ void __launch_bounds__(256)
 sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T* __restrict__ Dinv,
              T* X, int64_t ldx, int* ticket, int* ready, int* status)
 {
-    extern __shared__ unsigned char sw_smem_raw[];
+    extern __shared__ __align__(16) unsigned char sw_smem_raw[];
     SweepSmem<T>& sm = *reinterpret_cast<SweepSmem<T>*>(sw_smem_raw);
     __shared__ int s_p, s_ok;
+    constexpr int PER = kSwBS * kSwBS / 256;       // tile elements per thread
+    constexpr int XPER = kSwBS * kSwRhs / 256;     // x_j elements per thread
     const int t = threadIdx.x;
     const int nblk = int(ceildiv(n, kSwBS));
+    const int r = t % kSwBS, g = t / kSwBS;
+    const bool split = nrhs <= 4;
+    const int c0 = split ? 16 * g : 0, c1 = split ? c0 + 16 : kSwBS;   // columns of this thread's products
+    const int qb = split ? 0 : 4 * g;                                  // its first right-hand side
+    const T* Wall = Dinv + size_t(nblk) * kSwBS * kSwBS;
 
-    auto opM = [&](int64_t r, int64_t c) -> T {
-        return TRANS ? __ldg(&M[c + r * ldm]) : __ldg(&M[r + c * ldm]);
+    auto opM = [&](int64_t rr, int64_t c) -> T {
+        return TRANS ? __ldg(&M[c + rr * ldm]) : __ldg(&M[rr + c * ldm]);
+    };
+    // bounded acquire spin of thread 0 on ready[k]; 0 on timeout or error
+    auto wait_ready = [&](int k) -> int {
+        if (ld_acquire_i32(&ready[k]) != 0) return 1;
+        const uint64_t t0 = sw_globaltimer();
+        for (unsigned it = 1; ld_acquire_i32(&ready[k]) == 0; ++it) {
+            if ((it & 255u) == 0 &&
+                (ld_volatile_i32(status) != 0 || sw_globaltimer() - t0 > 2000000000ull)) {
+                atomicCAS(status, 0, SLT_ERR_TIMEOUT);
+                return 0;
+            }
+        }
+        return 1;
     };
 
     for (;;) {
-        if (t == 0) s_p = atomicAdd(ticket, 1);
+        if (t == 0) { s_p = atomicAdd(ticket, 1); s_ok = 1; }
         __syncthreads();
         const int p = s_p;
         if (p >= nblk) break;
@@ -131,76 +199,133 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
                                                   [&](int e, T v) { sm.Ds[e / kSwBS][e % kSwBS] = v; });
         }
         staged_copy<kSwBS * kSwRhs / 256, 256>(kSwBS * kSwRhs, [&](int e) {
-            const int r = e % kSwBS, q = e / kSwBS;
-            return (r < ni && q < nrhs) ? X[i0 + r + q * ldx] : T(0);
+            const int rr = e % kSwBS, q = e / kSwBS;
+            return (rr < ni && q < nrhs) ? X[i0 + rr + q * ldx] : T(0);
         }, [&](int e, T v) { sm.xi[e % kSwBS][e / kSwBS] = v; });
 
-        // accumulate op(M)(i, j) x_j over the solved blocks
-        const int r = t % kSwBS, g = t / kSwBS;           // 4 groups x 4 right-hand sides
-        T acc[4] = {T(0), T(0), T(0), T(0)};
-        for (int pq = 0; pq < p; ++pq) {
-            const int bj = FORWARD ? pq : nblk - 1 - pq;
+        // acc = sum over the blocks solved two or more steps earlier
+        T pre[PER], xpre[XPER];
+        auto fetch = [&](int k) {
+            const int bj = FORWARD ? k : nblk - 1 - k;
             const int64_t j0 = int64_t(bj) * kSwBS;
             const int nj = int(min64(kSwBS, n - j0));
-            __syncthreads();
-            staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) {
+            #pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int e = t + 256 * u;
                 const int rr = TRANS ? e / kSwBS : e % kSwBS, c = TRANS ? e % kSwBS : e / kSwBS;
-                return (rr < ni && c < nj) ? opM(i0 + rr, j0 + c) : T(0);
-            }, [&](int e, T v) {
-                const int rr = TRANS ? e / kSwBS : e % kSwBS, c = TRANS ? e % kSwBS : e / kSwBS;
-                sm.Ts[c][rr] = v;
-            });
-            if (t == 0) {
-                int ok = 1;
-                if (ld_acquire_i32(&ready[pq]) == 0) {
-                    const uint64_t t0 = sw_globaltimer();
-                    for (unsigned it = 1; ld_acquire_i32(&ready[pq]) == 0; ++it) {
-                        if ((it & 255u) == 0 &&
-                            (ld_volatile_i32(status) != 0 || sw_globaltimer() - t0 > 2000000000ull)) {
-                            atomicCAS(status, 0, SLT_ERR_TIMEOUT);
-                            ok = 0;
-                            break;
-                        }
-                    }
-                }
-                s_ok = ok;
+                pre[u] = (rr < ni && c < nj) ? opM(i0 + rr, j0 + c) : T(0);
             }
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u, rr = e % kSwBS, q = e / kSwBS;
+                xpre[u] = (rr < nj && q < nrhs) ? __ldcg(&X[j0 + rr + q * ldx]) : T(0);
+            }
+        };
+        auto put = [&]() {
+            #pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int e = t + 256 * u;
+                const int rr = TRANS ? e / kSwBS : e % kSwBS, c = TRANS ? e % kSwBS : e / kSwBS;
+                sm.Ts[c][rr] = pre[u];
+            }
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u;
+                sm.xs[e % kSwBS][e / kSwBS] = xpre[u];
+            }
+        };
+        T acc[4] = {T(0), T(0), T(0), T(0)};
+        const int K = p > 0 ? p - 1 : 0;
+        if (K > 0) {
+            if (t == 0) s_ok = wait_ready(0);
             __syncthreads();
             if (!s_ok) return;
-            staged_copy<kSwBS * kSwRhs / 256, 256>(kSwBS * kSwRhs, [&](int e) {
+            fetch(0);
+            put();
+            if (t == 0 && K > 1) s_ok = wait_ready(1);
+        }
+        __syncthreads();
+        for (int k = 0; k < K; ++k) {
+            const bool more = k + 1 < K;
+            if (more) {
+                if (!s_ok) return;
+                fetch(k + 1);
+            }
+            #pragma unroll 4
+            for (int c = c0; c < c1; ++c) axpy4(sm.Ts[c][r], &sm.xs[c][qb], acc);
+            __syncthreads();
+            if (more) {
+                put();
+                if (t == 0 && k + 2 < K) s_ok = wait_ready(k + 2);
+            }
+            __syncthreads();
+        }
+
+        // z = b_i - acc (in xi); W_i into Ts for the chain step
+        if (p > 0) {
+            const T* wsrc = Wall + size_t(bi) * kSwBS * kSwBS;
+            staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) { return wsrc[e]; },
+                                                  [&](int e, T v) { sm.Ts[e / kSwBS][e % kSwBS] = v; });
+        }
+        if (split) {
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) sm.red[g][r][u] = acc[u];
+            __syncthreads();
+            sm.xi[r][g] -= (sm.red[0][r][g] + sm.red[1][r][g]) + (sm.red[2][r][g] + sm.red[3][r][g]);
+        }
+        else {
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) sm.xi[r][qb + u] -= acc[u];
+        }
+        __syncthreads();
+
+        // y_i = inv(op(M)_ii) z
+        T y[4] = {T(0), T(0), T(0), T(0)};
+        #pragma unroll 4
+        for (int c = c0; c < c1; ++c) axpy4(sm.Ds[r][c], &sm.xi[c][qb], y);
+        if (split) {
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) sm.red[g][r][u] = y[u];
+            __syncthreads();
+            y[0] = (sm.red[0][r][g] + sm.red[1][r][g]) + (sm.red[2][r][g] + sm.red[3][r][g]);
+        }
+
+        // chain step: x_i = y_i - W_i x_{i-1}
+        if (p > 0) {
+            if (t == 0) s_ok = wait_ready(p - 1);
+            __syncthreads();
+            if (!s_ok) return;
+            const int bj = FORWARD ? bi - 1 : bi + 1;
+            const int64_t j0 = int64_t(bj) * kSwBS;
+            const int nj = int(min64(kSwBS, n - j0));
+            staged_copy<XPER, 256>(kSwBS * kSwRhs, [&](int e) {
                 const int rr = e % kSwBS, q = e / kSwBS;
                 return (rr < nj && q < nrhs) ? __ldcg(&X[j0 + rr + q * ldx]) : T(0);
             }, [&](int e, T v) { sm.xs[e % kSwBS][e / kSwBS] = v; });
             __syncthreads();
+            T v[4] = {T(0), T(0), T(0), T(0)};
             #pragma unroll 4
-            for (int c = 0; c < kSwBS; ++c) {
-                const T a = sm.Ts[c][r];
+            for (int c = c0; c < c1; ++c) axpy4(sm.Ts[r][c], &sm.xs[c][qb], v);
+            if (split) {
                 #pragma unroll
-                for (int u = 0; u < 4; ++u) acc[u] = fma(a, sm.xs[c][g * 4 + u], acc[u]);
+                for (int u = 0; u < 4; ++u) sm.red[g][r][u] = v[u];
+                __syncthreads();
+                y[0] -= (sm.red[0][r][g] + sm.red[1][r][g]) + (sm.red[2][r][g] + sm.red[3][r][g]);
+            }
+            else {
+                #pragma unroll
+                for (int u = 0; u < 4; ++u) y[u] -= v[u];
             }
         }
-        __syncthreads();
-        #pragma unroll
-        for (int u = 0; u < 4; ++u) sm.xi[r][g * 4 + u] -= acc[u];
-        __syncthreads();
-
-        // x_i = inv(op(M)_ii) (b_i - acc): a 64 x 64 matrix-vector product
-        {
-            T y[4] = {T(0), T(0), T(0), T(0)};
-            #pragma unroll 8
-            for (int c = 0; c < kSwBS; ++c) {
-                const T d = sm.Ds[r][c];
-                #pragma unroll
-                for (int u = 0; u < 4; ++u) y[u] = fma(d, sm.xi[c][g * 4 + u], y[u]);
+        if (r < ni) {
+            if (split) {
+                if (g < nrhs) X[i0 + r + g * ldx] = y[0];
             }
-            __syncthreads();
-            #pragma unroll
-            for (int u = 0; u < 4; ++u) sm.xi[r][g * 4 + u] = y[u];
-        }
-        __syncthreads();
-        for (int e = t; e < kSwBS * kSwRhs; e += 256) {
-            int rr = e % kSwBS, q = e / kSwBS;
-            if (rr < ni && q < nrhs) X[i0 + rr + q * ldx] = sm.xi[rr][q];
+            else {
+                #pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (qb + u < nrhs) X[i0 + r + (qb + u) * ldx] = y[u];
+            }
         }
         __threadfence();
         __syncthreads();
@@ -215,7 +340,7 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     if (n <= 0 || nrhs <= 0) return SLT_OK;
     if (nrhs > kSwRhs) return SLT_ERR_ARG;
     const int64_t nblk = ceildiv(n, kSwBS);
-    // flags layout: [ticket][ready x nblk][pad to 256 B][Dinv: nblk x 64 x 64]
+    // flags layout: [ticket][ready x nblk][pad to 256 B][Dinv: nblk x 64 x 64][W: nblk x 64 x 64]
     T* Dinv = reinterpret_cast<T*>(reinterpret_cast<char*>(flags) + ((sizeof(int) * size_t(nblk + 1) + 255) & ~size_t(255)));
     const size_t ti_smem = size_t(2) * kSwBS * (kSwBS + 1) * sizeof(T);
     static bool ti_cfg = false;
@@ -284,9 +409,9 @@ extern "C" int slt_ssweep(int kind, int64_t n, int64_t nrhs, const float* M, int
 }
 
 // Scratch of one sweep: ticket + ready flags, then the diagonal-block
-// inverses (sized for double).
+// inverses and the chain-step blocks W (sized for double).
 extern "C" size_t slt_sweep_flags_bytes(int64_t n)
 {
     const int64_t nblk = ceildiv(n, kSwBS);
-    return ((sizeof(int) * size_t(nblk + 1) + 255) & ~size_t(255)) + size_t(nblk) * kSwBS * kSwBS * sizeof(double);
+    return ((sizeof(int) * size_t(nblk + 1) + 255) & ~size_t(255)) + 2 * size_t(nblk) * kSwBS * kSwBS * sizeof(double);
 }
