@@ -7,22 +7,27 @@
 //   op(M) X = B,  op(M) lower (forward) or upper (backward), unit or not,
 //   op(M) = M or M^T, X overwritten in place, nrhs <= 16.
 //
-// Row blocks of 64 are taken in solve order through an atomic ticket.  The
-// block with ticket p accumulates op(M)(i, j) x_j over the blocks solved
-// two or more steps before it (tickets < p - 1), waiting on each block's
-// ready flag with a bounded acquire spin and fetching the next tile and its
-// x_j into registers while it multiplies the current one.  It then forms
+// Row blocks of 64 are taken in solve order through an atomic ticket, so a
+// block only ever waits for blocks that are already running.  The block
+// with ticket p accumulates op(M)(i, j) x_j over the blocks solved two or
+// more steps before it (tickets < p - 1), fetching the next tile into
+// registers while it multiplies the current one, forms
 // y_i = inv(op(M)_ii) (b_i - acc) before its predecessor has finished, and
-// the only work left on the chain of dependent blocks is
+// leaves only
 //     x_i = y_i - W_i x_{i-1},   W_i = inv(op(M)_ii) op(M)(i, i-1)
-// (i - 1: the predecessor in solve order), with W_i formed beside the
-// diagonal-block inverses before the sweep.  x_i is published with a
-// release flag.  Tickets are taken by running blocks in order, so a block
-// only ever waits for blocks that are already running.  The matrix is read
-// once (HBM-bound); the critical path is one 64 x 64 matrix-vector product
-// per block.  For up to 4 right-hand sides the four thread groups of a block
-// split the 64 columns of every product and add their partial sums in
-// shared memory; for more, each group owns 4 right-hand sides.
+// on the chain of dependent blocks (i - 1: the predecessor in solve order;
+// W_i is formed beside the diagonal-block inverses before the sweep).
+//
+// Solved values travel between blocks through a mailbox of 64-bit words,
+// 32 data bits and a 32-bit flag each (two words per double): one aligned
+// 64-bit store is single-copy atomic, so a reader that sees the flag sees
+// the data, and neither a fence nor a separate ready flag sits on the
+// chain.  Readers poll with a bounded spin.  The mailbox is cleared before
+// every launch.  The matrix is read once (HBM-bound); the critical path is
+// one 64 x 64 matrix-vector product and one L2 round trip per block.  For
+// up to 4 right-hand sides the four thread groups of a block split the 64
+// columns of every product and add their partial sums in shared memory;
+// for more, each group owns 4 right-hand sides.
 
 #include "common.cuh"
 #include "prof.h"
@@ -34,11 +39,54 @@ constexpr int kSwRhs = 16;
 
 template <typename T>
 struct SweepSmem {
-    T Ts[kSwBS][kSwBS + 1];    // off-diagonal tile, [col][row]; then W_i, [row][col]
+    T Ts[kSwBS][kSwBS + 1];    // off-diagonal tile, [col][row]
     T Ds[kSwBS][kSwBS + 1];    // inverse of the diagonal block, [row][col]
+    T Ws[kSwBS][kSwBS + 1];    // W_i, [row][col]
     T xs[kSwBS][kSwRhs];       // solved block x_j
     T xi[kSwBS][kSwRhs];       // this block's right-hand side
     T red[4][kSwBS][4];        // partial sums of the four column groups
+};
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Mailbox words: low half data, high half kMbFlag (the mailbox is zeroed
+// before each launch, so a word carrying the flag was written by this launch).
+constexpr unsigned long long kMbFlag = 0x5157ull << 32;
+
+template <typename T> struct Mailbox;
+template <> struct Mailbox<float> {
+    static constexpr int kWords = 1;
+    static __device__ __forceinline__ void put(unsigned long long* p, float v) {
+        st_relaxed_u64(p, kMbFlag | __float_as_uint(v));
+    }
+    static __device__ __forceinline__ bool get(const unsigned long long* p, float& v) {
+        const unsigned long long w = ld_relaxed_u64(p);
+        v = __uint_as_float(unsigned(w));
+        return (w & 0xffffffff00000000ull) == kMbFlag;
+    }
+};
+template <> struct Mailbox<double> {
+    static constexpr int kWords = 2;
+    static __device__ __forceinline__ void put(unsigned long long* p, double v) {
+        const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+        st_relaxed_u64(p, kMbFlag | (b & 0xffffffffull));
+        st_relaxed_u64(p + 1, kMbFlag | (b >> 32));
+    }
+    static __device__ __forceinline__ bool get(const unsigned long long* p, double& v) {
+        const unsigned long long w0 = ld_relaxed_u64(p), w1 = ld_relaxed_u64(p + 1);
+        v = __longlong_as_double(static_cast<long long>((w1 << 32) | (w0 & 0xffffffffull)));
+        return (w0 & 0xffffffff00000000ull) == kMbFlag && (w1 & 0xffffffff00000000ull) == kMbFlag;
+    }
 };
 
 // a[0..3] += v * s[0..3], s 16-byte aligned in shared memory
@@ -52,18 +100,6 @@ __device__ __forceinline__ void axpy4(double v, const double* s, double* a)
     const double2 x = *reinterpret_cast<const double2*>(s);
     const double2 y = *reinterpret_cast<const double2*>(s + 2);
     a[0] = fma(v, x.x, a[0]); a[1] = fma(v, x.y, a[1]); a[2] = fma(v, y.x, a[2]); a[3] = fma(v, y.y, a[3]);
-}
-
-__device__ __forceinline__ int ld_acquire_i32(const int* p)
-{
-    int v;
-    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release_i32(int* p, int v)
-{
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 
 __device__ __forceinline__ uint64_t sw_globaltimer()
@@ -148,18 +184,22 @@ trinv_kernel(int64_t n, const T* __restrict__ M, int64_t ldm, T* __restrict__ Di
     for (int j = 0; j < kSwBS / 4; ++j) wout[(wr + 4 * j) * kSwBS + wc] = w[j];
 }
 
+// mb: mailbox, word ((q * npad + row) * kWords + h) for solved value
+// (row, q), npad = 64 * ceil(n / 64).
 template <typename T, bool FORWARD, bool UNIT, bool TRANS>
 __global__ void __launch_bounds__(256)
 sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T* __restrict__ Dinv,
-             T* X, int64_t ldx, int* ticket, int* ready, int* status)
+             T* X, int64_t ldx, int* ticket, unsigned long long* mb, int* status)
 {
+    using MB = Mailbox<T>;
     extern __shared__ __align__(16) unsigned char sw_smem_raw[];
     SweepSmem<T>& sm = *reinterpret_cast<SweepSmem<T>*>(sw_smem_raw);
-    __shared__ int s_p, s_ok;
+    __shared__ int s_p;
     constexpr int PER = kSwBS * kSwBS / 256;       // tile elements per thread
     constexpr int XPER = kSwBS * kSwRhs / 256;     // x_j elements per thread
     const int t = threadIdx.x;
     const int nblk = int(ceildiv(n, kSwBS));
+    const int64_t npad = int64_t(nblk) * kSwBS;
     const int r = t % kSwBS, g = t / kSwBS;
     const bool split = nrhs <= 4;
     const int c0 = split ? 16 * g : 0, c1 = split ? c0 + 16 : kSwBS;   // columns of this thread's products
@@ -169,22 +209,23 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
     auto opM = [&](int64_t rr, int64_t c) -> T {
         return TRANS ? __ldg(&M[c + rr * ldm]) : __ldg(&M[rr + c * ldm]);
     };
-    // bounded acquire spin of thread 0 on ready[k]; 0 on timeout or error
-    auto wait_ready = [&](int k) -> int {
-        if (ld_acquire_i32(&ready[k]) != 0) return 1;
+    auto mbox = [&](int64_t row, int q) { return mb + (q * npad + row) * MB::kWords; };
+    // bounded poll of one mailbox value; false on timeout or error
+    auto spin = [&](const unsigned long long* a, T& v) -> bool {
+        if (MB::get(a, v)) return true;
         const uint64_t t0 = sw_globaltimer();
-        for (unsigned it = 1; ld_acquire_i32(&ready[k]) == 0; ++it) {
+        for (unsigned it = 1; !MB::get(a, v); ++it) {
             if ((it & 255u) == 0 &&
                 (ld_volatile_i32(status) != 0 || sw_globaltimer() - t0 > 2000000000ull)) {
                 atomicCAS(status, 0, SLT_ERR_TIMEOUT);
-                return 0;
+                return false;
             }
         }
-        return 1;
+        return true;
     };
 
     for (;;) {
-        if (t == 0) { s_p = atomicAdd(ticket, 1); s_ok = 1; }
+        if (t == 0) s_p = atomicAdd(ticket, 1);
         __syncthreads();
         const int p = s_p;
         if (p >= nblk) break;
@@ -192,20 +233,25 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
         const int64_t i0 = int64_t(bi) * kSwBS;
         const int ni = int(min64(kSwBS, n - i0));
 
-        // inverse of the diagonal block (row-major), and this block's RHS
+        // inverse of the diagonal block and W_i (row-major), this block's RHS
         {
             const T* dinv = Dinv + size_t(bi) * kSwBS * kSwBS;
             staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) { return dinv[e]; },
                                                   [&](int e, T v) { sm.Ds[e / kSwBS][e % kSwBS] = v; });
+            if (p > 0) {
+                const T* wsrc = Wall + size_t(bi) * kSwBS * kSwBS;
+                staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) { return wsrc[e]; },
+                                                      [&](int e, T v) { sm.Ws[e / kSwBS][e % kSwBS] = v; });
+            }
         }
         staged_copy<kSwBS * kSwRhs / 256, 256>(kSwBS * kSwRhs, [&](int e) {
             const int rr = e % kSwBS, q = e / kSwBS;
             return (rr < ni && q < nrhs) ? X[i0 + rr + q * ldx] : T(0);
         }, [&](int e, T v) { sm.xi[e % kSwBS][e / kSwBS] = v; });
 
-        // acc = sum over the blocks solved two or more steps earlier
-        T pre[PER], xpre[XPER];
-        auto fetch = [&](int k) {
+        T pre[PER], xv[XPER];
+        bool xok[XPER];
+        auto fetch_tile = [&](int k) {
             const int bj = FORWARD ? k : nblk - 1 - k;
             const int64_t j0 = int64_t(bj) * kSwBS;
             const int nj = int(min64(kSwBS, n - j0));
@@ -215,58 +261,79 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
                 const int rr = TRANS ? e / kSwBS : e % kSwBS, c = TRANS ? e % kSwBS : e / kSwBS;
                 pre[u] = (rr < ni && c < nj) ? opM(i0 + rr, j0 + c) : T(0);
             }
+        };
+        // one poll of x_k (block solved k-th); what is not there yet is finished by finish_x
+        auto try_x = [&](int k) {
+            const int bj = FORWARD ? k : nblk - 1 - k;
+            const int64_t j0 = int64_t(bj) * kSwBS;
+            const int nj = int(min64(kSwBS, n - j0));
             #pragma unroll
             for (int u = 0; u < XPER; ++u) {
                 const int e = t + 256 * u, rr = e % kSwBS, q = e / kSwBS;
-                xpre[u] = (rr < nj && q < nrhs) ? __ldcg(&X[j0 + rr + q * ldx]) : T(0);
+                if (rr < nj && q < nrhs) xok[u] = MB::get(mbox(j0 + rr, q), xv[u]);
+                else { xv[u] = T(0); xok[u] = true; }
             }
         };
-        auto put = [&]() {
+        auto finish_x = [&](int k) -> bool {
+            const int64_t j0 = int64_t(FORWARD ? k : nblk - 1 - k) * kSwBS;
+            bool ok = true;
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u, rr = e % kSwBS, q = e / kSwBS;
+                if (!xok[u] && ok) ok = spin(mbox(j0 + rr, q), xv[u]);
+            }
+            return ok;
+        };
+        auto put_x = [&]() {
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u;
+                sm.xs[e % kSwBS][e / kSwBS] = xv[u];
+            }
+        };
+        auto put_tile = [&]() {
             #pragma unroll
             for (int u = 0; u < PER; ++u) {
                 const int e = t + 256 * u;
                 const int rr = TRANS ? e / kSwBS : e % kSwBS, c = TRANS ? e % kSwBS : e / kSwBS;
                 sm.Ts[c][rr] = pre[u];
             }
-            #pragma unroll
-            for (int u = 0; u < XPER; ++u) {
-                const int e = t + 256 * u;
-                sm.xs[e % kSwBS][e / kSwBS] = xpre[u];
-            }
         };
+
+        // acc = sum over the blocks solved two or more steps earlier
         T acc[4] = {T(0), T(0), T(0), T(0)};
         const int K = p > 0 ? p - 1 : 0;
         if (K > 0) {
-            if (t == 0) s_ok = wait_ready(0);
-            __syncthreads();
-            if (!s_ok) return;
-            fetch(0);
-            put();
-            if (t == 0 && K > 1) s_ok = wait_ready(1);
+            fetch_tile(0);
+            try_x(0);
+            const bool ok = finish_x(0);
+            put_tile();
+            put_x();
+            if (__syncthreads_or(!ok)) return;
         }
-        __syncthreads();
+        else {
+            __syncthreads();
+        }
         for (int k = 0; k < K; ++k) {
             const bool more = k + 1 < K;
             if (more) {
-                if (!s_ok) return;
-                fetch(k + 1);
+                fetch_tile(k + 1);
+                try_x(k + 1);
             }
             #pragma unroll 4
             for (int c = c0; c < c1; ++c) axpy4(sm.Ts[c][r], &sm.xs[c][qb], acc);
             __syncthreads();
+            bool ok = true;
             if (more) {
-                put();
-                if (t == 0 && k + 2 < K) s_ok = wait_ready(k + 2);
+                ok = finish_x(k + 1);
+                put_tile();
+                put_x();
             }
-            __syncthreads();
+            if (__syncthreads_or(!ok)) return;
         }
+        if (p > 0) try_x(p - 1);       // in flight while y_i is formed
 
-        // z = b_i - acc (in xi); W_i into Ts for the chain step
-        if (p > 0) {
-            const T* wsrc = Wall + size_t(bi) * kSwBS * kSwBS;
-            staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) { return wsrc[e]; },
-                                                  [&](int e, T v) { sm.Ts[e / kSwBS][e % kSwBS] = v; });
-        }
+        // z = b_i - acc (in xi)
         if (split) {
             #pragma unroll
             for (int u = 0; u < 4; ++u) sm.red[g][r][u] = acc[u];
@@ -292,20 +359,12 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
 
         // chain step: x_i = y_i - W_i x_{i-1}
         if (p > 0) {
-            if (t == 0) s_ok = wait_ready(p - 1);
-            __syncthreads();
-            if (!s_ok) return;
-            const int bj = FORWARD ? bi - 1 : bi + 1;
-            const int64_t j0 = int64_t(bj) * kSwBS;
-            const int nj = int(min64(kSwBS, n - j0));
-            staged_copy<XPER, 256>(kSwBS * kSwRhs, [&](int e) {
-                const int rr = e % kSwBS, q = e / kSwBS;
-                return (rr < nj && q < nrhs) ? __ldcg(&X[j0 + rr + q * ldx]) : T(0);
-            }, [&](int e, T v) { sm.xs[e % kSwBS][e / kSwBS] = v; });
-            __syncthreads();
+            const bool ok = finish_x(p - 1);
+            put_x();
+            if (__syncthreads_or(!ok)) return;
             T v[4] = {T(0), T(0), T(0), T(0)};
             #pragma unroll 4
-            for (int c = c0; c < c1; ++c) axpy4(sm.Ts[r][c], &sm.xs[c][qb], v);
+            for (int c = c0; c < c1; ++c) axpy4(sm.Ws[r][c], &sm.xs[c][qb], v);
             if (split) {
                 #pragma unroll
                 for (int u = 0; u < 4; ++u) sm.red[g][r][u] = v[u];
@@ -319,17 +378,21 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
         }
         if (r < ni) {
             if (split) {
-                if (g < nrhs) X[i0 + r + g * ldx] = y[0];
+                if (g < nrhs) {
+                    MB::put(mbox(i0 + r, g), y[0]);
+                    X[i0 + r + g * ldx] = y[0];
+                }
             }
             else {
                 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    if (qb + u < nrhs) X[i0 + r + (qb + u) * ldx] = y[u];
+                    if (qb + u < nrhs) {
+                        MB::put(mbox(i0 + r, qb + u), y[u]);
+                        X[i0 + r + (qb + u) * ldx] = y[u];
+                    }
             }
         }
-        __threadfence();
         __syncthreads();
-        if (t == 0) st_release_i32(&ready[p], 1);
     }
 }
 
@@ -340,8 +403,11 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     if (n <= 0 || nrhs <= 0) return SLT_OK;
     if (nrhs > kSwRhs) return SLT_ERR_ARG;
     const int64_t nblk = ceildiv(n, kSwBS);
-    // flags layout: [ticket][ready x nblk][pad to 256 B][Dinv: nblk x 64 x 64][W: nblk x 64 x 64]
-    T* Dinv = reinterpret_cast<T*>(reinterpret_cast<char*>(flags) + ((sizeof(int) * size_t(nblk + 1) + 255) & ~size_t(255)));
+    const int64_t npad = nblk * kSwBS;
+    // scratch layout: [ticket, pad to 256 B][mailbox: kSwRhs x npad x 2 words]
+    // [Dinv: nblk x 64 x 64][W: nblk x 64 x 64] (sized for double)
+    unsigned long long* mb = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(flags) + 256);
+    T* Dinv = reinterpret_cast<T*>(reinterpret_cast<char*>(flags) + 256 + size_t(kSwRhs) * npad * 2 * 8);
     const size_t ti_smem = size_t(2) * kSwBS * (kSwBS + 1) * sizeof(T);
     static bool ti_cfg = false;
     if (!ti_cfg) {
@@ -352,7 +418,8 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     trinv_kernel<T, FORWARD, UNIT, TRANS><<<unsigned(nblk), 256, ti_smem, s>>>(n, M, ldm, Dinv);
     count_launch();
     SLT_CUDA_TRY(cudaGetLastError());
-    SLT_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * size_t(nblk + 1), s));
+    // ticket and the first nrhs columns of the mailbox
+    SLT_CUDA_TRY(cudaMemsetAsync(flags, 0, 256 + size_t(nrhs) * size_t(npad) * Mailbox<T>::kWords * 8, s));
     auto fn = sweep_kernel<T, FORWARD, UNIT, TRANS>;
     const size_t smem = sizeof(SweepSmem<T>);
     static bool cfg = false;
@@ -366,7 +433,7 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, smem));
     const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(nblk, int64_t(sms) * std::max(per, 1)));
     const int pidx = prof_begin(SLT_PROF_SWEEP, s);
-    fn<<<unsigned(grid), 256, smem, s>>>(n, int(nrhs), M, ldm, Dinv, X, ldx, flags, flags + 1, status);
+    fn<<<unsigned(grid), 256, smem, s>>>(n, int(nrhs), M, ldm, Dinv, X, ldx, flags, mb, status);
     count_launch();
     prof_end(pidx, s, double(n) * double(n) * double(nrhs), sizeof(T) * (double(n) * double(n) / 2 + 2.0 * n * nrhs));
     return slt_from_cuda(cudaGetLastError());
@@ -376,7 +443,7 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
 
 using namespace slt;
 
-// flags: device int[ceil(n/64) + 1] scratch; status: device int (timeouts).
+// flags: device scratch of slt_sweep_flags_bytes(n) bytes; status: device int (timeouts).
 // kind: 0 unit lower (L of LU), 1 upper non-unit (U of LU), 2 lower
 // non-unit (L of Cholesky), 3 lower^T non-unit (L^T of Cholesky), 4 upper^T
 // non-unit (U^T of LU), 5 unit lower^T (L^T of LU).
@@ -408,10 +475,10 @@ extern "C" int slt_ssweep(int kind, int64_t n, int64_t nrhs, const float* M, int
     }
 }
 
-// Scratch of one sweep: ticket + ready flags, then the diagonal-block
-// inverses and the chain-step blocks W (sized for double).
+// Scratch of one sweep: ticket, mailbox of solved values, diagonal-block
+// inverses and chain-step blocks W (sized for double).
 extern "C" size_t slt_sweep_flags_bytes(int64_t n)
 {
     const int64_t nblk = ceildiv(n, kSwBS);
-    return ((sizeof(int) * size_t(nblk + 1) + 255) & ~size_t(255)) + 2 * size_t(nblk) * kSwBS * kSwBS * sizeof(double);
+    return 256 + size_t(kSwRhs) * size_t(nblk) * kSwBS * 2 * 8 + 2 * size_t(nblk) * kSwBS * kSwBS * sizeof(double);
 }
