@@ -33,37 +33,50 @@ constexpr int kCpSub = 16;
 constexpr int kStage = kCpIB * kCpIB / kCpThreads;   // 64 x 64 tile elements per thread, loaded in one batch
 
 // One warp: Cholesky of the bw x bw (bw <= 16) lower block S (row-major,
-// row stride lds) in registers, lane r holding row r; the factor is written
-// back to S and the reciprocals of its diagonal to Rd[0 .. bw).  Returns 0,
-// or the 1-based column of the first non-positive pivot.
-template <typename T>
-__device__ int factor_16(T* S, int lds, int bw, T* Rd)
+// row stride lds) in registers, lane r holding row r (rows bw .. 15 padded
+// with the identity, which leaves the bw x bw factor unchanged); the factor
+// is written back to S and the reciprocals of its diagonal to Rd[0 .. bw).
+// Column j is scaled by 1 / sqrt(d) and broadcast through the 16-entry
+// shared vector col.  The columns are unrolled by compile-time recursion so
+// the row stays in registers.  Returns 0, or the 1-based column of the first
+// non-positive pivot (S is then left as it was).
+template <int C, int N, typename T>
+__device__ __forceinline__ void f16_update(T (&a)[N], const T aj, const T* col, int r)
 {
-    const unsigned FULL = 0xffffffffu;
+    if constexpr (C < N) {
+        a[C] = (r >= C) ? fma(-aj, col[C], a[C]) : a[C];
+        f16_update<C + 1, N>(a, aj, col, r);
+    }
+}
+
+template <int J, int N, typename T>
+__device__ __forceinline__ void f16_columns(T (&a)[N], T* Rd, T* col, int r, int& fail)
+{
+    if constexpr (J < N) {
+        const T d = __shfl_sync(0xffffffffu, a[J], J);
+        if (!fail && !(d > T(0))) fail = J + 1;
+        const T sd = sqrt(d);
+        const T rd = T(1) / sd;
+        a[J] = (r == J) ? sd : a[J] * rd;
+        if (r == J) Rd[J] = rd;
+        if (r < N) col[r] = a[J];
+        __syncwarp();
+        f16_update<J + 1, N>(a, a[J], col, r);
+        __syncwarp();
+        f16_columns<J + 1, N>(a, Rd, col, r, fail);
+    }
+}
+
+template <typename T>
+__device__ int factor_16(T* S, int lds, int bw, T* Rd, T* col)
+{
     const int r = threadIdx.x & 31;
     T a[kCpSub];
     #pragma unroll
-    for (int c = 0; c < kCpSub; ++c) a[c] = (r < bw && c <= r) ? S[r * lds + c] : T(0);
+    for (int c = 0; c < kCpSub; ++c)
+        a[c] = (c > r) ? T(0) : (r < bw) ? S[r * lds + c] : (c == r) ? T(1) : T(0);
     int fail = 0;
-    #pragma unroll
-    for (int j = 0; j < kCpSub; ++j) {
-        if (j < bw && !fail) {
-            const T d = __shfl_sync(FULL, a[j], j);
-            if (!(d > T(0))) {
-                fail = j + 1;
-            }
-            else {
-                const T sd = sqrt(d);
-                if (r == j) { a[j] = sd; Rd[j] = T(1) / sd; }
-                else if (r > j) a[j] = a[j] / sd;
-                #pragma unroll
-                for (int c = j + 1; c < kCpSub; ++c) {
-                    const T lcj = __shfl_sync(FULL, a[j], c);
-                    if (r >= c) a[c] = fma(-a[j], lcj, a[c]);
-                }
-            }
-        }
-    }
+    f16_columns<0, kCpSub>(a, Rd, col, r, fail);
     if (fail) return fail;
     if (r < bw) {
         #pragma unroll
@@ -105,7 +118,42 @@ struct CholPanelArgs {
     unsigned* diag_ready;  // index of the last diagonal block published by the lookahead
     unsigned* head_done;   // per step: blocks that solved rows needed by the others' update
     T* dinv_ws;         // per step: the diagonal block's 16 x 16 sub-block inverses, [16][4][16][17]
+    int vec;            // P 16-byte aligned and ld * sizeof(T) a multiple of 16: 4-vector access to P
 };
+
+// four consecutive elements of P (16-byte aligned), read through L2
+__device__ __forceinline__ void ld4_cg(const float* p, float* v)
+{
+    const float4 x = __ldcg(reinterpret_cast<const float4*>(p));
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+}
+__device__ __forceinline__ void ld4_cg(const double* p, double* v)
+{
+    const double2 x = __ldcg(reinterpret_cast<const double2*>(p));
+    const double2 y = __ldcg(reinterpret_cast<const double2*>(p + 2));
+    v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+}
+__device__ __forceinline__ void st4(float* p, const float* v)
+{
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double* p, const double* v)
+{
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+}
+// four consecutive elements of a 16-byte aligned shared array
+__device__ __forceinline__ void lds4(const float* p, float* v)
+{
+    const float4 x = *reinterpret_cast<const float4*>(p);
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double* v)
+{
+    const double2 x = *reinterpret_cast<const double2*>(p);
+    const double2 y = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+}
 
 constexpr int kCpDinv = (kCpIB / kCpSub) * kCpSub * (kCpSub + 1);   // inverses of one diagonal block
 
@@ -140,6 +188,7 @@ __device__ int factor_diag_block(T* D, T* Dinv, int kb)
 {
     __shared__ int s_f;
     __shared__ T s_rd[kCpIB / kCpSub][kCpSub];
+    __shared__ T s_col[kCpSub];
     const int t = threadIdx.x;
     if (t == 0) s_f = 0;
     __syncthreads();
@@ -147,7 +196,7 @@ __device__ int factor_diag_block(T* D, T* Dinv, int kb)
         const int bw = min(kCpSub, kb - jb);
         T* S = D + jb * (kCpIB + 1) + jb;
         if (t < 32) {
-            const int fail = factor_16(S, kCpIB + 1, bw, s_rd[jbi]);
+            const int fail = factor_16(S, kCpIB + 1, bw, s_rd[jbi], s_col);
             if (t == 0 && fail) s_f = jb + fail;
         }
         __syncthreads();
@@ -195,7 +244,7 @@ template <typename T>
 __global__ void __launch_bounds__(kCpThreads, 2)
 chol_panel_kernel(CholPanelArgs<T> a)
 {
-    extern __shared__ unsigned char cp_smem_raw[];
+    extern __shared__ __align__(16) unsigned char cp_smem_raw[];
     T* D = reinterpret_cast<T*>(cp_smem_raw);             // [64][65] factor, D[i*65 + l] = L(i,l)
     T* Xs = D + kCpIB * (kCpIB + 1);                        // [64][68] solved rows staging
     T* Us = Xs + kCpIB * 68;                                // [64][68] update operand
@@ -314,32 +363,50 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 if (i < kb && l < kb && i >= l) P[c0 + i + (c0 + l) * ld] = D[i * (kCpIB + 1) + l];
             }
         // ---- 3. rank-kb update of the owned rows in panel columns [c0+kb, nbk):
-        //      64 x 64 output tiles, 4 x 4 per thread, operands staged [l][row]
-        //      and [l][col] (row stride 68) so each thread reads two 4-vectors
-        //      per k step for 16 FMAs.
+        //      per 64-row tile of the block (its solved rows staged once,
+        //      [l][row], row stride 68) and per 64-column tile at or left of
+        //      the tile's last row (operand [l][col]), 64 x 64 outputs with 4
+        //      consecutive rows x 4 consecutive columns per thread: two
+        //      4-vector shared loads per k step for 16 FMAs.  The old values
+        //      of P are read before the product; whole tiles below the
+        //      diagonal move as 4-vectors.
         if (cbeg < a.nbk && !failed) {
             T* X3 = Xs;                                  // [64][68]
             T* U3 = Us;                                  // [64][68]
             const int64_t r0 = max64(rb, cbeg);
-            // rows tr + 16 i and columns tc + 16 j: lanes run along rows, so
-            // the final read-modify-write of P is two 64-byte segments per warp
-            const int tr = t & 15, tc = t >> 4;
-            // a column tile starting at or below the block's last row has no
-            // lower-triangular rows here, nor have the tiles after it
-            for (int64_t cb = cbeg; cb < a.nbk && cb < re; cb += kCpIB) {
-                const int nc = int(min64(kCpIB, a.nbk - cb));
+            const int tr = t & 15, tc = t >> 4;          // rows 4 tr + i, columns 4 tc + j
+            for (int64_t rr = r0; rr < re; rr += kCpIB) {
+                const int nr = int(min64(kCpIB, re - rr));
                 __syncthreads();
                 staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
-                    const int c = e % kCpIB, l = e / kCpIB;
-                    return (c < nc && l < kb) ? __ldcg(&P[cb + c + (c0 + l) * ld]) : T(0);
-                }, [&](int e, T v) { U3[(e / kCpIB) * 68 + e % kCpIB] = v; });
-                for (int64_t rr = max64(r0, cb); rr < re; rr += kCpIB) {
-                    const int nr = int(min64(kCpIB, re - rr));
+                    const int i = e % kCpIB, l = e / kCpIB;
+                    return (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
+                }, [&](int e, T v) { X3[(e / kCpIB) * 68 + e % kCpIB] = v; });
+                // a column tile starting past the row tile's last row has no
+                // lower-triangular entries here, nor have the tiles after it
+                for (int64_t cb = cbeg; cb < a.nbk && cb < rr + nr; cb += kCpIB) {
+                    const int nc = int(min64(kCpIB, a.nbk - cb));
                     __syncthreads();
                     staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
-                        const int i = e % kCpIB, l = e / kCpIB;
-                        return (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
-                    }, [&](int e, T v) { X3[(e / kCpIB) * 68 + e % kCpIB] = v; });
+                        const int c = e % kCpIB, l = e / kCpIB;
+                        return (c < nc && l < kb) ? __ldcg(&P[cb + c + (c0 + l) * ld]) : T(0);
+                    }, [&](int e, T v) { U3[(e / kCpIB) * 68 + e % kCpIB] = v; });
+                    const bool full = a.vec && nr == kCpIB && nc == kCpIB && rr >= cb + kCpIB;
+                    T* Pt = P + rr + 4 * tr + (cb + 4 * tc) * ld;      // element (4 tr, 4 tc) of the tile
+                    T old[4][4];                                        // [column j][row i]
+                    if (full) {
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) ld4_cg(Pt + j * ld, old[j]);
+                    }
+                    else {
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            #pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const int c = 4 * tc + j, ii = 4 * tr + i;
+                                old[j][i] = (c < nc && ii < nr && rr + ii >= cb + c) ? __ldcg(Pt + i + j * ld) : T(0);
+                            }
+                    }
                     __syncthreads();
                     T acc[4][4];
                     #pragma unroll
@@ -349,28 +416,31 @@ chol_panel_kernel(CholPanelArgs<T> a)
                     #pragma unroll 4
                     for (int l = 0; l < kb; ++l) {
                         T xr[4], uc[4];
-                        #pragma unroll
-                        for (int i = 0; i < 4; ++i) { xr[i] = X3[l * 68 + tr + 16 * i]; uc[i] = U3[l * 68 + tc + 16 * i]; }
+                        lds4(X3 + l * 68 + 4 * tr, xr);
+                        lds4(U3 + l * 68 + 4 * tc, uc);
                         #pragma unroll
                         for (int i = 0; i < 4; ++i)
                             #pragma unroll
                             for (int j = 0; j < 4; ++j) acc[i][j] = fma(xr[i], uc[j], acc[i][j]);
                     }
-                    T old[4][4];
-                    #pragma unroll
-                    for (int j = 0; j < 4; ++j)
+                    if (full) {
                         #pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            const int c = tc + 16 * j, ii = tr + 16 * i;
-                            if (c < nc && ii < nr && rr + ii >= cb + c) old[i][j] = __ldcg(&P[rr + ii + (cb + c) * ld]);
+                        for (int j = 0; j < 4; ++j) {
+                            T v[4];
+                            #pragma unroll
+                            for (int i = 0; i < 4; ++i) v[i] = old[j][i] - acc[i][j];
+                            st4(Pt + j * ld, v);
                         }
-                    #pragma unroll
-                    for (int j = 0; j < 4; ++j)
+                    }
+                    else {
                         #pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            const int c = tc + 16 * j, ii = tr + 16 * i;
-                            if (c < nc && ii < nr && rr + ii >= cb + c) P[rr + ii + (cb + c) * ld] = old[i][j] - acc[i][j];
-                        }
+                        for (int j = 0; j < 4; ++j)
+                            #pragma unroll
+                            for (int i = 0; i < 4; ++i) {
+                                const int c = 4 * tc + j, ii = 4 * tr + i;
+                                if (c < nc && ii < nr && rr + ii >= cb + c) Pt[i + j * ld] = old[j][i] - acc[i][j];
+                            }
+                    }
                 }
             }
         }
@@ -437,8 +507,9 @@ static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info
     unsigned* head_done = reinterpret_cast<unsigned*>(w + 264);
     T* dinv_ws = reinterpret_cast<T*>(w + 512);
     SLT_CUDA_TRY(cudaMemsetAsync(ws, 0, 512, stream));
+    const int vec = (reinterpret_cast<uintptr_t>(P) % 16 == 0) && ((ld * int64_t(sizeof(T))) % 16 == 0);
     CholPanelArgs<T> args{m, nbk, ld, R, info_offset, P, info, status, bar, next_fail, diag_ready, head_done,
-                          dinv_ws};
+                          dinv_ws, vec};
     void* kargs[] = { &args };
     const int pidx = prof_begin(SLT_PROF_POTRF, stream);
     SLT_CUDA_TRY(cudaLaunchCooperativeKernel((const void*) chol_panel_kernel<T>, dim3(unsigned(G)),
