@@ -264,6 +264,23 @@ chol_panel_kernel(CholPanelArgs<T> a)
         //      (below) and published L11 in P, the sub-block inverses and a
         //      failure word in the workspace; every block loads them.
         const int k = int(c0 / kCpIB);
+        // With 64-row blocks and a full 64-column next diagonal block, the
+        // owner of that block owns exactly its rows, and its whole update is
+        // D_next -= X X^T with X its own solved rows, formed in shared memory
+        // below without waiting for the other head rows.  (A narrower next
+        // block leaves owned rows below it in the panel: general path.)  The
+        // old block is fetched now, while the owner waits for this step's
+        // diagonal block.
+        const int64_t cnext = c0 + kb;
+        const bool fast = cnext + kCpIB <= a.nbk && a.rows_per_block == kCpIB && cnext == rb;
+        if (fast) {
+            const int kbn0 = int(min64(kCpIB, a.nbk - cnext));
+            __syncthreads();          // the block's own update of this tile in the previous step
+            staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                const int i = e % kCpIB, l = e / kCpIB;
+                return (i < kbn0 && l < kbn0 && i >= l) ? __ldcg(&P[cnext + i + (cnext + l) * ld]) : T(0);
+            }, [&](int e, T v) { Us[(e % kCpIB) * 68 + e / kCpIB] = v; });
+        }
         if (c0 > 0) {
             if (t == 0) s_abort = wait_at_least(a.diag_ready, unsigned(k), a.status) ? 0 : 1;
             __syncthreads();
@@ -350,7 +367,7 @@ chol_panel_kernel(CholPanelArgs<T> a)
         if (c0 == 0) {
             if (!grid_sync(a.bar, unsigned(G), a.status)) return;
         }
-        if (!failed && n_head > 0) {
+        if (!failed && n_head > 0 && !fast) {
             if (t == 0) s_abort = wait_at_least(&a.head_done[k], unsigned(n_head), a.status) ? 0 : 1;
             __syncthreads();
             if (s_abort) return;
@@ -370,7 +387,7 @@ chol_panel_kernel(CholPanelArgs<T> a)
         //      4-vector shared loads per k step for 16 FMAs.  The old values
         //      of P are read before the product; whole tiles below the
         //      diagonal move as 4-vectors.
-        if (cbeg < a.nbk && !failed) {
+        if (cbeg < a.nbk && !failed && !fast) {
             T* X3 = Xs;                                  // [64][68]
             T* U3 = Us;                                  // [64][68]
             const int64_t r0 = max64(rb, cbeg);
@@ -451,10 +468,45 @@ chol_panel_kernel(CholPanelArgs<T> a)
         if (!failed && cbeg < a.nbk && cbeg >= rb && cbeg < re) {
             const int kbn = int(min64(kCpIB, a.nbk - cbeg));
             __syncthreads();
-            staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
-                const int i = e % kCpIB, l = e / kCpIB;
-                return (i < kbn && l < kbn && i >= l) ? __ldcg(&P[cbeg + i + (cbeg + l) * ld]) : T(0);
-            }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
+            if (fast) {
+                // D = old - X X^T on the lower triangle, X = the solved rows in
+                // Xs (row-major, stride 65); the same FMA order as the update
+                // above, so the factor matches the general path bit for bit
+                const int tr = t & 15, tc = t >> 4;      // rows 4 tr + i, columns 4 tc + j
+                if (tc <= tr) {
+                    T acc[4][4];
+                    #pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+                    #pragma unroll 4
+                    for (int l = 0; l < kb; ++l) {
+                        T xr[4], xc[4];
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            xr[i] = Xs[(4 * tr + i) * (kCpIB + 1) + l];
+                            xc[i] = Xs[(4 * tc + i) * (kCpIB + 1) + l];
+                        }
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            #pragma unroll
+                            for (int j = 0; j < 4; ++j) acc[i][j] = fma(xr[i], xc[j], acc[i][j]);
+                    }
+                    #pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int row = 4 * tr + i, col = 4 * tc + j;
+                            if (row < kbn && col <= row) D[row * (kCpIB + 1) + col] = Us[row * 68 + col] - acc[i][j];
+                        }
+                }
+            }
+            else {
+                staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                    const int i = e % kCpIB, l = e / kCpIB;
+                    return (i < kbn && l < kbn && i >= l) ? __ldcg(&P[cbeg + i + (cbeg + l) * ld]) : T(0);
+                }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
+            }
             __syncthreads();
             const int f = factor_diag_block(D, Dinv, kbn);
             for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {

@@ -56,3 +56,34 @@ def test_potrf_known_answer_minij(orc, slt):
     assert slt.potrf(dA, slt.Options(nb=32)) == 0
     torch.cuda.synchronize()
     np.testing.assert_allclose(np.tril(to_host(dA)), np.tril(np.ones((70, 70))), atol=1e-13)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_potrf_two_blocks_per_sm(slt, dtype):
+    """n = 12288: the first panels need more 64-row blocks than SMs, so two
+    panel blocks share an SM.  The factor must be run-to-run identical (no
+    race between a block's own update and its next-step reads) and, in FP64,
+    solve to backward error <= 3 eps; checked on the device with torch."""
+    import torch
+    n = 12288
+    tdt = getattr(torch, dtype)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    G = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
+    A = G @ G.t() / n + torch.eye(n, device="cuda", dtype=torch.float64)
+    del G
+    outs = []
+    for _ in range(2):
+        a = slt.colmajor(A.to(tdt))
+        assert slt.potrf(a, slt.Options(nb=512)) == 0
+        torch.cuda.synchronize()
+        outs.append(torch.tril(a))
+    assert torch.equal(outs[0], outs[1])
+    if dtype == "float64":
+        L = outs[0]
+        b = torch.rand(n, 1, device="cuda", dtype=torch.float64, generator=g) * 2 - 1
+        x = torch.cholesky_solve(b, L)
+        r = b - A @ x
+        berr = float(r.abs().max() / (A.abs().sum(1).max() * x.abs().max()))
+        assert berr <= 3 * EPS, berr
+        Lref = torch.linalg.cholesky(A)
+        assert float((L - Lref).abs().max()) <= 1e-12 * float(A.abs().max())
