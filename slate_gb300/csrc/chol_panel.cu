@@ -40,6 +40,24 @@ constexpr int kStage = kCpIB * kCpIB / kCpThreads;   // 64 x 64 tile elements pe
 // shared vector col.  The columns are unrolled by compile-time recursion so
 // the row stays in registers.  Returns 0, or the 1-based column of the first
 // non-positive pivot (S is then left as it was).
+// sd = sqrt(d) and rd = 1 / sd.  FP32: the hardware reciprocal square root
+// refined by one Newton-Raphson step, y <- y (3 - d y^2) / 2, which takes
+// its ~2^-22 relative error below an ulp of the result (the division and
+// square root chain of the IEEE forms is the panel's critical path).
+// FP64: correctly rounded sqrt and division.
+__device__ __forceinline__ void pivot_scale(float d, float& sd, float& rd)
+{
+    float y = rsqrtf(d);
+    y = y * fmaf(-0.5f * d * y, y, 1.5f);
+    rd = y;
+    sd = d * y;
+}
+__device__ __forceinline__ void pivot_scale(double d, double& sd, double& rd)
+{
+    sd = sqrt(d);
+    rd = 1.0 / sd;
+}
+
 template <int C, int N, typename T>
 __device__ __forceinline__ void f16_update(T (&a)[N], const T aj, const T* col, int r)
 {
@@ -55,8 +73,8 @@ __device__ __forceinline__ void f16_columns(T (&a)[N], T* Rd, T* col, int r, int
     if constexpr (J < N) {
         const T d = __shfl_sync(0xffffffffu, a[J], J);
         if (!fail && !(d > T(0))) fail = J + 1;
-        const T sd = sqrt(d);
-        const T rd = T(1) / sd;
+        T sd, rd;
+        pivot_scale(d, sd, rd);
         a[J] = (r == J) ? sd : a[J] * rd;
         if (r == J) Rd[J] = rd;
         if (r < N) col[r] = a[J];
@@ -225,13 +243,49 @@ __device__ int factor_diag_block(T* D, T* Dinv, int kb)
             }
             bar_workers();
             // trailing update inside the block: D[i][c] -= sum_p D[i][jb+p] D[c][jb+p], jb+bw <= c <= i < kb
-            for (int e = w; e < below * below; e += kCpThreads - 32) {
-                const int i = jb + bw + e % below, c = jb + bw + e / below;
-                if (c > i) continue;
-                T acc = T(0);
-                for (int p = 0; p < bw; ++p)
-                    acc = fma(D[i * (kCpIB + 1) + jb + p], D[c * (kCpIB + 1) + jb + p], acc);
-                D[i * (kCpIB + 1) + c] -= acc;
+            // (bw = 16 whenever rows remain below).  4 x 4 output tiles on
+            // and below the diagonal, one per worker thread; every element
+            // sums its 16 products in order, as the one-element loop does.
+            if (below % 4 == 0) {
+                const int tb = below / 4;
+                if (w < tb * (tb + 1) / 2) {
+                    int ti = 0, tj = w;
+                    while (tj > ti) { tj -= ti + 1; ++ti; }
+                    const int i0 = jb + kCpSub + 4 * ti, c0 = jb + kCpSub + 4 * tj;
+                    T acc[4][4];
+                    #pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        #pragma unroll
+                        for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+                    #pragma unroll 2
+                    for (int p = 0; p < kCpSub; ++p) {
+                        T xi4[4], xc4[4];
+                        #pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            xi4[u] = D[(i0 + u) * (kCpIB + 1) + jb + p];
+                            xc4[u] = D[(c0 + u) * (kCpIB + 1) + jb + p];
+                        }
+                        #pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            #pragma unroll
+                            for (int v = 0; v < 4; ++v) acc[u][v] = fma(xi4[u], xc4[v], acc[u][v]);
+                    }
+                    #pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        #pragma unroll
+                        for (int v = 0; v < 4; ++v)
+                            if (c0 + v <= i0 + u) D[(i0 + u) * (kCpIB + 1) + c0 + v] -= acc[u][v];
+                }
+            }
+            else {
+                for (int e = w; e < below * below; e += kCpThreads - 32) {
+                    const int i = jb + bw + e % below, c = jb + bw + e / below;
+                    if (c > i) continue;
+                    T acc = T(0);
+                    for (int p = 0; p < bw; ++p)
+                        acc = fma(D[i * (kCpIB + 1) + jb + p], D[c * (kCpIB + 1) + jb + p], acc);
+                    D[i * (kCpIB + 1) + c] -= acc;
+                }
             }
         }
         __syncthreads();
