@@ -195,9 +195,9 @@ __device__ __forceinline__ bool wait_at_least(const unsigned* p, unsigned target
 // stride 65, lower triangle) factored in place by the whole CTA, in 16-column
 // steps: warp 0 factors the 16 x 16 diagonal sub-block; then warps 1-7 solve
 // the sub-block rows below it by forward substitution and update the rest of
-// the block (their own 224-thread barrier), while warp 0 inverts the
-// sub-block into Dinv for the panel's row solves -- the inversion stays off
-// the chain of sub-block steps.  Returns 0, or the 1-based column (within the
+// the block (their own 224-thread barrier).  At the end warps 0-3 invert the
+// four sub-blocks in parallel into Dinv for the panel's row solves, so no
+// inversion sits on the chain of sub-block steps.  Returns 0, or the 1-based column (within the
 // block) of the first non-positive pivot; the same value in every thread.
 __device__ __forceinline__ void bar_workers() { asm volatile("bar.sync 1, %0;" :: "n"(kCpThreads - 32) : "memory"); }
 
@@ -220,10 +220,7 @@ __device__ int factor_diag_block(T* D, T* Dinv, int kb)
         __syncthreads();
         if (s_f) break;
         const int below = kb - jb - bw;
-        if (t < 32) {
-            invert_16(S, kCpIB + 1, bw, s_rd[jbi], Dinv + jbi * kCpSub * (kCpSub + 1));
-        }
-        else if (below > 0) {
+        if (t >= 32 && below > 0) {
             const int w = t - 32;
             // rows i in [jb + bw, kb) of the sub-block column: X L^T = B, row by row
             if (w < below) {
@@ -289,6 +286,14 @@ __device__ int factor_diag_block(T* D, T* Dinv, int kb)
             }
         }
         __syncthreads();
+    }
+    // the sub-block inverses for the panel's row solves, one warp each, off
+    // the chain of sub-block steps
+    if (!s_f) {
+        const int q = t >> 5;
+        if (q * kCpSub < kb)
+            invert_16(D + q * kCpSub * (kCpIB + 1) + q * kCpSub, kCpIB + 1, min(kCpSub, kb - q * kCpSub), s_rd[q],
+                      Dinv + q * kCpSub * (kCpSub + 1));
     }
     __syncthreads();
     return s_f;
