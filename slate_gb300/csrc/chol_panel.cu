@@ -135,7 +135,7 @@ struct CholPanelArgs {
     int* next_fail;     // set when the lookahead factor of the next diagonal block fails
     unsigned* diag_ready;  // index of the last diagonal block published by the lookahead
     unsigned* head_done;   // per step: blocks that solved rows needed by the others' update
-    T* dinv_ws;         // per step: the diagonal block's 16 x 16 sub-block inverses, [16][4][16][17]
+    T* dinv_ws;         // per step: the diagonal block's transposed inverse, [16][64][64]
     int vec;            // P 16-byte aligned and ld * sizeof(T) a multiple of 16: 4-vector access to P
 };
 
@@ -173,7 +173,8 @@ __device__ __forceinline__ void lds4(const double* p, double* v)
     v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
 }
 
-constexpr int kCpDinv = (kCpIB / kCpSub) * kCpSub * (kCpSub + 1);   // inverses of one diagonal block
+constexpr int kCpDinv = (kCpIB / kCpSub) * kCpSub * (kCpSub + 1);   // sub-block inverses of one diagonal block
+constexpr int kCpLinv = kCpIB * kCpIB;                                 // transposed inverse of one diagonal block
 
 // Bounded acquire spin of thread 0 until *p >= target; false on timeout or
 // when another block has already failed (status set).
@@ -299,6 +300,71 @@ __device__ int factor_diag_block(T* D, T* Dinv, int kb)
     return s_f;
 }
 
+// The inverse of the factored kb x kb diagonal block L (D, row-major,
+// stride 65), stored transposed: Lt[l * 68 + c] = L^{-1}(c, l), zero above
+// the diagonal and outside kb.  The 16 x 16 diagonal blocks are the
+// sub-block inverses Dinv; below them, by increasing distance d = I - J,
+//     L^{-1}(I, J) = -Inv_I * sum_{K=J}^{I-1} L(I, K) L^{-1}(K, J)
+// (16 x 16 blocks), the sums staged in Tmp (768 entries).  Every thread of
+// the block takes part.
+// One level d of build_linv_t: for the block pairs (I, J) = (J + d, J),
+// Tmp = sum_{K=J}^{I-1} L(I, K) L^{-1}(K, J), then L^{-1}(I, J) = -Inv_I Tmp.
+// Fixed trip counts (16 d products; Inv_I is zero above its diagonal) so the
+// shared loads of every sum are issued ahead of its FMAs.
+template <int DD, typename T>
+__device__ __forceinline__ void linv_level(const T* D, const T* Dinv, T* Lt, T* Tmp, int nsub)
+{
+    const int npair = nsub - DD;
+    if (npair <= 0) return;
+    const int t = threadIdx.x;
+    for (int e = t; e < npair * 256; e += kCpThreads) {
+        const int J = e / 256, I = J + DD, i = (e % 256) / kCpSub, j = e % kCpSub;
+        const T* drow = D + (kCpSub * I + i) * (kCpIB + 1) + kCpSub * J;
+        const T* lcol = Lt + (kCpSub * J + j) * 68 + kCpSub * J;
+        T acc = T(0);
+        #pragma unroll
+        for (int kk = 0; kk < kCpSub * DD; ++kk) acc = fma(drow[kk], lcol[kk], acc);
+        Tmp[e] = acc;
+    }
+    __syncthreads();
+    for (int e = t; e < npair * 256; e += kCpThreads) {
+        const int J = e / 256, I = J + DD, i = (e % 256) / kCpSub, j = e % kCpSub;
+        const T* inv = Dinv + I * kCpSub * (kCpSub + 1) + i * (kCpSub + 1);
+        const T* tc = Tmp + J * 256 + j;
+        T acc = T(0);
+        #pragma unroll
+        for (int mm = 0; mm < kCpSub; ++mm) acc = fma(inv[mm], tc[mm * kCpSub], acc);
+        Lt[(kCpSub * J + j) * 68 + kCpSub * I + i] = -acc;
+    }
+    __syncthreads();
+}
+
+// The inverse of the factored kb x kb diagonal block L (D, row-major,
+// stride 65), stored transposed: Lt[l * 68 + c] = L^{-1}(c, l), zero above
+// the diagonal and outside kb.  The 16 x 16 diagonal blocks are the
+// sub-block inverses Dinv (zero above their diagonals); below them, by
+// increasing distance d = I - J,
+//     L^{-1}(I, J) = -Inv_I * sum_{K=J}^{I-1} L(I, K) L^{-1}(K, J)
+// (16 x 16 blocks), the sums staged in Tmp (768 entries).  Every thread of
+// the block takes part.
+template <typename T>
+__device__ void build_linv_t(const T* D, const T* Dinv, T* Lt, T* Tmp, int kb)
+{
+    const int t = threadIdx.x;
+    const int nsub = (kb + kCpSub - 1) / kCpSub;
+    for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+        const int l = e / kCpIB, c = e % kCpIB, q = c / kCpSub;
+        T v = T(0);
+        if (l / kCpSub == q && l <= c && c < kb)
+            v = Dinv[q * kCpSub * (kCpSub + 1) + (c % kCpSub) * (kCpSub + 1) + l % kCpSub];
+        Lt[l * 68 + c] = v;
+    }
+    __syncthreads();
+    linv_level<1>(D, Dinv, Lt, Tmp, nsub);
+    linv_level<2>(D, Dinv, Lt, Tmp, nsub);
+    linv_level<3>(D, Dinv, Lt, Tmp, nsub);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kCpThreads, 2)
 chol_panel_kernel(CholPanelArgs<T> a)
@@ -317,42 +383,45 @@ chol_panel_kernel(CholPanelArgs<T> a)
 
     for (int64_t c0 = 0; c0 < a.nbk; c0 += kCpIB) {
         const int kb = int(min64(kCpIB, a.nbk - c0));
-        // ---- 1. the factored diagonal block in shared memory.  First step:
-        //      every block factors it (no earlier step could).  Later steps:
+        // ---- 1. the inverse of the factored diagonal block in shared memory
+        //      (Us, transposed).  First step: every block factors the block
+        //      and inverts it itself (no earlier step could).  Later steps:
         //      its owner factored it during the previous step's update phase
-        //      (below) and published L11 in P, the sub-block inverses and a
-        //      failure word in the workspace; every block loads them.
+        //      (below) and published L11 in P, the inverse and a failure word
+        //      in the workspace; every block loads the inverse.
         const int k = int(c0 / kCpIB);
         // With 64-row blocks and a full 64-column next diagonal block, the
         // owner of that block owns exactly its rows, and its whole update is
         // D_next -= X X^T with X its own solved rows, formed in shared memory
         // below without waiting for the other head rows.  (A narrower next
         // block leaves owned rows below it in the panel: general path.)  The
-        // old block is fetched now, while the owner waits for this step's
-        // diagonal block.
+        // old block goes to D (free while the rows are solved), fetched while
+        // the owner waits for this step's diagonal block.
         const int64_t cnext = c0 + kb;
         const bool fast = cnext + kCpIB <= a.nbk && a.rows_per_block == kCpIB && cnext == rb;
-        if (fast) {
+        auto fetch_next_block = [&]() {
             const int kbn0 = int(min64(kCpIB, a.nbk - cnext));
             __syncthreads();          // the block's own update of this tile in the previous step
             staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
                 const int i = e % kCpIB, l = e / kCpIB;
                 return (i < kbn0 && l < kbn0 && i >= l) ? __ldcg(&P[cnext + i + (cnext + l) * ld]) : T(0);
-            }, [&](int e, T v) { Us[(e % kCpIB) * 68 + e / kCpIB] = v; });
-        }
+            }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
+        };
+        if (fast && c0 > 0) fetch_next_block();
         if (c0 > 0) {
             if (t == 0) s_abort = wait_at_least(a.diag_ready, unsigned(k), a.status) ? 0 : 1;
             __syncthreads();
             if (s_abort) return;
+            staged_copy<kStage, kCpThreads>(kCpLinv, [&](int e) {
+                return __ldcg(&a.dinv_ws[size_t(k) * kCpLinv + e]);
+            }, [&](int e, T v) { Us[(e / kCpIB) * 68 + e % kCpIB] = v; });
         }
-        staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
-            const int i = e % kCpIB, l = e / kCpIB;
-            return (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
-        }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
-        if (c0 > 0)
-            staged_copy<(kCpDinv + kCpThreads - 1) / kCpThreads, kCpThreads>(kCpDinv, [&](int e) {
-                return __ldcg(&a.dinv_ws[size_t(k) * kCpDinv + e]);
-            }, [&](int e, T v) { Dinv[e] = v; });
+        else {
+            staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                const int i = e % kCpIB, l = e / kCpIB;
+                return (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
+            }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
+        }
         if (t == 0) s_fail = (c0 > 0) ? ld_volatile_i32(a.next_fail) : 0;
         __syncthreads();
         if (c0 == 0) {
@@ -361,53 +430,55 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 s_fail = 1;
                 if (c0 >= rb && c0 < re) atomicCAS(a.info, 0, int(a.info_offset + c0 + f));
             }
+            if (f == 0) build_linv_t(D, Dinv, Us, Xs, kb);
+            // block 0 writes this factor back from D below; the owner of the
+            // next block (never block 0) may now reuse D
+            if (f == 0 && fast) fetch_next_block();
         }
         __syncthreads();
         const bool failed = s_fail != 0;
-        // ---- 2. solve the owned rows below the block: X L^T = B, 64 rows at a
-        //      time, 4 lanes per row; per 16-column sub-block subtract the
-        //      solved sub-blocks, then multiply by the sub-block inverse.
+        // ---- 2. solve the owned rows below the block: X = B L^{-T}, 64 rows at
+        //      a time, as one product with the inverse (Us) over 4 x 4
+        //      register tiles (rows 4 tr + i, columns 4 tc + j; column c
+        //      needs inverse rows l <= c).  The solved rows stay in Xs,
+        //      [l][row] with stride 68 -- the layout of the update operand.
         if (!failed) {
             const int64_t r0 = max64(rb, c0 + kb);
+            const int tr = t & 15, tc = t >> 4;
             for (int64_t rr = r0; rr < re; rr += kCpIB) {
                 const int nr = int(min64(kCpIB, re - rr));
                 __syncthreads();
                 staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
                     const int i = e % kCpIB, l = e / kCpIB;
                     return (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
-                }, [&](int e, T v) { Xs[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
+                }, [&](int e, T v) { Xs[(e / kCpIB) * 68 + e % kCpIB] = v; });
                 __syncthreads();
-                const int row = t >> 2, q = t & 3, lane = t & 31;
-                T* xr = Xs + row * (kCpIB + 1);
-                for (int jb = 0, jbi = 0; jb < kb; jb += kCpSub, ++jbi) {
-                    const int bw = min(kCpSub, kb - jb);
-                    const T* Di = Dinv + jbi * kCpSub * (kCpSub + 1);
-                    T y[4];
+                T acc[4][4];
+                #pragma unroll
+                for (int i = 0; i < 4; ++i)
                     #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int c = q + 4 * u;
-                        T acc = (c < bw) ? xr[jb + c] : T(0);
-                        if (c < bw)
-                            for (int p = 0; p < jb; ++p) acc = fma(-xr[p], D[(jb + c) * (kCpIB + 1) + p], acc);
-                        y[u] = acc;
-                    }
-                    T out[4] = {T(0), T(0), T(0), T(0)};
+                    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+                const int lmax = min(kb, 4 * tc + 4);
+                #pragma unroll 4
+                for (int l = 0; l < lmax; ++l) {
+                    T xr[4], li[4];
+                    lds4(Xs + l * 68 + 4 * tr, xr);
+                    lds4(Us + l * 68 + 4 * tc, li);
                     #pragma unroll
-                    for (int p = 0; p < kCpSub; ++p) {
-                        const T zp = __shfl_sync(0xffffffffu, y[p / 4], (lane & ~3) | (p & 3));
+                    for (int i = 0; i < 4; ++i)
                         #pragma unroll
-                        for (int u = 0; u < 4; ++u) out[u] = fma(zp, Di[(q + 4 * u) * (kCpSub + 1) + p], out[u]);
-                    }
-                    __syncwarp();
-                    #pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                        if (q + 4 * u < bw) xr[jb + q + 4 * u] = out[u];
-                    __syncwarp();
+                        for (int j = 0; j < 4; ++j) acc[i][j] = fma(xr[i], li[j], acc[i][j]);
+                }
+                __syncthreads();
+                #pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const T v[4] = {acc[0][j], acc[1][j], acc[2][j], acc[3][j]};
+                    st4(Xs + (4 * tc + j) * 68 + 4 * tr, v);
                 }
                 __syncthreads();
                 for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
                     int i = e % kCpIB, l = e / kCpIB;
-                    if (i < nr && l < kb) P[rr + i + (c0 + l) * ld] = Xs[i * (kCpIB + 1) + l];
+                    if (i < nr && l < kb) P[rr + i + (c0 + l) * ld] = Xs[l * 68 + i];
                 }
             }
         }
@@ -454,10 +525,12 @@ chol_panel_kernel(CholPanelArgs<T> a)
             for (int64_t rr = r0; rr < re; rr += kCpIB) {
                 const int nr = int(min64(kCpIB, re - rr));
                 __syncthreads();
-                staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
-                    const int i = e % kCpIB, l = e / kCpIB;
-                    return (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
-                }, [&](int e, T v) { X3[(e / kCpIB) * 68 + e % kCpIB] = v; });
+                // one row tile per block: the solve left exactly these rows in Xs
+                if (a.rows_per_block != kCpIB)
+                    staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                        const int i = e % kCpIB, l = e / kCpIB;
+                        return (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
+                    }, [&](int e, T v) { X3[(e / kCpIB) * 68 + e % kCpIB] = v; });
                 // a column tile starting past the row tile's last row has no
                 // lower-triangular entries here, nor have the tiles after it
                 for (int64_t cb = cbeg; cb < a.nbk && cb < rr + nr; cb += kCpIB) {
@@ -528,9 +601,10 @@ chol_panel_kernel(CholPanelArgs<T> a)
             const int kbn = int(min64(kCpIB, a.nbk - cbeg));
             __syncthreads();
             if (fast) {
-                // D = old - X X^T on the lower triangle, X = the solved rows in
-                // Xs (row-major, stride 65); the same FMA order as the update
-                // above, so the factor matches the general path bit for bit
+                // D (the old block, fetched at the start of the step) -= X X^T
+                // on the lower triangle, X = the solved rows in Xs ([l][row],
+                // stride 68); the same FMA order as the update above, so the
+                // factor matches the general path bit for bit
                 const int tr = t & 15, tc = t >> 4;      // rows 4 tr + i, columns 4 tc + j
                 if (tc <= tr) {
                     T acc[4][4];
@@ -541,11 +615,8 @@ chol_panel_kernel(CholPanelArgs<T> a)
                     #pragma unroll 4
                     for (int l = 0; l < kb; ++l) {
                         T xr[4], xc[4];
-                        #pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            xr[i] = Xs[(4 * tr + i) * (kCpIB + 1) + l];
-                            xc[i] = Xs[(4 * tc + i) * (kCpIB + 1) + l];
-                        }
+                        lds4(Xs + l * 68 + 4 * tr, xr);
+                        lds4(Xs + l * 68 + 4 * tc, xc);
                         #pragma unroll
                         for (int i = 0; i < 4; ++i)
                             #pragma unroll
@@ -556,7 +627,7 @@ chol_panel_kernel(CholPanelArgs<T> a)
                         #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             const int row = 4 * tr + i, col = 4 * tc + j;
-                            if (row < kbn && col <= row) D[row * (kCpIB + 1) + col] = Us[row * 68 + col] - acc[i][j];
+                            if (row < kbn && col <= row) D[row * (kCpIB + 1) + col] -= acc[i][j];
                         }
                 }
             }
@@ -568,11 +639,13 @@ chol_panel_kernel(CholPanelArgs<T> a)
             }
             __syncthreads();
             const int f = factor_diag_block(D, Dinv, kbn);
+            if (f == 0) build_linv_t(D, Dinv, Us, Xs, kbn);
             for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
                 int i = e % kCpIB, l = e / kCpIB;
                 if (i < kbn && l < kbn && i >= l) P[cbeg + i + (cbeg + l) * ld] = D[i * (kCpIB + 1) + l];
             }
-            for (int e = t; e < kCpDinv; e += kCpThreads) a.dinv_ws[size_t(k + 1) * kCpDinv + e] = Dinv[e];
+            for (int e = t; e < kCpLinv; e += kCpThreads)
+                a.dinv_ws[size_t(k + 1) * kCpLinv + e] = Us[(e / kCpIB) * 68 + e % kCpIB];
             if (t == 0 && f) {
                 atomicCAS(a.info, 0, int(a.info_offset + cbeg + f));
                 *reinterpret_cast<volatile int*>(a.next_fail) = 1;
@@ -635,10 +708,10 @@ static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info
 using namespace slt;
 
 // Device scratch of one panel launch: grid barrier, lookahead failure word
-// and the next diagonal block's sub-block inverses.
+// and, per 64-column step, the diagonal block's transposed inverse.
 extern "C" size_t slt_chol_panel_ws_bytes(void)
 {
-    return 512 + size_t(16) * kCpDinv * sizeof(double);
+    return 512 + size_t(16) * kCpLinv * sizeof(double);
 }
 
 // Factor the Cholesky column panel with top-left P (the diagonal element),
