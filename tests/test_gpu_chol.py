@@ -59,13 +59,15 @@ def test_potrf_known_answer_minij(orc, slt):
 
 
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
-def test_potrf_two_blocks_per_sm(slt, dtype):
+@pytest.mark.parametrize("n", [12288, 20480])
+def test_potrf_two_blocks_per_sm(slt, dtype, n):
     """n = 12288: the first panels need more 64-row blocks than SMs, so two
-    panel blocks share an SM.  The factor must be run-to-run identical (no
-    race between a block's own update and its next-step reads) and, in FP64,
-    solve to backward error <= 3 eps; checked on the device with torch."""
+    panel blocks share an SM.  n = 20480: the first panels give every block
+    two 64-row tiles (the general owner path and a multi-tile row solve).
+    The factor must be run-to-run identical (no race between a block's own
+    update and its next-step reads) and, in FP64, solve to backward error
+    <= 3 eps and match torch's Cholesky; checked on the device with torch."""
     import torch
-    n = 12288
     tdt = getattr(torch, dtype)
     g = torch.Generator(device="cuda").manual_seed(11)
     G = torch.randn(n, n, device="cuda", dtype=torch.float64, generator=g)
