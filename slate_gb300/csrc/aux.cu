@@ -7,13 +7,14 @@
 // R = B - A X (src/gesv_mixed.cc:198-204, src/posv_mixed.cc:201-205) and of
 // the solve sweeps (internal::gemmA, src/internal/internal_gemmA.cc).
 //
-// Skinny products (few right-hand sides) stream A once: a block owns 256 rows
-// and a segment of the columns, keeps one accumulator per right-hand side
-// per row in registers, and writes a partial sum per segment; a second
-// launch adds the segments in a fixed order (deterministic, no atomics).
-// The symmetric variant reads only the lower triangle: tile (I,J) with
-// J > I is read as the transpose of the stored tile (J,I) through shared
-// memory.
+// Skinny products (few right-hand sides) stream A once: a block owns 64 rows
+// and a segment of the columns (64 x 64 tiles, the next tile fetched into
+// registers while the current one is used), keeps one accumulator per
+// right-hand side per row in registers, and writes a partial sum per
+// segment; a second launch adds the segments in a fixed order
+// (deterministic, no atomics).  The symmetric variant reads only the lower
+// triangle: tile (I,J) with J > I is read as the transpose of the stored
+// tile (J,I) through shared memory.
 
 #include "common.cuh"
 #include "prof.h"

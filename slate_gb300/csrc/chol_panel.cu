@@ -6,21 +6,24 @@
 // Here the whole nb-wide panel (rows r0..n-1, columns r0..r0+nb-1) is one
 // cooperative persistent launch.  Block b owns a band of R rows (R a
 // multiple of 64).  For each 64-column step k:
-//   1. every block loads the factored 64 x 64 diagonal block and its 16 x 16
-//      sub-block inverses (step 0: every block factors it itself);
-//   2. every block solves its own rows below it, X = B L^{-T}; the blocks
-//      owning rows of the remaining panel columns ("head" rows, the update
-//      operand of everyone) count themselves done in a per-step counter;
+//   1. every block loads the published inverse of the factored 64 x 64
+//      diagonal block (step 0: every block factors and inverts it itself);
+//   2. every block solves its own rows below it, X = B L^{-T}, as one
+//      register-tiled product with that inverse; the blocks owning rows of
+//      the remaining panel columns ("head" rows, the update operand of
+//      everyone) count themselves done in a per-step counter;
 //   3. every block waits for that counter (a grid barrier at step 0 only) and
 //      updates its rows in the remaining panel columns (rank-64 update);
 //   4. the owner of the next diagonal block -- its only update tile is that
-//      block -- factors it at once and publishes it (L11 in P, the inverses
+//      block -- factors it at once and publishes it (L11 in P, its inverse
 //      and a failure word in the workspace, then a release of the step
-//      number); the next step's blocks wait for exactly that.
+//      number); the next step's blocks wait for exactly that.  With 64-row
+//      blocks the owner skips step 3: it forms the block as D - X X^T from
+//      its own solved rows, still in shared memory.
 // No grid-wide barrier separates the steps: the critical path is the owner
-// chain solve -> diagonal tile update -> factor.  Every wait is a bounded
-// acquire spin (common.cuh), and the cooperative launch keeps all blocks
-// resident, so every awaited block is running.
+// chain solve -> diagonal block update -> factor -> inverse.  Every wait is
+// a bounded acquire spin (common.cuh), and the cooperative launch keeps all
+// blocks resident, so every awaited block is running.
 
 #include "common.cuh"
 #include "prof.h"
@@ -370,9 +373,9 @@ __global__ void __launch_bounds__(kCpThreads, 2)
 chol_panel_kernel(CholPanelArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char cp_smem_raw[];
-    T* D = reinterpret_cast<T*>(cp_smem_raw);             // [64][65] factor, D[i*65 + l] = L(i,l)
-    T* Xs = D + kCpIB * (kCpIB + 1);                        // [64][68] solved rows staging
-    T* Us = Xs + kCpIB * 68;                                // [64][68] update operand
+    T* D = reinterpret_cast<T*>(cp_smem_raw);             // [64][65] diagonal block, D[i*65 + l] = L(i,l)
+    T* Xs = D + kCpIB * (kCpIB + 1);                        // [64][68] solved rows, Xs[l*68 + i]
+    T* Us = Xs + kCpIB * 68;                                // [64][68] inverse (transposed), then update operand
     T* Dinv = Us + kCpIB * 68;                              // [4][16][17] sub-block inverses
     __shared__ int s_fail, s_abort;
     const int G = gridDim.x, b = blockIdx.x, t = threadIdx.x;
