@@ -65,13 +65,18 @@ typedef struct slt_options {
 } slt_options;
 
 /* Refinement of the mixed solvers.  SLT_REFINE_IR is SLATE's gesv_mixed loop
- * (src/gesv_mixed.cc:210-262); SLT_REFINE_IR_GMRES runs that loop while the
- * residual falls by at least half per step and, once it stalls, continues
- * each unconverged column with FGMRES-IR preconditioned by the same
- * low-precision factors (the gesv_mixed_gmres iteration) before any FP64
- * fallback.  The gmres entry points always run FGMRES-IR. */
+ * (src/gesv_mixed.cc:210-262); SLT_REFINE_GMRES makes slt_dsgesv_device /
+ * slt_dsposv_device run SLATE's gesv_mixed_gmres iteration
+ * (src/gesv_mixed_gmres.cc:110-410) instead, as the gmres entry points do;
+ * SLT_REFINE_IR_GMRES runs the IR loop while the residual falls by at least
+ * half per step and, once it stalls, continues each unconverged column with
+ * FGMRES-IR preconditioned by the same low-precision factors before any FP64
+ * fallback.  The gmres entry points always run FGMRES-IR.  The LAPACK-
+ * compatible entry points read it from SLATE_LAPACK_REFINE (ir | gmres |
+ * ir+gmres, default ir). */
 enum slt_refine {
     SLT_REFINE_IR = 0,
+    SLT_REFINE_GMRES = 1,
     SLT_REFINE_IR_GMRES = 2
 };
 
@@ -184,15 +189,18 @@ int slt_dsposv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, co
 
 /* FP64 residual R = B - A X (A n x n general, or symmetric with lower
  * storage when sym_lower != 0), as the kernel layer's slt_dresidual
- * computes it, but with no device allocation and no caller scratch, for
- * callers that cannot allocate where they need it: inside a stream capture,
- * under an allocator that forbids side allocations, or in a latency-bound
- * loop that cannot pay cudaMalloc's device synchronisation.  Its partial sums
- * live in one 16 MiB library-owned __device__ array per device, so
- * n * min(nrhs, 16) may not exceed 2,097,152 (else SLT_ERR_LIMIT, nothing
- * launched).  Calls that overlap on the GPU share that array and race; the
- * first call on a device looks up the array's address and should come before
- * any stream capture.  No counterpart in SLATE. */
+ * computes it, but with no device allocation and no caller scratch.  It is
+ * for callers that cannot allocate device memory where they need a residual:
+ * programs whose device memory belongs to their own pool or to a framework
+ * allocator that forbids side allocations, and code that must not call
+ * cudaMalloc / cudaFree (which can synchronise the whole device) at that
+ * point.  Its partial sums live in one 16 MiB library-owned __device__ array
+ * per device, held until the process exits, so n * min(nrhs, 16) may not
+ * exceed 2,097,152 (else SLT_ERR_LIMIT, nothing launched).  Calls that
+ * overlap on the GPU share that array and race: serialise them.  The first
+ * call on a device looks up the array's device address (with that device
+ * current) and should come before any stream capture.  No counterpart in
+ * SLATE. */
 int slt_dresidual_noalloc(int64_t n, int64_t nrhs, const double* dA, int64_t lda, int sym_lower,
                           const double* dB, int64_t ldb, const double* dX, int64_t ldx,
                           double* dR, int64_t ldr, slt_stream_t stream);
@@ -249,7 +257,9 @@ double slt_timer(const char* name);
 /* LAPACK-compatible entry points (lapack_api/lapack_*.cc).  Host memory.     */
 /* Tile size from SLATE_LAPACK_NB (default 512), inner blocking from          */
 /* SLATE_LAPACK_IB (default 32), factorisation precision of the mixed solvers */
-/* from SLATE_LAPACK_FACTOR_PRECISION (fp32 | tf32 | bf16 | fp16, default fp32).*/
+/* from SLATE_LAPACK_FACTOR_PRECISION (fp32 | tf32 | tf32x3 | bf16 | fp16 |   */
+/* fp8, default fp32), their refinement from SLATE_LAPACK_REFINE (ir | gmres  */
+/* | ir+gmres, default ir).                                                   */
 
 /* lapack_api/lapack_gesv.cc:32 */
 void slate_dgesv(const int* n, const int* nrhs, double* a, const int* lda, int* ipiv,

@@ -766,13 +766,89 @@ inline void rot(double* x, double* y, double c, double s)
     *x = tx; *y = ty;
 }
 
+// One right-hand side of gesv_mixed_gmres / posv_mixed_gmres
+// (src/gesv_mixed_gmres.cc:225-395): right-preconditioned FGMRES with restart
+// min(30, itermax, nb-1), CGS2 orthogonalisation and Givens rotations,
+// starting from the x it is given.  Returns whether the stopping test held;
+// *iter: the Arnoldi steps taken.
+bool fgmres_column(bool chol, int64_t n, const double* A, int64_t lda, LoFactor& lo, const double* B,
+                   double* X, int64_t itermax, int64_t restart, double cte, int64_t* iter)
+{
+    int64_t R1 = restart + 1;
+    std::vector<double> V(size_t(n)*R1), W(size_t(n)*R1), R(n), z(R1);
+    std::vector<double> H(size_t(R1)*R1, 0.0), S(R1, 0.0), gc(std::max<int64_t>(restart, 1)),
+                        gs(std::max<int64_t>(restart, 1));
+    int64_t iiter = 0;
+    double cx = 0, cr = 0;
+    *iter = 0;
+    while (iiter < itermax) {
+        residual(n, 1, A, lda, chol, B, n, X, n, R.data());
+        col_max(n, 1, X, n, &cx);
+        col_max(n, 1, R.data(), n, &cr);
+        if (converged(&cr, &cx, 1, cte)) { *iter = iiter; return true; }
+        double* v0 = V.data();
+        std::copy(R.begin(), R.end(), v0);
+        double ares = 0;
+        for (int64_t i = 0; i < n; ++i) ares += v0[i]*v0[i];
+        ares = std::sqrt(ares);
+        if (ares == 0) { *iter = iiter; return false; }
+        double inv = 1.0 / ares;
+        for (int64_t i = 0; i < n; ++i) v0[i] *= inv;
+        S[0] = ares;
+        for (int64_t i = 1; i < R1; ++i) S[i] = 0;
+        int64_t j = 0;
+        for (; j < restart && iiter < itermax && !converged(&ares, &cx, 1, cte); ++j, ++iiter) {
+            double* vj1 = V.data() + (j+1)*n;
+            double* wj1 = W.data() + (j+1)*n;
+            lo.solve(1, V.data() + j*n, n, wj1, n);
+            if (chol) residual(n, 1, A, lda, true, std::vector<double>(n, 0.0).data(), n, wj1, n, vj1);
+            else gemm('N', 'N', n, 1, n, 1.0, A, lda, wj1, n, 0.0, vj1, n);
+            if (chol) for (int64_t i = 0; i < n; ++i) vj1[i] = -vj1[i];
+            // CGS2
+            double* hj = H.data() + j*R1;
+            gemm('T', 'N', j+1, 1, n, 1.0, V.data(), n, vj1, n, 0.0, hj, R1);
+            gemm('N', 'N', n, 1, j+1, -1.0, V.data(), n, hj, R1, 1.0, vj1, n);
+            gemm('T', 'N', j+1, 1, n, 1.0, V.data(), n, vj1, n, 0.0, z.data(), R1);
+            gemm('N', 'N', n, 1, j+1, -1.0, V.data(), n, z.data(), R1, 1.0, vj1, n);
+            for (int64_t i = 0; i <= j; ++i) hj[i] += z[i];
+            double nrm = 0;
+            for (int64_t i = 0; i < n; ++i) nrm += vj1[i]*vj1[i];
+            nrm = std::sqrt(nrm);
+            double sc = 1.0 / nrm;
+            for (int64_t i = 0; i < n; ++i) vj1[i] *= sc;
+            hj[j+1] = nrm;
+            for (int64_t i = 0; i < j; ++i) rot(&hj[i], &hj[i+1], gc[i], gs[i]);
+            rotg(hj[j], hj[j+1], &gc[j], &gs[j]);
+            rot(&hj[j], &hj[j+1], gc[j], gs[j]);
+            rot(&S[j], &S[j+1], gc[j], gs[j]);
+            ares = std::abs(S[j+1]);
+        }
+        // X += W(:, 1:j) * (H(0:j-1, 0:j-1)^{-1} S(0:j-1))
+        std::vector<double> y(S.begin(), S.begin() + j);
+        for (int64_t r = j - 1; r >= 0; --r) {
+            double s = y[r];
+            for (int64_t c = r + 1; c < j; ++c) s -= H[r + c*R1] * y[c];
+            y[r] = s / H[r + r*R1];
+        }
+        for (int64_t c = 0; c < j; ++c) {
+            const double* w = W.data() + (c+1)*n;
+            for (int64_t i = 0; i < n; ++i) X[i] += w[i] * y[c];
+        }
+    }
+    *iter = iiter;
+    return false;
+}
+
 // gesv_mixed_gmres / posv_mixed_gmres (src/gesv_mixed_gmres.cc:110-410,
-// src/posv_mixed_gmres.cc:109-436): right-preconditioned FGMRES with restart
-// min(30, itermax, nb-1), CGS2 orthogonalisation and Givens rotations; one
-// right-hand side.
-int64_t mixed_gmres(bool chol, int64_t n, double* A, int64_t lda, int64_t* pt, int64_t* po,
-                    const double* B, double* X, int64_t nb, int64_t ib, int nthreads,
-                    int64_t itermax, double tol, int use_fallback, int64_t* iter)
+// src/posv_mixed_gmres.cc:109-436).  SLATE takes one right-hand side; with
+// nrhs > 1 every column is an independent instance of that iteration sharing
+// the one factorisation.  iter: the largest column count when all converge,
+// else -(itermax+1) (the fallback then solves every column); col_iter, when
+// given, receives each column's count (-(itermax+1) where it failed).
+int64_t mixed_gmres(bool chol, int64_t n, int64_t nrhs, double* A, int64_t lda, int64_t* pt, int64_t* po,
+                    const double* B, int64_t ldb, double* X, int64_t ldx, int64_t nb, int64_t ib,
+                    int nthreads, int64_t itermax, double tol, int use_fallback, int64_t* iter,
+                    int64_t* col_iter = nullptr)
 {
     const double eps = std::numeric_limits<double>::epsilon();
     if (tol <= 0) tol = eps * std::sqrt(double(n));
@@ -781,81 +857,106 @@ int64_t mixed_gmres(bool chol, int64_t n, double* A, int64_t lda, int64_t* pt, i
     double cte = Anorm * tol;
     LoFactor lo{chol, n, nb, ib, nthreads, {}, {}, {}};
     int64_t info = lo.factor(A, lda);
-    bool conv = false;
+    bool conv = true;
     *iter = 0;
     if (info != 0) {
         *iter = -3;
+        conv = false;
     }
     else {
         if (!chol) { std::copy(lo.pt.begin(), lo.pt.end(), pt); std::copy(lo.po.begin(), lo.po.end(), po); }
-        int64_t R1 = restart + 1;
-        std::vector<double> V(size_t(n)*R1), W(size_t(n)*R1), R(n), z(R1);
-        std::vector<double> H(size_t(R1)*R1, 0.0), S(R1, 0.0), gc(std::max<int64_t>(restart, 1)),
-                            gs(std::max<int64_t>(restart, 1));
-        lo.solve(1, B, n, X, n);
-        int64_t iiter = 0;
-        double cx = 0, cr = 0;
-        while (iiter < itermax) {
-            residual(n, 1, A, lda, chol, B, n, X, n, R.data());
-            col_max(n, 1, X, n, &cx);
-            col_max(n, 1, R.data(), n, &cr);
-            if (converged(&cr, &cx, 1, cte)) { *iter = iiter; conv = true; break; }
-            double* v0 = V.data();
-            std::copy(R.begin(), R.end(), v0);
-            double ares = 0;
-            for (int64_t i = 0; i < n; ++i) ares += v0[i]*v0[i];
-            ares = std::sqrt(ares);
-            if (ares == 0) { *iter = iiter; conv = false; break; }
-            double inv = 1.0 / ares;
-            for (int64_t i = 0; i < n; ++i) v0[i] *= inv;
-            S[0] = ares;
-            for (int64_t i = 1; i < R1; ++i) S[i] = 0;
-            int64_t j = 0;
-            for (; j < restart && iiter < itermax && !converged(&ares, &cx, 1, cte); ++j, ++iiter) {
-                double* vj1 = V.data() + (j+1)*n;
-                double* wj1 = W.data() + (j+1)*n;
-                lo.solve(1, V.data() + j*n, n, wj1, n);
-                if (chol) residual(n, 1, A, lda, true, std::vector<double>(n, 0.0).data(), n, wj1, n, vj1);
-                else gemm('N', 'N', n, 1, n, 1.0, A, lda, wj1, n, 0.0, vj1, n);
-                if (chol) for (int64_t i = 0; i < n; ++i) vj1[i] = -vj1[i];
-                // CGS2
-                double* hj = H.data() + j*R1;
-                gemm('T', 'N', j+1, 1, n, 1.0, V.data(), n, vj1, n, 0.0, hj, R1);
-                gemm('N', 'N', n, 1, j+1, -1.0, V.data(), n, hj, R1, 1.0, vj1, n);
-                gemm('T', 'N', j+1, 1, n, 1.0, V.data(), n, vj1, n, 0.0, z.data(), R1);
-                gemm('N', 'N', n, 1, j+1, -1.0, V.data(), n, z.data(), R1, 1.0, vj1, n);
-                for (int64_t i = 0; i <= j; ++i) hj[i] += z[i];
-                double nrm = 0;
-                for (int64_t i = 0; i < n; ++i) nrm += vj1[i]*vj1[i];
-                nrm = std::sqrt(nrm);
-                double sc = 1.0 / nrm;
-                for (int64_t i = 0; i < n; ++i) vj1[i] *= sc;
-                hj[j+1] = nrm;
-                for (int64_t i = 0; i < j; ++i) rot(&hj[i], &hj[i+1], gc[i], gs[i]);
-                rotg(hj[j], hj[j+1], &gc[j], &gs[j]);
-                rot(&hj[j], &hj[j+1], gc[j], gs[j]);
-                rot(&S[j], &S[j+1], gc[j], gs[j]);
-                ares = std::abs(S[j+1]);
-            }
-            // X += W(:, 1:j) * (H(0:j-1, 0:j-1)^{-1} S(0:j-1))
-            std::vector<double> y(S.begin(), S.begin() + j);
-            for (int64_t r = j - 1; r >= 0; --r) {
-                double s = y[r];
-                for (int64_t c = r + 1; c < j; ++c) s -= H[r + c*R1] * y[c];
-                y[r] = s / H[r + r*R1];
-            }
-            for (int64_t c = 0; c < j; ++c) {
-                const double* w = W.data() + (c+1)*n;
-                for (int64_t i = 0; i < n; ++i) X[i] += w[i] * y[c];
-            }
+        std::vector<double> b(n), x(n);
+        for (int64_t c = 0; c < nrhs; ++c) {
+            std::copy(B + c*ldb, B + c*ldb + n, b.begin());
+            lo.solve(1, b.data(), n, x.data(), n);
+            int64_t it = 0;
+            const bool cc = fgmres_column(chol, n, A, lda, lo, b.data(), x.data(), itermax, restart, cte, &it);
+            std::copy(x.begin(), x.end(), X + c*ldx);
+            if (col_iter) col_iter[c] = cc ? it : -itermax - 1;
+            conv = conv && cc;
+            if (cc) *iter = std::max(*iter, it);
         }
     }
     if (!conv) {
         if (info == 0) *iter = -itermax - 1;
         if (use_fallback)
-            info = fallback_solve(chol, n, 1, A, lda, nb, ib, nthreads, pt, po, B, n, X, n);
+            info = fallback_solve(chol, n, nrhs, A, lda, nb, ib, nthreads, pt, po, B, ldb, X, ldx);
     }
     return info;
+}
+
+// Prescribed-spectrum test matrix, the CPU statement of the library's
+// device generator (slate_gb300/csrc/matgen.cu): A = Q1 diag(sigma) Q2^T
+// (spd = 0) or Q diag(sigma) Q^T (spd = 1), sigma geo (dist 0) or logrand
+// (dist 1) of condition number cond (SLATE's matgen/generate_sigma.hh:73-125),
+// Q a product of log2(n) butterfly levels: level l rotates rows (i, i + 2^l)
+// inside blocks of 2^(l+1) by the angle 2 pi u (u from Philox(i, l, seed)),
+// after a sign flip of row i by the low bit of the second Philox word.
+void generate_sigma(int64_t n, double cond, int dist, int spd, int64_t seed, double* A, int64_t lda)
+{
+    auto unit = [](uint64_t bits) { return double(bits >> 11) / double(uint64_t(1) << 53); };
+    for (int64_t j = 0; j < n; ++j)
+        std::fill(A + j*lda, A + j*lda + n, 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        double sg;
+        if (dist == 0) sg = (n > 1) ? std::pow(cond, -double(i) / double(n - 1)) : 1.0;
+        else {
+            uint64_t b[2];
+            philox2x64(uint64_t(i), 0ull, uint64_t(seed), b);
+            sg = std::exp(unit(b[0]) * std::log(1.0 / cond));
+            if (n >= 2 && i == 0) sg = 1.0;
+            if (n >= 2 && i == 1) sg = 1.0 / cond;
+        }
+        A[i + i*lda] = sg;
+    }
+    int levels = 0;
+    while ((int64_t(1) << levels) < n) ++levels;
+    std::vector<int64_t> pi, pk;
+    std::vector<double> rc, rs, rsi, qc, qs, qsi;
+    auto rots = [&](int l, int64_t sd, std::vector<double>& c, std::vector<double>& sn, std::vector<double>& si) {
+        c.resize(pi.size()); sn.resize(pi.size()); si.resize(pi.size());
+        for (size_t p = 0; p < pi.size(); ++p) {
+            uint64_t b[2];
+            philox2x64(uint64_t(pi[p]), uint64_t(l), uint64_t(sd), b);
+            const double th = 6.283185307179586 * unit(b[0]);
+            c[p] = std::cos(th);
+            sn[p] = std::sin(th);
+            si[p] = (b[1] & 1) ? -1.0 : 1.0;
+        }
+    };
+    for (int l = 0; l < levels; ++l) {
+        const int64_t h = int64_t(1) << l;
+        pi.clear(); pk.clear();
+        for (int64_t i0 = 0; i0 < n; i0 += 2*h)
+            for (int64_t i = i0; i < std::min(i0 + h, n); ++i)
+                if (i + h < n) { pi.push_back(i); pk.push_back(i + h); }
+        if (pi.empty()) continue;
+        rots(l, seed + 101, rc, rs, rsi);
+        if (spd) { qc = rc; qs = rs; qsi = rsi; }
+        else rots(l, seed + 202, qc, qs, qsi);
+        const int64_t np = int64_t(pi.size());
+        // rows: A <- R_l A
+        #pragma omp parallel for schedule(static)
+        for (int64_t j = 0; j < n; ++j) {
+            double* col = A + j*lda;
+            for (int64_t p = 0; p < np; ++p) {
+                const double xi = rsi[p] * col[pi[p]], yk = col[pk[p]];
+                col[pi[p]] = rc[p] * xi + rs[p] * yk;
+                col[pk[p]] = -rs[p] * xi + rc[p] * yk;
+            }
+        }
+        // columns: A <- A R_l^T
+        #pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < np; ++p) {
+            double* x = A + pi[p]*lda;
+            double* y = A + pk[p]*lda;
+            for (int64_t r = 0; r < n; ++r) {
+                const double xi = qsi[p] * x[r], yk = y[r];
+                x[r] = qc[p] * xi + qs[p] * yk;
+                y[r] = -qs[p] * xi + qc[p] * yk;
+            }
+        }
+    }
 }
 
 } // namespace
@@ -1029,7 +1130,7 @@ int64_t orc_dgesv_mixed_gmres(int64_t n, double* A, int64_t lda, int64_t* piv_ti
                               int64_t ib, int panel_threads, int64_t itermax, double tol,
                               int use_fallback, int64_t* iter)
 {
-    return mixed_gmres(false, n, A, lda, piv_tile, piv_off, B, X, nb, ib, panel_threads,
+    return mixed_gmres(false, n, 1, A, lda, piv_tile, piv_off, B, n, X, n, nb, ib, panel_threads,
                        itermax, tol, use_fallback, iter);
 }
 
@@ -1037,8 +1138,29 @@ int64_t orc_dposv_mixed_gmres(int64_t n, double* A, int64_t lda, const double* B
                               int64_t nb, int64_t itermax, double tol, int use_fallback,
                               int64_t* iter)
 {
-    return mixed_gmres(true, n, A, lda, nullptr, nullptr, B, X, nb, 16, 1, itermax, tol,
+    return mixed_gmres(true, n, 1, A, lda, nullptr, nullptr, B, n, X, n, nb, 16, 1, itermax, tol,
                        use_fallback, iter);
+}
+// Several right-hand sides, each an independent FGMRES-IR instance sharing
+// one factorisation; col_iter (nrhs entries) receives each column's count.
+int64_t orc_dgesv_mixed_gmres_nrhs(int64_t n, int64_t nrhs, double* A, int64_t lda, int64_t* piv_tile,
+                                   int64_t* piv_off, const double* B, int64_t ldb, double* X, int64_t ldx,
+                                   int64_t nb, int64_t ib, int panel_threads, int64_t itermax, double tol,
+                                   int use_fallback, int64_t* iter, int64_t* col_iter)
+{
+    return mixed_gmres(false, n, nrhs, A, lda, piv_tile, piv_off, B, ldb, X, ldx, nb, ib, panel_threads,
+                       itermax, tol, use_fallback, iter, col_iter);
+}
+int64_t orc_dposv_mixed_gmres_nrhs(int64_t n, int64_t nrhs, double* A, int64_t lda, const double* B,
+                                   int64_t ldb, double* X, int64_t ldx, int64_t nb, int64_t itermax,
+                                   double tol, int use_fallback, int64_t* iter, int64_t* col_iter)
+{
+    return mixed_gmres(true, n, nrhs, A, lda, nullptr, nullptr, B, ldb, X, ldx, nb, 16, 1, itermax, tol,
+                       use_fallback, iter, col_iter);
+}
+void orc_dgenerate_sigma(int64_t n, double cond, int dist, int spd, int64_t seed, double* A, int64_t lda)
+{
+    generate_sigma(n, cond, dist, spd, seed, A, lda);
 }
 
 // Tester check (test/test_gesv.cc:330-380):

@@ -44,6 +44,8 @@ def lib():
         L.orc_dposv_mixed.restype = i64
         L.orc_dgesv_mixed_gmres.restype = i64
         L.orc_dposv_mixed_gmres.restype = i64
+        L.orc_dposv_mixed_gmres_nrhs.restype = i64
+        L.orc_dgesv_mixed_gmres_nrhs.restype = i64
         L.orc_backward_error.restype = dbl
         L.orc_get_threads.restype = ctypes.c_int
         _LIB = L
@@ -59,6 +61,53 @@ def ref_lib():
             return None
         _REF = ctypes.CDLL(path)
     return _REF
+
+
+_REF_GETRF = None
+
+
+def ref_getrf_lib():
+    """SLATE's own tile LU panel (src/internal/Tile_getrf.hh) built by
+    oracle/build_ref.sh, or None."""
+    global _REF_GETRF
+    if _REF_GETRF is None:
+        path = os.path.join(_HERE, "_ref", "libref_getrf.so")
+        if not os.path.exists(path):
+            return None
+        L = ctypes.CDLL(path)
+        for f in (L.ref_getrf_panel_d, L.ref_getrf_d):
+            f.restype = i64
+        _REF_GETRF = L
+    return _REF_GETRF
+
+
+def ref_getrf_panel(A, nb, ib, threshold=1.0, threads=1):
+    """SLATE's tile::getrf on the m x nb panel A (tiles of nb rows), run by
+    `threads` panel threads as internal::getrf_panel<HostTask> does.  Returns
+    (info, piv_tile, piv_off, factored panel)."""
+    L = ref_getrf_lib()
+    P = np.asfortranarray(np.array(A, dtype=np.float64))
+    m = P.shape[0]
+    d = min(m, nb)
+    pt = np.zeros(max(d, 1), np.int64)
+    po = np.zeros(max(d, 1), np.int64)
+    info = L.ref_getrf_panel_d(i64(m), i64(nb), i64(nb), _p(P), i64(max(m, 1)), i64(ib), ctypes.c_int(threads),
+                               dbl(threshold), _p(pt), _p(po))
+    return int(info), pt[:d], po[:d], P
+
+
+def ref_getrf(A, nb, ib, threshold=1.0, threads=1):
+    """Right-looking LU whose panels are SLATE's tile::getrf.  Returns (info,
+    piv_tile, piv_off, factors)."""
+    L = ref_getrf_lib()
+    P = np.asfortranarray(np.array(A, dtype=np.float64))
+    m, n = P.shape
+    mn = min(m, n)
+    pt = np.zeros(max(mn, 1), np.int64)
+    po = np.zeros(max(mn, 1), np.int64)
+    info = L.ref_getrf_d(i64(m), i64(n), _p(P), i64(max(m, 1)), i64(nb), i64(ib), ctypes.c_int(threads),
+                         dbl(threshold), _p(pt), _p(po))
+    return int(info), pt[:mn], po[:mn], P
 
 
 def _p(a):
@@ -241,6 +290,46 @@ def posv_mixed_gmres(A, b, nb, itermax=30, tol=0.0, use_fallback=True):
                                        i64(itermax), dbl(tol), ctypes.c_int(int(use_fallback)),
                                        ctypes.byref(it))
     return int(info), X, int(it.value)
+
+
+def posv_mixed_gmres_nrhs(A, B, nb, itermax=30, tol=0.0, use_fallback=True):
+    """posv_mixed_gmres on every column of B (independent FGMRES-IR instances
+    sharing one factorisation).  Returns (info, X, iter, per-column iters)."""
+    n, nrhs = B.shape
+    B = np.asfortranarray(B)
+    X = np.zeros((n, nrhs), order="F")
+    it = i64(0)
+    ci = np.zeros(nrhs, np.int64)
+    info = lib().orc_dposv_mixed_gmres_nrhs(i64(n), i64(nrhs), _p(A), i64(n), _p(B), i64(n), _p(X), i64(n),
+                                            i64(nb), i64(itermax), dbl(tol), ctypes.c_int(int(use_fallback)),
+                                            ctypes.byref(it), _p(ci))
+    return int(info), X, int(it.value), ci
+
+
+def gesv_mixed_gmres_nrhs(A, B, nb, ib=16, itermax=30, tol=0.0, use_fallback=True, panel_threads=1):
+    """gesv_mixed_gmres on every column of B.  Returns (info, X, iter,
+    per-column iters, pivot tiles, pivot offsets)."""
+    n, nrhs = B.shape
+    B = np.asfortranarray(B)
+    X = np.zeros((n, nrhs), order="F")
+    pt = np.zeros(n, np.int64)
+    po = np.zeros(n, np.int64)
+    it = i64(0)
+    ci = np.zeros(nrhs, np.int64)
+    info = lib().orc_dgesv_mixed_gmres_nrhs(i64(n), i64(nrhs), _p(A), i64(n), _p(pt), _p(po), _p(B), i64(n),
+                                            _p(X), i64(n), i64(nb), i64(ib), ctypes.c_int(panel_threads),
+                                            i64(itermax), dbl(tol), ctypes.c_int(int(use_fallback)),
+                                            ctypes.byref(it), _p(ci))
+    return int(info), X, int(it.value), ci, pt, po
+
+
+def generate_sigma(n, cond, dist="geo", spd=False, seed=1):
+    """Prescribed-spectrum matrix, the CPU statement of the library's device
+    generator (same Philox draws; cos/sin may differ in the last bit)."""
+    A = np.empty((n, n), order="F")
+    lib().orc_dgenerate_sigma(i64(n), dbl(cond), ctypes.c_int({"geo": 0, "logrand": 1}[dist]),
+                              ctypes.c_int(int(bool(spd))), i64(seed), _p(A), i64(n))
+    return A
 
 
 # ---------------------------------------------------------------------------

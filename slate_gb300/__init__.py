@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_HERE, "libslate_gb300.so")
 
 PREC_FP64, PREC_FP32, PREC_TF32, PREC_BF16, PREC_FP16 = 0, 1, 2, 3, 4
 _PREC_NAMES = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "fp16": 4, "fp8": 5, "tf32x3": 6}
-_REFINE_NAMES = {"ir": 0, "ir+gmres": 2}
+_REFINE_NAMES = {"ir": 0, "gmres": 1, "ir+gmres": 2}
 
 
 class SlateError(RuntimeError):
@@ -50,7 +50,7 @@ class Options:
     pivot_threshold: float = 1.0
     factor_precision: object = "fp32"
     gemm_engine: int = 0
-    refine: object = "ir"          # "ir" (SLATE) or "ir+gmres" (GMRES-IR once IR stalls)
+    refine: object = "ir"          # "ir" (SLATE's IR), "gmres" (FGMRES-IR) or "ir+gmres" (GMRES-IR once IR stalls)
     equilibrate: int = -1          # -1 auto (on for bf16/fp16), 0 off, 1 on
     lo_retry: int = -1             # -1 auto (on for bf16/fp16): FP32 retry before the FP64 fallback
     depth: int = 2                 # Option::Depth of gesv_rbt's butterflies

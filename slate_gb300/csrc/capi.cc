@@ -142,6 +142,12 @@ slt_options lapack_opts()
         else if (v == "fp8") o.factor_precision = SLT_PREC_FP8;
         else if (v == "tf32x3") o.factor_precision = SLT_PREC_TF32X3;
     }
+    if (const char* p = std::getenv("SLATE_LAPACK_REFINE")) {
+        std::string v(p);
+        if (v == "ir") o.refine = SLT_REFINE_IR;
+        else if (v == "gmres") o.refine = SLT_REFINE_GMRES;
+        else if (v == "ir+gmres") o.refine = SLT_REFINE_IR_GMRES;
+    }
     return o;
 }
 
@@ -350,6 +356,9 @@ int slt_dsgesv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, int* d_i
                       int* iter, int64_t* info)
 {
     slt_options o = resolve(opts);
+    if (o.refine == SLT_REFINE_GMRES)
+        return gesv_mixed_gmres_dev(0, n, nrhs, dA, lda, d_ipiv, dB, ldb, dX, ldx, o, iter, info,
+                                    as_stream(stream));
     return gesv_mixed_dev(0, n, nrhs, dA, lda, d_ipiv, dB, ldb, dX, ldx, o, iter, info, as_stream(stream));
 }
 
@@ -367,6 +376,9 @@ int slt_dsposv_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, const do
                       int64_t* info)
 {
     slt_options o = resolve(opts);
+    if (o.refine == SLT_REFINE_GMRES)
+        return gesv_mixed_gmres_dev(1, n, nrhs, dA, lda, nullptr, dB, ldb, dX, ldx, o, iter, info,
+                                    as_stream(stream));
     return gesv_mixed_dev(1, n, nrhs, dA, lda, nullptr, dB, ldb, dX, ldx, o, iter, info, as_stream(stream));
 }
 

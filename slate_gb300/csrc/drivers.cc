@@ -422,129 +422,247 @@ bool converged(const double* cr, const double* cx, int64_t k, double cte)
     return true;
 }
 
-// Right-preconditioned FGMRES(restart) for one right-hand side
-// (src/gesv_mixed_gmres.cc:225-395): CGS2 Arnoldi in FP64 on the GPU, the
-// preconditioner the low-precision factors, Givens rotations and the small
-// triangular solve on the host.  Starts from the x it is given.
-struct Fgmres {
+// Right-preconditioned FGMRES(restart) (src/gesv_mixed_gmres.cc:225-395),
+// run for up to 16 right-hand sides in lockstep.  Every column is its own
+// instance of SLATE's single-right-hand-side iteration -- CGS2 Arnoldi in
+// FP64 on the GPU, the low-precision factors as preconditioner, Givens
+// rotations and the small triangular solve on the host -- with its own
+// restart cycles and stopping test.  What the columns share is the traffic:
+// each tick applies the preconditioner to every column that is in an
+// Arnoldi step with one sweep pair over the factors, and forms every
+// product A w (Arnoldi step) and residual b - A x (start of a restart cycle)
+// with one pass over A, instead of one pass per column.  Starts from the x it
+// is given.
+struct FgmresBlock {
+    static constexpr int64_t kMaxCols = 16;
     int chol;
     int64_t n;
     const double* A;
     int64_t lda;
     LoFactor& lo;
     double cte;
-    int64_t restart = 0, R1 = 1;
-    DevBuf nws, scal, V, W, Wlo;
+    int64_t restart = 0, R1 = 1, SC = 0;
+    DevBuf nws, scal, V, W, Z, Bg, Rg, Wlo;
+    std::vector<double> hs;
 
-    Fgmres(int chol_, int64_t n_, const double* A_, int64_t lda_, LoFactor& lo_, double cte_)
+    struct Col {
+        int64_t c = 0;             // column of B and X
+        int st = 0;                // 0: start of a restart cycle, 1: Arnoldi step, 2: done
+        int64_t iiter = 0, j = 0;
+        double cx = 0, ares = 0;
+        bool conv = false, stopped = false;
+        int citer = 0;
+        std::vector<double> H, S, gc, gs, y;
+    };
+
+    FgmresBlock(int chol_, int64_t n_, const double* A_, int64_t lda_, LoFactor& lo_, double cte_)
         : chol(chol_), n(n_), A(A_), lda(lda_), lo(lo_), cte(cte_) {}
 
     int init(int64_t itermax, int64_t nb, cudaStream_t s) {
         restart = std::max<int64_t>(0, std::min<int64_t>(std::min<int64_t>(30, itermax), std::min(nb, n) - 1));
         R1 = restart + 1;
-        TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, 1)), s));
-        TRY(scal.alloc(sizeof(double) * (4 + 4 * R1), s));
-        TRY(V.alloc(sizeof(double) * size_t(n) * size_t(R1), s));
-        TRY(W.alloc(sizeof(double) * size_t(n) * size_t(R1), s));
-        return Wlo.alloc(sizeof(float) * size_t(n), s);
+        SC = 4 + 3 * R1;           // per column: cx, cr, ares, nrm | h | z | y
+        const size_t nn = size_t(n);
+        TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, kMaxCols)), s));
+        TRY(scal.alloc(sizeof(double) * size_t(SC * kMaxCols), s));
+        TRY(V.alloc(sizeof(double) * nn * size_t(R1 * kMaxCols), s));
+        TRY(W.alloc(sizeof(double) * nn * size_t(R1 * kMaxCols), s));
+        TRY(Z.alloc(sizeof(double) * nn * size_t(kMaxCols), s));
+        TRY(Bg.alloc(sizeof(double) * nn * size_t(kMaxCols), s));
+        TRY(Rg.alloc(sizeof(double) * nn * size_t(kMaxCols), s));
+        hs.assign(size_t(SC * kMaxCols), 0.0);
+        return Wlo.alloc(sizeof(float) * nn * size_t(kMaxCols), s);
     }
 
-    // Runs until the stopping test holds or itermax Arnoldi steps are spent.
-    // *used: the steps taken; *conv: whether the test held.  SLATE's loop
-    // tests the true residual only at the top of a restart cycle, so a cycle
-    // that ends on the budget is never tested; final_check (used by the
-    // IR -> GMRES-IR chain, which is not SLATE's driver) tests it once more.
-    int run(const double* b, int64_t ldb, double* x, int64_t ldx, int64_t itermax, int* used, bool* conv,
-            cudaStream_t s, bool final_check = false) {
-        double* Vd = V.as<double>();
-        double* Wd = W.as<double>();
-        float* wlo = Wlo.as<float>();
-        double* dsc = scal.as<double>();
-        double* dh = dsc + 4;
-        double* dz = dh + R1;
-        double* dy = dz + R1;
-        std::vector<double> H(size_t(R1) * size_t(R1)), S(R1), gc(R1), gs(R1), hh(2 * R1);
-        *conv = false;
-        int64_t iiter = 0;
-        int citer = 0;
-        bool stopped = false;
-        while (iiter < itermax) {
-            // residual and stopping test
-            TRY(slt_dresidual(n, 1, A, lda, chol, b, ldb, x, ldx, Vd, n, nws.p, s));
-            TRY(slt_dcolmax(n, 1, x, ldx, dsc, s));
-            TRY(slt_dcolmax(n, 1, Vd, n, dsc + 1, s));
-            TRY(slt_dnrm2(n, Vd, dsc + 2, s));
-            double hv[3];
-            TRY(read_doubles(dsc, hv, 3, s));
-            const double cx = hv[0], cr = hv[1];
-            if (cr <= cx * cte) { citer = int(iiter); *conv = true; stopped = true; break; }
-            double ares = hv[2];
-            if (ares == 0) { citer = int(iiter); stopped = true; break; }
-            TRY(slt_dgeadd(n, 1, 1.0 / ares, Vd, n, 0.0, Vd, n, s));
-            S.assign(R1, 0.0);
-            S[0] = ares;
-            int64_t j = 0;
-            for (; j < restart && iiter < itermax && !(ares <= cx * cte); ++j, ++iiter) {
+    double* Vc(int64_t q) const { return V.as<double>() + size_t(q) * size_t(n) * size_t(R1); }
+    double* Wc(int64_t q) const { return W.as<double>() + size_t(q) * size_t(n) * size_t(R1); }
+    double* Sc(int64_t q) const { return scal.as<double>() + q * SC; }
+
+    static int copy_col(const double* src, double* dst, int64_t n, cudaStream_t s) {
+        SLT_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice, s));
+        return SLT_OK;
+    }
+
+    // End of a restart cycle: x += W(:, 1:j) H(0:j-1, 0:j-1)^{-1} S(0:j-1).
+    int cycle_end(Col& cl, int64_t q, double* X, int64_t ldx, cudaStream_t s) {
+        const int64_t j = cl.j;
+        if (j > 0) {
+            cl.y.assign(cl.S.begin(), cl.S.begin() + j);
+            for (int64_t rr = j - 1; rr >= 0; --rr) {
+                double sum = cl.y[rr];
+                for (int64_t cc = rr + 1; cc < j; ++cc) sum -= cl.H[rr + cc * R1] * cl.y[cc];
+                cl.y[rr] = sum / cl.H[rr + rr * R1];
+            }
+            double* dy = Sc(q) + 4 + 2 * R1;
+            SLT_CUDA_TRY(cudaMemcpyAsync(dy, cl.y.data(), sizeof(double) * size_t(j), cudaMemcpyHostToDevice, s));
+            TRY(slt_dgemm_skinny(n, 1, j, 1.0, Wc(q) + n, n, 0, dy, R1, 1.0, X + cl.c * ldx, ldx, nws.p, s));
+        }
+        cl.st = 0;
+        return SLT_OK;
+    }
+
+    // The loop condition of the Arnoldi steps; false ends the restart cycle.
+    bool keep_going(const Col& cl, int64_t itermax) const {
+        return cl.j < restart && cl.iiter < itermax && !(cl.ares <= cl.cx * cte);
+    }
+
+    // R(:, 0:k) = Bg(:, 0:k) - A Z(:, 0:k), in chunks of 16 columns.
+    int products(int64_t k, cudaStream_t s) {
+        return slt_dresidual(n, k, A, lda, chol, Bg.as<double>(), n, Z.as<double>(), n, Rg.as<double>(), n,
+                             nws.p, s);
+    }
+
+    // Runs the columns cols[0..k) (k <= 16) until each one's stopping test
+    // holds or it has spent itermax Arnoldi steps.  used[i]: the steps column
+    // cols[i] took; conv[i]: whether its test held.  SLATE's loop tests the
+    // true residual only at the top of a restart cycle, so a cycle that ends
+    // on the budget is never tested; final_check (used by the IR -> GMRES-IR
+    // chain, which is not SLATE's driver) tests it once more.
+    int run(const int64_t* cols, int64_t k, const double* B, int64_t ldb, double* X, int64_t ldx,
+            int64_t itermax, int* used, bool* conv, cudaStream_t s, bool final_check = false) {
+        std::vector<Col> cl(k);
+        for (int64_t q = 0; q < k; ++q) {
+            cl[q].c = cols[q];
+            cl[q].H.assign(size_t(R1 * R1), 0.0);
+            cl[q].S.assign(R1, 0.0);
+            cl[q].gc.assign(R1, 0.0);
+            cl[q].gs.assign(R1, 0.0);
+        }
+        double* z = Z.as<double>();
+        double* bg = Bg.as<double>();
+        double* rg = Rg.as<double>();
+        std::vector<int64_t> arn, st;
+        for (;;) {
+            arn.clear();
+            st.clear();
+            for (int64_t q = 0; q < k; ++q) {
+                if (cl[q].st == 0 && !(cl[q].iiter < itermax)) cl[q].st = 2;   // budget spent
+                if (cl[q].st == 1) arn.push_back(q);
+                else if (cl[q].st == 0) st.push_back(q);
+            }
+            if (arn.empty() && st.empty()) break;
+            const int64_t na = int64_t(arn.size()), ns = int64_t(st.size());
+            // preconditioner: w = M^{-1} v_j for every column in an Arnoldi step
+            for (int64_t i = 0; i < na; ++i) {
+                const Col& c = cl[arn[i]];
+                TRY(copy_col(Vc(arn[i]) + c.j * n, z + i * n, n, s));
+            }
+            if (na) {
+                TRY(lo.solve(na, z, n, z, n, Wlo.as<float>(), s));
+                for (int64_t i = 0; i < na; ++i)
+                    TRY(copy_col(z + i * n, Wc(arn[i]) + (cl[arn[i]].j + 1) * n, n, s));
+                SLT_CUDA_TRY(cudaMemsetAsync(bg, 0, sizeof(double) * size_t(n) * size_t(na), s));
+            }
+            // one pass over A: -A w (Arnoldi steps) and b - A x (cycle starts)
+            for (int64_t i = 0; i < ns; ++i) {
+                const Col& c = cl[st[i]];
+                TRY(copy_col(X + c.c * ldx, z + (na + i) * n, n, s));
+                TRY(copy_col(B + c.c * ldb, bg + (na + i) * n, n, s));
+            }
+            TRY(products(na + ns, s));
+            for (int64_t i = 0; i < na; ++i) {
+                const int64_t q = arn[i];
+                const int64_t j = cl[q].j;
+                double* Vd = Vc(q);
                 double* vj1 = Vd + (j + 1) * n;
-                double* wj1 = Wd + (j + 1) * n;
-                TRY(lo.solve(1, Vd + j * n, n, wj1, n, wlo, s));
-                TRY(slt_dgemm_skinny(n, 1, n, 1.0, A, lda, chol, wj1, n, 0.0, vj1, n, nws.p, s));
+                double* dh = Sc(q) + 4;
+                double* dz = dh + R1;
+                TRY(slt_dgeadd(n, 1, -1.0, rg + i * n, n, 0.0, vj1, n, s));
                 // CGS2
                 TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dh, R1, s));
                 TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dh, R1, 1.0, vj1, n, nws.p, s));
                 TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dz, R1, s));
                 TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dz, R1, 1.0, vj1, n, nws.p, s));
-                TRY(slt_dnrm2(n, vj1, dsc + 3, s));
-                TRY(read_doubles(dh, hh.data(), 2 * R1, s));
-                double nrm = 0;
-                TRY(read_doubles(dsc + 3, &nrm, 1, s));
-                TRY(slt_dgeadd(n, 1, 1.0 / nrm, vj1, n, 0.0, vj1, n, s));
-                double* hj = H.data() + j * R1;
-                for (int64_t i = 0; i <= j; ++i) hj[i] = hh[i] + hh[R1 + i];
+                TRY(slt_dnrm2(n, vj1, Sc(q) + 3, s));
+            }
+            for (int64_t i = 0; i < ns; ++i) {
+                const int64_t q = st[i];
+                TRY(copy_col(rg + (na + i) * n, Vc(q), n, s));
+                TRY(slt_dcolmax(n, 1, X + cl[q].c * ldx, ldx, Sc(q), s));
+                TRY(slt_dcolmax(n, 1, Vc(q), n, Sc(q) + 1, s));
+                TRY(slt_dnrm2(n, Vc(q), Sc(q) + 2, s));
+            }
+            TRY(read_doubles(scal.as<double>(), hs.data(), k * SC, s));
+            // host side of every column
+            for (int64_t i = 0; i < ns; ++i) {
+                const int64_t q = st[i];
+                Col& c = cl[q];
+                const double* h = hs.data() + q * SC;
+                c.cx = h[0];
+                const double cr = h[1];
+                if (cr <= c.cx * cte) { c.citer = int(c.iiter); c.conv = true; c.stopped = true; c.st = 2; continue; }
+                c.ares = h[2];
+                if (c.ares == 0) { c.citer = int(c.iiter); c.stopped = true; c.st = 2; continue; }
+                TRY(slt_dgeadd(n, 1, 1.0 / c.ares, Vc(q), n, 0.0, Vc(q), n, s));
+                c.S.assign(R1, 0.0);
+                c.S[0] = c.ares;
+                c.j = 0;
+                c.st = 1;
+                if (!keep_going(c, itermax)) TRY(cycle_end(c, q, X, ldx, s));
+            }
+            for (int64_t i = 0; i < na; ++i) {
+                const int64_t q = arn[i];
+                Col& c = cl[q];
+                const int64_t j = c.j;
+                const double* h = hs.data() + q * SC;
+                const double nrm = h[3];
+                TRY(slt_dgeadd(n, 1, 1.0 / nrm, Vc(q) + (j + 1) * n, n, 0.0, Vc(q) + (j + 1) * n, n, s));
+                double* hj = c.H.data() + j * R1;
+                for (int64_t r = 0; r <= j; ++r) hj[r] = h[4 + r] + h[4 + R1 + r];
                 hj[j + 1] = nrm;
                 auto rot = [](double* xx, double* yy, double cc, double ss) {
                     double tx = cc * *xx + ss * *yy;
                     double ty = cc * *yy - ss * *xx;
                     *xx = tx; *yy = ty;
                 };
-                for (int64_t i = 0; i < j; ++i) rot(&hj[i], &hj[i + 1], gc[i], gs[i]);
+                for (int64_t r = 0; r < j; ++r) rot(&hj[r], &hj[r + 1], c.gc[r], c.gs[r]);
                 {
                     double a = hj[j], bb = hj[j + 1];
                     double roe = std::fabs(a) > std::fabs(bb) ? a : bb;
                     double scale = std::fabs(a) + std::fabs(bb);
-                    if (scale == 0) { gc[j] = 1; gs[j] = 0; }
+                    if (scale == 0) { c.gc[j] = 1; c.gs[j] = 0; }
                     else {
                         double rr = scale * std::sqrt((a / scale) * (a / scale) + (bb / scale) * (bb / scale));
                         rr = std::copysign(1.0, roe) * rr;
-                        gc[j] = a / rr; gs[j] = bb / rr;
+                        c.gc[j] = a / rr; c.gs[j] = bb / rr;
                     }
                 }
-                rot(&hj[j], &hj[j + 1], gc[j], gs[j]);
-                rot(&S[j], &S[j + 1], gc[j], gs[j]);
-                ares = std::fabs(S[j + 1]);
+                rot(&hj[j], &hj[j + 1], c.gc[j], c.gs[j]);
+                rot(&c.S[j], &c.S[j + 1], c.gc[j], c.gs[j]);
+                c.ares = std::fabs(c.S[j + 1]);
+                c.j = j + 1;
+                c.iiter += 1;
+                if (!keep_going(c, itermax)) TRY(cycle_end(c, q, X, ldx, s));
             }
-            // x += W(:, 1:j) H(0:j-1, 0:j-1)^{-1} S(0:j-1)
-            if (j > 0) {
-                std::vector<double> y(S.begin(), S.begin() + j);
-                for (int64_t rr = j - 1; rr >= 0; --rr) {
-                    double sum = y[rr];
-                    for (int64_t cc = rr + 1; cc < j; ++cc) sum -= H[rr + cc * R1] * y[cc];
-                    y[rr] = sum / H[rr + rr * R1];
+        }
+        if (final_check) {
+            // columns that ended on the budget: test the true residual once more
+            int64_t nf = 0;
+            std::vector<int64_t> fq;
+            for (int64_t q = 0; q < k; ++q)
+                if (!cl[q].stopped) {
+                    TRY(copy_col(X + cl[q].c * ldx, z + nf * n, n, s));
+                    TRY(copy_col(B + cl[q].c * ldb, bg + nf * n, n, s));
+                    fq.push_back(q);
+                    ++nf;
                 }
-                SLT_CUDA_TRY(cudaMemcpyAsync(dy, y.data(), sizeof(double) * size_t(j), cudaMemcpyHostToDevice, s));
-                TRY(slt_dgemm_skinny(n, 1, j, 1.0, Wd + n, n, 0, dy, R1, 1.0, x, ldx, nws.p, s));
-                SLT_CUDA_TRY(cudaStreamSynchronize(s));
+            if (nf) {
+                TRY(products(nf, s));
+                for (int64_t i = 0; i < nf; ++i) {
+                    TRY(slt_dcolmax(n, 1, X + cl[fq[i]].c * ldx, ldx, Sc(fq[i]), s));
+                    TRY(slt_dcolmax(n, 1, rg + i * n, n, Sc(fq[i]) + 1, s));
+                }
+                TRY(read_doubles(scal.as<double>(), hs.data(), k * SC, s));
+                for (int64_t i = 0; i < nf; ++i) {
+                    const double* h = hs.data() + fq[i] * SC;
+                    if (h[1] <= h[0] * cte) cl[fq[i]].conv = true;
+                }
             }
         }
-        if (!stopped && final_check) {
-            TRY(slt_dresidual(n, 1, A, lda, chol, b, ldb, x, ldx, Vd, n, nws.p, s));
-            TRY(slt_dcolmax(n, 1, x, ldx, dsc, s));
-            TRY(slt_dcolmax(n, 1, Vd, n, dsc + 1, s));
-            double hv[2];
-            TRY(read_doubles(dsc, hv, 2, s));
-            if (hv[1] <= hv[0] * cte) *conv = true;
+        for (int64_t q = 0; q < k; ++q) {
+            used[q] = cl[q].stopped ? cl[q].citer : int(cl[q].iiter);
+            conv[q] = cl[q].conv;
         }
-        *used = stopped ? citer : int(iiter);
         return SLT_OK;
     }
 };
@@ -664,19 +782,23 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
         if (!conv && chain && itermax - ir_steps > 0) {
             // GMRES-IR on the stalled columns, preconditioned by the same factors
             tm.start(std::string(pfx) + "::gmres");
-            Fgmres g(chol, n, A, lda, lo, cte);
+            FgmresBlock g(chol, n, A, lda, lo, cte);
             TRY(g.init(itermax - ir_steps, nb, s));
-            std::vector<double> hx(h.begin(), h.begin() + nrhs), hr(h.begin() + nrhs, h.end());
+            std::vector<int64_t> todo;
+            for (int64_t c = 0; c < nrhs; ++c)
+                if (!(h[nrhs + c] <= h[c] * cte)) todo.push_back(c);
             bool all = true;
             int worst = 0;
-            for (int64_t c = 0; c < nrhs; ++c) {
-                if (hr[c] <= hx[c] * cte) continue;
-                int used = 0;
-                bool cc = false;
-                TRY(g.run(B + c * ldb, ldb, X + c * ldx, ldx, itermax - ir_steps, &used, &cc, s, true));
-                all = all && cc;
-                worst = std::max(worst, used);
-                if (!cc && stop_early) break;
+            for (size_t g0 = 0; g0 < todo.size(); g0 += FgmresBlock::kMaxCols) {
+                const int64_t k = std::min<int64_t>(FgmresBlock::kMaxCols, int64_t(todo.size() - g0));
+                int used[FgmresBlock::kMaxCols];
+                bool cc[FgmresBlock::kMaxCols];
+                TRY(g.run(todo.data() + g0, k, B, ldb, X, ldx, itermax - ir_steps, used, cc, s, true));
+                for (int64_t q = 0; q < k; ++q) {
+                    all = all && cc[q];
+                    worst = std::max(worst, used[q]);
+                }
+                if (!all && stop_early) break;
             }
             tm.stop(std::string(pfx) + "::gmres");
             if (all) { conv = true; *iter = int(ir_steps + worst); }
@@ -843,7 +965,7 @@ static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, i
     TRY(nws.alloc(slt_norm_ws_bytes(n), s));
     TRY(scal.alloc(sizeof(double) * 4, s));
     TRY(st.alloc(2 * sizeof(int), s));
-    TRY(Wlo.alloc(sizeof(float) * size_t(n), s));
+    TRY(Wlo.alloc(sizeof(float) * size_t(n) * size_t(nrhs), s));
     SLT_CUDA_TRY(cudaMemsetAsync(st.p, 0, 2 * sizeof(int), s));
     FactorCtx fc{st.as<int>(), st.as<int>() + 1};
 
@@ -866,20 +988,28 @@ static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, i
         all_conv = false;
     }
     else {
-        Fgmres g(chol, n, A, lda, lo, cte);
+        FgmresBlock g(chol, n, A, lda, lo, cte);
         TRY(g.init(itermax, nb, s));
-        for (int64_t c = 0; c < nrhs; ++c) {
-            const double* b = B + c * ldb;
-            double* x = X + c * ldx;
-            TRY(lo.solve(1, b, ldb, x, ldx, Wlo.as<float>(), s));
-            int citer = 0;
-            bool conv = false;
-            TRY(g.run(b, ldb, x, ldx, itermax, &citer, &conv, s));
-            if (!conv) { all_conv = false; citer = int(-itermax - 1); }
-            // a first attempt that the FP32 retry will redo: one failed column decides it
-            if (!conv && stop_early) { worst_iter = citer; break; }
-            worst_iter = (c == 0) ? citer : (citer < 0 || worst_iter < 0 ? std::min(worst_iter, citer)
-                                                                        : std::max(worst_iter, citer));
+        tm.start(std::string(pfx) + (chol ? "::potrs_lo" : "::getrs_lo"));
+        TRY(lo.solve(nrhs, B, ldb, X, ldx, Wlo.as<float>(), s));
+        tm.stop(std::string(pfx) + (chol ? "::potrs_lo" : "::getrs_lo"));
+        std::vector<int64_t> cols(nrhs);
+        for (int64_t c = 0; c < nrhs; ++c) cols[c] = c;
+        bool stop = false;
+        for (int64_t g0 = 0; g0 < nrhs && !stop; g0 += FgmresBlock::kMaxCols) {
+            const int64_t k = std::min<int64_t>(FgmresBlock::kMaxCols, nrhs - g0);
+            int used[FgmresBlock::kMaxCols];
+            bool cc[FgmresBlock::kMaxCols];
+            TRY(g.run(cols.data() + g0, k, B, ldb, X, ldx, itermax, used, cc, s));
+            for (int64_t q = 0; q < k; ++q) {
+                const int64_t c = g0 + q;
+                int citer = used[q];
+                if (!cc[q]) { all_conv = false; citer = int(-itermax - 1); }
+                // a first attempt that the FP32 retry will redo: one failed column decides it
+                if (!cc[q] && stop_early) { worst_iter = citer; stop = true; break; }
+                worst_iter = (c == 0) ? citer : (citer < 0 || worst_iter < 0 ? std::min(worst_iter, citer)
+                                                                            : std::max(worst_iter, citer));
+            }
         }
         *iter = worst_iter;
     }

@@ -8,7 +8,7 @@ namespace slt {
 
 // The options the LAPACK-compatible entry points run with: the SLATE_LAPACK_*
 // environment (SLATE_LAPACK_NB, default 512; SLATE_LAPACK_IB, default 32;
-// SLATE_LAPACK_FACTOR_PRECISION), unless a LapackOptsScope is active on the
+// SLATE_LAPACK_FACTOR_PRECISION; SLATE_LAPACK_REFINE), unless a LapackOptsScope is active on the
 // calling thread.
 slt_options lapack_opts();
 
