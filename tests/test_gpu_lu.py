@@ -232,3 +232,56 @@ def test_getrf_calu(orc, slt, m, n, nb):
         torch.cuda.synchronize()
         X = to_host(dB)
         assert np.abs(B - A @ X).sum(0).max() / (n * np.abs(A).sum(0).max() * np.abs(X).sum(0).max()) <= 3 * EPS
+
+
+def _slate_fixture():
+    import json
+    import os
+    import sys
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, gold)
+    import make_golden
+    return make_golden, json.load(open(os.path.join(gold, "slate_getrf.json")))
+
+
+def test_getrf_pivots_match_slate_panel_code(orc, slt):
+    """Whole-matrix pivots against LUs whose panels are SLATE's own
+    tile::getrf (tests/golden/slate_getrf.json, one panel thread: the GPU's
+    tie order), wherever the pivot margin exceeds rounding."""
+    import torch
+    mg, data = _slate_fixture()
+    inputs = {name: (A, nb, ib) for name, A, nb, ib in mg.getrf_full_inputs(orc)}
+    for c in data["full"]:
+        if c["threads"] != 1:
+            continue
+        A, nb, ib = inputs[c["name"]]
+        m, n = A.shape
+        dA = to_dev(A)
+        info, ipiv = slt.getrf(dA, slt.Options(nb=nb, ib=ib))
+        torch.cuda.synchronize()
+        assert info == c["info"]
+        k = np.arange(min(m, n)) // nb
+        sip = (k + np.array(c["piv_tile"])) * nb + np.array(c["piv_off"]) + 1
+        gip = slt.ipiv_to_lapack(ipiv, nb)
+        margin = orc.getrf(np.asfortranarray(A.copy()), nb, ib, margins=True)[4]
+        robust = margin > 1 + 1e3 * max(m, n) * EPS
+        assert np.array_equal(gip[robust], sip[robust]), c["name"]
+
+
+def test_getrf_panel_ties_match_slate_panel_code(orc, slt):
+    """Exact ties, a zero column and tiny pivots: one panel on the GPU against
+    SLATE's panel code with one thread (bit-exact pivots and info)."""
+    import torch
+    mg, data = _slate_fixture()
+    inputs = {name: (A, nb, ib) for name, A, nb, ib in mg.getrf_panel_inputs(orc)}
+    for c in data["panels"]:
+        if c["threads"] != 1 or c["name"] not in ("ties", "zerocol", "tiny", "zeros"):
+            continue
+        A, nb, ib = inputs[c["name"]]
+        dA = to_dev(A)
+        info, ipiv = slt.getrf(dA, slt.Options(nb=nb, ib=ib, pivot_threshold=c["threshold"]))
+        torch.cuda.synchronize()
+        assert info == c["info"], (c["name"], c["threshold"])
+        rel = ipiv.cpu().numpy().astype(np.int64)
+        srel = np.array(c["piv_tile"]) * nb + np.array(c["piv_off"])
+        assert np.array_equal(rel, srel), (c["name"], c["threshold"], rel[:8], srel[:8])

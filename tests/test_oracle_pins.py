@@ -60,3 +60,65 @@ def test_deterministic_kinds_match_reference_prints(orc, kind):
     assert ref.shape == (20, 20)
     a = orc.generate_kind(kind, 20, 20)
     np.testing.assert_allclose(_printed(a), ref, rtol=1e-12, atol=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# LU panel: the oracle's restatement against SLATE's own tile::getrf
+# (src/internal/Tile_getrf.hh), compiled from the SLATE sources.
+def _getrf_inputs(orc):
+    import sys
+    sys.path.insert(0, GOLD)
+    import make_golden
+    return make_golden
+
+
+def test_getrf_panel_fixtures_bit_exact(orc):
+    """Pivots, info and the factored panel (bit for bit) of SLATE's panel
+    code, for Philox panels and edge cases, under 1, 2 and 4 panel threads
+    and thresholds 1, 0.5 and 0."""
+    import hashlib
+    mg = _getrf_inputs(orc)
+    data = json.load(open(os.path.join(GOLD, "slate_getrf.json")))
+    inputs = {name: (A, nb, ib) for name, A, nb, ib in mg.getrf_panel_inputs(orc)}
+    assert len(data["panels"]) >= 90
+    for c in data["panels"]:
+        A, nb, ib = inputs[c["name"]]
+        P = np.asfortranarray(A.copy())
+        info, pt, po, _, _ = orc.getrf(P, nb, ib, panel_threads=c["threads"], threshold=c["threshold"])
+        key = (c["name"], c["threads"], c["threshold"])
+        assert info == c["info"], key
+        assert pt.tolist() == c["piv_tile"] and po.tolist() == c["piv_off"], key
+        assert hashlib.sha256(P.tobytes(order="F")).hexdigest() == c["factor_sha256"], key
+
+
+def test_getrf_full_fixtures_pivots(orc):
+    """Whole-matrix pivot sequences of LUs whose panels are SLATE's."""
+    mg = _getrf_inputs(orc)
+    data = json.load(open(os.path.join(GOLD, "slate_getrf.json")))
+    inputs = {name: (A, nb, ib) for name, A, nb, ib in mg.getrf_full_inputs(orc)}
+    for c in data["full"]:
+        A, nb, ib = inputs[c["name"]]
+        info, pt, po, _, _ = orc.getrf(np.asfortranarray(A.copy()), nb, ib, panel_threads=c["threads"])
+        assert info == c["info"]
+        assert pt.tolist() == c["piv_tile"] and po.tolist() == c["piv_off"], (c["name"], c["threads"])
+
+
+def test_getrf_panel_against_reference_build(orc):
+    """Random panels against SLATE's panel code itself, where it was built."""
+    if orc.ref_getrf_lib() is None:
+        pytest.skip("oracle/_ref not built (SLATE sources absent on this host)")
+    rng = np.random.default_rng(11)
+    for t in range(40):
+        nb = int(rng.choice([8, 16, 32, 48]))
+        m = int(rng.integers(1, 5)) * nb + int(rng.integers(0, nb))
+        ib = int(rng.choice([4, 8, 16, nb]))
+        thr = float(rng.choice([1.0, 0.5, 0.1, 0.0]))
+        T = int(rng.integers(1, 5))
+        A = orc.generate(int(rng.choice([1, 2, 3])), 900 + t, m, nb)
+        if t % 5 == 0:
+            A = np.asfortranarray(np.round(A * 2))          # exact ties
+        rinfo, rpt, rpo, R = orc.ref_getrf_panel(A, nb, ib, thr, T)
+        P = np.asfortranarray(A.copy())
+        info, pt, po, _, _ = orc.getrf(P, nb, ib, panel_threads=T, threshold=thr)
+        assert info == rinfo and np.array_equal(pt, rpt) and np.array_equal(po, rpo), (t, m, nb, ib, thr, T)
+        assert np.array_equal(P, R), (t, m, nb, ib, thr, T)
