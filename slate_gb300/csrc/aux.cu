@@ -180,12 +180,7 @@ static int launch_rowop_nr(dim3 grid, cudaStream_t stream, int64_t m, int64_t k,
                            int64_t lda, const double* X, int64_t ldx, int64_t tps, double* part)
 {
     constexpr size_t smem = rowop_smem_bytes(NR);
-    static bool configured = false;
-    if (!configured) {
-        SLT_CUDA_TRY(cudaFuncSetAttribute(rowop_kernel<MODE, SYM, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          int(smem)));
-        configured = true;
-    }
+    SLT_SMEM_ONCE((rowop_kernel<MODE, SYM, NR>), smem);
     rowop_kernel<MODE, SYM, NR><<<grid, 256, smem, stream>>>(m, k, nrhs, A, lda, X, ldx, tps, part);
     return SLT_OK;
 }
@@ -630,6 +625,10 @@ int dresidual_into(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sy
     if (size_t(n) * size_t(chunk) > ws_doubles) return SLT_ERR_LIMIT;
     SLT_CUDA_TRY(cudaMemcpy2DAsync(R, size_t(ldr) * sizeof(double), B, size_t(ldb) * sizeof(double),
                                    size_t(n) * sizeof(double), size_t(nrhs), cudaMemcpyDeviceToDevice, stream));
+    // Each chunk of up to 16 columns reuses the scratch from offset 0: its
+    // product launch writes the partial sums and its reduction reads them
+    // before the next chunk's product overwrites them, which holds only
+    // because all of them run in order on the one stream.
     for (int64_t c0 = 0; c0 < nrhs; c0 += kMaxRhs) {
         const int64_t nc = std::min<int64_t>(kMaxRhs, nrhs - c0);
         int64_t nseg, tps;

@@ -673,11 +673,7 @@ static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info
     if (!coop) return SLT_ERR_NOT_SUPPORTED;
     const size_t smem = (size_t(kCpIB) * (kCpIB + 1) + size_t(2) * kCpIB * 68 +
                          size_t(kCpIB / kCpSub) * kCpSub * (kCpSub + 1)) * sizeof(T);
-    static bool cfg = false;
-    if (!cfg) {
-        SLT_CUDA_TRY(cudaFuncSetAttribute(chol_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        cfg = true;
-    }
+    SLT_SMEM_ONCE(chol_panel_kernel<T>, smem);
     int per_sm = 0;
     SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chol_panel_kernel<T>, kCpThreads, smem));
     if (per_sm < 1) return SLT_ERR_NOT_SUPPORTED;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <algorithm>
 
@@ -14,6 +15,47 @@ namespace slt {
 // (%globaltimer), far longer than any legitimate wait, after which the
 // waiting block records SLT_ERR_TIMEOUT and leaves.
 constexpr unsigned long long kWaitNs = 2000000000ull;
+
+// Kernel attributes set by cudaFuncSetAttribute belong to the current
+// device, so a set-up that a launch needs runs once per device: one bit per
+// device index.  Thread-safe; two threads racing on a first call both run
+// the (idempotent) set-up.
+class DeviceOnce {
+public:
+    template <typename F> int run(F&& f) {
+        int dev = 0;
+        const cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return slt_from_cuda(e);
+        const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+        if (bit && (done_.load(std::memory_order_acquire) & bit)) return SLT_OK;
+        const int rc = f();
+        if (rc == SLT_OK && bit) done_.fetch_or(bit, std::memory_order_acq_rel);
+        return rc;
+    }
+private:
+    std::atomic<unsigned long long> done_{0};
+};
+
+// Sets a kernel's dynamic shared-memory limit once per device.
+#define SLT_SMEM_ONCE(kernel, bytes)                                                              \
+    do {                                                                                          \
+        static ::slt::DeviceOnce once_;                                                           \
+        const int rc_ = once_.run([&] {                                                           \
+            return slt_from_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                                      int(bytes)));                               \
+        });                                                                                       \
+        if (rc_) return rc_;                                                                      \
+    } while (0)
+
+// The same, storing the status in rcvar instead of returning it.
+#define SLT_SMEM_ONCE_INTO(rcvar, kernel, bytes)                                                  \
+    do {                                                                                          \
+        static ::slt::DeviceOnce once_;                                                           \
+        rcvar = once_.run([&] {                                                                   \
+            return slt_from_cuda(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                                      int(bytes)));                               \
+        });                                                                                       \
+    } while (0)
 
 __device__ __forceinline__ unsigned long long globaltimer()
 {

@@ -626,12 +626,7 @@ static int launch_panel(int64_t prows, int64_t nbk, int64_t ib, T* P, int64_t ld
     int* flags = reinterpret_cast<int*>(base + 256 + ((sizeof(PanelExchange<double>) + 255) & ~size_t(255)));
     const int pidx = prof_begin(SLT_PROF_PANEL, stream);
     if (staged <= kPanelStagedMax) {
-        static bool cfg2 = false;
-        if (!cfg2) {
-            SLT_CUDA_TRY(cudaFuncSetAttribute(getrf_panel2_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              int(kPanelStagedMax)));
-            cfg2 = true;
-        }
+        SLT_SMEM_ONCE(getrf_panel2_kernel<T>, kPanelStagedMax);
         int per2 = 0;
         SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, getrf_panel2_kernel<T>, kPanelThreads,
                                                                    staged));

@@ -1,13 +1,13 @@
 // noalloc.cu -- an FP64 residual entry point that allocates nothing.
 //
 // Some callers cannot allocate device memory at the point where they need a
-// residual: code running while a CUDA stream is being captured into a graph
-// (a cudaMalloc there is illegal or breaks the capture), applications whose
-// device memory is owned by their own pool or by a framework allocator that
-// forbids side allocations, and latency-critical refinement loops that cannot
-// afford cudaMalloc's implicit device-wide synchronisation.  For them this
-// file keeps the residual's partial-sum scratch in a fixed, library-owned
-// __device__ array instead of allocating it per call.
+// residual: applications whose device memory is owned by their own pool or
+// by a framework allocator that forbids side allocations, code that must not
+// call cudaMalloc / cudaFree at that point (both can synchronise the whole
+// device), and latency-critical refinement loops that cannot afford that
+// synchronisation.  For them this file keeps the residual's partial-sum
+// scratch in a fixed, library-owned __device__ array instead of allocating it
+// per call; the caller passes A, B, X and R as usual.
 //
 // Limits and behaviour:
 //  * the scratch holds kNoAllocScratchDoubles doubles (16 MiB); a call needs

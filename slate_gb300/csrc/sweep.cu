@@ -409,12 +409,7 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     unsigned long long* mb = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(flags) + 256);
     T* Dinv = reinterpret_cast<T*>(reinterpret_cast<char*>(flags) + 256 + size_t(kSwRhs) * npad * 2 * 8);
     const size_t ti_smem = size_t(2) * kSwBS * (kSwBS + 1) * sizeof(T);
-    static bool ti_cfg = false;
-    if (!ti_cfg) {
-        SLT_CUDA_TRY(cudaFuncSetAttribute(trinv_kernel<T, FORWARD, UNIT, TRANS>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(ti_smem)));
-        ti_cfg = true;
-    }
+    SLT_SMEM_ONCE((trinv_kernel<T, FORWARD, UNIT, TRANS>), ti_smem);
     trinv_kernel<T, FORWARD, UNIT, TRANS><<<unsigned(nblk), 256, ti_smem, s>>>(n, M, ldm, Dinv);
     count_launch();
     SLT_CUDA_TRY(cudaGetLastError());
@@ -422,11 +417,7 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     SLT_CUDA_TRY(cudaMemsetAsync(flags, 0, 256 + size_t(nrhs) * size_t(npad) * Mailbox<T>::kWords * 8, s));
     auto fn = sweep_kernel<T, FORWARD, UNIT, TRANS>;
     const size_t smem = sizeof(SweepSmem<T>);
-    static bool cfg = false;
-    if (!cfg) {
-        SLT_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        cfg = true;
-    }
+    SLT_SMEM_ONCE(fn, smem);
     int dev = 0, sms = 0, per = 0;
     SLT_CUDA_TRY(cudaGetDevice(&dev));
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -873,44 +873,38 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
                 const int64_t tiles = (mp / kTcBM) * (np / kTcBN);
                 const unsigned grid1 = unsigned(std::min<int64_t>(tiles, g_sms));
                 if (tf32) {
-                    static bool cfg = false;
-                    if (!cfg) { cudaFuncSetAttribute(tc_update_persistent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psm)); cfg = true; }
-                    tc_update_persistent<1><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(2, kTcBM, kTcBN));
+                    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<1>, psm);
+                    if (!rc) tc_update_persistent<1><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(2, kTcBM, kTcBN));
                 }
                 else if (fp8) {
-                    static bool cfg = false;
-                    if (!cfg) { cudaFuncSetAttribute(tc_update_persistent<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psm)); cfg = true; }
-                    tc_update_persistent<2><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(0, kTcBM, kTcBN));
+                    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<2>, psm);
+                    if (!rc) tc_update_persistent<2><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(0, kTcBM, kTcBN));
                 }
                 else {
-                    static bool cfg = false;
-                    if (!cfg) { cudaFuncSetAttribute(tc_update_persistent<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(psm)); cfg = true; }
+                    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<0>, psm);
                     const uint32_t fmt = tier == SLT_PREC_BF16 ? 1u : 0u;
-                    tc_update_persistent<0><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(fmt, kTcBM, kTcBN));
+                    if (!rc) tc_update_persistent<0><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(fmt, kTcBM, kTcBN));
                 }
             }
             else {
             const size_t smem = tc_smem_bytes();
             dim3 grid(unsigned(mp / kTcBM), unsigned(np / kTcBN));
             if (tf32) {
-                static bool cfg = false;
-                if (!cfg) { cudaFuncSetAttribute(tc_update_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); cfg = true; }
-                tc_update_kernel<1><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(2, kTcBM, kTcBN));
+                SLT_SMEM_ONCE_INTO(rc, tc_update_kernel<1>, smem);
+                if (!rc) tc_update_kernel<1><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(2, kTcBM, kTcBN));
             }
             else if (fp8) {
-                static bool cfg = false;
-                if (!cfg) { cudaFuncSetAttribute(tc_update_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); cfg = true; }
-                tc_update_kernel<2><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(0, kTcBM, kTcBN));
+                SLT_SMEM_ONCE_INTO(rc, tc_update_kernel<2>, smem);
+                if (!rc) tc_update_kernel<2><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(0, kTcBM, kTcBN));
             }
             else {
-                static bool cfg = false;
-                if (!cfg) { cudaFuncSetAttribute(tc_update_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)); cfg = true; }
+                SLT_SMEM_ONCE_INTO(rc, tc_update_kernel<0>, smem);
                 const uint32_t fmt = tier == SLT_PREC_BF16 ? 1u : 0u;
-                tc_update_kernel<0><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(fmt, kTcBM, kTcBN));
+                if (!rc) tc_update_kernel<0><<<grid, kTcThreads, smem, stream>>>(mapA, mapB, args, make_idesc(fmt, kTcBM, kTcBN));
             }
             }
             count_launch();
-            rc = slt_from_cuda(cudaGetLastError());
+            if (!rc) rc = slt_from_cuda(cudaGetLastError());
             double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);
             prof_end(pidx, stream, 2.0 * mn * double(k), 8.0 * mn + double(esize) * double(kpad) * double(m + n));
         }

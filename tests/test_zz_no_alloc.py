@@ -1,13 +1,15 @@
 """The allocation-free FP64 residual (slt_dresidual_noalloc) against the
-allocating entry point (slt_dresidual), through the C ABI.
+allocating entry point (slt_dresidual) and against a host FP64 B - A X,
+through the C ABI.
 
-Callers that cannot allocate (inside a stream capture, under an allocator
-that forbids side allocations, in latency-bound loops) use the variant whose
-scratch is a fixed library-owned device array.  Two calls in a row must each
-match the allocating residual: the second call must not see the first call's
-leftovers in the shared scratch.  Tolerance: the two entry points may split
-the columns into different segments, so sums are compared to 1e-13 relative
-to sum_j |A(i,j)| |X(j)| + |B(i)|.
+Callers whose device memory belongs to their own pool or to an allocator
+that forbids side allocations, or that must not call cudaMalloc where they
+need a residual, use the variant whose scratch is a fixed library-owned
+device array.  Two calls in a row must each match the allocating residual:
+the second call must not see the first call's leftovers in the shared
+scratch.  Tolerance: the two entry points may split the columns into
+different segments, so sums are compared to 1e-13 relative to
+sum_j |A(i,j)| |X(j)| + |B(i)|; the host residual is held to the same bound.
 """
 import ctypes
 
@@ -65,6 +67,10 @@ def test_noalloc_matches_allocating_residual_twice(orc, slt, n, nrhs, sym):
         R1, R2 = to_host(dR1), to_host(dR2)
         scale = _scale(A, X, B, sym)
         assert np.all(np.abs(R1 - R2) <= 1e-13 * scale), float(np.max(np.abs(R1 - R2) / scale))
+        # independent of the library's kernels: the residual in host FP64
+        Af = np.tril(A) + np.tril(A, -1).T if sym else A
+        Rh = B - Af @ X
+        assert np.all(np.abs(R1 - Rh) <= 1e-13 * scale), float(np.max(np.abs(R1 - Rh) / scale))
 
 
 def test_noalloc_rejects_oversized_problem_without_launching(slt):
