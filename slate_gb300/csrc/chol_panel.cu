@@ -671,6 +671,7 @@ static int launch_chol_panel(int64_t m, int64_t nbk, T* P, int64_t ld, int* info
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) return SLT_ERR_NOT_SUPPORTED;
+    sms = capped_sms(sms);
     const size_t smem = (size_t(kCpIB) * (kCpIB + 1) + size_t(2) * kCpIB * 68 +
                          size_t(kCpIB / kCpSub) * kCpSub * (kCpSub + 1)) * sizeof(T);
     SLT_SMEM_ONCE(chol_panel_kernel<T>, smem);

@@ -6,12 +6,15 @@
 // tests of the refinement loops, the Givens rotations of GMRES, info).
 
 #include "drivers.h"
+#include "driver_table.h"
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -47,6 +50,48 @@ double timer_value(const char* name)
 
 void timers_clear() { t_timers.clear(); }
 
+
+// ---------------------------------------------------------------------------
+// Workspace pool: one per device, release threshold "never", so that the
+// physical memory of a call's workspace stays mapped for the next call.
+static std::mutex g_pool_mtx;
+static cudaMemPool_t g_pools[64] = {};
+
+cudaMemPool_t workspace_pool()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); return nullptr; }
+    std::lock_guard<std::mutex> lk(g_pool_mtx);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        uint64_t keep = ~uint64_t(0);
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        cudaGetLastError();
+        g_pools[dev] = pool;
+    }
+    return g_pools[dev];
+}
+
+} // namespace slt
+
+// Returns the memory the library's workspace pool holds on the current device
+// (for callers that need it back between solves).
+extern "C" int slt_release_workspace(void)
+{
+    cudaMemPool_t pool = slt::workspace_pool();
+    if (!pool) return SLT_OK;
+    SLT_CUDA_TRY(cudaDeviceSynchronize());
+    SLT_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+    return SLT_OK;
+}
+
+namespace slt {
 
 // ---------------------------------------------------------------------------
 // Type dispatch onto the kernel layer.
@@ -142,6 +187,93 @@ int finish_factor(FactorCtx& fc, int64_t* info, cudaStream_t s)
 }
 
 // ---------------------------------------------------------------------------
+// Lookahead (Option::Lookahead, src/getrf.cc:39,120-135, src/potrf.cc:41-61):
+// after the panel of step k, the next block column is updated first, on the
+// caller's stream, and the rest of the trailing matrix on a second,
+// lower-priority stream, so that the panel of step k+1 runs while the update
+// of step k is still going.  The two get disjoint shares of the SMs: the
+// panel launches take `panel_sms` SMs, the trailing update the rest
+// (slt_set_sm_cap).  Events order the streams:
+//   panel k+1       after  lookahead update k       (same stream)
+//   swaps / lookahead update k+1   after  rest update k   (ev_rest)
+//   rest update k   after  panel k and the U12 solve of step k (ev_row)
+// The autotuned choices (driver_table.h) for a factorisation of order n:
+// kind 0 getrf, 1 potrf; cls 0 FP64, 1 FP32 SIMT, 2 tensor cores.
+static const DriverTune& driver_tune(int kind, int cls, int64_t n)
+{
+    const DriverTune* last = nullptr;
+    for (const DriverTune& t : kDriverTable) {
+        if (t.kind != kind || t.cls != cls) continue;
+        last = &t;
+        if (n <= t.max_n) return t;
+    }
+    static const DriverTune none{kind, cls, 0, 0, 1};
+    return last ? *last : none;
+}
+
+template <typename T>
+static int update_class(const slt_options& o)
+{
+    if (sizeof(T) == 8) return 0;
+    const int p = o.factor_precision;
+    return (p == SLT_PREC_TF32 || p == SLT_PREC_BF16 || p == SLT_PREC_FP16 || p == SLT_PREC_FP8 ||
+            p == SLT_PREC_TF32X3) ? 2 : 1;
+}
+
+// SMs given to the panel while an update runs beside it: SLT_LOOKAHEAD_PANEL_SMS
+// when set (the tuner's override; 0 turns the overlap off), else the table's.
+static int lookahead_panel_sms(const DriverTune& t, int sms)
+{
+    if (const char* e = std::getenv("SLT_LOOKAHEAD_PANEL_SMS")) return std::atoi(e);
+    return std::min(t.panel_sms, sms);
+}
+
+struct Lookahead {
+    bool on = false;
+    cudaStream_t s = nullptr, su = nullptr;
+    cudaEvent_t ev_row = nullptr, ev_rest = nullptr;
+    int sms = 0, panel_sms = 0;
+    bool rest_pending = false;
+
+    int init(const slt_options& o, const DriverTune& tune, int64_t n, int64_t nb, cudaStream_t stream) {
+        s = stream;
+        const int64_t depth = o.lookahead;
+        if (depth <= 0 || n <= 2 * nb) return SLT_OK;
+        int dev = 0;
+        SLT_CUDA_TRY(cudaGetDevice(&dev));
+        SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        panel_sms = lookahead_panel_sms(tune, sms);
+        if (panel_sms <= 0 || panel_sms >= sms) return SLT_OK;
+        int lo = 0, hi = 0;
+        SLT_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        SLT_CUDA_TRY(cudaStreamCreateWithPriority(&su, cudaStreamNonBlocking, lo));
+        SLT_CUDA_TRY(cudaEventCreateWithFlags(&ev_row, cudaEventDisableTiming));
+        SLT_CUDA_TRY(cudaEventCreateWithFlags(&ev_rest, cudaEventDisableTiming));
+        on = true;
+        return SLT_OK;
+    }
+    // the caller's stream waits for the last rest update
+    int join() {
+        if (!on || !rest_pending) return SLT_OK;
+        SLT_CUDA_TRY(cudaStreamWaitEvent(s, ev_rest, 0));
+        rest_pending = false;
+        return SLT_OK;
+    }
+    ~Lookahead() {
+        if (su) { join(); cudaStreamDestroy(su); }
+        if (ev_row) cudaEventDestroy(ev_row);
+        if (ev_rest) cudaEventDestroy(ev_rest);
+    }
+};
+
+// Scoped SM budget for the launches issued on this thread.
+struct SmCap {
+    int prev;
+    explicit SmCap(int sms) : prev(slt_set_sm_cap(sms)) {}
+    ~SmCap() { slt_set_sm_cap(prev); }
+};
+
+// ---------------------------------------------------------------------------
 // LU: right-looking, one cooperative panel launch per block column, then the
 // panel's interchanges on both sides, the U12 solve and the trailing GEMM
 // (impl::getrf, src/getrf.cc:22-244).  MethodLU::NoPiv is the panel's
@@ -170,6 +302,11 @@ int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_opti
         TRY(W.alloc(sizeof(T) * size_t(m) * size_t(std::min(nb, n)), s));
         TRY(plan0.alloc(sizeof(int) * size_t(1 + 4 * nb), s));
     }
+    const DriverTune& tune = driver_tune(0, update_class<T>(o), std::min(m, n));
+    slt_options ot = o;
+    if (ot.gemm_engine == 0) ot.gemm_engine = tune.engine;
+    Lookahead la;
+    TRY(la.init(o, tune, std::min(m, n), nb, s));
     for (int64_t r0 = 0; r0 < mn; r0 += nb) {
         const int64_t nbk = std::min(nb, n - r0);
         const int64_t prows = m - r0;
@@ -180,7 +317,11 @@ int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_opti
         if (calu)
             SLT_CUDA_TRY(cudaMemcpy2DAsync(W.p, sizeof(T) * size_t(prows), P, sizeof(T) * size_t(lda),
                                            sizeof(T) * size_t(prows), size_t(nbk), cudaMemcpyDeviceToDevice, s));
-        TRY(k_panel(prows, nbk, ib, thr, P, lda, ipiv + r0, fc.d_info, r0, pws.p, fc.d_status, s));
+        {
+            // the panel shares the GPU with the previous step's rest update
+            SmCap cap(la.rest_pending ? la.panel_sms : 0);
+            TRY(k_panel(prows, nbk, ib, thr, P, lda, ipiv + r0, fc.d_info, r0, pws.p, fc.d_status, s));
+        }
         TRY(slt_swap_plan(ipiv + r0, diag, r0, plan.as<int>(), s));
         if (calu && prows > diag) {
             // W <- the panel's interchanges applied to the original panel;
@@ -193,16 +334,40 @@ int getrf_dev(int64_t m, int64_t n, T* A, int64_t lda, int* ipiv, const slt_opti
             TRY(k_trsm_runn(prows - diag, diag, P, lda, P + diag, lda, s));
         }
         const int64_t c1 = r0 + nbk;
+        // the interchanges touch every column to the right: the previous
+        // rest update must be done with them
+        TRY(la.join());
         TRY(k_laswp(plan.as<int>(), 2 * diag, A + c1 * lda, lda, n - c1, s));
         TRY(k_laswp(plan.as<int>(), 2 * diag, A, lda, r0, s));
         if (c1 < n) {
             TRY(k_trsm_llnu(diag, n - c1, P, lda, A + r0 + c1 * lda, lda, s));
-            if (r0 + diag < m)
-                TRY(k_gemm('N', m - r0 - diag, n - c1, diag, T(-1), A + (r0 + diag) + r0 * lda, lda,
-                           A + r0 + c1 * lda, lda, T(1), A + (r0 + diag) + c1 * lda, lda, 0, o, s));
+            if (r0 + diag < m) {
+                const int64_t rows = m - r0 - diag;
+                const T* L21 = A + (r0 + diag) + r0 * lda;
+                if (!la.on || n - c1 <= nb) {
+                    TRY(k_gemm('N', rows, n - c1, diag, T(-1), L21, lda, A + r0 + c1 * lda, lda, T(1),
+                               A + (r0 + diag) + c1 * lda, lda, 0, ot, s));
+                }
+                else {
+                    // rest of the trailing matrix on the second stream
+                    const int64_t c2 = c1 + nb;
+                    SLT_CUDA_TRY(cudaEventRecord(la.ev_row, s));
+                    SLT_CUDA_TRY(cudaStreamWaitEvent(la.su, la.ev_row, 0));
+                    {
+                        SmCap cap(la.sms - la.panel_sms);
+                        TRY(k_gemm('N', rows, n - c2, diag, T(-1), L21, lda, A + r0 + c2 * lda, lda, T(1),
+                                   A + (r0 + diag) + c2 * lda, lda, 0, ot, la.su));
+                    }
+                    SLT_CUDA_TRY(cudaEventRecord(la.ev_rest, la.su));
+                    la.rest_pending = true;
+                    // lookahead: the next block column first, on the caller's stream
+                    TRY(k_gemm('N', rows, nb, diag, T(-1), L21, lda, A + r0 + c1 * lda, lda, T(1),
+                               A + (r0 + diag) + c1 * lda, lda, 0, ot, s));
+                }
+            }
         }
     }
-    return SLT_OK;
+    return la.join();
 }
 
 // getrs NoTrans: W = P B, forward sweep with unit L, backward with U
@@ -282,16 +447,45 @@ int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc,
     const int64_t nb = eff_nb(o);
     DevBuf bar;
     TRY(bar.alloc(slt_chol_panel_ws_bytes(), s));
+    const DriverTune& tune = driver_tune(1, update_class<T>(o), n);
+    slt_options ot = o;
+    if (ot.gemm_engine == 0) ot.gemm_engine = tune.engine;
+    Lookahead la;
+    TRY(la.init(o, tune, n, nb, s));
     for (int64_t r0 = 0; r0 < n; r0 += nb) {
         const int64_t kb = std::min(nb, n - r0);
-        // the whole column panel (diagonal block and everything below) in one launch
-        TRY(k_chol_panel(n - r0, kb, A + r0 + r0 * lda, lda, fc.d_info, r0, bar.p, fc.d_status, s));
+        {
+            // the whole column panel (diagonal block and everything below) in
+            // one launch, beside the previous step's rest update
+            SmCap cap(la.rest_pending ? la.panel_sms : 0);
+            TRY(k_chol_panel(n - r0, kb, A + r0 + r0 * lda, lda, fc.d_info, r0, bar.p, fc.d_status, s));
+        }
         const int64_t t0 = r0 + kb;
-        if (t0 < n)
-            TRY(k_gemm('T', n - t0, n - t0, kb, T(-1), A + t0 + r0 * lda, lda, A + t0 + r0 * lda, lda, T(1),
-                       A + t0 + t0 * lda, lda, 1, o, s));
+        if (t0 >= n) break;
+        const T* L = A + t0 + r0 * lda;
+        if (!la.on || n - t0 <= nb) {
+            TRY(la.join());
+            TRY(k_gemm('T', n - t0, n - t0, kb, T(-1), L, lda, L, lda, T(1), A + t0 + t0 * lda, lda, 1, ot, s));
+            continue;
+        }
+        // rest of the trailing matrix (columns t0 + nb ...) on the second stream
+        const int64_t t2 = t0 + nb;
+        SLT_CUDA_TRY(cudaEventRecord(la.ev_row, s));
+        // the previous rest update wrote block column t0: it must be done
+        // before the lookahead update below
+        TRY(la.join());
+        SLT_CUDA_TRY(cudaStreamWaitEvent(la.su, la.ev_row, 0));
+        {
+            SmCap cap(la.sms - la.panel_sms);
+            TRY(k_gemm('T', n - t2, n - t2, kb, T(-1), A + t2 + r0 * lda, lda, A + t2 + r0 * lda, lda, T(1),
+                       A + t2 + t2 * lda, lda, 1, ot, la.su));
+        }
+        SLT_CUDA_TRY(cudaEventRecord(la.ev_rest, la.su));
+        la.rest_pending = true;
+        // lookahead: block column t0 (rows t0 .. n), lower part of its diagonal tile
+        TRY(k_gemm('T', n - t0, nb, kb, T(-1), L, lda, L, lda, T(1), A + t0 + t0 * lda, lda, 1, ot, s));
     }
-    return SLT_OK;
+    return la.join();
 }
 
 // potrs lower: forward with L, backward with L^T (src/potrs.cc:55-78).

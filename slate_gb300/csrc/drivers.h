@@ -40,7 +40,14 @@ int slt_dscal(int64_t n, const double* num, const double* den, double* x, cudaSt
 
 namespace slt {
 
-// Device workspace owned by one driver call (stream-ordered pool).
+// The library's stream-ordered memory pool on the current device (created on
+// first use).  Unlike the device's default pool it keeps freed memory
+// reserved between driver calls, so a repeated solve does not map its
+// workspace afresh each time; slt_release_workspace() hands it back.
+cudaMemPool_t workspace_pool();
+
+// Device workspace owned by one driver call (stream-ordered, from the
+// library's pool).
 struct DevBuf {
     void* p = nullptr;
     cudaStream_t s = nullptr;
@@ -51,7 +58,8 @@ struct DevBuf {
     int alloc(size_t bytes, cudaStream_t stream) {
         s = stream;
         if (bytes == 0) bytes = 16;
-        cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+        cudaMemPool_t pool = workspace_pool();
+        cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, stream) : cudaMallocAsync(&p, bytes, stream);
         if (e != cudaSuccess) { p = nullptr; cudaGetLastError(); return SLT_ERR_NOMEM; }
         return SLT_OK;
     }

@@ -16,11 +16,12 @@
 
 namespace slt {
 
+// One BM x BN output tile at (row0, col0).
 template <typename T, int BM, int BN, int BK, int TM, int TN, bool TRANSB>
-__global__ void __launch_bounds__((BM / TM) * (BN / TN))
-gemm_simt_kernel(int64_t m, int64_t n, int64_t k, T alpha, const T* __restrict__ A, int64_t lda,
-                 const T* __restrict__ B, int64_t ldb, T beta, T* __restrict__ C, int64_t ldc,
-                 int lower)
+__device__ __forceinline__ void
+gemm_simt_tile(int64_t row0, int64_t col0, int64_t m, int64_t n, int64_t k, T alpha, const T* __restrict__ A,
+               int64_t lda, const T* __restrict__ B, int64_t ldb, T beta, T* __restrict__ C, int64_t ldc,
+               int lower)
 {
     constexpr int NT = (BM / TM) * (BN / TN);
     constexpr int RM = BM / TM;          // row groups
@@ -29,8 +30,6 @@ gemm_simt_kernel(int64_t m, int64_t n, int64_t k, T alpha, const T* __restrict__
     __shared__ T As[2][BK][BM];
     __shared__ T Bs[2][BK][BN];
 
-    const int64_t row0 = int64_t(blockIdx.x) * BM;
-    const int64_t col0 = int64_t(blockIdx.y) * BN;
     if (lower && row0 + BM - 1 < col0) return;
 
     const int t = threadIdx.x;
@@ -118,20 +117,35 @@ gemm_simt_kernel(int64_t m, int64_t n, int64_t k, T alpha, const T* __restrict__
     }
 }
 
+// The launch walks the output tiles with a grid stride (columns of tiles in
+// order, rows fastest), so a grid smaller than the tile count -- an SM budget
+// set with slt_set_sm_cap -- still covers C.
+template <typename T, int BM, int BN, int BK, int TM, int TN, bool TRANSB>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+gemm_simt_kernel(int64_t m, int64_t n, int64_t k, T alpha, const T* __restrict__ A, int64_t lda,
+                 const T* __restrict__ B, int64_t ldb, T beta, T* __restrict__ C, int64_t ldc,
+                 int lower)
+{
+    const int64_t tm = ceildiv(m, BM), tiles = tm * ceildiv(n, BN);
+    for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        __syncthreads();          // the previous tile's shared-memory reads are done
+        gemm_simt_tile<T, BM, BN, BK, TM, TN, TRANSB>((t % tm) * BM, (t / tm) * BN, m, n, k, alpha, A, lda,
+                                                      B, ldb, beta, C, ldc, lower);
+    }
+}
+
 // FP64 tensor-core GEMM: mma.sync.m16n8k4 .f64, 64x64 CTA tile, 4 warps of
 // 32x32, BK = 16, register-staged double buffering.
 template <bool TRANSB>
-__global__ void __launch_bounds__(128)
-dgemm_dmma_kernel(int64_t m, int64_t n, int64_t k, double alpha, const double* __restrict__ A,
-                  int64_t lda, const double* __restrict__ B, int64_t ldb, double beta,
-                  double* __restrict__ C, int64_t ldc, int lower)
+__device__ __forceinline__ void
+dgemm_dmma_tile(int64_t row0, int64_t col0, int64_t m, int64_t n, int64_t k, double alpha,
+                const double* __restrict__ A, int64_t lda, const double* __restrict__ B, int64_t ldb,
+                double beta, double* __restrict__ C, int64_t ldc, int lower)
 {
     constexpr int BM = 64, BN = 64, BK = 16, PAD = 4, NT = 128;
     __shared__ double As[2][BK][BM + PAD];
     __shared__ double Bs[2][BK][BN + PAD];
 
-    const int64_t row0 = int64_t(blockIdx.x) * BM;
-    const int64_t col0 = int64_t(blockIdx.y) * BN;
     if (lower && row0 + BM - 1 < col0) return;
 
     const int t = threadIdx.x;
@@ -232,6 +246,47 @@ dgemm_dmma_kernel(int64_t m, int64_t n, int64_t k, double alpha, const double* _
             }
 }
 
+template <bool TRANSB>
+__global__ void __launch_bounds__(128)
+dgemm_dmma_kernel(int64_t m, int64_t n, int64_t k, double alpha, const double* __restrict__ A,
+                  int64_t lda, const double* __restrict__ B, int64_t ldb, double beta,
+                  double* __restrict__ C, int64_t ldc, int lower)
+{
+    const int64_t tm = ceildiv(m, 64), tiles = tm * ceildiv(n, 64);
+    for (int64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+        __syncthreads();          // the previous tile's shared-memory reads are done
+        dgemm_dmma_tile<TRANSB>((t % tm) * 64, (t / tm) * 64, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                                lower);
+    }
+}
+
+// Launch shape of a tile-walking GEMM: one block per tile, or, under an SM
+// budget, one block per budgeted SM.  Those blocks reserve more than half of
+// an SM's shared memory (unused by the kernel), so no two share an SM and the
+// SMs outside the budget stay free for the panel that runs beside the update;
+// the FP64 and FP32 pipes are saturated by one 256-thread block per SM.
+constexpr size_t kCapSmem = 120 * 1024;
+
+struct GemmLaunch {
+    unsigned grid;
+    size_t smem;
+};
+
+template <typename K>
+static int gemm_launch(K kernel, int64_t tiles, GemmLaunch* out)
+{
+    const int cap = slt_sm_cap();
+    if (cap <= 0) {
+        *out = {unsigned(tiles), 0};
+        return SLT_OK;
+    }
+    // set on every capped launch: kernels of one signature share this
+    // template instance, so a once-per-instance flag would miss the second
+    SLT_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kCapSmem)));
+    *out = {unsigned(std::max<int64_t>(1, std::min<int64_t>(tiles, cap))), kCapSmem};
+    return SLT_OK;
+}
+
 static int g_dgemm_engine = 0;   // 0: not chosen yet
 
 } // namespace slt
@@ -247,23 +302,22 @@ extern "C" int slt_dgemm(char transb, int64_t m, int64_t n, int64_t k, double al
     if (m == 0 || n == 0) return SLT_OK;
     if (engine == 0) engine = g_dgemm_engine ? g_dgemm_engine : 1;
     const int pidx = prof_begin(SLT_PROF_GEMM64, stream);
+    const int64_t tiles = ceildiv(m, 64) * ceildiv(n, 64);
+    GemmLaunch L;
     if (engine == 2) {
-        dim3 grid(unsigned(ceildiv(m, 64)), unsigned(ceildiv(n, 64)));
-        if (transb == 'N')
-            dgemm_dmma_kernel<false><<<grid, 128, 0, stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-        else
-            dgemm_dmma_kernel<true><<<grid, 128, 0, stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-    slt::count_launch();
+        auto kf = transb == 'N' ? dgemm_dmma_kernel<false> : dgemm_dmma_kernel<true>;
+        const int rc = gemm_launch(kf, tiles, &L);
+        if (rc) return rc;
+        kf<<<L.grid, 128, L.smem, stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+        slt::count_launch();
     }
     else {
-        dim3 grid(unsigned(ceildiv(m, 64)), unsigned(ceildiv(n, 64)));
-        if (transb == 'N')
-            gemm_simt_kernel<double, 64, 64, 8, 4, 4, false><<<grid, 256, 0, stream>>>(
-                m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-        else
-            gemm_simt_kernel<double, 64, 64, 8, 4, 4, true><<<grid, 256, 0, stream>>>(
-                m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-    slt::count_launch();
+        auto kf = transb == 'N' ? gemm_simt_kernel<double, 64, 64, 8, 4, 4, false>
+                                : gemm_simt_kernel<double, 64, 64, 8, 4, 4, true>;
+        const int rc = gemm_launch(kf, tiles, &L);
+        if (rc) return rc;
+        kf<<<L.grid, 256, L.smem, stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+        slt::count_launch();
     }
     {
         double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);
@@ -278,14 +332,14 @@ extern "C" int slt_sgemm(char transb, int64_t m, int64_t n, int64_t k, float alp
 {
     if (m < 0 || n < 0 || k < 0 || (transb != 'N' && transb != 'T')) return SLT_ERR_ARG;
     if (m == 0 || n == 0) return SLT_OK;
-    dim3 grid(unsigned(ceildiv(m, 128)), unsigned(ceildiv(n, 128)));
+    const int64_t tiles = ceildiv(m, 128) * ceildiv(n, 128);
+    auto kf = transb == 'N' ? gemm_simt_kernel<float, 128, 128, 8, 8, 8, false>
+                            : gemm_simt_kernel<float, 128, 128, 8, 8, 8, true>;
+    GemmLaunch L;
+    const int rc = gemm_launch(kf, tiles, &L);
+    if (rc) return rc;
     const int pidx = prof_begin(SLT_PROF_GEMM32, stream);
-    if (transb == 'N')
-        gemm_simt_kernel<float, 128, 128, 8, 8, 8, false><<<grid, 256, 0, stream>>>(
-            m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-    else
-        gemm_simt_kernel<float, 128, 128, 8, 8, 8, true><<<grid, 256, 0, stream>>>(
-            m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+    kf<<<L.grid, 256, L.smem, stream>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, lower);
     slt::count_launch();
     {
         double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);

@@ -600,6 +600,7 @@ static int launch_panel(int64_t prows, int64_t nbk, int64_t ib, T* P, int64_t ld
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) return SLT_ERR_NOT_SUPPORTED;
+    sms = capped_sms(sms);
     int per_sm = 0;
     SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, getrf_panel_kernel<T>,
                                                                kPanelThreads, 0));

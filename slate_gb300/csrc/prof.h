@@ -18,4 +18,7 @@ namespace slt {
 void count_launch();
 int prof_begin(int kind, cudaStream_t s);
 void prof_end(int idx, cudaStream_t s, double flops, double bytes);
+// The SM count a launcher may use on the calling thread: sms, or the cap set
+// by slt_set_sm_cap when it is smaller.
+int capped_sms(int sms);
 }

@@ -29,6 +29,10 @@ static std::vector<Rec> g_recs;
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+static thread_local int t_sm_cap = 0;
+
+int capped_sms(int sms) { return (t_sm_cap > 0 && t_sm_cap < sms) ? t_sm_cap : sms; }
+
 int prof_begin(int kind, cudaStream_t s)
 {
     if (!g_on.load(std::memory_order_relaxed)) return -1;
@@ -93,3 +97,12 @@ extern "C" int slt_profile_read(int kind, double* flops, double* bytes, double* 
     if (launches) *launches = c;
     return SLT_OK;
 }
+
+extern "C" int slt_set_sm_cap(int sms)
+{
+    const int prev = slt::t_sm_cap;
+    slt::t_sm_cap = sms > 0 ? sms : 0;
+    return prev;
+}
+
+extern "C" int slt_sm_cap(void) { return slt::t_sm_cap; }

@@ -27,6 +27,24 @@ extern "C" {
 #define SLT_ERR_CUDA_BASE   1000
 #endif
 
+/* ---- SM budget ---------------------------------------------------------------
+ * Number of SMs that the panel and trailing-update launchers may occupy with
+ * the launches that the calling thread issues next (0: all).  The lookahead
+ * schedule of the drivers gives the panel of step k+1 and the update of step
+ * k disjoint shares of the SMs, so the two run side by side.  Returns the
+ * previous value. */
+int slt_set_sm_cap(int sms);
+int slt_sm_cap(void);
+
+/* ---- type-generic helpers (type 0 float, 1 double, 2 complex<float>,
+ * 3 complex<double>; complex arrays interleave real and imaginary parts) ----
+ * xtranspose: B (n x m) = A^T, or A^H when conj != 0 (complex types).
+ * xcopy_tri: the lower (upper = 0) or upper (upper = 1) triangle of D <- S. */
+int slt_xtranspose(int type, int64_t m, int64_t n, const void* A, int64_t lda, void* B, int64_t ldb, int conj,
+                   cudaStream_t stream);
+int slt_xcopy_tri(int type, int upper, int64_t n, const void* S, int64_t lds, void* D, int64_t ldd,
+                  cudaStream_t stream);
+
 /* ---- trailing-matrix update GEMM:  C = alpha A op(B) + beta C --------------
  * transb 'N': B is k x n;  'T': B is n x k (C -= A B^T, the Cholesky update).
  * lower != 0: only the lower triangle (i >= j) of C is computed and written.

@@ -871,7 +871,7 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
                 }
                 const size_t psm = tcp_smem_bytes();
                 const int64_t tiles = (mp / kTcBM) * (np / kTcBN);
-                const unsigned grid1 = unsigned(std::min<int64_t>(tiles, g_sms));
+                const unsigned grid1 = unsigned(std::min<int64_t>(tiles, capped_sms(g_sms)));
                 if (tf32) {
                     SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<1>, psm);
                     if (!rc) tc_update_persistent<1><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(2, kTcBM, kTcBN));
