@@ -3,7 +3,8 @@
  *
  * Names and argument meaning follow SLATE's generated C API
  * (tools/c_api/generate_matrix.py, src/c_api/wrappers.cc:692-1080,
- * include/slate/c_api/types.h), for real single and double precision:
+ * include/slate/c_api/types.h), for single and double precision, real
+ * (r32, r64) and complex (c32, c64):
  *   slate_Options_create / _destroy / _copy / _set_<Option> / _get_<Option>
  *   slate_Pivots_create / _destroy
  *   slate_Matrix_create_fromScaLAPACK_{r32,r64} / slate_Matrix_destroy_*
@@ -43,6 +44,11 @@ typedef struct slate_Pivots_struct* slate_Pivots;
 typedef struct slate_Matrix_struct_r64* slate_Matrix_r64;
 typedef struct slate_Matrix_struct_r32* slate_Matrix_r32;
 typedef struct slate_HermitianMatrix_struct_r64* slate_HermitianMatrix_r64;
+typedef struct slate_Matrix_struct_c32* slate_Matrix_c32;
+typedef struct slate_Matrix_struct_c64* slate_Matrix_c64;
+typedef struct slate_HermitianMatrix_struct_r32* slate_HermitianMatrix_r32;
+typedef struct slate_HermitianMatrix_struct_c32* slate_HermitianMatrix_c32;
+typedef struct slate_HermitianMatrix_struct_c64* slate_HermitianMatrix_c64;
 
 slate_Options slate_Options_create(void);
 void slate_Options_destroy(slate_Options opts);
@@ -128,6 +134,49 @@ void slate_chol_solve_using_factor_r64(slate_HermitianMatrix_r64 A, slate_Matrix
 void slate_chol_inverse_using_factor_r64(slate_HermitianMatrix_r64 A, slate_Options opts);
 double slate_chol_rcondest_using_factor_r64(slate_Norm norm, slate_HermitianMatrix_r64 A, double Anorm,
                                             slate_Options opts);
+
+/* Complex precisions (c32 = complex<float>, c64 = complex<double>; the
+ * arrays hold interleaved real and imaginary parts, the layout of C99
+ * float/double _Complex) and the single-precision Cholesky forms: SLATE's
+ * c32 / c64 / r32 instantiations of the same wrappers
+ * (src/c_api/wrappers.cc:692-1080). */
+slate_Matrix_c32 slate_Matrix_create_fromScaLAPACK_c32(int64_t m, int64_t n, void* A, int64_t lda, int64_t mb,
+                                                       int64_t nb, int p, int q, slate_mpi_comm_t mpi_comm);
+slate_Matrix_c64 slate_Matrix_create_fromScaLAPACK_c64(int64_t m, int64_t n, void* A, int64_t lda, int64_t mb,
+                                                       int64_t nb, int p, int q, slate_mpi_comm_t mpi_comm);
+void slate_Matrix_destroy_c32(slate_Matrix_c32 A);
+void slate_Matrix_destroy_c64(slate_Matrix_c64 A);
+slate_HermitianMatrix_r32 slate_HermitianMatrix_create_fromScaLAPACK_r32(slate_Uplo uplo, int64_t n, float* A,
+                                                                         int64_t lda, int64_t nb, int p, int q,
+                                                                         slate_mpi_comm_t mpi_comm);
+slate_HermitianMatrix_c32 slate_HermitianMatrix_create_fromScaLAPACK_c32(slate_Uplo uplo, int64_t n, void* A,
+                                                                         int64_t lda, int64_t nb, int p, int q,
+                                                                         slate_mpi_comm_t mpi_comm);
+slate_HermitianMatrix_c64 slate_HermitianMatrix_create_fromScaLAPACK_c64(slate_Uplo uplo, int64_t n, void* A,
+                                                                         int64_t lda, int64_t nb, int p, int q,
+                                                                         slate_mpi_comm_t mpi_comm);
+void slate_HermitianMatrix_destroy_r32(slate_HermitianMatrix_r32 A);
+void slate_HermitianMatrix_destroy_c32(slate_HermitianMatrix_c32 A);
+void slate_HermitianMatrix_destroy_c64(slate_HermitianMatrix_c64 A);
+
+void slate_lu_solve_c32(slate_Matrix_c32 A, slate_Matrix_c32 B, slate_Options opts);
+void slate_lu_factor_c32(slate_Matrix_c32 A, slate_Pivots pivots, slate_Options opts);
+void slate_lu_solve_using_factor_c32(slate_Matrix_c32 A, slate_Pivots pivots, slate_Matrix_c32 B,
+                                     slate_Options opts);
+void slate_lu_solve_c64(slate_Matrix_c64 A, slate_Matrix_c64 B, slate_Options opts);
+void slate_lu_factor_c64(slate_Matrix_c64 A, slate_Pivots pivots, slate_Options opts);
+void slate_lu_solve_using_factor_c64(slate_Matrix_c64 A, slate_Pivots pivots, slate_Matrix_c64 B,
+                                     slate_Options opts);
+
+void slate_chol_solve_r32(slate_HermitianMatrix_r32 A, slate_Matrix_r32 B, slate_Options opts);
+void slate_chol_factor_r32(slate_HermitianMatrix_r32 A, slate_Options opts);
+void slate_chol_solve_using_factor_r32(slate_HermitianMatrix_r32 A, slate_Matrix_r32 B, slate_Options opts);
+void slate_chol_solve_c32(slate_HermitianMatrix_c32 A, slate_Matrix_c32 B, slate_Options opts);
+void slate_chol_factor_c32(slate_HermitianMatrix_c32 A, slate_Options opts);
+void slate_chol_solve_using_factor_c32(slate_HermitianMatrix_c32 A, slate_Matrix_c32 B, slate_Options opts);
+void slate_chol_solve_c64(slate_HermitianMatrix_c64 A, slate_Matrix_c64 B, slate_Options opts);
+void slate_chol_factor_c64(slate_HermitianMatrix_c64 A, slate_Options opts);
+void slate_chol_solve_using_factor_c64(slate_HermitianMatrix_c64 A, slate_Matrix_c64 B, slate_Options opts);
 
 /* Outcome of the last C-API call on this thread (no counterpart in SLATE,
  * whose C wrappers throw). */

@@ -187,6 +187,54 @@ int slt_dsposv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, co
                             int64_t ldb, double* dX, int64_t ldx, const slt_options* opts,
                             slt_stream_t stream, int* iter, int64_t* info);
 
+/* Single precision forms of getrs (Trans / ConjTrans), potrs and posv
+ * (lower), as the double ones above. */
+int slt_sgetrs_trans_device(char trans, int64_t n, int64_t nrhs, const float* dLU, int64_t lda,
+                            const int* d_ipiv, float* dB, int64_t ldb, const slt_options* opts,
+                            slt_stream_t stream);
+int slt_spotrs_device(int64_t n, int64_t nrhs, const float* dL, int64_t lda, float* dB, int64_t ldb,
+                      const slt_options* opts, slt_stream_t stream);
+int slt_sposv_device(int64_t n, int64_t nrhs, float* dA, int64_t lda, float* dB, int64_t ldb,
+                     const slt_options* opts, slt_stream_t stream, int64_t* info);
+
+/* Complex precisions: 'c' = complex<float>, 'z' = complex<double>.  Arrays
+ * are column-major with interleaved (real, imaginary) pairs, the layout of
+ * std::complex, C99 _Complex and cuComplex; pivots and info as for the real
+ * forms; the Cholesky forms use the lower triangle of a Hermitian matrix.
+ * SLATE's complex instantiations of getrf / getrs (trans 'N', 'T', 'C') /
+ * gesv / potrf / potrs / posv (src/getrf.cc, src/getrs.cc, src/gesv.cc,
+ * src/potrf.cc, src/potrs.cc, src/posv.cc). */
+int slt_cgetrf_device(int64_t m, int64_t n, void* dA, int64_t lda, int* d_ipiv, const slt_options* opts,
+                      slt_stream_t stream, int64_t* info);
+int slt_zgetrf_device(int64_t m, int64_t n, void* dA, int64_t lda, int* d_ipiv, const slt_options* opts,
+                      slt_stream_t stream, int64_t* info);
+int slt_cgetrs_device(char trans, int64_t n, int64_t nrhs, const void* dLU, int64_t lda, const int* d_ipiv,
+                      void* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream);
+int slt_zgetrs_device(char trans, int64_t n, int64_t nrhs, const void* dLU, int64_t lda, const int* d_ipiv,
+                      void* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream);
+int slt_cgesv_device(int64_t n, int64_t nrhs, void* dA, int64_t lda, int* d_ipiv, void* dB, int64_t ldb,
+                     const slt_options* opts, slt_stream_t stream, int64_t* info);
+int slt_zgesv_device(int64_t n, int64_t nrhs, void* dA, int64_t lda, int* d_ipiv, void* dB, int64_t ldb,
+                     const slt_options* opts, slt_stream_t stream, int64_t* info);
+int slt_cpotrf_device(int64_t n, void* dA, int64_t lda, const slt_options* opts, slt_stream_t stream,
+                      int64_t* info);
+int slt_zpotrf_device(int64_t n, void* dA, int64_t lda, const slt_options* opts, slt_stream_t stream,
+                      int64_t* info);
+int slt_cpotrs_device(int64_t n, int64_t nrhs, const void* dL, int64_t lda, void* dB, int64_t ldb,
+                      const slt_options* opts, slt_stream_t stream);
+int slt_zpotrs_device(int64_t n, int64_t nrhs, const void* dL, int64_t lda, void* dB, int64_t ldb,
+                      const slt_options* opts, slt_stream_t stream);
+int slt_cposv_device(int64_t n, int64_t nrhs, void* dA, int64_t lda, void* dB, int64_t ldb,
+                     const slt_options* opts, slt_stream_t stream, int64_t* info);
+int slt_zposv_device(int64_t n, int64_t nrhs, void* dA, int64_t lda, void* dB, int64_t ldb,
+                     const slt_options* opts, slt_stream_t stream, int64_t* info);
+/* slate::gesv_mixed<complex<double>, complex<float>>, src/gesv_mixed.cc:105-289
+ * (complex<float> LU, complex<double> refinement, fallback to a complex<double>
+ * LU; A unchanged unless the fallback ran). */
+int slt_zcgesv_device(int64_t n, int64_t nrhs, void* dA, int64_t lda, int* d_ipiv, const void* dB, int64_t ldb,
+                      void* dX, int64_t ldx, const slt_options* opts, slt_stream_t stream, int* iter,
+                      int64_t* info);
+
 /* FP64 residual R = B - A X (A n x n general, or symmetric with lower
  * storage when sym_lower != 0), as the kernel layer's slt_dresidual
  * computes it, but with no device allocation and no caller scratch.  It is
@@ -248,6 +296,14 @@ long long slt_launch_count(void);
 void slt_profile_enable(int on);
 int slt_profile_read(int kind, double* flops, double* bytes, double* seconds, long long* launches);
 
+/* Device workspace of the drivers comes from a stream-ordered pool owned by
+ * the library, one per device, which keeps freed memory reserved for the
+ * next call (a repeated solve does not map its workspace afresh).  This
+ * returns the pool's unused memory on the current device to the system
+ * (synchronises the device).  SLATE frees its workspace with
+ * Matrix::releaseWorkspace (include/slate/BaseMatrix.hh). */
+int slt_release_workspace(void);
+
 /* Seconds spent in named phases of the last driver call on this thread
  * (the keys of SLATE's slate::timers map, e.g. "gesv_mixed::getrf_lo");
  * returns -1 if the key is unknown. */
@@ -304,6 +360,57 @@ void slate_dsposv_(const char* uplo, const int* n, const int* nrhs, double* a, c
 void slate_dposv_(const char* uplo, const int* n, const int* nrhs, double* a, const int* lda,
                   double* b, const int* ldb, int* info);
 void slate_dpotrf_(const char* uplo, const int* n, double* a, const int* lda, int* info);
+/* The other precisions of the same entry points (lapack_api/lapack_gesv.cc:
+ * 25-45, lapack_getrf.cc, lapack_getrs.cc:19-22, lapack_posv.cc:22-25,
+ * lapack_potrf.cc:20-23, lapack_gesv_mixed.cc:30-33), each also exported with
+ * a trailing underscore.  Complex arrays (void*) hold interleaved (real,
+ * imaginary) pairs: std::complex, C99 _Complex, Fortran COMPLEX. */
+void slate_sgetrs(const char* trans, const int* n, const int* nrhs, float* a, const int* lda, int* ipiv,
+                  float* b, const int* ldb, int* info);
+void slate_cgetrs(const char* trans, const int* n, const int* nrhs, void* a, const int* lda, int* ipiv,
+                  void* b, const int* ldb, int* info);
+void slate_zgetrs(const char* trans, const int* n, const int* nrhs, void* a, const int* lda, int* ipiv,
+                  void* b, const int* ldb, int* info);
+void slate_cgesv(const int* n, const int* nrhs, void* a, const int* lda, int* ipiv, void* b, const int* ldb,
+                 int* info);
+void slate_zgesv(const int* n, const int* nrhs, void* a, const int* lda, int* ipiv, void* b, const int* ldb,
+                 int* info);
+void slate_cgetrf(const int* m, const int* n, void* a, const int* lda, int* ipiv, int* info);
+void slate_zgetrf(const int* m, const int* n, void* a, const int* lda, int* ipiv, int* info);
+void slate_sposv(const char* uplo, const int* n, const int* nrhs, float* a, const int* lda, float* b,
+                 const int* ldb, int* info);
+void slate_cposv(const char* uplo, const int* n, const int* nrhs, void* a, const int* lda, void* b,
+                 const int* ldb, int* info);
+void slate_zposv(const char* uplo, const int* n, const int* nrhs, void* a, const int* lda, void* b,
+                 const int* ldb, int* info);
+void slate_spotrf(const char* uplo, const int* n, float* a, const int* lda, int* info);
+void slate_cpotrf(const char* uplo, const int* n, void* a, const int* lda, int* info);
+void slate_zpotrf(const char* uplo, const int* n, void* a, const int* lda, int* info);
+void slate_zcgesv(const int* n, const int* nrhs, void* a, const int* lda, int* ipiv, void* b, const int* ldb,
+                  void* x, const int* ldx, void* work, void* swork, int* iter, int* info);
+void slate_sgetrs_(const char* trans, const int* n, const int* nrhs, float* a, const int* lda, int* ipiv,
+                   float* b, const int* ldb, int* info);
+void slate_cgetrs_(const char* trans, const int* n, const int* nrhs, void* a, const int* lda, int* ipiv,
+                   void* b, const int* ldb, int* info);
+void slate_zgetrs_(const char* trans, const int* n, const int* nrhs, void* a, const int* lda, int* ipiv,
+                   void* b, const int* ldb, int* info);
+void slate_cgesv_(const int* n, const int* nrhs, void* a, const int* lda, int* ipiv, void* b, const int* ldb,
+                  int* info);
+void slate_zgesv_(const int* n, const int* nrhs, void* a, const int* lda, int* ipiv, void* b, const int* ldb,
+                  int* info);
+void slate_cgetrf_(const int* m, const int* n, void* a, const int* lda, int* ipiv, int* info);
+void slate_zgetrf_(const int* m, const int* n, void* a, const int* lda, int* ipiv, int* info);
+void slate_sposv_(const char* uplo, const int* n, const int* nrhs, float* a, const int* lda, float* b,
+                  const int* ldb, int* info);
+void slate_cposv_(const char* uplo, const int* n, const int* nrhs, void* a, const int* lda, void* b,
+                  const int* ldb, int* info);
+void slate_zposv_(const char* uplo, const int* n, const int* nrhs, void* a, const int* lda, void* b,
+                  const int* ldb, int* info);
+void slate_spotrf_(const char* uplo, const int* n, float* a, const int* lda, int* info);
+void slate_cpotrf_(const char* uplo, const int* n, void* a, const int* lda, int* info);
+void slate_zpotrf_(const char* uplo, const int* n, void* a, const int* lda, int* info);
+void slate_zcgesv_(const int* n, const int* nrhs, void* a, const int* lda, int* ipiv, void* b, const int* ldb,
+                   void* x, const int* ldx, void* work, void* swork, int* iter, int* info);
 /* lapack_api/lapack_getri.cc, lapack_potri.cc, lapack_gecon.cc, lapack_pocon.cc
  * (gecon / pocon take the factors without pivots, as LAPACK's do; work and
  * iwork are not used) */

@@ -145,7 +145,7 @@ def _dev(x, dtype=None):
         raise TypeError("expected a CUDA tensor")
     if dtype is not None and x.dtype != dtype:
         raise TypeError("expected dtype %s, got %s" % (dtype, x.dtype))
-    if x.dim() != 2 or x.stride(0) != 1:
+    if x.dim() != 2 or (x.stride(0) != 1 and x.shape[0] > 1):
         raise ValueError("expected a column-major 2-D tensor (use slate_gb300.colmajor)")
     return ctypes.c_void_p(x.data_ptr())
 
@@ -160,6 +160,34 @@ def _opts(opts):
     return ctypes.byref(o._c()), o
 
 
+def _prefix(t):
+    """SLATE's precision letter of a tensor: s, d, c (complex<float>) or z."""
+    import torch
+    p = {torch.float32: "s", torch.float64: "d", torch.complex64: "c", torch.complex128: "z"}.get(t.dtype)
+    if p is None:
+        raise TypeError("unsupported dtype %s" % t.dtype)
+    return p
+
+
+_I64, _VP, _OPTP = ctypes.c_int64, ctypes.c_void_p, ctypes.POINTER(_Options)
+_DP = ctypes.POINTER(ctypes.c_int64)
+_SIGS = {
+    "getrf": [_I64, _I64, _VP, _I64, _VP, _OPTP, _VP, _DP],
+    "getrs_c": [ctypes.c_char, _I64, _I64, _VP, _I64, _VP, _VP, _I64, _OPTP, _VP],
+    "gesv": [_I64, _I64, _VP, _I64, _VP, _VP, _I64, _OPTP, _VP, _DP],
+    "potrf": [_I64, _VP, _I64, _OPTP, _VP, _DP],
+    "potrs": [_I64, _I64, _VP, _I64, _VP, _I64, _OPTP, _VP],
+    "posv": [_I64, _I64, _VP, _I64, _VP, _I64, _OPTP, _VP, _DP],
+}
+
+
+def _entry(name, sig):
+    f = getattr(lib(), name)
+    f.argtypes = _SIGS[sig]
+    f.restype = ctypes.c_int
+    return f
+
+
 def _ipiv_buf(n, device):
     import torch
     return torch.zeros(max(n, 1), dtype=torch.int32, device=device)
@@ -168,14 +196,14 @@ def _ipiv_buf(n, device):
 # ---------------------------------------------------------------------------
 # SLATE drivers (include/slate/slate.hh:503-770)
 def getrf(A, opts=None):
-    """LU with partial pivoting in place (slate::getrf).  Returns (info, ipiv)
-    with ipiv per panel (row of panel k relative to row k*nb)."""
-    import torch
+    """LU with partial pivoting in place (slate::getrf), float32 / float64 /
+    complex64 / complex128.  Returns (info, ipiv) with ipiv per panel (row of
+    panel k relative to row k*nb)."""
     po, o = _opts(opts)
     m, n = A.shape
     ipiv = _ipiv_buf(min(m, n), A.device)
     info = ctypes.c_int64(0)
-    f = lib().slt_dgetrf_device if A.dtype == torch.float64 else lib().slt_sgetrf_device
+    f = _entry("slt_%sgetrf_device" % _prefix(A), "getrf")
     _check(f(m, n, _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), po, _stream(), ctypes.byref(info)))
     return int(info.value), ipiv[:min(m, n)]
 
@@ -183,20 +211,21 @@ def getrf(A, opts=None):
 def getrs(A, ipiv, B, opts=None, trans="N"):
     """Solve op(A) X = B with the factors of getrf, op = trans ('N', 'T' or
     'C'); B is overwritten (slate::getrs)."""
-    import torch
     po, o = _opts(opts)
     n = A.shape[0]
-    if trans.upper() != "N":
-        if A.dtype != torch.float64:
-            raise TypeError("transposed getrs is FP64")
-        f = lib().slt_dgetrs_trans_device
-        f.restype = ctypes.c_int
-        f.argtypes = [ctypes.c_char, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
-                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(_Options), ctypes.c_void_p]
-        _check(f(trans.upper().encode(), n, B.shape[1], _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), _dev(B),
-                 _ld(B), po, _stream()))
+    p = _prefix(A)
+    t = trans.upper()
+    if p in "cz":
+        f = _entry("slt_%sgetrs_device" % p, "getrs_c")
+        _check(f(t.encode(), n, B.shape[1], _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), _dev(B), _ld(B), po,
+                 _stream()))
         return
-    f = lib().slt_dgetrs_device if A.dtype == torch.float64 else lib().slt_sgetrs_device
+    if t != "N":
+        f = _entry("slt_%sgetrs_trans_device" % p, "getrs_c")
+        _check(f(t.encode(), n, B.shape[1], _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), _dev(B), _ld(B), po,
+                 _stream()))
+        return
+    f = lib().slt_dgetrs_device if p == "d" else lib().slt_sgetrs_device
     _check(f(n, B.shape[1], _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), _dev(B), _ld(B), po,
              _stream()))
 
@@ -230,40 +259,44 @@ def pocondest(L, anorm, norm="1", opts=None):
 
 def gesv(A, B, opts=None):
     """slate::gesv: A <- LU, B <- X.  Returns (info, ipiv)."""
-    import torch
     po, o = _opts(opts)
     n = A.shape[0]
+    p = _prefix(A)
+    if p == "s":
+        info, ipiv = getrf(A, opts)
+        if info == 0:
+            getrs(A, ipiv, B, opts)
+        return info, ipiv
     ipiv = _ipiv_buf(n, A.device)
     info = ctypes.c_int64(0)
-    _check(lib().slt_dgesv_device(n, B.shape[1], _dev(A, torch.float64), _ld(A), ctypes.c_void_p(ipiv.data_ptr()),
-                                  _dev(B, torch.float64), _ld(B), po, _stream(), ctypes.byref(info)))
+    f = _entry("slt_%sgesv_device" % p, "gesv")
+    _check(f(n, B.shape[1], _dev(A), _ld(A), ctypes.c_void_p(ipiv.data_ptr()), _dev(B, A.dtype), _ld(B), po,
+             _stream(), ctypes.byref(info)))
     return int(info.value), ipiv[:n]
 
 
 def potrf(A, opts=None):
-    """Cholesky A = L L^T of the lower triangle in place (slate::potrf).  Returns info."""
-    import torch
+    """Cholesky A = L L^H of the lower triangle in place (slate::potrf).  Returns info."""
     po, o = _opts(opts)
-    n = A.shape[0]
     info = ctypes.c_int64(0)
-    f = lib().slt_dpotrf_device if A.dtype == torch.float64 else lib().slt_spotrf_device
-    _check(f(n, _dev(A), _ld(A), po, _stream(), ctypes.byref(info)))
+    f = _entry("slt_%spotrf_device" % _prefix(A), "potrf")
+    _check(f(A.shape[0], _dev(A), _ld(A), po, _stream(), ctypes.byref(info)))
     return int(info.value)
 
 
 def potrs(A, B, opts=None):
-    import torch
+    """slate::potrs with potrf's lower factor; B <- X."""
     po, o = _opts(opts)
-    _check(lib().slt_dpotrs_device(A.shape[0], B.shape[1], _dev(A, torch.float64), _ld(A),
-                                   _dev(B, torch.float64), _ld(B), po, _stream()))
+    f = _entry("slt_%spotrs_device" % _prefix(A), "potrs")
+    _check(f(A.shape[0], B.shape[1], _dev(A), _ld(A), _dev(B, A.dtype), _ld(B), po, _stream()))
 
 
 def posv(A, B, opts=None):
-    import torch
+    """slate::posv (lower): A <- L, B <- X.  Returns info."""
     po, o = _opts(opts)
     info = ctypes.c_int64(0)
-    _check(lib().slt_dposv_device(A.shape[0], B.shape[1], _dev(A, torch.float64), _ld(A),
-                                  _dev(B, torch.float64), _ld(B), po, _stream(), ctypes.byref(info)))
+    f = _entry("slt_%sposv_device" % _prefix(A), "posv")
+    _check(f(A.shape[0], B.shape[1], _dev(A), _ld(A), _dev(B, A.dtype), _ld(B), po, _stream(), ctypes.byref(info)))
     return int(info.value)
 
 
@@ -285,8 +318,22 @@ def _mixed(fn, chol, A, B, X, opts):
 
 
 def gesv_mixed(A, B, X, opts=None):
-    """slate::gesv_mixed: low-precision LU + FP64 iterative refinement.
+    """slate::gesv_mixed: low-precision LU + FP64 iterative refinement
+    (complex128: gesv_mixed<complex<double>, complex<float>>, zcgesv).
     Returns (info, iter, ipiv)."""
+    import torch
+    if A.dtype == torch.complex128:
+        po, o = _opts(opts)
+        n = A.shape[0]
+        info = ctypes.c_int64(0)
+        it = ctypes.c_int(0)
+        ipiv = _ipiv_buf(n, A.device)
+        f = lib().slt_zcgesv_device
+        f.restype = ctypes.c_int
+        _check(f(ctypes.c_int64(n), ctypes.c_int64(B.shape[1]), _dev(A), ctypes.c_int64(_ld(A)),
+                 ctypes.c_void_p(ipiv.data_ptr()), _dev(B, A.dtype), ctypes.c_int64(_ld(B)), _dev(X, A.dtype),
+                 ctypes.c_int64(_ld(X)), po, _stream(), ctypes.byref(it), ctypes.byref(info)))
+        return int(info.value), int(it.value), ipiv[:n]
     return _mixed(lib().slt_dsgesv_device, False, A, B, X, opts)
 
 

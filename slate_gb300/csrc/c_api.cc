@@ -141,6 +141,54 @@ int getrs_dev_any<float>(int64_t n, int64_t nrhs, const float* A, int64_t lda, c
                          int64_t ldb, const slt_options* o, cudaStream_t s)
 { return slt_sgetrs_device(n, nrhs, A, lda, ipiv, B, ldb, o, s); }
 
+// complex elements as the C API passes them (interleaved real, imaginary)
+struct CX32 { float re, im; };
+struct CX64 { double re, im; };
+
+template <>
+int getrf_dev_any<CX32>(int64_t n, CX32* A, int64_t lda, int* ipiv, const slt_options* o, cudaStream_t s,
+                        int64_t* info)
+{ return slt_cgetrf_device(n, n, A, lda, ipiv, o, s, info); }
+template <>
+int getrf_dev_any<CX64>(int64_t n, CX64* A, int64_t lda, int* ipiv, const slt_options* o, cudaStream_t s,
+                        int64_t* info)
+{ return slt_zgetrf_device(n, n, A, lda, ipiv, o, s, info); }
+template <>
+int getrs_dev_any<CX32>(int64_t n, int64_t nrhs, const CX32* A, int64_t lda, const int* ipiv, CX32* B,
+                        int64_t ldb, const slt_options* o, cudaStream_t s)
+{ return slt_cgetrs_device('N', n, nrhs, A, lda, ipiv, B, ldb, o, s); }
+template <>
+int getrs_dev_any<CX64>(int64_t n, int64_t nrhs, const CX64* A, int64_t lda, const int* ipiv, CX64* B,
+                        int64_t ldb, const slt_options* o, cudaStream_t s)
+{ return slt_zgetrs_device('N', n, nrhs, A, lda, ipiv, B, ldb, o, s); }
+
+// Cholesky device entry points and type code (slt_xtranspose) per type.
+template <typename T> struct CholDev;
+template <> struct CholDev<float> {
+    static constexpr int type = 0;
+    static int potrf(int64_t n, float* A, int64_t lda, const slt_options* o, cudaStream_t s, int64_t* info)
+    { return slt_spotrf_device(n, A, lda, o, s, info); }
+    static int potrs(int64_t n, int64_t r, const float* A, int64_t lda, float* B, int64_t ldb, const slt_options* o,
+                     cudaStream_t s)
+    { return slt_spotrs_device(n, r, A, lda, B, ldb, o, s); }
+};
+template <> struct CholDev<CX32> {
+    static constexpr int type = 2;
+    static int potrf(int64_t n, CX32* A, int64_t lda, const slt_options* o, cudaStream_t s, int64_t* info)
+    { return slt_cpotrf_device(n, A, lda, o, s, info); }
+    static int potrs(int64_t n, int64_t r, const CX32* A, int64_t lda, CX32* B, int64_t ldb, const slt_options* o,
+                     cudaStream_t s)
+    { return slt_cpotrs_device(n, r, A, lda, B, ldb, o, s); }
+};
+template <> struct CholDev<CX64> {
+    static constexpr int type = 3;
+    static int potrf(int64_t n, CX64* A, int64_t lda, const slt_options* o, cudaStream_t s, int64_t* info)
+    { return slt_zpotrf_device(n, A, lda, o, s, info); }
+    static int potrs(int64_t n, int64_t r, const CX64* A, int64_t lda, CX64* B, int64_t ldb, const slt_options* o,
+                     cudaStream_t s)
+    { return slt_zpotrs_device(n, r, A, lda, B, ldb, o, s); }
+};
+
 // lu_factor (+ lu_solve_using_factor when B is given): A <- LU, pivots
 // recorded in P, B <- X.  SLATE skips the solve when info != 0.
 template <typename T>
@@ -299,6 +347,60 @@ int chol_run(CMat<double>* A, CMat<double>* B, slate_Options h, CholOp op, int64
         else {
             std::vector<double> hbuf(size_t(n) * size_t(n));
             SLT_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), src, sizeof(double) * hbuf.size(), cudaMemcpyDeviceToHost, s));
+            SLT_CUDA_TRY(cudaStreamSynchronize(s));
+            for (int64_t j = 0; j < n; ++j)
+                for (int64_t i = up ? 0 : j; i < (up ? j + 1 : n); ++i)
+                    A->data[i + j * A->ld] = hbuf[size_t(i) + size_t(j) * size_t(n)];
+        }
+    }
+    if (B) TRY(vb.close(*B, s));
+    SLT_CUDA_TRY(cudaStreamSynchronize(s));
+    return SLT_OK;
+}
+
+// chol_run for the other precisions (no inverse): the referenced triangle is
+// brought to lower storage (conjugate-transposed when uplo = 'U'), factored
+// or solved with, and written back to the referenced triangle only.
+template <typename T>
+int chol_run_any(CMat<T>* A, CMat<T>* B, slate_Options h, CholOp op, int64_t* info)
+{
+    *info = 0;
+    if (op == kInverse) return SLT_ERR_NOT_SUPPORTED;
+    const bool needs_b = op == kSolve || op == kSolveFactored;
+    if (!A || A->m != A->n || (needs_b && (!B || B->m != A->n))) return SLT_ERR_ARG;
+    const int64_t n = A->n;
+    if (n == 0) return SLT_OK;
+    cudaStream_t s = cstream();
+    if (!s) return SLT_ERR_NO_DEVICE;
+    slt_options o = opts_for(h, A->nb);
+    const bool up = A->uplo == 'U';
+    constexpr int ty = CholDev<T>::type;
+    DevBuf L, T2;
+    TRY(L.alloc(sizeof(T) * size_t(n) * size_t(n), s));
+    SLT_CUDA_TRY(cudaMemcpy2DAsync(L.p, size_t(n) * sizeof(T), A->data, size_t(A->ld) * sizeof(T),
+                                   size_t(n) * sizeof(T), size_t(n),
+                                   A->dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    if (up) {
+        TRY(T2.alloc(sizeof(T) * size_t(n) * size_t(n), s));
+        TRY(slt_xtranspose(ty, n, n, L.p, n, T2.p, n, 1, s));
+        std::swap(L.p, T2.p);
+    }
+    View<T> vb;
+    if (B) TRY(vb.open(*B, s));
+    if (op == kFactor || op == kSolve) TRY(CholDev<T>::potrf(n, L.as<T>(), n, &o, s, info));
+    if (needs_b && *info == 0 && B->n > 0) TRY(CholDev<T>::potrs(n, B->n, L.as<T>(), n, vb.p, vb.ld, &o, s));
+    if (op != kSolveFactored) {
+        const void* src = L.p;
+        if (up) {
+            TRY(slt_xtranspose(ty, n, n, L.p, n, T2.p, n, 1, s));
+            src = T2.p;
+        }
+        if (A->dev) {
+            TRY(slt_xcopy_tri(ty, up ? 1 : 0, n, src, n, A->data, A->ld, s));
+        }
+        else {
+            std::vector<T> hbuf(size_t(n) * size_t(n));
+            SLT_CUDA_TRY(cudaMemcpyAsync(hbuf.data(), src, sizeof(T) * hbuf.size(), cudaMemcpyDeviceToHost, s));
             SLT_CUDA_TRY(cudaStreamSynchronize(s));
             for (int64_t j = 0; j < n; ++j)
                 for (int64_t i = up ? 0 : j; i < (up ? j + 1 : n); ++i)
@@ -531,6 +633,82 @@ double slate_lu_rcondest_using_factor_r64(slate_Norm norm, slate_Matrix_r64 A, d
     finish(st, 0);
     return r;
 }
+
+// ---- complex precisions and single-precision Cholesky (SLATE's c32 / c64 /
+// r32 instantiations, src/c_api/wrappers.cc:692-1080)
+#define SLT_CMAT(R, T)                                                                                          \
+slate_Matrix_##R slate_Matrix_create_fromScaLAPACK_##R(int64_t m, int64_t n, void* A, int64_t lda, int64_t mb, \
+                                                       int64_t nb, int p, int q, slate_mpi_comm_t)               \
+{ return reinterpret_cast<slate_Matrix_##R>(make<T>(m, n, static_cast<T*>(A), lda, mb, nb, p, q, 'G')); }       \
+void slate_Matrix_destroy_##R(slate_Matrix_##R A) { delete reinterpret_cast<CMat<T>*>(A); }                     \
+slate_HermitianMatrix_##R slate_HermitianMatrix_create_fromScaLAPACK_##R(slate_Uplo uplo, int64_t n, void* A,   \
+                                                                         int64_t lda, int64_t nb, int p, int q,  \
+                                                                         slate_mpi_comm_t)                       \
+{                                                                                                                \
+    const char u = (uplo == 'u' || uplo == 'U') ? 'U' : (uplo == 'l' || uplo == 'L') ? 'L' : 0;                 \
+    if (!u) return nullptr;                                                                                      \
+    return reinterpret_cast<slate_HermitianMatrix_##R>(make<T>(n, n, static_cast<T*>(A), lda, nb, nb, p, q, u)); \
+}                                                                                                                \
+void slate_HermitianMatrix_destroy_##R(slate_HermitianMatrix_##R A) { delete reinterpret_cast<CMat<T>*>(A); }
+SLT_CMAT(c32, CX32)
+SLT_CMAT(c64, CX64)
+#undef SLT_CMAT
+
+slate_HermitianMatrix_r32 slate_HermitianMatrix_create_fromScaLAPACK_r32(slate_Uplo uplo, int64_t n, float* A,
+                                                                         int64_t lda, int64_t nb, int p, int q,
+                                                                         slate_mpi_comm_t)
+{
+    const char u = (uplo == 'u' || uplo == 'U') ? 'U' : (uplo == 'l' || uplo == 'L') ? 'L' : 0;
+    if (!u) return nullptr;
+    return reinterpret_cast<slate_HermitianMatrix_r32>(make<float>(n, n, A, lda, nb, nb, p, q, u));
+}
+void slate_HermitianMatrix_destroy_r32(slate_HermitianMatrix_r32 A) { delete reinterpret_cast<CMat<float>*>(A); }
+
+#define SLT_CLU(R, T)                                                                                           \
+void slate_lu_solve_##R(slate_Matrix_##R A, slate_Matrix_##R B, slate_Options opts)                             \
+{                                                                                                                \
+    int64_t info = 0;                                                                                            \
+    slate_Pivots_struct P;                                                                                       \
+    const int rc = lu_run<T>(reinterpret_cast<CMat<T>*>(A), &P, reinterpret_cast<CMat<T>*>(B), opts, &info);    \
+    finish(rc, info);                                                                                            \
+}                                                                                                                \
+void slate_lu_factor_##R(slate_Matrix_##R A, slate_Pivots pivots, slate_Options opts)                           \
+{                                                                                                                \
+    int64_t info = 0;                                                                                            \
+    const int rc = lu_run<T>(reinterpret_cast<CMat<T>*>(A), pivots, nullptr, opts, &info);                       \
+    finish(rc, info);                                                                                            \
+}                                                                                                                \
+void slate_lu_solve_using_factor_##R(slate_Matrix_##R A, slate_Pivots pivots, slate_Matrix_##R B,               \
+                                     slate_Options opts)                                                         \
+{ finish(lu_solve_factored<T>(reinterpret_cast<CMat<T>*>(A), pivots, reinterpret_cast<CMat<T>*>(B), opts), 0); }
+SLT_CLU(c32, CX32)
+SLT_CLU(c64, CX64)
+#undef SLT_CLU
+
+#define SLT_CCHOL(R, T)                                                                                         \
+void slate_chol_solve_##R(slate_HermitianMatrix_##R A, slate_Matrix_##R B, slate_Options opts)                  \
+{                                                                                                                \
+    int64_t info = 0;                                                                                            \
+    const int rc = chol_run_any<T>(reinterpret_cast<CMat<T>*>(A), reinterpret_cast<CMat<T>*>(B), opts, kSolve, &info); \
+    finish(rc, info);                                                                                            \
+}                                                                                                                \
+void slate_chol_factor_##R(slate_HermitianMatrix_##R A, slate_Options opts)                                     \
+{                                                                                                                \
+    int64_t info = 0;                                                                                            \
+    const int rc = chol_run_any<T>(reinterpret_cast<CMat<T>*>(A), nullptr, opts, kFactor, &info);               \
+    finish(rc, info);                                                                                            \
+}                                                                                                                \
+void slate_chol_solve_using_factor_##R(slate_HermitianMatrix_##R A, slate_Matrix_##R B, slate_Options opts)     \
+{                                                                                                                \
+    int64_t info = 0;                                                                                            \
+    const int rc = chol_run_any<T>(reinterpret_cast<CMat<T>*>(A), reinterpret_cast<CMat<T>*>(B), opts,           \
+                                   kSolveFactored, &info);                                                       \
+    finish(rc, info);                                                                                            \
+}
+SLT_CCHOL(r32, float)
+SLT_CCHOL(c32, CX32)
+SLT_CCHOL(c64, CX64)
+#undef SLT_CCHOL
 
 int64_t slate_gb300_last_info(void) { return g_info; }
 int slate_gb300_last_status(void) { return g_status; }

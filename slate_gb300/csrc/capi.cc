@@ -391,6 +391,42 @@ int slt_dsposv_gmres_device(int64_t n, int64_t nrhs, double* dA, int64_t lda, co
                                 as_stream(stream));
 }
 
+int slt_sgetrs_trans_device(char trans, int64_t n, int64_t nrhs, const float* dLU, int64_t lda, const int* d_ipiv,
+                            float* dB, int64_t ldb, const slt_options* opts, slt_stream_t stream)
+{
+    if (trans == 'N' || trans == 'n') return slt_sgetrs_device(n, nrhs, dLU, lda, d_ipiv, dB, ldb, opts, stream);
+    if (trans != 'T' && trans != 't' && trans != 'C' && trans != 'c') return SLT_ERR_ARG;
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    Status st;
+    int rc = st.init(s);
+    if (rc) return rc;
+    rc = getrs_trans_dev<float>(n, nrhs, dLU, lda, d_ipiv, o.nb > 0 ? o.nb : 512, dB, ldb, st.fc.d_status, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, nullptr, s);
+}
+
+int slt_spotrs_device(int64_t n, int64_t nrhs, const float* dL, int64_t lda, float* dB, int64_t ldb,
+                      const slt_options* opts, slt_stream_t stream)
+{
+    cudaStream_t s = as_stream(stream);
+    slt_options o = resolve(opts);
+    Status st;
+    int rc = st.init(s);
+    if (rc) return rc;
+    rc = potrs_dev<float>(n, nrhs, dL, lda, o.nb, dB, ldb, st.fc.d_status, s);
+    if (rc) return rc;
+    return finish_factor(st.fc, nullptr, s);
+}
+
+int slt_sposv_device(int64_t n, int64_t nrhs, float* dA, int64_t lda, float* dB, int64_t ldb,
+                     const slt_options* opts, slt_stream_t stream, int64_t* info)
+{
+    int rc = slt_spotrf_device(n, dA, lda, opts, stream, info);
+    if (rc || *info != 0) return rc;       // SLATE skips the solve when info != 0 (src/posv.cc:85-91)
+    return slt_spotrs_device(n, nrhs, dA, lda, dB, ldb, opts, stream);
+}
+
 int slt_dgenerate_device(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
                          double* dA, int64_t lda, slt_stream_t stream)
 {
