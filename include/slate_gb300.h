@@ -62,6 +62,12 @@ typedef struct slt_options {
     int64_t depth;            /* Option::Depth of gesv_rbt's butterflies, default 2 */
     int     method_lu;        /* Option::MethodLU: 'P' partial pivoting (default,
                                  also '*'), 'N' no pivoting, 'C' CALU      */
+    int     residual_engine;  /* FP64 residuals of the mixed solvers: 0 auto
+                                 (tensor cores when a residual covers >= 2
+                                 columns at n >= 1024 and the digit planes,
+                                 16 n^2 bytes, fit), 1 FP64 FMA (SLATE's FP64
+                                 gemm / hemm), 2 tensor cores (FP64-accurate
+                                 digit-split products, digit_residual.cu)   */
 } slt_options;
 
 /* Refinement of the mixed solvers.  SLT_REFINE_IR is SLATE's gesv_mixed loop
@@ -303,6 +309,26 @@ int slt_profile_read(int kind, double* flops, double* bytes, double* seconds, lo
  * (synchronises the device).  SLATE frees its workspace with
  * Matrix::releaseWorkspace (include/slate/BaseMatrix.hh). */
 int slt_release_workspace(void);
+
+/* Memory helpers of the header-only C++ API (include/slate_gb300.hh), which
+ * keeps SLATE's tile storage (slate::MatrixStorage, include/slate/internal/
+ * MatrixStorage.hh) without including CUDA headers: device allocation on the
+ * current device, a synchronous 2-D copy between any host / device pointers
+ * (unified addressing picks the direction), and whether a pointer is device
+ * (or managed) memory. */
+int slt_device_malloc(size_t bytes, void** p);
+int slt_device_free(void* p);
+int slt_memcpy2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t height);
+int slt_is_device_pointer(const void* p);
+
+/* Type-generic device helpers (type 0 float, 1 double, 2 complex<float>,
+ * 3 complex<double>; stream 0 = the default stream): B (n x m) = A^T, or A^H
+ * when conj != 0; the lower (upper = 0) or upper (upper = 1) triangle of D
+ * <- S.  No counterpart in SLATE (its Tile transposes are host / BLAS++). */
+int slt_xtranspose(int type, int64_t m, int64_t n, const void* A, int64_t lda, void* B, int64_t ldb, int conj,
+                   slt_stream_t stream);
+int slt_xcopy_tri(int type, int upper, int64_t n, const void* S, int64_t lds, void* D, int64_t ldd,
+                  slt_stream_t stream);
 
 /* Seconds spent in named phases of the last driver call on this thread
  * (the keys of SLATE's slate::timers map, e.g. "gesv_mixed::getrf_lo");

@@ -35,7 +35,7 @@ class _Options(ctypes.Structure):
                 ("use_fallback", ctypes.c_int), ("pivot_threshold", ctypes.c_double),
                 ("factor_precision", ctypes.c_int), ("gemm_engine", ctypes.c_int),
                 ("refine", ctypes.c_int), ("equilibrate", ctypes.c_int), ("lo_retry", ctypes.c_int),
-                ("depth", ctypes.c_int64), ("method_lu", ctypes.c_int)]
+                ("depth", ctypes.c_int64), ("method_lu", ctypes.c_int), ("residual_engine", ctypes.c_int)]
 
 
 @dataclass
@@ -55,6 +55,7 @@ class Options:
     lo_retry: int = -1             # -1 auto (on for bf16/fp16): FP32 retry before the FP64 fallback
     depth: int = 2                 # Option::Depth of gesv_rbt's butterflies
     method_lu: str = "P"           # Option::MethodLU: "P" partial pivoting, "N" none, "C" CALU
+    residual_engine: int = 0       # FP64 residuals: 0 auto, 1 FP64 FMA, 2 tensor cores (digit splitting)
 
     def _c(self):
         p = self.factor_precision
@@ -64,7 +65,8 @@ class Options:
                         float(self.pivot_threshold), p, int(self.gemm_engine),
                         _REFINE_NAMES[self.refine] if isinstance(self.refine, str) else int(self.refine),
                         int(self.equilibrate), int(self.lo_retry), int(self.depth),
-                        ord(self.method_lu[0]) if isinstance(self.method_lu, str) else int(self.method_lu))
+                        ord(self.method_lu[0]) if isinstance(self.method_lu, str) else int(self.method_lu),
+                        int(self.residual_engine))
 
 
 _lib = None

@@ -171,6 +171,7 @@ void slt_options_default(slt_options* o)
     o->factor_precision = SLT_PREC_FP32;
     o->gemm_engine = 0;
     o->refine = SLT_REFINE_IR;
+    o->residual_engine = 0;
     o->equilibrate = -1;
     o->lo_retry = -1;
     o->depth = 2;
@@ -425,6 +426,35 @@ int slt_sposv_device(int64_t n, int64_t nrhs, float* dA, int64_t lda, float* dB,
     int rc = slt_spotrf_device(n, dA, lda, opts, stream, info);
     if (rc || *info != 0) return rc;       // SLATE skips the solve when info != 0 (src/posv.cc:85-91)
     return slt_spotrs_device(n, nrhs, dA, lda, dB, ldb, opts, stream);
+}
+
+// ---- memory helpers of the header-only C++ API (tile storage of
+// Matrix::insertLocalTiles, workspace tiles, copies between tile instances)
+int slt_device_malloc(size_t bytes, void** p)
+{
+    if (!p) return SLT_ERR_ARG;
+    *p = nullptr;
+    const cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 16);
+    if (e != cudaSuccess) { cudaGetLastError(); *p = nullptr; return SLT_ERR_NOMEM; }
+    return SLT_OK;
+}
+
+int slt_device_free(void* p) { return p ? slt_from_cuda(cudaFree(p)) : SLT_OK; }
+
+int slt_memcpy2d(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t height)
+{
+    if (width == 0 || height == 0) return SLT_OK;
+    return slt_from_cuda(cudaMemcpy2D(dst, dpitch, src, spitch, width, height, cudaMemcpyDefault));
+}
+
+int slt_is_device_pointer(const void* p)
+{
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
 int slt_dgenerate_device(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,

@@ -932,8 +932,9 @@ static int xcopy_tri_t(int upper, int64_t n, const void* S, int64_t lds, void* D
 } // namespace slt
 
 extern "C" int slt_xtranspose(int type, int64_t m, int64_t n, const void* A, int64_t lda, void* B, int64_t ldb,
-                              int conj_, cudaStream_t s)
+                              int conj_, slt_stream_t stream)
 {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     switch (type) {
     case 0: return xtranspose_t<float>(m, n, A, lda, B, ldb, 0, s);
     case 1: return xtranspose_t<double>(m, n, A, lda, B, ldb, 0, s);
@@ -944,8 +945,9 @@ extern "C" int slt_xtranspose(int type, int64_t m, int64_t n, const void* A, int
 }
 
 extern "C" int slt_xcopy_tri(int type, int upper, int64_t n, const void* S, int64_t lds, void* D, int64_t ldd,
-                             cudaStream_t s)
+                             slt_stream_t stream)
 {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     switch (type) {
     case 0: return xcopy_tri_t<float>(upper, n, S, lds, D, ldd, s);
     case 1: return xcopy_tri_t<double>(upper, n, S, lds, D, ldd, s);

@@ -36,15 +36,6 @@ extern "C" {
 int slt_set_sm_cap(int sms);
 int slt_sm_cap(void);
 
-/* ---- type-generic helpers (type 0 float, 1 double, 2 complex<float>,
- * 3 complex<double>; complex arrays interleave real and imaginary parts) ----
- * xtranspose: B (n x m) = A^T, or A^H when conj != 0 (complex types).
- * xcopy_tri: the lower (upper = 0) or upper (upper = 1) triangle of D <- S. */
-int slt_xtranspose(int type, int64_t m, int64_t n, const void* A, int64_t lda, void* B, int64_t ldb, int conj,
-                   cudaStream_t stream);
-int slt_xcopy_tri(int type, int upper, int64_t n, const void* S, int64_t lds, void* D, int64_t ldd,
-                  cudaStream_t stream);
-
 /* ---- trailing-matrix update GEMM:  C = alpha A op(B) + beta C --------------
  * transb 'N': B is k x n;  'T': B is n x k (C -= A B^T, the Cholesky update).
  * lower != 0: only the lower triangle (i >= j) of C is computed and written.
