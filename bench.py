@@ -80,6 +80,8 @@ def parse():
     p.add_argument("--kappas", default=None, help="comma list (configs 3, 4 --sweep)")
     p.add_argument("--precs", default=None, help="comma list (configs 3, 4 --sweep)")
     p.add_argument("--refine", default="ir+gmres", help="configs 3: ir | ir+gmres")
+    p.add_argument("--residual-engine", type=int, default=0,
+                   help="FP64 residuals: 0 auto, 1 FP64 FMA, 2 tensor-core digit products")
     a = p.parse_args()
     w = WORKLOADS.get(a.config)
     if w is not None:
@@ -577,7 +579,7 @@ def measured_peaks(torch, dev):
 
 # kernel classes of the library's launch profiler (include/slate_gb300.h)
 PROF_CLASSES = ((1, "gemm64"), (2, "gemm32_simt"), (3, "gemm_tc"), (4, "panel"), (5, "trsm"), (6, "laswp"),
-                (7, "fp64_residual"), (8, "chol_panel"), (9, "convert"), (10, "sweep"))
+                (7, "fp64_residual"), (8, "chol_panel"), (9, "convert"), (10, "sweep"), (11, "digit_residual"))
 
 
 def _roofline(dom, d, peaks, fp_peaks, steps, t_step):
@@ -651,7 +653,7 @@ def main():
     n, nrhs = args.n, args.nrhs
     A, B, Xt = make_headline_system(slt, torch, args, dev)
     X = slt.colmajor(torch.zeros(n, nrhs, dtype=torch.float64, device=dev))
-    opts = slt.Options(nb=args.nb, ib=32, factor_precision=args.prec)
+    opts = slt.Options(nb=args.nb, ib=32, factor_precision=args.prec, residual_engine=args.residual_engine)
     solve = slt.posv_mixed_gmres if w["routine"] == "posv_mixed_gmres" else slt.posv_mixed
 
     def barrier():

@@ -1,0 +1,630 @@
+// digit_residual.cu -- the FP64 residual R = B - A X of the refinement loops
+// on the BF16 tensor cores (tcgen05), for up to 16 right-hand sides.
+//
+// SLATE forms b - A x in double once per refinement step (gesv_mixed:
+// src/gesv_mixed.cc:240-285, posv_mixed: src/posv_mixed.cc:230-290, and the
+// Arnoldi products of gesv_mixed_gmres / posv_mixed_gmres,
+// src/gesv_mixed_gmres.cc:250-330).  On GB300 FP64 arithmetic runs at about
+// 1.2 TFLOP/s, so a 16-column product with A of order 65536 costs ~120 ms
+// while one read of A costs 5 ms.  Here the product is formed on the tensor
+// cores by splitting both operands into integer digits (the Ozaki scheme:
+// Ozaki, Ogita, Oishi, Rump, Numer. Algorithms 59 (2012) 95-118; integer
+// digits as in Ootomo, Ozaki, Yokota, IJHPCA 38 (2024)):
+//
+//  * row i of A is scaled by 2^-ea_i and column c of X by 2^-ex_c (powers of
+//    two, exact) so that every |a'| and |x'| is below 1/2;
+//  * v = a' is split into eight balanced base-128 digits, d = rint(128 v),
+//    v <- 128 v - d (exact in FP64), |d| <= 64: an integer exact in BF16, and
+//    a' = sum_{p<8} d_p 128^-(p+1) + r with |r| <= 2^-57;
+//  * a' x' = sum_w S_w 128^-(w+2) with S_w = sum_k sum_{p+q=w} d_p d_q; the
+//    weight classes w >= 8 lie below 2^-53 of the product scale and are
+//    dropped, so 8 classes remain;
+//  * the tensor cores form the eight class sums for one chunk of 256 k in
+//    FP32: every digit product is an integer of magnitude <= 2^12 and every
+//    partial sum at most 256 * 8 * 2^12 = 2^23, so FP32 accumulation is
+//    exact in any order;
+//  * per chunk the epilogue folds the class sums exactly into two int64
+//    words, hi = sum_{w<4} S_w 2^(7(3-w)) and lo = sum_{w>=4} S_w 2^(7(7-w));
+//    split-K segments add in int64 (exact), and the last kernel forms
+//    r = (b - hi 2^(e-35)) - lo 2^(e-63), e = ea_i + ex_c.
+//
+// The computed A x differs from the exact one by at most about
+// 2^-50 n max_k |a_ik| max_k |x_kc| (the dropped digits and classes), and
+// typically by 2^-56 sqrt(n) of that scale: as accurate as an FP64 product.
+//
+// Layout in HBM.  The digit planes of A are BF16, K-major (row i of plane p
+// contiguous over k), zero-padded to rows_pad = 128-multiple rows and
+// ldk = 64-multiple columns: 16 n^2 bytes, twice the FP64 matrix, written
+// once per solve.  The digits of X (per call) are 128 rows (plane q, column c
+// at row 16 q + c) of ldk BF16.
+//
+// The MMA.  A CTA takes a 128-row block of A and a K segment.  Per 64 k it
+// loads the X digit tile (128 x 64) into the upper half of a 32 KB stage
+// whose lower half is zero, and the eight A digit tiles (128 x 64 each).  For
+// A plane p the B descriptor starts 16 p rows before the X tile, so MMA row
+// j = 16 w + c of B is X plane w - p (zero for w < p): one
+// tcgen05.mma M128 N128 K16 accumulates plane p into all eight class
+// accumulators D[:, 16 w + c] at once.  32 MMAs per 64 k; D is double
+// buffered in TMEM (2 x 128 columns) so the epilogue of one chunk overlaps
+// the next chunk's MMAs.  Warp 0 issues TMA loads, warp 1 the MMAs, warps
+// 2-5 fold the accumulators (one TMEM lane quarter each).  Every mbarrier
+// wait is bounded; on timeout the CTA records SLT_ERR_TIMEOUT, drains its
+// own copies and MMAs, frees its TMEM and returns.
+
+#include "common.cuh"
+#include "drivers.h"
+#include "prof.h"
+#include "slate_gb300.h"
+#include "tc_ptx.cuh"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <climits>
+
+namespace slt {
+
+constexpr int kDgPlanes = 8;          // digits per operand
+constexpr int kDgBM = 128;            // rows of A per CTA (MMA M)
+constexpr int kDgBK = 64;             // k per stage: 128 bytes of BF16
+constexpr int kDgChunk = 4;           // k-blocks per accumulator flush (256 k)
+constexpr int kDgAStages = 8;
+constexpr int kDgXStages = 2;
+constexpr int kDgThreads = 192;
+constexpr int kDgCols = 16;           // right-hand sides per call
+constexpr uint32_t kDgATile = kDgBM * 128;          // 16 KB
+constexpr uint32_t kDgXHalf = 128 * 128;            // 128 rows x 128 bytes
+constexpr uint32_t kDgXStage = 2 * kDgXHalf;        // zero half + digit half
+// exponent words: "no non-zero entry" (the byte pattern 0x80 of a memset)
+// and "a non-finite entry" (above any frexp exponent)
+constexpr int kDgNone = int(0x80808080u);
+constexpr int kDgBad = 1 << 20;
+
+__device__ __forceinline__ int dg_scale(int e) { return e == kDgNone ? 0 : e + 1; }
+
+// frexp exponent of |v| (v != 0, finite), or kDgBad for Inf / NaN
+__device__ __forceinline__ int dg_exp_of(double v)
+{
+    if (!(fabs(v) <= 1.7976931348623157e308)) return kDgBad;
+    int e;
+    frexp(v, &e);
+    return e;
+}
+
+// Row exponents from rows [i] over columns [j0, j1) of column-major A; with
+// sym (lower storage) only the stored part j <= i.  grid (ceil(m/256), segs).
+__global__ void __launch_bounds__(256)
+dg_rowexp_kernel(int64_t m, int64_t n, const double* __restrict__ A, int64_t lda, int sym, int64_t cps, int* ex)
+{
+    const int64_t i = int64_t(blockIdx.x) * 256 + threadIdx.x;
+    if (i >= m) return;
+    const int64_t j0 = int64_t(blockIdx.y) * cps;
+    int64_t j1 = j0 + cps < n ? j0 + cps : n;
+    if (sym && j1 > i + 1) j1 = i + 1;
+    double mx = 0.0;
+    bool bad = false;
+    for (int64_t j = j0; j < j1; ++j) {
+        const double v = fabs(A[i + j * lda]);
+        bad |= !(v <= 1.7976931348623157e308);
+        mx = fmax(mx, v);
+    }
+    if (bad) atomicMax(ex + i, kDgBad);
+    else if (mx > 0.0) atomicMax(ex + i, dg_exp_of(mx));
+}
+
+// Column exponents: column c of the m x ncols column-major matrix over rows
+// [r0, m), r0 = c + 1 with sym (the part of row c of a symmetric matrix held
+// in its lower-storage column c), else 0.  grid (ncols, segs).
+__global__ void __launch_bounds__(256)
+dg_colexp_kernel(int64_t m, const double* __restrict__ A, int64_t lda, int sym, int64_t rps, int* ex)
+{
+    __shared__ double smx[256];
+    __shared__ int sbad;
+    const int64_t c = blockIdx.x;
+    const int64_t lo = sym ? c + 1 : 0;
+    const int64_t s0 = int64_t(blockIdx.y) * rps, s1 = int64_t(blockIdx.y + 1) * rps;
+    const int64_t r0 = s0 > lo ? s0 : lo;
+    const int64_t r1 = s1 < m ? s1 : m;
+    if (threadIdx.x == 0) sbad = 0;
+    __syncthreads();
+    double mx = 0.0;
+    bool bad = false;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += 256) {
+        const double v = fabs(A[r + c * lda]);
+        bad |= !(v <= 1.7976931348623157e308);
+        mx = fmax(mx, v);
+    }
+    smx[threadIdx.x] = mx;
+    if (bad) sbad = 1;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) smx[threadIdx.x] = fmax(smx[threadIdx.x], smx[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (sbad) atomicMax(ex + c, kDgBad);
+        else if (smx[0] > 0.0) atomicMax(ex + c, dg_exp_of(smx[0]));
+    }
+}
+
+// The eight digits of a' = v 2^-e (|a'| < 1/2), packed four BF16 per 8 bytes
+// for four consecutive k.
+__device__ __forceinline__ void dg_digits4(const double (&v)[4], int e, uint2 (&out)[kDgPlanes])
+{
+    double t[4];
+    #pragma unroll
+    for (int u = 0; u < 4; ++u) t[u] = (e >= kDgBad) ? 0.0 : ldexp(v[u], -e);
+    #pragma unroll
+    for (int p = 0; p < kDgPlanes; ++p) {
+        unsigned short h[4];
+        #pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double s = t[u] * 128.0;
+            const double d = rint(s);
+            t[u] = s - d;
+            h[u] = __bfloat16_as_ushort(__float2bfloat16_rn(float(d)));
+        }
+        out[p].x = uint32_t(h[0]) | (uint32_t(h[1]) << 16);
+        out[p].y = uint32_t(h[2]) | (uint32_t(h[3]) << 16);
+    }
+}
+
+// Digit planes of A: the 64 x 64 tile (rows I0.., k K0..) of plane p at
+// planes + p pstride + i ldk + k.  A column-major; with sym only its lower
+// triangle is read (element (i, k), k > i, is A(k, i)).  Rows >= n and
+// k >= n are written as zeros.  grid (ldk / 64, rows_pad / 64), 256 threads.
+__global__ void __launch_bounds__(256)
+dg_split_a_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym, const int* __restrict__ rexp,
+                  __nv_bfloat16* planes, int64_t ldk, int64_t pstride)
+{
+    __shared__ double T[64][65];
+    const int64_t I0 = int64_t(blockIdx.y) * 64, K0 = int64_t(blockIdx.x) * 64;
+    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
+    if (sym && K0 > I0) {
+        // strictly above the diagonal: element (i, k) = A(k, i), contiguous in k
+        for (int ii = ty; ii < 64; ii += 4) {
+            const int64_t i = I0 + ii, k = K0 + tx;
+            T[ii][tx] = (i < n && k < n) ? A[k + i * lda] : 0.0;
+        }
+    }
+    else {
+        for (int kk = ty; kk < 64; kk += 4) {
+            const int64_t i = I0 + tx, k = K0 + kk;
+            T[tx][kk] = (i < n && k < n && !(sym && k > i)) ? A[i + k * lda] : 0.0;
+        }
+        if (sym && K0 == I0) {
+            __syncthreads();
+            for (int kk = ty; kk < 64; kk += 4)
+                if (kk > tx) T[tx][kk] = T[kk][tx];
+        }
+    }
+    __syncthreads();
+    const int kq = (threadIdx.x & 15) * 4;
+    for (int r = threadIdx.x >> 4; r < 64; r += 16) {
+        const int64_t i = I0 + r;
+        const int e = i < n ? dg_scale(rexp[i]) : 0;
+        double v[4] = {T[r][kq], T[r][kq + 1], T[r][kq + 2], T[r][kq + 3]};
+        uint2 d[kDgPlanes];
+        dg_digits4(v, e, d);
+        __nv_bfloat16* dst = planes + i * ldk + K0 + kq;
+        #pragma unroll
+        for (int p = 0; p < kDgPlanes; ++p)
+            *reinterpret_cast<uint2*>(dst + int64_t(p) * pstride) = d[p];
+    }
+}
+
+// Digits of X (n x nrhs, column-major): plane q of column c at row 16 q + c of
+// xd (128 rows of ldk), zeros for k >= n and c >= nrhs.  grid (ldk / 1024, 16).
+__global__ void __launch_bounds__(256)
+dg_split_x_kernel(int64_t n, int nrhs, const double* __restrict__ X, int64_t ldx, const int* __restrict__ cexp,
+                  __nv_bfloat16* xd, int64_t ldk)
+{
+    const int c = blockIdx.y;
+    const int64_t k = (int64_t(blockIdx.x) * 256 + threadIdx.x) * 4;
+    if (k >= ldk) return;
+    const int e = c < nrhs ? dg_scale(cexp[c]) : 0;
+    double v[4];
+    #pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = (c < nrhs && k + u < n) ? X[k + u + int64_t(c) * ldx] : 0.0;
+    uint2 d[kDgPlanes];
+    dg_digits4(v, e, d);
+    #pragma unroll
+    for (int q = 0; q < kDgPlanes; ++q)
+        *reinterpret_cast<uint2*>(xd + int64_t(q * kDgCols + c) * ldk + k) = d[q];
+}
+
+struct DgArgs {
+    int64_t rows_pad;       // rows of one A plane
+    int rb;                 // 128-row blocks
+    int kb_total;           // 64-k blocks
+    int kb_per_seg;
+    int segs;
+    long long* part;        // [segs][2][16][rows_pad]: hi, lo
+    int* status;
+};
+
+__device__ __forceinline__ void dg_fail(int* status, volatile int* abort_flag)
+{
+    atomicCAS(status, 0, SLT_ERR_TIMEOUT);
+    *abort_flag = 1;
+}
+
+__global__ void __launch_bounds__(kDgThreads, 1)
+dg_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapX, DgArgs a,
+               uint32_t idesc)
+{
+    constexpr int S = kDgAStages, XS = kDgXStages;
+    extern __shared__ __align__(1024) unsigned char dg_smem_raw[];
+    const uint32_t raw = smem_u32(dg_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char* gbase = dg_smem_raw + (base - raw);
+    const uint32_t a0 = base, x0 = base + S * kDgATile;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + S * kDgATile + XS * kDgXStage);
+    // afull[S] aempty[S] xfull[XS] xempty[XS] tfull[2] tempty[2] fin
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 2 * XS + 5);
+    __shared__ int s_abort;
+    volatile int* abort_flag = &s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t afull0 = smem_u32(bars), aempty0 = afull0 + 8 * S;
+    const uint32_t xfull0 = aempty0 + 8 * S, xempty0 = xfull0 + 8 * XS;
+    const uint32_t tfull0 = xempty0 + 8 * XS, tempty0 = tfull0 + 16, fin = tempty0 + 16;
+    const int64_t items = int64_t(a.rb) * a.segs;
+
+    // zero halves of the X stages (read by the MMAs of planes p >= 1)
+    for (uint32_t off = threadIdx.x * 16; off < kDgXHalf; off += kDgThreads * 16)
+        for (int xs = 0; xs < XS; ++xs)
+            *reinterpret_cast<uint4*>(gbase + S * kDgATile + xs * kDgXStage + off) = make_uint4(0, 0, 0, 0);
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        for (int s = 0; s < S; ++s) { mbar_init(afull0 + 8 * s, 1); mbar_init(aempty0 + 8 * s, 1); }
+        for (int s = 0; s < XS; ++s) { mbar_init(xfull0 + 8 * s, 1); mbar_init(xempty0 + 8 * s, 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(tfull0 + 8 * b, 1); mbar_init(tempty0 + 8 * b, 4); }
+        mbar_init(fin, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (warp == 1) tmem_alloc(smem_u32(tmem_slot), 256);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer
+            long long ia = 0, ix = 0;
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x) {
+                const int row0 = int(t % a.rb) * kDgBM;
+                const int seg = int(t / a.rb);
+                const int kb0 = seg * a.kb_per_seg, kb1 = min(a.kb_total, kb0 + a.kb_per_seg);
+                for (int kb = kb0; kb < kb1 && ok; ++kb) {
+                    const int xs = int(ix % XS);
+                    if (!mbar_wait(xempty0 + 8 * xs, uint32_t((ix / XS) & 1) ^ 1u) || *abort_flag) {
+                        dg_fail(a.status, abort_flag);
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(xfull0 + 8 * xs, kDgXHalf);
+                    tma_load_2d(x0 + xs * kDgXStage + kDgXHalf, &mapX, xfull0 + 8 * xs, kb * kDgBK, 0);
+                    ++ix;
+                    for (int p = 0; p < kDgPlanes; ++p) {
+                        const int s = int(ia % S);
+                        if (!mbar_wait(aempty0 + 8 * s, uint32_t((ia / S) & 1) ^ 1u) || *abort_flag) {
+                            dg_fail(a.status, abort_flag);
+                            ok = false;
+                            break;
+                        }
+                        mbar_expect_tx(afull0 + 8 * s, kDgATile);
+                        tma_load_2d(a0 + s * kDgATile, &mapA, afull0 + 8 * s, kb * kDgBK,
+                                    int(int64_t(p) * a.rows_pad) + row0);
+                        ++ia;
+                    }
+                }
+            }
+            // drain: the last armed phase of every stage lands before exit
+            for (int s = 0; s < S && s < ia; ++s) {
+                const long long last = s + ((ia - 1 - s) / S) * S;
+                mbar_wait(afull0 + 8 * s, uint32_t((last / S) & 1));
+            }
+            for (int s = 0; s < XS && s < ix; ++s) {
+                const long long last = s + ((ix - 1 - s) / XS) * XS;
+                mbar_wait(xfull0 + 8 * s, uint32_t((last / XS) & 1));
+            }
+        }
+    }
+    else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer
+            long long ia = 0, ix = 0, lt = 0;
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x) {
+                const int seg = int(t / a.rb);
+                const int kb0 = seg * a.kb_per_seg, kb1 = min(a.kb_total, kb0 + a.kb_per_seg);
+                for (int kc = kb0; kc < kb1 && ok; kc += kDgChunk, ++lt) {
+                    const int buf = int(lt & 1);
+                    if (!mbar_wait(tempty0 + 8 * buf, uint32_t((lt >> 1) & 1) ^ 1u) || *abort_flag) {
+                        dg_fail(a.status, abort_flag);
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t tacc = taddr + uint32_t(buf * 128);
+                    const int kend = min(kb1, kc + kDgChunk);
+                    for (int kb = kc; kb < kend && ok; ++kb) {
+                        const int xs = int(ix % XS);
+                        if (!mbar_wait(xfull0 + 8 * xs, uint32_t((ix / XS) & 1)) || *abort_flag) {
+                            dg_fail(a.status, abort_flag);
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t xrows = x0 + xs * kDgXStage + kDgXHalf;
+                        for (int p = 0; p < kDgPlanes; ++p) {
+                            const int s = int(ia % S);
+                            if (!mbar_wait(afull0 + 8 * s, uint32_t((ia / S) & 1)) || *abort_flag) {
+                                dg_fail(a.status, abort_flag);
+                                ok = false;
+                                break;
+                            }
+                            tc_fence_after();
+                            const uint64_t da = sw128_desc(a0 + s * kDgATile);
+                            // 16 p rows (2048 p bytes) before the X digits: rows of
+                            // classes w < p fall in the zero half
+                            const uint64_t db = sw128_desc(xrows - uint32_t(p) * 2048u);
+                            #pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                umma<0>(tacc, da + uint64_t(2 * k), db + uint64_t(2 * k), idesc,
+                                        (kb == kc && p == 0 && k == 0) ? 0u : 1u);
+                            umma_commit(aempty0 + 8 * s);
+                            ++ia;
+                        }
+                        if (!ok) break;
+                        umma_commit(xempty0 + 8 * xs);
+                        ++ix;
+                    }
+                    if (!ok) break;
+                    umma_commit(tfull0 + 8 * buf);
+                }
+            }
+            // every MMA issued above has completed before TMEM is freed
+            umma_commit(fin);
+            if (!mbar_wait(fin, 0u)) atomicCAS(a.status, 0, SLT_ERR_TIMEOUT);
+        }
+    }
+    else {
+        // ---- epilogue warps 2..5: TMEM lanes 32 q .. 32 q + 31, q = warp % 4
+        const int q = warp & 3;
+        long long lt = 0;
+        bool ok = true;
+        for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x) {
+            const int row0 = int(t % a.rb) * kDgBM;
+            const int seg = int(t / a.rb);
+            const int kb0 = seg * a.kb_per_seg, kb1 = min(a.kb_total, kb0 + a.kb_per_seg);
+            long long hi[kDgCols], lo[kDgCols];
+            #pragma unroll
+            for (int c = 0; c < kDgCols; ++c) { hi[c] = 0; lo[c] = 0; }
+            for (int kc = kb0; kc < kb1; kc += kDgChunk, ++lt) {
+                const int buf = int(lt & 1);
+                bool ready = mbar_wait(tfull0 + 8 * buf, uint32_t((lt >> 1) & 1));
+                ready = __all_sync(0xffffffffu, ready && !*abort_flag);
+                if (!ready) {
+                    if (lane == 0) dg_fail(a.status, abort_flag);
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t tl = taddr + (uint32_t(q * 32) << 16) + uint32_t(buf * 128);
+                #pragma unroll 1
+                for (int h = 0; h < 4; ++h) {     // classes 2h and 2h + 1
+                    float v[32];
+                    tmem_ld32(tl + uint32_t(h * 32), v);
+                    // class w weighs 2^(7(3-w)) in hi (w < 4), 2^(7(7-w)) in lo
+                    const long long m0 = (h & 1) ? (1ll << 7) : (1ll << 21);
+                    const long long m1 = (h & 1) ? 1ll : (1ll << 14);
+                    #pragma unroll
+                    for (int c = 0; c < kDgCols; ++c) {
+                        const long long f = __float2ll_rn(v[c]) * m0 + __float2ll_rn(v[16 + c]) * m1;
+                        if (h < 2) hi[c] += f;
+                        else lo[c] += f;
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
+            }
+            if (!ok) break;
+            const int64_t r = int64_t(row0) + q * 32 + lane;
+            long long* ph = a.part + (int64_t(seg) * 2 * kDgCols) * a.rows_pad + r;
+            #pragma unroll
+            for (int c = 0; c < kDgCols; ++c) {
+                ph[int64_t(c) * a.rows_pad] = hi[c];
+                ph[int64_t(kDgCols + c) * a.rows_pad] = lo[c];
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) tmem_dealloc(taddr, 256);
+}
+
+// R(i, c) = B(i, c) - sum over segments of (hi 2^(e-35) + lo 2^(e-63)),
+// e = ea_i + ex_c; NaN where row i of A or column c of X holds Inf / NaN.
+// grid (ceil(n / 256), nrhs).
+__global__ void __launch_bounds__(256)
+dg_reduce_kernel(int64_t n, int64_t rows_pad, int segs, const long long* __restrict__ part,
+                 const int* __restrict__ rexp, const int* __restrict__ cexp, const double* __restrict__ B,
+                 int64_t ldb, double* R, int64_t ldr)
+{
+    const int64_t i = int64_t(blockIdx.x) * 256 + threadIdx.x;
+    const int c = blockIdx.y;
+    if (i >= n) return;
+    long long hi = 0, lo = 0;
+    for (int s = 0; s < segs; ++s) {
+        const long long* p = part + (int64_t(s) * 2 * kDgCols + c) * rows_pad + i;
+        hi += p[0];
+        lo += p[int64_t(kDgCols) * rows_pad];
+    }
+    double r;
+    if (rexp[i] >= kDgBad || cexp[c] >= kDgBad) {
+        r = __longlong_as_double(0x7ff8000000000000ll);
+    }
+    else {
+        const int e = dg_scale(rexp[i]) + dg_scale(cexp[c]);
+        const double yh = double(hi);
+        // hi - yh is exact in int64 whenever |yh| < 2^62; fold it into lo
+        if (fabs(yh) < 4.611686018427387904e18) lo += (hi - (long long) yh) * (1ll << 28);
+        r = (B[i + c * ldb] - ldexp(yh, e - 35)) - ldexp(double(lo), e - 63);
+    }
+    R[i + c * ldr] = r;
+}
+
+static size_t dg_smem_bytes()
+{
+    return 1024 + size_t(kDgAStages) * kDgATile + size_t(kDgXStages) * kDgXStage + 256;
+}
+
+// Split-K segments: the count that minimises waves x (k-blocks per item + 2).
+static void dg_plan(int64_t rb, int64_t kb_total, int sms, int* segs, int* kps)
+{
+    double best = -1;
+    *segs = 1;
+    *kps = int(kb_total);
+    for (int64_t s = 1; s <= std::min<int64_t>(kb_total, 64); ++s) {
+        const int64_t k = ceildiv(kb_total, s);
+        const int64_t se = ceildiv(kb_total, k);
+        const int64_t waves = ceildiv(rb * se, int64_t(sms));
+        const double cost = double(waves) * double(k + 2);
+        if (best < 0 || cost < best) { best = cost; *segs = int(se); *kps = int(k); }
+    }
+}
+
+size_t DigitMatrix::bytes_for(int64_t n)
+{
+    const int64_t ldk = ceildiv(n, kDgBK) * kDgBK, rp = ceildiv(n, kDgBM) * kDgBM;
+    return size_t(kDgPlanes) * size_t(rp) * size_t(ldk) * 2;
+}
+
+void DigitMatrix::release()
+{
+    planes.reset();
+    rexp.reset();
+    cexp.reset();
+    xplanes.reset();
+    part.reset();
+    status.reset();
+    ready = false;
+}
+
+int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cudaStream_t s)
+{
+    release();
+    if (n_ <= 0 || lda < n_) return SLT_ERR_ARG;
+    // grid rows (rows_pad / 64 <= 65535) and 32-bit TMA row coordinates
+    if (n_ > (int64_t(1) << 22)) return SLT_ERR_NOT_SUPPORTED;
+    n = n_;
+    ldk = ceildiv(n, kDgBK) * kDgBK;
+    rows_pad = ceildiv(n, kDgBM) * kDgBM;
+    pstride = rows_pad * ldk;
+    int dev = 0, nsm = 0;
+    SLT_CUDA_TRY(cudaGetDevice(&dev));
+    SLT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    sms = capped_sms(nsm);
+    dg_plan(rows_pad / kDgBM, ldk / kDgBK, sms, &segs, &kb_per_seg);
+    TRY(planes.alloc(bytes_for(n), s));
+    TRY(rexp.alloc(sizeof(int) * size_t(rows_pad), s));
+    TRY(cexp.alloc(sizeof(int) * kDgCols, s));
+    TRY(xplanes.alloc(size_t(kDgPlanes) * kDgCols * size_t(ldk) * 2, s));
+    TRY(part.alloc(size_t(segs) * 2 * kDgCols * size_t(rows_pad) * sizeof(long long), s));
+    TRY(status.alloc(sizeof(int), s));
+    SLT_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(int), s));
+    SLT_CUDA_TRY(cudaMemsetAsync(rexp.p, 0x80, sizeof(int) * size_t(rows_pad), s));
+
+    // row exponents: the stored row, and for sym the stored column below the diagonal
+    const int64_t cps = 4096;
+    dg_rowexp_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(ceildiv(n, cps))), 256, 0, s>>>(
+        n, n, A, lda, sym, cps, rexp.as<int>());
+    count_launch();
+    if (sym) {
+        dg_colexp_kernel<<<dim3(unsigned(n), 1), 256, 0, s>>>(n, A, lda, 1, n, rexp.as<int>());
+        count_launch();
+    }
+    dg_split_a_kernel<<<dim3(unsigned(ldk / 64), unsigned(rows_pad / 64)), 256, 0, s>>>(
+        n, A, lda, sym, rexp.as<int>(), planes.as<__nv_bfloat16>(), ldk, pstride);
+    count_launch();
+    SLT_CUDA_TRY(cudaGetLastError());
+
+    TRY(tma_map_2d(&mapA, planes.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, ldk, int64_t(kDgPlanes) * rows_pad,
+                   ldk * 2, kDgBK, kDgBM, CU_TENSOR_MAP_SWIZZLE_128B));
+    TRY(tma_map_2d(&mapX, xplanes.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, ldk, int64_t(kDgPlanes) * kDgCols,
+                   ldk * 2, kDgBK, kDgPlanes * kDgCols, CU_TENSOR_MAP_SWIZZLE_128B));
+    ready = true;
+    return SLT_OK;
+}
+
+int DigitMatrix::residual(int64_t nrhs, const double* B, int64_t ldb, const double* X, int64_t ldx, double* R,
+                          int64_t ldr, cudaStream_t s)
+{
+    if (!ready) return SLT_ERR_ARG;
+    if (nrhs <= 0) return SLT_OK;
+    if (nrhs > kDgCols || ldb < n || ldx < n || ldr < n) return SLT_ERR_ARG;
+    static DeviceOnce once;
+    TRY(once.run([] {
+        return slt_from_cuda(cudaFuncSetAttribute(dg_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  int(dg_smem_bytes())));
+    }));
+    SLT_CUDA_TRY(cudaMemsetAsync(cexp.p, 0x80, sizeof(int) * kDgCols, s));
+    const int64_t rps = 16384;
+    dg_colexp_kernel<<<dim3(unsigned(nrhs), unsigned(ceildiv(n, rps))), 256, 0, s>>>(n, X, ldx, 0, rps,
+                                                                                   cexp.as<int>());
+    count_launch();
+    dg_split_x_kernel<<<dim3(unsigned(ceildiv(ldk, 1024)), kDgCols), 256, 0, s>>>(
+        n, int(nrhs), X, ldx, cexp.as<int>(), xplanes.as<__nv_bfloat16>(), ldk);
+    count_launch();
+
+    DgArgs args{rows_pad, int(rows_pad / kDgBM), int(ldk / kDgBK), kb_per_seg, segs, part.as<long long>(),
+                status.as<int>()};
+    const int64_t items = int64_t(args.rb) * segs;
+    const unsigned grid = unsigned(std::min<int64_t>(items, sms));
+    const uint32_t idesc = make_idesc(1u, kDgBM, 128);       // BF16 x BF16 -> FP32, M 128, N 128
+    const int pidx = prof_begin(SLT_PROF_DIGIT, s);
+    dg_gemm_kernel<<<grid, kDgThreads, dg_smem_bytes(), s>>>(mapA, mapX, args, idesc);
+    count_launch();
+    // algorithmic: 2 n^2 nrhs flops of the FP64 product; bytes: the digit planes of A
+    prof_end(pidx, s, 2.0 * double(n) * double(n) * double(nrhs), double(bytes_for(n)));
+    SLT_CUDA_TRY(cudaGetLastError());
+    dg_reduce_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(nrhs)), 256, 0, s>>>(
+        n, rows_pad, segs, part.as<long long>(), rexp.as<int>(), cexp.as<int>(), B, ldb, R, ldr);
+    count_launch();
+    return slt_from_cuda(cudaGetLastError());
+}
+
+int DigitMatrix::check_status(cudaStream_t s)
+{
+    if (!status.p) return SLT_OK;
+    int h = 0;
+    SLT_CUDA_TRY(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SLT_CUDA_TRY(cudaStreamSynchronize(s));
+    return h;
+}
+
+} // namespace slt
+
+using namespace slt;
+
+// One-shot digit residual (prepare, one product, status): R = B - A X for
+// nrhs <= 16, A of order n (sym_lower: symmetric, lower storage).  The
+// drivers keep the digit planes for a whole solve instead.
+extern "C" int slt_dresidual_digits(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower,
+                                    const double* B, int64_t ldb, const double* X, int64_t ldx, double* R,
+                                    int64_t ldr, cudaStream_t stream)
+{
+    if (n < 0 || nrhs < 0 || nrhs > kDgCols) return SLT_ERR_ARG;
+    if (n == 0 || nrhs == 0) return SLT_OK;
+    DigitMatrix dm;
+    TRY(dm.prepare(n, A, lda, sym_lower, stream));
+    TRY(dm.residual(nrhs, B, ldb, X, ldx, R, ldr, stream));
+    return dm.check_status(stream);
+}

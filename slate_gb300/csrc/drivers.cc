@@ -616,6 +616,55 @@ bool converged(const double* cr, const double* cx, int64_t k, double cte)
     return true;
 }
 
+// The FP64 products of one refinement solve, R = B - A X for at most 16
+// columns per call (SLATE's gemm / hemm in double, src/gesv_mixed.cc:262,
+// src/posv_mixed.cc:271): FP64 FMA (slt_dresidual), or FP64-accurate digit
+// products on the tensor cores (DigitMatrix, split from A on first use and
+// kept for the solve).  engine (Options.residual_engine): 0 auto -- the
+// tensor cores for products of >= 4 columns at n >= 2048, where they beat
+// the FP64 units even counting the split --, 1 FP64, 2 tensor cores.  When
+// the digit planes cannot be allocated the FP64 path runs.
+struct Residual {
+    int64_t n;
+    const double* A;
+    int64_t lda;
+    int sym;
+    int engine;
+    DevBuf ws;
+    DigitMatrix dm;
+    bool dm_failed = false;
+
+    Residual(int64_t n_, const double* A_, int64_t lda_, int sym_, int engine_)
+        : n(n_), A(A_), lda(lda_), sym(sym_), engine(engine_) {}
+
+    bool use_digits(int64_t nc) const {
+        if (engine == 1 || dm_failed) return false;
+        if (engine == 2) return true;
+        return nc >= 4 && n >= 2048;
+    }
+
+    int compute(int64_t nc, const double* B, int64_t ldb, const double* X, int64_t ldx, double* R, int64_t ldr,
+                cudaStream_t s) {
+        if (nc <= 0) return SLT_OK;
+        if (use_digits(nc)) {
+            if (!dm.ready) {
+                const int rc = dm.prepare(n, A, lda, sym, s);
+                if (rc == SLT_ERR_NOMEM || rc == SLT_ERR_NOT_SUPPORTED) {
+                    dm.release();
+                    dm_failed = true;
+                }
+                else if (rc) return rc;
+            }
+            if (dm.ready) return dm.residual(nc, B, ldb, X, ldx, R, ldr, s);
+        }
+        if (!ws.p) TRY(ws.alloc(slt_residual_ws_bytes(n, 16), s));
+        return slt_dresidual(n, nc, A, lda, sym, B, ldb, X, ldx, R, ldr, ws.p, s);
+    }
+
+    // the bounded-wait status of the tensor-core products (synchronises)
+    int status(cudaStream_t s) { return dm.ready ? dm.check_status(s) : SLT_OK; }
+};
+
 // Right-preconditioned FGMRES(restart) (src/gesv_mixed_gmres.cc:225-395),
 // run for up to 16 right-hand sides in lockstep.  Every column is its own
 // instance of SLATE's single-right-hand-side iteration -- CGS2 Arnoldi in
@@ -635,6 +684,7 @@ struct FgmresBlock {
     int64_t lda;
     LoFactor& lo;
     double cte;
+    Residual& res;
     int64_t restart = 0, R1 = 1, SC = 0;
     DevBuf nws, scal, V, W, Z, Bg, Rg, Wlo;
     std::vector<double> hs;
@@ -649,15 +699,15 @@ struct FgmresBlock {
         std::vector<double> H, S, gc, gs, y;
     };
 
-    FgmresBlock(int chol_, int64_t n_, const double* A_, int64_t lda_, LoFactor& lo_, double cte_)
-        : chol(chol_), n(n_), A(A_), lda(lda_), lo(lo_), cte(cte_) {}
+    FgmresBlock(int chol_, int64_t n_, const double* A_, int64_t lda_, LoFactor& lo_, double cte_, Residual& res_)
+        : chol(chol_), n(n_), A(A_), lda(lda_), lo(lo_), cte(cte_), res(res_) {}
 
     int init(int64_t itermax, int64_t nb, cudaStream_t s) {
         restart = std::max<int64_t>(0, std::min<int64_t>(std::min<int64_t>(30, itermax), std::min(nb, n) - 1));
         R1 = restart + 1;
         SC = 4 + 3 * R1;           // per column: cx, cr, ares, nrm | h | z | y
         const size_t nn = size_t(n);
-        TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, kMaxCols)), s));
+        TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, 1)), s));
         TRY(scal.alloc(sizeof(double) * size_t(SC * kMaxCols), s));
         TRY(V.alloc(sizeof(double) * nn * size_t(R1 * kMaxCols), s));
         TRY(W.alloc(sizeof(double) * nn * size_t(R1 * kMaxCols), s));
@@ -702,8 +752,7 @@ struct FgmresBlock {
 
     // R(:, 0:k) = Bg(:, 0:k) - A Z(:, 0:k), in chunks of 16 columns.
     int products(int64_t k, cudaStream_t s) {
-        return slt_dresidual(n, k, A, lda, chol, Bg.as<double>(), n, Z.as<double>(), n, Rg.as<double>(), n,
-                             nws.p, s);
+        return res.compute(k, Bg.as<double>(), n, Z.as<double>(), n, Rg.as<double>(), n, s);
     }
 
     // Runs the columns cols[0..k) (k <= 16) until each one's stopping test
@@ -912,7 +961,7 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
     const bool chain = o.refine == SLT_REFINE_IR_GMRES;
 
     DevBuf nws, scal, R, Wlo, st, col;
-    TRY(nws.alloc(std::max(slt_norm_ws_bytes(n), slt_residual_ws_bytes(n, std::min<int64_t>(nrhs, 16))), s));
+    TRY(nws.alloc(slt_norm_ws_bytes(n), s));
     TRY(scal.alloc(sizeof(double) * 4, s));
     TRY(R.alloc(sizeof(double) * size_t(n) * size_t(nrhs), s));
     TRY(Wlo.alloc(sizeof(float) * size_t(n) * size_t(nrhs), s));
@@ -937,12 +986,12 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
     double* dcx = col.as<double>();
     double* dcr = dcx + nrhs;
     const int64_t rhs_chunks = (nrhs + 15) / 16;
+    Residual res(n, A, lda, chol, o.residual_engine);
     auto residual = [&]() -> int {
         tm.start(std::string(pfx) + (chol ? "::hemm_hi" : "::gemm_hi"));
         for (int64_t c = 0; c < rhs_chunks; ++c) {
             int64_t c0 = c * 16, nc = std::min<int64_t>(16, nrhs - c0);
-            TRY(slt_dresidual(n, nc, A, lda, chol, B + c0 * ldb, ldb, X + c0 * ldx, ldx,
-                              R.as<double>() + c0 * n, n, nws.p, s));
+            TRY(res.compute(nc, B + c0 * ldb, ldb, X + c0 * ldx, ldx, R.as<double>() + c0 * n, n, s));
         }
         tm.stop(std::string(pfx) + (chol ? "::hemm_hi" : "::gemm_hi"));
         TRY(slt_dcolmax(n, nrhs, X, ldx, dcx, s));
@@ -976,7 +1025,7 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
         if (!conv && chain && itermax - ir_steps > 0) {
             // GMRES-IR on the stalled columns, preconditioned by the same factors
             tm.start(std::string(pfx) + "::gmres");
-            FgmresBlock g(chol, n, A, lda, lo, cte);
+            FgmresBlock g(chol, n, A, lda, lo, cte, res);
             TRY(g.init(itermax - ir_steps, nb, s));
             std::vector<int64_t> todo;
             for (int64_t c = 0; c < nrhs; ++c)
@@ -999,6 +1048,8 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
         }
     }
     *info = linfo;
+    TRY(res.status(s));
+    res.dm.release();
     if (!conv) {
         if (linfo == 0) *iter = int(-itermax - 1);
         if (o.use_fallback)
@@ -1177,12 +1228,13 @@ static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, i
     *info = linfo;
     bool all_conv = true;
     int worst_iter = 0;
+    Residual res(n, A, lda, chol, o.residual_engine);
     if (linfo != 0) {
         *iter = -3;
         all_conv = false;
     }
     else {
-        FgmresBlock g(chol, n, A, lda, lo, cte);
+        FgmresBlock g(chol, n, A, lda, lo, cte, res);
         TRY(g.init(itermax, nb, s));
         tm.start(std::string(pfx) + (chol ? "::potrs_lo" : "::getrs_lo"));
         TRY(lo.solve(nrhs, B, ldb, X, ldx, Wlo.as<float>(), s));
@@ -1207,6 +1259,8 @@ static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, i
         }
         *iter = worst_iter;
     }
+    TRY(res.status(s));
+    res.dm.release();
     if (!all_conv) {
         if (linfo == 0 && *iter >= 0) *iter = int(-itermax - 1);
         if (o.use_fallback)

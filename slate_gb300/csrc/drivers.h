@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "slt_kernels.h"
@@ -64,6 +65,33 @@ struct DevBuf {
         return SLT_OK;
     }
     template <typename T> T* as() const { return static_cast<T*>(p); }
+    void reset() {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+    }
+};
+
+// A of order n split once into the BF16 digit planes of the tensor-core
+// residual (digit_residual.cu); residual() then forms R = B - A X for up to
+// 16 right-hand sides per call with FP64 accuracy.  The planes take 16 n^2
+// bytes (bytes_for); A must not change while they are in use.
+struct DigitMatrix {
+    int64_t n = 0, ldk = 0, rows_pad = 0, pstride = 0;
+    int segs = 1, kb_per_seg = 0, sms = 0;
+    bool ready = false;
+    DevBuf planes, rexp, cexp, xplanes, part, status;
+    CUtensorMap mapA, mapX;
+    DigitMatrix() = default;
+    DigitMatrix(const DigitMatrix&) = delete;
+    DigitMatrix& operator=(const DigitMatrix&) = delete;
+    int prepare(int64_t n, const double* A, int64_t lda, int sym_lower, cudaStream_t s);
+    int residual(int64_t nrhs, const double* B, int64_t ldb, const double* X, int64_t ldx, double* R,
+                 int64_t ldr, cudaStream_t s);
+    // SLT_OK, or SLT_ERR_TIMEOUT when a bounded wait of a product ran out
+    // (synchronises the stream)
+    int check_status(cudaStream_t s);
+    void release();
+    static size_t bytes_for(int64_t n);
 };
 
 // Timers: the slate::timers keys of the reference drivers, measured with CUDA

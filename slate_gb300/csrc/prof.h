@@ -13,6 +13,7 @@
 #define SLT_PROF_POTRF     8   /* diagonal-block Cholesky                   */
 #define SLT_PROF_CONVERT   9   /* precision conversion                      */
 #define SLT_PROF_SWEEP    10   /* one-launch triangular solve sweeps        */
+#define SLT_PROF_DIGIT    11   /* tensor-core digit-split FP64 residual     */
 
 namespace slt {
 void count_launch();

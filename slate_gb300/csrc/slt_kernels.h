@@ -166,6 +166,12 @@ size_t slt_residual_ws_bytes(int64_t n, int64_t nrhs);
 int slt_dresidual(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower,
                   const double* B, int64_t ldb, const double* X, int64_t ldx,
                   double* R, int64_t ldr, void* ws, cudaStream_t stream);
+/* R = B - A X with FP64 accuracy on the BF16 tensor cores (digit splitting,
+ * digit_residual.cu), nrhs <= 16, one call with its own workspace: the
+ * drivers keep the digit planes of A for a whole solve instead. */
+int slt_dresidual_digits(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower,
+                         const double* B, int64_t ldb, const double* X, int64_t ldx,
+                         double* R, int64_t ldr, cudaStream_t stream);
 /* Philox matrix generator identical to SLATE's slate::random::generate. */
 int slt_dgenerate(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
                   double* A, int64_t lda, cudaStream_t stream);

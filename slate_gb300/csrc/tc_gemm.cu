@@ -31,6 +31,7 @@
 #include "common.cuh"
 #include "prof.h"
 #include "slate_gb300.h"
+#include "tc_ptx.cuh"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -46,137 +47,6 @@ constexpr int kTcBM = 128;
 constexpr int kTcBN = 128;
 constexpr int kTcStages = 4;
 constexpr int kTcThreads = 128;
-constexpr long long kTcSpin = 1ll << 24;
-
-// ---------------------------------------------------------------------------
-// PTX wrappers
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t done;
-    asm volatile("{\n\t.reg .pred P1;\n\t"
-                 "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
-                 "selp.b32 %0, 1, 0, P1;\n\t}"
-                 : "=r"(done) : "r"(bar), "r"(parity) : "memory");
-    return done != 0;
-}
-
-__device__ __forceinline__ uint64_t globaltimer_ns()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Bounded wait (about two seconds of wall time, and an iteration cap);
-// returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = globaltimer_ns();
-    for (long long it = 0; it < kTcSpin; ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63) == 0 && globaltimer_ns() - t0 > 2000000000ull) return false;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y)
-{
-    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-                 " [%0], [%1, {%3, %4}], [%2];"
-                 :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols)
-{
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 :: "r"(dst_smem), "r"(ncols) : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
-{
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(taddr), "r"(ncols) : "memory");
-}
-
-template <int KIND>   // 0: kind::f16 (BF16/FP16 operands), 1: kind::tf32, 2: kind::f8f6f4 (E4M3)
-__device__ __forceinline__ void umma(uint32_t taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
-{
-    if (KIND == 0)
-        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                     :: "r"(taddr), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
-    else if (KIND == 2)
-        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                     "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}"
-                     :: "r"(taddr), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
-    else
-        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-                     :: "r"(taddr), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint32_t bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                 :: "r"(bar) : "memory");
-}
-
-// 32 lanes x 32 consecutive fp32 columns of TMEM into registers.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
-{
-    uint32_t r[32];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-                 "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-                   "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-                   "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    #pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (SBO), start address in 16-byte units.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
-{
-    uint64_t d = 0;
-    d |= uint64_t((saddr >> 4) & 0x3FFFu);          // start address
-    d |= uint64_t(1) << 16;                          // leading byte offset (unused for SW128 K-major)
-    d |= uint64_t(1024 >> 4) << 32;                  // stride byte offset
-    d |= uint64_t(1) << 46;                          // descriptor version
-    d |= uint64_t(2) << 61;                          // SWIZZLE_128B
-    return d;
-}
-
-// Instruction descriptor: D fp32, A/B format, both K-major, M = 128, N = BN.
-__host__ __device__ constexpr uint32_t make_idesc(uint32_t ab_format, int M, int N)
-{
-    return (1u << 4) | (ab_format << 7) | (ab_format << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
-}
 
 struct TcArgs {
     int64_t m, n, kpad;
@@ -319,11 +189,6 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
 // it to C with a TMA tensor reduce (cp.reduce.async.bulk.tensor .add), so the
 // read-modify-write of C is done by the memory system with full overlap.
 constexpr int kPThreads = 192;
-
-__device__ __forceinline__ void mbar_arrive(uint32_t bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
-}
 
 __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, uint32_t src, int x, int y)
 {
@@ -692,6 +557,21 @@ static int get_encode()
         cudaGetLastError();
     });
     return g_encode ? SLT_OK : SLT_ERR_NOT_SUPPORTED;
+}
+
+// 2-D tiled map: inner dimension `inner` elements (contiguous), `outer` rows
+// `stride_bytes` apart, box box_inner x box_outer.
+int tma_map_2d(CUtensorMap* map, void* ptr, CUtensorMapDataType dt, int64_t inner, int64_t outer,
+               int64_t stride_bytes, int box_inner, int box_outer, CUtensorMapSwizzle swz)
+{
+    if (get_encode()) return SLT_ERR_NOT_SUPPORTED;
+    cuuint64_t dims[2] = {cuuint64_t(inner), cuuint64_t(outer)};
+    cuuint64_t strides[1] = {cuuint64_t(stride_bytes)};
+    cuuint32_t box[2] = {cuuint32_t(box_inner), cuuint32_t(box_outer)};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, dt, 2, ptr, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? SLT_OK : SLT_ERR_ARG;
 }
 
 // 2-D map over a packed operand: inner dim = kpad elements, outer = rpad rows,
