@@ -13,8 +13,9 @@
 //
 //  * row i of A is scaled by 2^-ea_i and column c of X by 2^-ex_c (powers of
 //    two, exact) so that every |a'| and |x'| is below 1/2;
-//  * v = a' is split into eight balanced base-128 digits, d = rint(128 v),
-//    v <- 128 v - d (exact in FP64), |d| <= 64: an integer exact in BF16, and
+//  * a' is rounded to F = round(a' 2^56), |F| < 2^55, in int64 arithmetic on
+//    the bits of the double, and F is split into eight balanced base-128
+//    digits d_p in [-64, 64] (integers, exact in BF16):
 //    a' = sum_{p<8} d_p 128^-(p+1) + r with |r| <= 2^-57;
 //  * a' x' = sum_w S_w 128^-(w+2) with S_w = sum_k sum_{p+q=w} d_p d_q; the
 //    weight classes w >= 8 lie below 2^-53 of the product scale and are
@@ -75,97 +76,121 @@ constexpr int kDgCols = 16;           // right-hand sides per call
 constexpr uint32_t kDgATile = kDgBM * 128;          // 16 KB
 constexpr uint32_t kDgXHalf = 128 * 128;            // 128 rows x 128 bytes
 constexpr uint32_t kDgXStage = 2 * kDgXHalf;        // zero half + digit half
-// exponent words: "no non-zero entry" (the byte pattern 0x80 of a memset)
-// and "a non-finite entry" (above any frexp exponent)
-constexpr int kDgNone = int(0x80808080u);
-constexpr int kDgBad = 1 << 20;
+// Exponent keys.  key(v) = 0 for v = 0, 2047 for Inf / NaN, else
+// max(biased exponent of v, 1); keys are monotone in |v|, and for the largest
+// key K of a row, |v| < 2^(K - 1022) for every v of the row, so the scale
+// exponent e = K - 1021 gives |v 2^-e| < 1/2.  Rows and columns keep the
+// maximum key (atomicMax on a zeroed word).
+constexpr int kDgBadKey = 2047;
 
-__device__ __forceinline__ int dg_scale(int e) { return e == kDgNone ? 0 : e + 1; }
-
-// frexp exponent of |v| (v != 0, finite), or kDgBad for Inf / NaN
-__device__ __forceinline__ int dg_exp_of(double v)
+__device__ __forceinline__ int dg_key(double v)
 {
-    if (!(fabs(v) <= 1.7976931348623157e308)) return kDgBad;
-    int e;
-    frexp(v, &e);
-    return e;
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7fffffffffffffffull;
+    if (b == 0) return 0;
+    const int be = int(b >> 52);
+    return be == 0 ? 1 : be;
 }
 
-// Row exponents from rows [i] over columns [j0, j1) of column-major A; with
-// sym (lower storage) only the stored part j <= i.  grid (ceil(m/256), segs).
-__global__ void __launch_bounds__(256)
-dg_rowexp_kernel(int64_t m, int64_t n, const double* __restrict__ A, int64_t lda, int sym, int64_t cps, int* ex)
-{
-    const int64_t i = int64_t(blockIdx.x) * 256 + threadIdx.x;
-    if (i >= m) return;
-    const int64_t j0 = int64_t(blockIdx.y) * cps;
-    int64_t j1 = j0 + cps < n ? j0 + cps : n;
-    if (sym && j1 > i + 1) j1 = i + 1;
-    double mx = 0.0;
-    bool bad = false;
-    for (int64_t j = j0; j < j1; ++j) {
-        const double v = fabs(A[i + j * lda]);
-        bad |= !(v <= 1.7976931348623157e308);
-        mx = fmax(mx, v);
-    }
-    if (bad) atomicMax(ex + i, kDgBad);
-    else if (mx > 0.0) atomicMax(ex + i, dg_exp_of(mx));
-}
+__device__ __forceinline__ int dg_scale(int key) { return key == 0 ? 0 : key - 1021; }
 
-// Column exponents: column c of the m x ncols column-major matrix over rows
-// [r0, m), r0 = c + 1 with sym (the part of row c of a symmetric matrix held
-// in its lower-storage column c), else 0.  grid (ncols, segs).
+// Maximum keys of the rows of A (general: over the whole row; sym, lower
+// storage: over the stored part j <= i and, through the columns, over the
+// part held in column i below the diagonal).  Block: rows I0 .. I0 + 63 and
+// four 64-column tiles from J0.  grid (ceil(n / 256), ceil(n / 64)).
 __global__ void __launch_bounds__(256)
-dg_colexp_kernel(int64_t m, const double* __restrict__ A, int64_t lda, int sym, int64_t rps, int* ex)
+dg_akeys_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym, int* key)
 {
-    __shared__ double smx[256];
-    __shared__ int sbad;
-    const int64_t c = blockIdx.x;
-    const int64_t lo = sym ? c + 1 : 0;
-    const int64_t s0 = int64_t(blockIdx.y) * rps, s1 = int64_t(blockIdx.y + 1) * rps;
-    const int64_t r0 = s0 > lo ? s0 : lo;
-    const int64_t r1 = s1 < m ? s1 : m;
-    if (threadIdx.x == 0) sbad = 0;
-    __syncthreads();
-    double mx = 0.0;
-    bool bad = false;
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += 256) {
-        const double v = fabs(A[r + c * lda]);
-        bad |= !(v <= 1.7976931348623157e308);
-        mx = fmax(mx, v);
-    }
-    smx[threadIdx.x] = mx;
-    if (bad) sbad = 1;
-    __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
-        if (threadIdx.x < w) smx[threadIdx.x] = fmax(smx[threadIdx.x], smx[threadIdx.x + w]);
+    __shared__ int K[64][65];
+    const int64_t I0 = int64_t(blockIdx.y) * 64;
+    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
+    int rmax = 0;
+    for (int t = 0; t < 4; ++t) {
+        const int64_t J0 = (int64_t(blockIdx.x) * 4 + t) * 64;
+        if (J0 >= n || (sym && J0 > I0)) break;
+        for (int kk = ty; kk < 64; kk += 4) {
+            const int64_t i = I0 + tx, j = J0 + kk;
+            K[tx][kk] = (i < n && j < n && !(sym && j > i)) ? dg_key(A[i + j * lda]) : 0;
+        }
+        __syncthreads();
+        if (threadIdx.x < 64) {
+            for (int c = 0; c < 64; ++c) rmax = max(rmax, K[threadIdx.x][c]);
+        }
+        else if (sym && threadIdx.x < 128) {
+            const int c = threadIdx.x - 64;
+            int cm = 0;
+            for (int r = 0; r < 64; ++r) cm = max(cm, K[r][c]);
+            if (cm && J0 + c < n) atomicMax(key + J0 + c, cm);
+        }
         __syncthreads();
     }
+    if (threadIdx.x < 64 && rmax && I0 + threadIdx.x < n) atomicMax(key + I0 + threadIdx.x, rmax);
+}
+
+// Maximum keys of the columns of an m x ncols column-major matrix.
+// grid (ncols, segs), rps rows per segment.
+__global__ void __launch_bounds__(256)
+dg_colkeys_kernel(int64_t m, const double* __restrict__ X, int64_t ldx, int64_t rps, int* key)
+{
+    __shared__ int red[8];
+    const int64_t c = blockIdx.x;
+    const int64_t r0 = int64_t(blockIdx.y) * rps;
+    const int64_t r1 = r0 + rps < m ? r0 + rps : m;
+    int mx = 0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += 256) mx = max(mx, dg_key(X[r + c * ldx]));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
     if (threadIdx.x == 0) {
-        if (sbad) atomicMax(ex + c, kDgBad);
-        else if (smx[0] > 0.0) atomicMax(ex + c, dg_exp_of(smx[0]));
+        for (int w = 1; w < 8; ++w) mx = max(mx, red[w]);
+        if (mx) atomicMax(key + c, mx);
     }
 }
 
-// The eight digits of a' = v 2^-e (|a'| < 1/2), packed four BF16 per 8 bytes
-// for four consecutive k.
-__device__ __forceinline__ void dg_digits4(const double (&v)[4], int e, uint2 (&out)[kDgPlanes])
+// F = round(v 2^(56 - e)), rounding half away from zero, for |v 2^-e| < 1/2:
+// |F| < 2^55.  Integer arithmetic on the bits of v (FP64 instructions issue
+// at a small fraction of the integer rate on this part).
+__device__ __forceinline__ long long dg_fixed(double v, int e)
 {
-    double t[4];
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    const int be = int((b >> 52) & 0x7ff);
+    long long m = static_cast<long long>(b & 0xFFFFFFFFFFFFFull);
+    int x = -1074;                          // v = m 2^x
+    if (be != 0) { m |= 1ll << 52; x = be - 1075; }
+    const int sh = x - e + 56;
+    long long F = 0;
+    if (sh >= 0) F = m << sh;               // m 2^sh < 2^55, so sh < 55
+    else if (sh > -64) F = (m + (1ll << (-sh - 1))) >> (-sh);
+    return (b >> 63) ? -F : F;
+}
+
+// The eight balanced base-128 digits of F (d_0 most significant), each in
+// [-64, 64] and exact in BF16, packed four BF16 per 8 bytes for four
+// consecutive k: F = sum_p d_p 128^(7 - p), taken from the low end.  A key of
+// 2047 (Inf / NaN in the row or column) gives zero digits; the reduction
+// writes NaN for it.
+__device__ __forceinline__ void dg_digits4(const double (&v)[4], int key, uint2 (&out)[kDgPlanes])
+{
+    const int e = dg_scale(key);
+    int d[4][kDgPlanes];
     #pragma unroll
-    for (int u = 0; u < 4; ++u) t[u] = (e >= kDgBad) ? 0.0 : ldexp(v[u], -e);
+    for (int u = 0; u < 4; ++u) {
+        long long F = key == kDgBadKey ? 0 : dg_fixed(v[u], e);
+        #pragma unroll
+        for (int p = kDgPlanes - 1; p > 0; --p) {
+            int r = int(F & 127);
+            r -= (r >= 64) ? 128 : 0;
+            d[u][p] = r;
+            F = (F - r) >> 7;
+        }
+        d[u][0] = int(F);
+    }
     #pragma unroll
     for (int p = 0; p < kDgPlanes; ++p) {
-        unsigned short h[4];
+        uint32_t h[4];
         #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const double s = t[u] * 128.0;
-            const double d = rint(s);
-            t[u] = s - d;
-            h[u] = __bfloat16_as_ushort(__float2bfloat16_rn(float(d)));
-        }
-        out[p].x = uint32_t(h[0]) | (uint32_t(h[1]) << 16);
-        out[p].y = uint32_t(h[2]) | (uint32_t(h[3]) << 16);
+        for (int u = 0; u < 4; ++u) h[u] = __bfloat16_as_ushort(__float2bfloat16_rn(float(d[u][p])));
+        out[p].x = h[0] | (h[1] << 16);
+        out[p].y = h[2] | (h[3] << 16);
     }
 }
 
@@ -202,10 +227,10 @@ dg_split_a_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym,
     const int kq = (threadIdx.x & 15) * 4;
     for (int r = threadIdx.x >> 4; r < 64; r += 16) {
         const int64_t i = I0 + r;
-        const int e = i < n ? dg_scale(rexp[i]) : 0;
+        const int key = i < n ? rexp[i] : 0;
         double v[4] = {T[r][kq], T[r][kq + 1], T[r][kq + 2], T[r][kq + 3]};
         uint2 d[kDgPlanes];
-        dg_digits4(v, e, d);
+        dg_digits4(v, key, d);
         __nv_bfloat16* dst = planes + i * ldk + K0 + kq;
         #pragma unroll
         for (int p = 0; p < kDgPlanes; ++p)
@@ -222,12 +247,12 @@ dg_split_x_kernel(int64_t n, int nrhs, const double* __restrict__ X, int64_t ldx
     const int c = blockIdx.y;
     const int64_t k = (int64_t(blockIdx.x) * 256 + threadIdx.x) * 4;
     if (k >= ldk) return;
-    const int e = c < nrhs ? dg_scale(cexp[c]) : 0;
+    const int key = c < nrhs ? cexp[c] : 0;
     double v[4];
     #pragma unroll
     for (int u = 0; u < 4; ++u) v[u] = (c < nrhs && k + u < n) ? X[k + u + int64_t(c) * ldx] : 0.0;
     uint2 d[kDgPlanes];
-    dg_digits4(v, e, d);
+    dg_digits4(v, key, d);
     #pragma unroll
     for (int q = 0; q < kDgPlanes; ++q)
         *reinterpret_cast<uint2*>(xd + int64_t(q * kDgCols + c) * ldk + k) = d[q];
@@ -468,7 +493,7 @@ dg_reduce_kernel(int64_t n, int64_t rows_pad, int segs, const long long* __restr
         lo += p[int64_t(kDgCols) * rows_pad];
     }
     double r;
-    if (rexp[i] >= kDgBad || cexp[c] >= kDgBad) {
+    if (rexp[i] == kDgBadKey || cexp[c] == kDgBadKey) {
         r = __longlong_as_double(0x7ff8000000000000ll);
     }
     else {
@@ -540,17 +565,12 @@ int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cuda
     TRY(part.alloc(size_t(segs) * 2 * kDgCols * size_t(rows_pad) * sizeof(long long), s));
     TRY(status.alloc(sizeof(int), s));
     SLT_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(int), s));
-    SLT_CUDA_TRY(cudaMemsetAsync(rexp.p, 0x80, sizeof(int) * size_t(rows_pad), s));
+    SLT_CUDA_TRY(cudaMemsetAsync(rexp.p, 0, sizeof(int) * size_t(rows_pad), s));
 
-    // row exponents: the stored row, and for sym the stored column below the diagonal
-    const int64_t cps = 4096;
-    dg_rowexp_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(ceildiv(n, cps))), 256, 0, s>>>(
-        n, n, A, lda, sym, cps, rexp.as<int>());
+    // row keys: one pass over the stored part of A
+    dg_akeys_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(ceildiv(n, 64))), 256, 0, s>>>(
+        n, A, lda, sym, rexp.as<int>());
     count_launch();
-    if (sym) {
-        dg_colexp_kernel<<<dim3(unsigned(n), 1), 256, 0, s>>>(n, A, lda, 1, n, rexp.as<int>());
-        count_launch();
-    }
     dg_split_a_kernel<<<dim3(unsigned(ldk / 64), unsigned(rows_pad / 64)), 256, 0, s>>>(
         n, A, lda, sym, rexp.as<int>(), planes.as<__nv_bfloat16>(), ldk, pstride);
     count_launch();
@@ -575,10 +595,10 @@ int DigitMatrix::residual(int64_t nrhs, const double* B, int64_t ldb, const doub
         return slt_from_cuda(cudaFuncSetAttribute(dg_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   int(dg_smem_bytes())));
     }));
-    SLT_CUDA_TRY(cudaMemsetAsync(cexp.p, 0x80, sizeof(int) * kDgCols, s));
+    SLT_CUDA_TRY(cudaMemsetAsync(cexp.p, 0, sizeof(int) * kDgCols, s));
     const int64_t rps = 16384;
-    dg_colexp_kernel<<<dim3(unsigned(nrhs), unsigned(ceildiv(n, rps))), 256, 0, s>>>(n, X, ldx, 0, rps,
-                                                                                   cexp.as<int>());
+    dg_colkeys_kernel<<<dim3(unsigned(nrhs), unsigned(ceildiv(n, rps))), 256, 0, s>>>(n, X, ldx, rps,
+                                                                                    cexp.as<int>());
     count_launch();
     dg_split_x_kernel<<<dim3(unsigned(ceildiv(ldk, 1024)), kDgCols), 256, 0, s>>>(
         n, int(nrhs), X, ldx, cexp.as<int>(), xplanes.as<__nv_bfloat16>(), ldk);

@@ -686,7 +686,7 @@ struct FgmresBlock {
     double cte;
     Residual& res;
     int64_t restart = 0, R1 = 1, SC = 0;
-    DevBuf nws, scal, V, W, Z, Bg, Rg, Wlo;
+    DevBuf nws, scal, V, W, Z, Bg, Rg, Wlo, cgsws;
     std::vector<double> hs;
 
     struct Col {
@@ -715,6 +715,7 @@ struct FgmresBlock {
         TRY(Bg.alloc(sizeof(double) * nn * size_t(kMaxCols), s));
         TRY(Rg.alloc(sizeof(double) * nn * size_t(kMaxCols), s));
         hs.assign(size_t(SC * kMaxCols), 0.0);
+        TRY(cgsws.alloc(slt_cgs_ws_bytes(R1), s));
         return Wlo.alloc(sizeof(float) * nn * size_t(kMaxCols), s);
     }
 
@@ -803,20 +804,16 @@ struct FgmresBlock {
                 TRY(copy_col(B + c.c * ldb, bg + (na + i) * n, n, s));
             }
             TRY(products(na + ns, s));
-            for (int64_t i = 0; i < na; ++i) {
-                const int64_t q = arn[i];
-                const int64_t j = cl[q].j;
-                double* Vd = Vc(q);
-                double* vj1 = Vd + (j + 1) * n;
-                double* dh = Sc(q) + 4;
-                double* dz = dh + R1;
-                TRY(slt_dgeadd(n, 1, -1.0, rg + i * n, n, 0.0, vj1, n, s));
-                // CGS2
-                TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dh, R1, s));
-                TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dh, R1, 1.0, vj1, n, nws.p, s));
-                TRY(slt_dgemm_skinny_t(j + 1, 1, n, 1.0, Vd, n, vj1, n, 0.0, dz, R1, s));
-                TRY(slt_dgemm_skinny(n, 1, j + 1, -1.0, Vd, n, 0, dz, R1, 1.0, vj1, n, nws.p, s));
-                TRY(slt_dnrm2(n, vj1, Sc(q) + 3, s));
+            if (na) {
+                // CGS2 of every Arnoldi column in one set of launches:
+                // v_{j+1} = -(A w), orthogonalised twice against v_0 .. v_j
+                slt_cgs_cols cc{};
+                cc.na = int(na);
+                for (int64_t i = 0; i < na; ++i) {
+                    cc.q[i] = int(arn[i]);
+                    cc.j[i] = int(cl[arn[i]].j);
+                }
+                TRY(slt_dcgs2(n, V.as<double>(), R1, &cc, rg, scal.as<double>(), SC, cgsws.p, s));
             }
             for (int64_t i = 0; i < ns; ++i) {
                 const int64_t q = st[i];

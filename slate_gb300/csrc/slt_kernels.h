@@ -172,6 +172,23 @@ int slt_dresidual(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym
 int slt_dresidual_digits(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower,
                          const double* B, int64_t ldb, const double* X, int64_t ldx,
                          double* R, int64_t ldr, cudaStream_t stream);
+/* Classical Gram-Schmidt applied twice (CGS2) for the columns of one block
+ * FGMRES step (arnoldi.cu).  Column i of the step uses basis slot q[i] of V
+ * (slot q: n x R1 doubles at V + q n R1) and its step j[i]: the new vector
+ * V_q(:, j+1) = -W(:, i) is orthogonalised against V_q(:, 0:j); the two
+ * coefficient vectors go to scal[q SC + 4 ..] and scal[q SC + 4 + R1 ..],
+ * the norm of the result to scal[q SC + 3].  R1 <= 32.
+ * ws: slt_cgs_ws_bytes(R1) bytes. */
+#define kSltCgsMaxCols 16
+#define kSltCgsMaxSeg 64
+typedef struct slt_cgs_cols {
+    int na;                    /* active columns, <= 16 */
+    int q[kSltCgsMaxCols];     /* basis slot */
+    int j[kSltCgsMaxCols];     /* step: basis vectors 0..j exist */
+} slt_cgs_cols;
+size_t slt_cgs_ws_bytes(int64_t R1);
+int slt_dcgs2(int64_t n, double* V, int64_t R1, const slt_cgs_cols* cols, const double* W, double* scal,
+              int64_t SC, void* ws, cudaStream_t stream);
 /* Philox matrix generator identical to SLATE's slate::random::generate. */
 int slt_dgenerate(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
                   double* A, int64_t lda, cudaStream_t stream);

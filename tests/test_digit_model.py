@@ -5,8 +5,9 @@ sums the digit products of weight classes w = p + q <= 7 in FP32 over chunks
 of 256 k, folds the class sums into two int64 words and scales the result.
 These tests check, with numpy on the host, the facts the kernel relies on:
 
-* the split is exact up to its stated remainder: a' = sum_p d_p 128^-(p+1)
-  + r, |r| <= 2^-57, |d_p| <= 64 (so every digit is exact in BF16);
+* the split is exact up to its stated remainder: F = round(a' 2^56) taken
+  from the bits of the double, a' = sum_p d_p 128^-(p+1) + r, |r| <= 2^-57,
+  |d_p| <= 64 (so every digit is exact in BF16);
 * FP32 class sums over 256 k are exact whatever the order of accumulation
   (every partial sum is an integer of magnitude <= 2^23);
 * the int64 fold and the final scaling reproduce A x within the bound
@@ -19,29 +20,49 @@ import pytest
 PLANES = 8
 
 
-def _exps(M):
-    """frexp exponent + 1 of each row's max |entry| (0 for a zero row)."""
-    m = np.abs(M).max(axis=1)
-    _, e = np.frexp(m)
-    return np.where(m > 0, e + 1, 0).astype(np.int64)
+def _keys(M):
+    """Per row: the largest key max(biased exponent, 1) over the non-zero
+    entries (0 for a zero row), and the scale exponent key - 1021."""
+    b = np.ascontiguousarray(M, dtype=np.float64).view(np.uint64) & np.uint64(0x7FFFFFFFFFFFFFFF)
+    be = (b >> np.uint64(52)).astype(np.int64)
+    key = np.where(b == 0, 0, np.maximum(be, 1)).max(axis=1)
+    return np.where(key == 0, 0, key - 1021).astype(np.int64)
+
+
+def _fixed(M, e):
+    """F = round(v 2^(56 - e)), half away from zero, from the bits of v."""
+    b = np.ascontiguousarray(M, dtype=np.float64).view(np.uint64)
+    be = ((b >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
+    m = (b & np.uint64((1 << 52) - 1)).astype(np.int64)
+    x = np.where(be == 0, -1074, be - 1075)
+    m = np.where(be == 0, m, m | (1 << 52))
+    sh = x - e[:, None] + 56
+    up = m << np.clip(sh, 0, 62)
+    k = np.clip(-sh, 1, 63)
+    dn = (m + (np.int64(1) << (k - 1))) >> k
+    F = np.where(sh >= 0, up, np.where(sh > -64, dn, 0))
+    return np.where((b >> np.uint64(63)).astype(bool), -F, F)
 
 
 def _split(M, e):
-    t = np.ldexp(M, -e[:, None])
-    out = []
-    for _ in range(PLANES):
-        s = t * 128.0
-        d = np.rint(s)
-        t = s - d
-        out.append(d)
-    return out, t
+    """Eight balanced base-128 digits (d_0 most significant) and F."""
+    F = _fixed(M, e)
+    d = [None] * PLANES
+    G = F.copy()
+    for p in range(PLANES - 1, 0, -1):
+        r = G & 127
+        r = np.where(r >= 64, r - 128, r)
+        d[p] = r.astype(np.float64)
+        G = (G - r) >> 7
+    d[0] = G.astype(np.float64)
+    return d, F
 
 
 def _digit_product(A, x):
     """A x (x one column) the way the kernel forms it."""
     n = A.shape[0]
-    ea = _exps(A)
-    ex = _exps(x.reshape(1, -1))[0]
+    ea = _keys(A)
+    ex = _keys(x.reshape(1, -1))[0]
     da, _ = _split(A, ea)
     dx, _ = _split(x.reshape(1, -1), np.array([ex]))
     hi = np.zeros(n, dtype=np.int64)
@@ -72,15 +93,19 @@ def test_split_is_exact_up_to_remainder():
     A = rng.standard_normal((64, 300)) * np.ldexp(1.0, rng.integers(-60, 60, size=(64, 1)))
     A[3] = 0.0
     A[5, ::7] = 1e-300
-    e = _exps(A)
-    d, r = _split(A, e)
-    assert np.abs(np.ldexp(A, -e[:, None])).max() < 0.5
+    A[6, :] = 5e-324 * rng.integers(0, 1000, 300)       # subnormal row
+    A[7, 0] = 0.5 - 2.0 ** -54                            # rounds up to the top of the range
+    e = _keys(A)
+    d, F = _split(A, e)
+    sc = np.ldexp(A, -e[:, None])
+    assert np.abs(sc).max() < 0.5
+    assert np.abs(F).max() < 2 ** 55
     for p in range(PLANES):
         assert np.abs(d[p]).max() <= 64
-        assert np.all(d[p] == np.rint(d[p]))
-    assert np.abs(r).max() <= 0.5      # remainder in units of 128^-8 = 2^-56
-    rec = sum(np.ldexp(d[p], -7 * (p + 1)) for p in range(PLANES))
-    assert np.all(np.abs(np.ldexp(A, -e[:, None]) - rec) <= 2.0 ** -57)
+    rec = sum(d[p].astype(np.int64) * 128 ** (PLANES - 1 - p) for p in range(PLANES))
+    assert np.array_equal(rec, F)
+    # |a' - F 2^-56| <= 2^-57
+    assert np.all(np.abs(sc - np.ldexp(F.astype(np.float64), -56)) <= 2.0 ** -57)
 
 
 def test_fp32_class_sums_are_exact_at_the_limit():
