@@ -84,6 +84,26 @@ int to_host(const DevBuf& d, T* h, int64_t m, int64_t n, int64_t ld, cudaStream_
     return SLT_OK;
 }
 
+// The referenced triangle of an n x n column-major array (lower: rows
+// j0 .. n of columns j0 .. j0 + 511; upper: rows 0 .. j0 + 511), one 2-D copy
+// per 512-column block: half the bytes of the whole array.  The diagonal
+// blocks travel whole; the drivers leave their other triangle as it is, so
+// copying the result back restores the caller's values there.
+template <typename T>
+int tri_copy(bool lower, int64_t n, const T* src, int64_t lds, T* dst, int64_t ldd, cudaMemcpyKind kind,
+             cudaStream_t s)
+{
+    constexpr int64_t kB = 512;
+    for (int64_t j0 = 0; j0 < n; j0 += kB) {
+        const int64_t w = std::min(kB, n - j0);
+        const int64_t r0 = lower ? j0 : 0;
+        const int64_t rows = lower ? n - j0 : j0 + w;
+        SLT_CUDA_TRY(cudaMemcpy2DAsync(dst + r0 + j0 * ldd, size_t(ldd) * sizeof(T), src + r0 + j0 * lds,
+                                       size_t(lds) * sizeof(T), size_t(rows) * sizeof(T), size_t(w), kind, s));
+    }
+    return SLT_OK;
+}
+
 // Per-panel relative pivots -> LAPACK 1-based global ipiv, and back.
 void ipiv_to_lapack(const std::vector<int>& rel, int64_t nb, int* ipiv, int64_t cnt)
 {
@@ -666,7 +686,9 @@ static void lapack_potrf_impl(char uplo, int n, double* a, int lda, int* info, i
     cudaStream_t s = lapack_stream();
     slt_options o = lapack_opts();
     DevBuf dA, dB, tmp;
-    if (to_device(a, n, n, lda, dA, s)) { *info = -100; return; }
+    // only the referenced triangle crosses the link, both ways
+    if (dA.alloc(sizeof(double) * size_t(n) * size_t(n), s) ||
+        tri_copy<double>(!up, n, a, lda, dA.as<double>(), n, cudaMemcpyHostToDevice, s)) { *info = -100; return; }
     if (b && to_device(b, n, nrhs, ldb, dB, s)) { *info = -100; return; }
     if (lower_view(uplo, n, dA, tmp, s)) { *info = -100; return; }
     int64_t inf = 0;
@@ -678,13 +700,8 @@ static void lapack_potrf_impl(char uplo, int n, double* a, int lda, int* info, i
         if (rc) { *info = -1000 + rc; return; }
         std::swap(dA.p, tmp.p);
     }
-    // write back only the referenced triangle
-    std::vector<double> h(size_t(n) * size_t(n));
-    if (cudaMemcpyAsync(h.data(), dA.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+    if (tri_copy<double>(!up, n, dA.as<double>(), n, a, lda, cudaMemcpyDeviceToHost, s) ||
         (b && to_host(dB, b, n, nrhs, ldb, s)) || cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
-    for (int j = 0; j < n; ++j)
-        for (int i = 0; i < n; ++i)
-            if (up ? (i <= j) : (i >= j)) a[i + size_t(j) * lda] = h[i + size_t(j) * n];
     *info = int(inf);
 }
 
@@ -704,15 +721,27 @@ static void lapack_dsposv_impl(char uplo, int n, int nrhs, double* a, int lda, d
     cudaStream_t s = lapack_stream();
     slt_options o = lapack_opts();
     DevBuf dA, dB, dX, tmp;
-    if (to_device(a, n, n, lda, dA, s) || to_device(b, n, nrhs, ldb, dB, s) ||
+    // phase timers of the host entry point (slt_timer("dsposv::h2d") etc.)
+    TimerSet tm(s);
+    tm.start("dsposv::h2d");
+    // only the referenced triangle crosses the link
+    if (dA.alloc(sizeof(double) * size_t(n) * size_t(n), s) ||
+        tri_copy<double>(!up, n, a, lda, dA.as<double>(), n, cudaMemcpyHostToDevice, s) ||
+        to_device(b, n, nrhs, ldb, dB, s) ||
         dX.alloc(sizeof(double) * size_t(n) * size_t(std::max(nrhs, 1)), s)) { *info = -100; return; }
     if (lower_view(uplo, n, dA, tmp, s)) { *info = -100; return; }
+    tm.stop("dsposv::h2d");
     int64_t inf = 0;
     int it = 0;
+    tm.start("dsposv::solve");
     int rc = slt_dsposv_device(n, nrhs, dA.as<double>(), n, dB.as<double>(), n, dX.as<double>(), n, &o, s,
                                &it, &inf);
     if (rc) { *info = -1000 + rc; return; }
-    if (to_host(dX, x, n, nrhs, ldx, s) || cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
+    tm.stop("dsposv::solve");
+    tm.start("dsposv::d2h");
+    if (to_host(dX, x, n, nrhs, ldx, s)) { *info = -100; return; }
+    tm.stop("dsposv::d2h");
+    if (cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
     if (it < 0) {
         // the FP64 fallback ran: A holds its Cholesky factor (referenced triangle)
         if (up) {
@@ -720,12 +749,8 @@ static void lapack_dsposv_impl(char uplo, int n, int nrhs, double* a, int lda, d
             if (rc) { *info = -1000 + rc; return; }
             std::swap(dA.p, tmp.p);
         }
-        std::vector<double> h(size_t(n) * size_t(n));
-        if (cudaMemcpyAsync(h.data(), dA.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        if (tri_copy<double>(!up, n, dA.as<double>(), n, a, lda, cudaMemcpyDeviceToHost, s) ||
             cudaStreamSynchronize(s) != cudaSuccess) { *info = -100; return; }
-        for (int j = 0; j < n; ++j)
-            for (int i = 0; i < n; ++i)
-                if (up ? (i <= j) : (i >= j)) a[i + size_t(j) * lda] = h[i + size_t(j) * n];
     }
     *iter = it;
     *info = int(inf);

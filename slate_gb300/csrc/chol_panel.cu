@@ -135,7 +135,7 @@ struct CholPanelArgs {
     int* info;
     int* status;
     GridBarrier* bar;
-    int* next_fail;     // set when the lookahead factor of the next diagonal block fails
+    int* next_fail;     // 1 + the step whose diagonal block failed (its lookahead factor)
     unsigned* diag_ready;  // index of the last diagonal block published by the lookahead
     unsigned* head_done;   // per step: blocks that solved rows needed by the others' update
     T* dinv_ws;         // per step: the diagonal block's transposed inverse, [16][64][64]
@@ -425,7 +425,14 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 return (i < kb && l < kb && i >= l) ? __ldcg(&P[c0 + i + (c0 + l) * ld]) : T(0);
             }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
         }
-        if (t == 0) s_fail = (c0 > 0) ? ld_volatile_i32(a.next_fail) : 0;
+        // next_fail holds 1 + the step whose diagonal block failed; the owner
+        // of that block writes it during the step before, possibly before a
+        // slower block has started that step, so only a failure of this
+        // step's (or an earlier) block counts here
+        if (t == 0) {
+            const int nf = (c0 > 0) ? ld_volatile_i32(a.next_fail) : 0;
+            s_fail = (nf != 0 && nf - 1 <= k) ? 1 : 0;
+        }
         __syncthreads();
         if (c0 == 0) {
             const int f = factor_diag_block(D, Dinv, kb);
@@ -651,7 +658,7 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 a.dinv_ws[size_t(k + 1) * kCpLinv + e] = Us[(e / kCpIB) * 68 + e % kCpIB];
             if (t == 0 && f) {
                 atomicCAS(a.info, 0, int(a.info_offset + cbeg + f));
-                *reinterpret_cast<volatile int*>(a.next_fail) = 1;
+                *reinterpret_cast<volatile int*>(a.next_fail) = k + 2;     // 1 + step k + 1
             }
             __threadfence();
             __syncthreads();

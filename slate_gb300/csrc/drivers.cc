@@ -228,6 +228,14 @@ static int lookahead_panel_sms(const DriverTune& t, int sms)
     return std::min(t.panel_sms, sms);
 }
 
+// Panels per deferred trailing update of potrf (1: update after every
+// panel): SLT_UPDATE_DEPTH when set (the tuner's override), else the table's.
+static int64_t update_depth(const DriverTune& t)
+{
+    if (const char* e = std::getenv("SLT_UPDATE_DEPTH")) return std::max(1, std::atoi(e));
+    return std::max(1, t.depth);
+}
+
 struct Lookahead {
     bool on = false;
     cudaStream_t s = nullptr, su = nullptr;
@@ -452,6 +460,31 @@ int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc,
     if (ot.gemm_engine == 0) ot.gemm_engine = tune.engine;
     Lookahead la;
     TRY(la.init(o, tune, n, nb, s));
+    const int64_t depth = update_depth(tune);
+    if (!la.on && depth > 1) {
+        // Deferred trailing update: the panels of a block of `depth` panels
+        // are factored one after the other, each block column first brought
+        // up to date with the block's earlier panels (a GEMM with k = the
+        // columns factored so far in the block), and the rest of the
+        // trailing matrix takes one update with k = depth * nb.  Same
+        // factor L; the trailing matrix is read and written once per block
+        // instead of once per panel.
+        for (int64_t r0 = 0; r0 < n; r0 += depth * nb) {
+            const int64_t sb = std::min(depth * nb, n - r0);
+            for (int64_t c = r0; c < r0 + sb; c += nb) {
+                const int64_t kb = std::min(nb, n - c);
+                if (c > r0)
+                    TRY(k_gemm('T', n - c, kb, c - r0, T(-1), A + c + r0 * lda, lda, A + c + r0 * lda, lda, T(1),
+                               A + c + c * lda, lda, 1, ot, s));
+                TRY(k_chol_panel(n - c, kb, A + c + c * lda, lda, fc.d_info, c, bar.p, fc.d_status, s));
+            }
+            const int64_t t0 = r0 + sb;
+            if (t0 >= n) break;
+            const T* L = A + t0 + r0 * lda;
+            TRY(k_gemm('T', n - t0, n - t0, sb, T(-1), L, lda, L, lda, T(1), A + t0 + t0 * lda, lda, 1, ot, s));
+        }
+        return SLT_OK;
+    }
     for (int64_t r0 = 0; r0 < n; r0 += nb) {
         const int64_t kb = std::min(nb, n - r0);
         {
@@ -582,7 +615,8 @@ struct LoFactor {
         const double u = o.factor_precision == SLT_PREC_BF16 ? 0x1p-8
                        : o.factor_precision == SLT_PREC_FP8  ? 0x1p-4 : 0x1p-11;
         for (int attempt = 0;; ++attempt) {
-            TRY(slt_convert_d2s_scaled(n, n, Ahi, lda, r, c, A.as<float>(), ld, s));
+            // the factor reads and writes the lower triangle only
+            TRY(slt_convert_d2s_scaled_lower(n, Ahi, lda, r, A.as<float>(), ld, s));
             if (attempt > 0) {
                 sigma = u * double(int64_t(1) << (3 * (attempt - 1)));
                 TRY(slt_sshift_diag(n, float(sigma), A.as<float>(), ld, s));

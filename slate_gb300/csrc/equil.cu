@@ -111,24 +111,26 @@ __device__ __forceinline__ int pow2_exponent(double s)
 // B = D(r_i * A_ij * c_j); SCALED = false: B = D(A) (r, c unused).  Each
 // thread handles four rows of one column (1024 rows per block), so that every
 // warp keeps four coalesced loads in flight.
-template <typename S, typename D, bool SCALED>
+// LOWER: only the lower triangle (i >= j) is read and written.
+template <typename S, typename D, bool SCALED, bool LOWER = false>
 __global__ void convert_scaled_kernel(int64_t m, int64_t n, const S* __restrict__ A, int64_t lda,
                                       const double* __restrict__ r, const double* __restrict__ c,
                                       D* __restrict__ B, int64_t ldb)
 {
     const int64_t i0 = int64_t(blockIdx.x) * 1024 + threadIdx.x;
-    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    const int64_t jend = LOWER ? min64(n, int64_t(blockIdx.x) * 1024 + 1024) : n;
+    for (int64_t j = blockIdx.y; j < jend; j += gridDim.y) {
         const int kc = (SCALED && c) ? pow2_exponent(c[j]) : 0;
         S v[4];
         #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int64_t i = i0 + 256 * k;
-            v[k] = i < m ? A[i + j * lda] : S(0);
+            v[k] = (i < m && (!LOWER || i >= j)) ? A[i + j * lda] : S(0);
         }
         #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int64_t i = i0 + 256 * k;
-            if (i < m) {
+            if (i < m && (!LOWER || i >= j)) {
                 if (SCALED) B[i + j * ldb] = D(scale_pow2(double(v[k]), (r ? pow2_exponent(r[i]) : 0) + kc));
                 else B[i + j * ldb] = D(v[k]);
             }
@@ -177,6 +179,19 @@ extern "C" int slt_convert_d2s_scaled(int64_t m, int64_t n, const double* A, int
     dim3 g(unsigned(ceildiv(m, 1024)), unsigned(std::min<int64_t>(n, 65535)));
     if (r || c) convert_scaled_kernel<double, float, true><<<g, 256, 0, stream>>>(m, n, A, lda, r, c, B, ldb);
     else convert_scaled_kernel<double, float, false><<<g, 256, 0, stream>>>(m, n, A, lda, r, c, B, ldb);
+    count_launch();
+    return slt_from_cuda(cudaGetLastError());
+}
+
+// The lower triangle of B (float, n x n) = diag(d) A diag(d) on the lower
+// triangle of A; d may be null.  The strictly upper part of B is not written.
+extern "C" int slt_convert_d2s_scaled_lower(int64_t n, const double* A, int64_t lda, const double* d, float* B,
+                                            int64_t ldb, cudaStream_t stream)
+{
+    if (n <= 0) return SLT_OK;
+    dim3 g(unsigned(ceildiv(n, 1024)), unsigned(std::min<int64_t>(n, 65535)));
+    if (d) convert_scaled_kernel<double, float, true, true><<<g, 256, 0, stream>>>(n, n, A, lda, d, d, B, ldb);
+    else convert_scaled_kernel<double, float, false, true><<<g, 256, 0, stream>>>(n, n, A, lda, d, d, B, ldb);
     count_launch();
     return slt_from_cuda(cudaGetLastError());
 }

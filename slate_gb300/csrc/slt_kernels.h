@@ -189,6 +189,10 @@ typedef struct slt_cgs_cols {
 size_t slt_cgs_ws_bytes(int64_t R1);
 int slt_dcgs2(int64_t n, double* V, int64_t R1, const slt_cgs_cols* cols, const double* W, double* scal,
               int64_t SC, void* ws, cudaStream_t stream);
+/* Lower triangle of B (float) = diag(d) A diag(d) (d may be null), the
+ * strictly upper part of B untouched: the Cholesky factor's working copy. */
+int slt_convert_d2s_scaled_lower(int64_t n, const double* A, int64_t lda, const double* d, float* B,
+                                 int64_t ldb, cudaStream_t stream);
 /* Philox matrix generator identical to SLATE's slate::random::generate. */
 int slt_dgenerate(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
                   double* A, int64_t lda, cudaStream_t stream);

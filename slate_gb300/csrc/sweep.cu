@@ -32,6 +32,8 @@
 #include "common.cuh"
 #include "prof.h"
 
+#include <type_traits>
+
 namespace slt {
 
 constexpr int kSwBS = 64;
@@ -396,6 +398,268 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 sweep for 5 to 16 right-hand sides (the preconditioner of the block
+// FGMRES).  Same ticket order, mailbox and chain step as sweep_kernel; the
+// products with the blocks solved two or more steps earlier differ:
+//  * the tiles stream through a ring of kS16 shared-memory stages filled with
+//    cp.async (zero-filled outside the matrix), so kS16 - 1 tiles are in
+//    flight while one is multiplied;
+//  * thread t owns a 4 x 4 register tile -- 4 rows by 4 right-hand sides --
+//    over one quarter (16 columns) of every tile: two 16-byte shared loads per
+//    16 FMAs; the four quarters are added once per block row.
+// Tile layout in a stage: [column][row] for op(M) = M (rows of a column
+// contiguous, as in memory), [row][column] for op(M) = M^T; the thread's
+// rows are 4 consecutive ones for M and 4 rows 16 apart for M^T, so that
+// both layouts are read without bank conflicts.
+constexpr int kS16 = 3;
+constexpr int kSwLd = kSwBS + 4;       // stage row stride (floats), 16-byte rows
+
+struct Sweep16Smem {
+    float Ts[kS16][kSwBS][kSwLd];      // tile ring; the last block row's partial sums reuse it
+    float Ds[kSwBS][kSwBS + 1];        // inverse of the diagonal block, [row][col]
+    float Ws[kSwBS][kSwBS + 1];        // W_i, [row][col]
+    float xs[kS16][kSwBS][kSwRhs];     // solved blocks x_k, [row][rhs]
+    float xi[kSwBS][kSwRhs];           // this block's right-hand side
+};
+
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, bool valid)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;"
+                 :: "r"(dst), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" :: "n"(N) : "memory"); }
+
+template <bool FORWARD, bool UNIT, bool TRANS>
+__global__ void __launch_bounds__(256)
+sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, const float* __restrict__ Dinv,
+               float* X, int64_t ldx, int* ticket, unsigned long long* mb, int* status, int vec)
+{
+    using MB = Mailbox<float>;
+    extern __shared__ __align__(16) unsigned char sw_smem_raw[];
+    Sweep16Smem& sm = *reinterpret_cast<Sweep16Smem*>(sw_smem_raw);
+    __shared__ int s_p;
+    constexpr int XPER = kSwBS * kSwRhs / 256;
+    const int t = threadIdx.x;
+    const int nblk = int(ceildiv(n, kSwBS));
+    const int64_t npad = int64_t(nblk) * kSwBS;
+    const int r = t % kSwBS, g = t / kSwBS, qb = 4 * g;    // row / right-hand sides outside the products
+    const int kq = t >> 6, tr = t & 15, tc = (t >> 4) & 3;  // product tile: column quarter, rows, rhs
+    const float* Wall = Dinv + size_t(nblk) * kSwBS * kSwBS;
+
+    auto mbox = [&](int64_t row, int q) { return mb + (q * npad + row) * MB::kWords; };
+    auto spin = [&](const unsigned long long* a, float& v) -> bool {
+        if (MB::get(a, v)) return true;
+        const uint64_t t0 = sw_globaltimer();
+        for (unsigned it = 1; !MB::get(a, v); ++it) {
+            if ((it & 255u) == 0 &&
+                (ld_volatile_i32(status) != 0 || sw_globaltimer() - t0 > 2000000000ull)) {
+                atomicCAS(status, 0, SLT_ERR_TIMEOUT);
+                return false;
+            }
+        }
+        return true;
+    };
+
+    for (;;) {
+        if (t == 0) s_p = atomicAdd(ticket, 1);
+        __syncthreads();
+        const int p = s_p;
+        if (p >= nblk) break;
+        const int bi = FORWARD ? p : nblk - 1 - p;
+        const int64_t i0 = int64_t(bi) * kSwBS;
+        const int ni = int(min64(kSwBS, n - i0));
+
+        {
+            const float* dinv = Dinv + size_t(bi) * kSwBS * kSwBS;
+            staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) { return dinv[e]; },
+                                                  [&](int e, float v) { sm.Ds[e / kSwBS][e % kSwBS] = v; });
+            if (p > 0) {
+                const float* wsrc = Wall + size_t(bi) * kSwBS * kSwBS;
+                staged_copy<kSwBS * kSwBS / 256, 256>(kSwBS * kSwBS, [&](int e) { return wsrc[e]; },
+                                                      [&](int e, float v) { sm.Ws[e / kSwBS][e % kSwBS] = v; });
+            }
+        }
+        staged_copy<kSwBS * kSwRhs / 256, 256>(kSwBS * kSwRhs, [&](int e) {
+            const int rr = e % kSwBS, q = e / kSwBS;
+            return (rr < ni && q < nrhs) ? X[i0 + rr + q * ldx] : 0.f;
+        }, [&](int e, float v) { sm.xi[e % kSwBS][e / kSwBS] = v; });
+
+        // tile of the k-th solved block into ring stage st
+        auto issue_tile = [&](int k, int st) {
+            const int bj = FORWARD ? k : nblk - 1 - k;
+            const int64_t j0 = int64_t(bj) * kSwBS;
+            const int nj = int(min64(kSwBS, n - j0));
+            float* base = &sm.Ts[st][0][0];
+            if (vec && ni == kSwBS && nj == kSwBS) {
+                #pragma unroll
+                for (int u = 0; u < kSwBS * kSwBS / (4 * 256); ++u) {
+                    const int e = t + 256 * u;                 // 16-byte chunk: 4 consecutive rows (cols for TRANS)
+                    const int a = (e % (kSwBS / 4)) * 4, b = e / (kSwBS / 4);
+                    const float* src = TRANS ? &M[(j0 + a) + (i0 + b) * ldm] : &M[(i0 + a) + (j0 + b) * ldm];
+                    cp_async16(static_cast<uint32_t>(__cvta_generic_to_shared(base + b * kSwLd + a)), src);
+                }
+            }
+            else {
+                #pragma unroll 4
+                for (int u = 0; u < kSwBS * kSwBS / 256; ++u) {
+                    const int e = t + 256 * u;
+                    const int a = e % kSwBS, b = e / kSwBS;    // a: contiguous index in memory
+                    const bool ok = TRANS ? (a < nj && b < ni) : (a < ni && b < nj);
+                    const float* src = ok ? (TRANS ? &M[(j0 + a) + (i0 + b) * ldm] : &M[(i0 + a) + (j0 + b) * ldm]) : M;
+                    cp_async4(static_cast<uint32_t>(__cvta_generic_to_shared(base + b * kSwLd + a)), src, ok);
+                }
+            }
+        };
+        float xv[XPER];
+        bool xok[XPER];
+        auto try_x = [&](int k) {
+            const int64_t j0 = int64_t(FORWARD ? k : nblk - 1 - k) * kSwBS;
+            const int nj = int(min64(kSwBS, n - j0));
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u, rr = e % kSwBS, q = e / kSwBS;
+                if (rr < nj && q < nrhs) xok[u] = MB::get(mbox(j0 + rr, q), xv[u]);
+                else { xv[u] = 0.f; xok[u] = true; }
+            }
+        };
+        auto finish_x = [&](int k) -> bool {
+            const int64_t j0 = int64_t(FORWARD ? k : nblk - 1 - k) * kSwBS;
+            bool ok = true;
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u, rr = e % kSwBS, q = e / kSwBS;
+                if (!xok[u] && ok) ok = spin(mbox(j0 + rr, q), xv[u]);
+            }
+            return ok;
+        };
+        auto put_x = [&](int st) {
+            #pragma unroll
+            for (int u = 0; u < XPER; ++u) {
+                const int e = t + 256 * u;
+                sm.xs[st][e % kSwBS][e / kSwBS] = xv[u];
+            }
+        };
+
+        // acc = sum over the blocks solved two or more steps earlier
+        float acc[4][4];
+        #pragma unroll
+        for (int i = 0; i < 4; ++i)
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+        const int K = p > 0 ? p - 1 : 0;
+        if (K > 0) {
+            #pragma unroll
+            for (int st = 0; st < kS16 - 1; ++st) {
+                if (st < K) issue_tile(st, st);
+                cp_async_commit();
+            }
+            try_x(0);
+            const bool ok = finish_x(0);
+            put_x(0);
+            if (__syncthreads_or(!ok)) { cp_async_wait<0>(); return; }
+        }
+        for (int k = 0; k < K; ++k) {
+            const int st = k % kS16;
+            if (k + kS16 - 1 < K) issue_tile(k + kS16 - 1, (k + kS16 - 1) % kS16);
+            cp_async_commit();
+            const bool more = k + 1 < K;
+            if (more) try_x(k + 1);
+            cp_async_wait<kS16 - 1>();          // this thread's copies of tile k
+            __syncthreads();                    // everyone's
+            const float* Tt = &sm.Ts[st][0][0];
+            if (!TRANS) {
+                #pragma unroll 4
+                for (int c = 16 * kq; c < 16 * kq + 16; ++c) {
+                    const float4 a = *reinterpret_cast<const float4*>(Tt + c * kSwLd + 4 * tr);
+                    const float4 x = *reinterpret_cast<const float4*>(&sm.xs[st][c][4 * tc]);
+                    const float av[4] = {a.x, a.y, a.z, a.w}, xw[4] = {x.x, x.y, x.z, x.w};
+                    #pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], xw[j], acc[i][j]);
+                }
+            }
+            else {
+                #pragma unroll
+                for (int c = 16 * kq; c < 16 * kq + 16; c += 4) {
+                    float av[4][4], xw[4][4];
+                    #pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float4 a = *reinterpret_cast<const float4*>(Tt + (tr + 16 * i) * kSwLd + c);
+                        av[i][0] = a.x; av[i][1] = a.y; av[i][2] = a.z; av[i][3] = a.w;
+                    }
+                    #pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float4 x = *reinterpret_cast<const float4*>(&sm.xs[st][c + u][4 * tc]);
+                        xw[u][0] = x.x; xw[u][1] = x.y; xw[u][2] = x.z; xw[u][3] = x.w;
+                    }
+                    #pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            #pragma unroll
+                            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i][u], xw[u][j], acc[i][j]);
+                }
+            }
+            bool ok = true;
+            if (more) {
+                ok = finish_x(k + 1);
+                put_x((k + 1) % kS16);
+            }
+            if (__syncthreads_or(!ok)) { cp_async_wait<0>(); return; }
+        }
+        cp_async_wait<0>();
+        if (p > 0) try_x(p - 1);       // in flight while y_i is formed
+
+        // the four column quarters' partial sums, then z = b_i - acc (in xi)
+        float (*red)[kSwBS][kSwRhs] = reinterpret_cast<float (*)[kSwBS][kSwRhs]>(&sm.Ts[0][0][0]);
+        #pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int row = TRANS ? tr + 16 * i : 4 * tr + i;
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) red[kq][row][4 * tc + j] = acc[i][j];
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int u = 0; u < 4; ++u)
+            sm.xi[r][qb + u] -= (red[0][r][qb + u] + red[1][r][qb + u]) + (red[2][r][qb + u] + red[3][r][qb + u]);
+        __syncthreads();
+
+        // y_i = inv(op(M)_ii) z
+        float y[4] = {0.f, 0.f, 0.f, 0.f};
+        #pragma unroll 4
+        for (int c = 0; c < kSwBS; ++c) axpy4(sm.Ds[r][c], &sm.xi[c][qb], y);
+
+        // chain step: x_i = y_i - W_i x_{i-1}
+        if (p > 0) {
+            const bool ok = finish_x(p - 1);
+            put_x(0);
+            if (__syncthreads_or(!ok)) return;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            #pragma unroll 4
+            for (int c = 0; c < kSwBS; ++c) axpy4(sm.Ws[r][c], &sm.xs[0][c][qb], v);
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) y[u] -= v[u];
+        }
+        if (r < ni) {
+            #pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (qb + u < nrhs) {
+                    MB::put(mbox(i0 + r, qb + u), y[u]);
+                    X[i0 + r + (qb + u) * ldx] = y[u];
+                }
+        }
+        __syncthreads();
+    }
+}
+
 template <typename T, bool FORWARD, bool UNIT, bool TRANS>
 static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, int64_t ldx, int* flags,
                         int* status, cudaStream_t s)
@@ -415,6 +679,25 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     SLT_CUDA_TRY(cudaGetLastError());
     // ticket and the first nrhs columns of the mailbox
     SLT_CUDA_TRY(cudaMemsetAsync(flags, 0, 256 + size_t(nrhs) * size_t(npad) * Mailbox<T>::kWords * 8, s));
+    if (std::is_same<T, float>::value && nrhs > 4) {
+        // 5 to 16 right-hand sides in FP32: the cp.async / register-tile variant
+        auto fn16 = sweep16_kernel<FORWARD, UNIT, TRANS>;
+        const size_t smem16 = sizeof(Sweep16Smem);
+        SLT_SMEM_ONCE(fn16, smem16);
+        int dev = 0, sms = 0, per = 0;
+        SLT_CUDA_TRY(cudaGetDevice(&dev));
+        SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn16, 256, smem16));
+        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(nblk, int64_t(sms) * std::max(per, 1)));
+        const int vec = (reinterpret_cast<uintptr_t>(M) % 16 == 0) && ((ldm * int64_t(sizeof(T))) % 16 == 0);
+        const int pidx = prof_begin(SLT_PROF_SWEEP, s);
+        fn16<<<unsigned(grid), 256, smem16, s>>>(n, int(nrhs), reinterpret_cast<const float*>(M), ldm,
+                                                 reinterpret_cast<const float*>(Dinv), reinterpret_cast<float*>(X),
+                                                 ldx, flags, mb, status, vec);
+        count_launch();
+        prof_end(pidx, s, double(n) * double(n) * double(nrhs), sizeof(T) * (double(n) * double(n) / 2 + 2.0 * n * nrhs));
+        return slt_from_cuda(cudaGetLastError());
+    }
     auto fn = sweep_kernel<T, FORWARD, UNIT, TRANS>;
     const size_t smem = sizeof(SweepSmem<T>);
     SLT_SMEM_ONCE(fn, smem);

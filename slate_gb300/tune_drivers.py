@@ -7,14 +7,17 @@ factorisation of a seeded matrix for every candidate
 * SMs given to the panel while the previous step's trailing update runs
   beside it (0 = no overlap; the rest of the SMs go to the update);
 * for FP64, the update engine (1 DFMA, 2 DMMA);
+* for potrf without overlap, the panels per deferred trailing update
+  (1, 2, 4 or 8: the trailing matrix is read and written once per that many
+  panels);
 
 and keeps the fastest per bucket.  The library reads the table when it is
 built, so run ``__graft_entry__.build()`` after regenerating it.
 
     python -m slate_gb300.tune_drivers [--out PATH] [--reps 2] [--quick]
 
-The candidates are forced through SLT_LOOKAHEAD_PANEL_SMS (read by the
-library on every call) and Options.gemm_engine.
+The candidates are forced through SLT_LOOKAHEAD_PANEL_SMS and
+SLT_UPDATE_DEPTH (read by the library on every call) and Options.gemm_engine.
 """
 import argparse
 import os
@@ -24,6 +27,7 @@ import time
 HEADER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "driver_table.h")
 
 PANEL_SMS = [0, 10, 19, 38, 57]
+DEPTHS = [2, 4, 8]
 SIZES = {
     (0, 0): [2048, 4096, 8192, 16384],
     (0, 1): [4096, 8192, 16384, 32768],
@@ -67,24 +71,28 @@ def tune(reps=2, quick=False, log=print):
             prec = {0: "fp64", 1: "fp32", 2: "fp16"}[cls]
             engines = [1, 2] if cls == 0 else [1]
             results = {}
-            for e in engines:
-                for p in PANEL_SMS:
-                    os.environ["SLT_LOOKAHEAD_PANEL_SMS"] = str(p)
-                    o = slt.Options(nb=512, ib=32, factor_precision=prec, gemm_engine=e)
+            cands = [(p, e, 1) for e in engines for p in PANEL_SMS]
+            if kind == 1:
+                cands += [(0, e, d) for e in engines for d in DEPTHS]
+            for p, e, d in cands:
+                os.environ["SLT_LOOKAHEAD_PANEL_SMS"] = str(p)
+                os.environ["SLT_UPDATE_DEPTH"] = str(d)
+                o = slt.Options(nb=512, ib=32, factor_precision=prec, gemm_engine=e)
 
-                    def run():
-                        A.copy_(A0)
-                        info = slt.getrf(A, o)[0] if kind == 0 else slt.potrf(A, o)
-                        assert info == 0, info
+                def run():
+                    A.copy_(A0)
+                    info = slt.getrf(A, o)[0] if kind == 0 else slt.potrf(A, o)
+                    assert info == 0, info
 
-                    run()
-                    results[(p, e)] = _time(torch, run, reps)
+                run()
+                results[(p, e, d)] = _time(torch, run, reps)
             os.environ.pop("SLT_LOOKAHEAD_PANEL_SMS", None)
+            os.environ.pop("SLT_UPDATE_DEPTH", None)
             best = min(results, key=results.get)
-            rows.append((kind, cls, n, best[0], best[1], results))
-            log("%s %s n=%d: best panel_sms=%d engine=%d (%s)" % (
-                "getrf" if kind == 0 else "potrf", CLASS_NAME[cls], n, best[0], best[1],
-                ", ".join("%d/%d %.1f ms" % (p, e, t * 1e3) for (p, e), t in sorted(results.items()))))
+            rows.append((kind, cls, n, best[0], best[1], best[2], results))
+            log("%s %s n=%d: best panel_sms=%d engine=%d depth=%d (%s)" % (
+                "getrf" if kind == 0 else "potrf", CLASS_NAME[cls], n, best[0], best[1], best[2],
+                ", ".join("%d/%d/%d %.1f ms" % (p, e, d, t * 1e3) for (p, e, d), t in sorted(results.items()))))
             del A, A0
             torch.cuda.empty_cache()
     return rows
@@ -97,14 +105,15 @@ def write(rows, path=HEADER):
              "// 1 potrf) and update class (0 FP64, 1 FP32 SIMT, 2 tensor cores: TF32 /",
              "// BF16 / FP16 / FP8 / 3xTF32): the SMs given to the panel while the rest of",
              "// the previous step's trailing update runs beside it (0: no overlap) and the",
-             "// FP64 update engine (1 DFMA with 64 x 64 tiles, 2 DMMA m16n8k4).  The tile",
-             "// size nb stays the caller's (Option::BlockSize): the pivot format of getrf",
-             "// and getrs depends on it.  Timings: panel SMs / engine, one factorisation, nb 512.",
+             "// FP64 update engine (1 DFMA with 64 x 64 tiles, 2 DMMA m16n8k4) and, for potrf",
+             "// without overlap, the panels per deferred trailing update.  The tile size nb",
+             "// stays the caller's (Option::BlockSize): the pivot format of getrf and getrs",
+             "// depends on it.  Timings: panel SMs / engine / depth, one factorisation, nb 512.",
              "#pragma once",
              "",
              "#include <cstdint>",
              "",
-             "struct DriverTune { int kind; int cls; int64_t max_n; int panel_sms; int engine; };",
+             "struct DriverTune { int kind; int cls; int64_t max_n; int panel_sms; int engine; int depth; };",
              "",
              "static const DriverTune kDriverTable[] = {"]
     by = {}
@@ -112,11 +121,11 @@ def write(rows, path=HEADER):
         by.setdefault((r[0], r[1]), []).append(r)
     for key in sorted(by):
         group = sorted(by[key], key=lambda r: r[2])
-        for i, (kind, cls, n, p, e, res) in enumerate(group):
+        for i, (kind, cls, n, p, e, d, res) in enumerate(group):
             mx = "int64_t(1) << 62" if i == len(group) - 1 else "%d" % n
-            times = ", ".join("%d/%d %.1f" % (pp, ee, t * 1e3) for (pp, ee), t in sorted(res.items()))
-            lines.append("    {%d, %d, %s, %d, %d},   // %s %s n=%d: %s ms" % (
-                kind, cls, mx, p, e, "getrf" if kind == 0 else "potrf", CLASS_NAME[cls], n, times))
+            times = ", ".join("%d/%d/%d %.1f" % (pp, ee, dd, t * 1e3) for (pp, ee, dd), t in sorted(res.items()))
+            lines.append("    {%d, %d, %s, %d, %d, %d},   // %s %s n=%d: %s ms" % (
+                kind, cls, mx, p, e, d, "getrf" if kind == 0 else "potrf", CLASS_NAME[cls], n, times))
     lines.append("};")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")

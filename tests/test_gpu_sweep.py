@@ -69,7 +69,9 @@ def _reference(kind, M, B):
     return solve_triangular(M, B, lower=(uplo == "L"), trans=trans, unit_diagonal=unit)
 
 
-CASES = [(1, 1), (64, 4), (65, 3), (200, 1), (1000, 5), (4100, 4), (777, 16)]
+# (> 4 right-hand sides in FP32 take the cp.async / register-tile kernel:
+#  16-byte copies when the leading dimension allows, 4-byte copies otherwise)
+CASES = [(1, 1), (64, 4), (65, 3), (200, 1), (1000, 5), (4100, 4), (777, 16), (4100, 16), (999, 16), (130, 8)]
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])

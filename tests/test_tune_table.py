@@ -47,26 +47,29 @@ from slate_gb300 import tune_drivers as td
 
 
 def _parse_drivers(text):
-    rows = re.findall(r"\{(\d), (\d), (int64_t\(1\) << 62|\d+), (\d+), (\d)\}", text)
-    return [(int(k), int(c), (1 << 62) if "<<" in m else int(m), int(p), int(e)) for k, c, m, p, e in rows]
+    rows = re.findall(r"\{(\d), (\d), (int64_t\(1\) << 62|\d+), (\d+), (\d)(?:, (\d))?\}", text)
+    return [(int(k), int(c), (1 << 62) if "<<" in m else int(m), int(p), int(e), int(d) if d else 1)
+            for k, c, m, p, e, d in rows]
 
 
 def test_driver_header_roundtrip(tmp_path):
-    rows = [(0, 0, 2048, 19, 1, {(0, 1): 0.1, (19, 1): 0.08}), (0, 0, 4096, 10, 2, {(10, 2): 0.2}),
-            (1, 2, 8192, 0, 1, {(0, 1): 0.3})]
+    rows = [(0, 0, 2048, 19, 1, 1, {(0, 1, 1): 0.1, (19, 1, 1): 0.08}), (0, 0, 4096, 10, 2, 1, {(10, 2, 1): 0.2}),
+            (1, 2, 8192, 0, 1, 4, {(0, 1, 1): 0.3, (0, 1, 4): 0.2})]
     p = tmp_path / "d.h"
     td.write(rows, str(p))
-    assert _parse_drivers(p.read_text()) == [(0, 0, 2048, 19, 1), (0, 0, 1 << 62, 10, 2), (1, 2, 1 << 62, 0, 1)]
+    assert _parse_drivers(p.read_text()) == [(0, 0, 2048, 19, 1, 1), (0, 0, 1 << 62, 10, 2, 1),
+                                             (1, 2, 1 << 62, 0, 1, 4)]
 
 
 def test_committed_driver_table_is_valid():
     with open(td.HEADER) as f:
         rows = _parse_drivers(f.read())
-    keys = {(k, c) for k, c, _, _, _ in rows}
+    keys = {(k, c) for k, c, _, _, _, _ in rows}
     assert keys == {(k, c) for k in (0, 1) for c in (0, 1, 2)}
     for key in keys:
         group = [r for r in rows if (r[0], r[1]) == key]
         assert [r[2] for r in group] == sorted(r[2] for r in group)
         assert group[-1][2] == 1 << 62                  # the last bucket takes every larger n
-    for _, _, _, p, e in rows:
-        assert 0 <= p < 152 and e in (1, 2)
+    for k, _, _, p, e, d in rows:
+        assert 0 <= p < 152 and e in (1, 2) and d in (1, 2, 4, 8)
+        assert d == 1 or (k == 1 and p == 0)          # deferred updates: potrf without overlap
