@@ -128,6 +128,65 @@ cudaStream_t lapack_stream()
     return ls.s;
 }
 
+// Second stream of the LAPACK entry points: host-to-device copies of A that
+// the solve consumes while they are still arriving.
+cudaStream_t lapack_copy_stream()
+{
+    static thread_local LapackStream ls;
+    return ls.s;
+}
+
+// The lower triangle of the host array a (n x n, leading dimension lda) into
+// the device array d (leading dimension n) on the copy stream cs, in the
+// order the left-looking factor reads it: all 512 x 512 diagonal blocks
+// first (the equilibration scales need the diagonal), then the columns
+// below them block by block, one event per block.  cs first waits for
+// `ready` (d allocated on the compute stream).
+struct StreamedLower {
+    static constexpr int64_t kB = 512;
+    std::vector<cudaEvent_t> ev;
+    cudaEvent_t ev_diag = nullptr, ev_ready = nullptr;
+    InputArrival arr;
+    cudaStream_t s_ = nullptr;
+    ~StreamedLower() {
+        // whatever happened, the compute stream (which frees d) waits for the copies
+        if (s_) join(s_);
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+        if (ev_diag) cudaEventDestroy(ev_diag);
+        if (ev_ready) cudaEventDestroy(ev_ready);
+    }
+    int start(int64_t n, const double* a, int64_t lda, double* d, cudaStream_t s, cudaStream_t cs) {
+        const int64_t nblk = (n + kB - 1) / kB;
+        SLT_CUDA_TRY(cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming));
+        SLT_CUDA_TRY(cudaEventCreateWithFlags(&ev_diag, cudaEventDisableTiming));
+        ev.assign(size_t(nblk), nullptr);
+        for (auto& e : ev) SLT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        SLT_CUDA_TRY(cudaEventRecord(ev_ready, s));
+        SLT_CUDA_TRY(cudaStreamWaitEvent(cs, ev_ready, 0));
+        arr.ev = ev.data();
+        arr.nev = nblk;
+        arr.blk = kB;
+        s_ = s;
+        for (int64_t j0 = 0; j0 < n; j0 += kB) {
+            const int64_t w = std::min(kB, n - j0);
+            SLT_CUDA_TRY(cudaMemcpy2DAsync(d + j0 + j0 * n, size_t(n) * 8, a + j0 + j0 * lda, size_t(lda) * 8,
+                                           size_t(w) * 8, size_t(w), cudaMemcpyHostToDevice, cs));
+        }
+        SLT_CUDA_TRY(cudaEventRecord(ev_diag, cs));
+        for (int64_t j0 = 0, b = 0; j0 < n; j0 += kB, ++b) {
+            const int64_t w = std::min(kB, n - j0), r0 = j0 + w;
+            if (r0 < n)
+                SLT_CUDA_TRY(cudaMemcpy2DAsync(d + r0 + j0 * n, size_t(n) * 8, a + r0 + j0 * lda, size_t(lda) * 8,
+                                               size_t(n - r0) * 8, size_t(w), cudaMemcpyHostToDevice, cs));
+            SLT_CUDA_TRY(cudaEventRecord(ev[size_t(b)], cs));
+        }
+        arr.ev_diag = ev_diag;
+        return SLT_OK;
+    }
+    // the compute stream waits for every copy (before d is freed or reused)
+    int join(cudaStream_t s) const { return arr.wait_all(s); }
+};
+
 template <typename T>
 int getrf_device_impl(int64_t m, int64_t n, T* dA, int64_t lda, int* d_ipiv, const slt_options* opts,
                       slt_stream_t stream, int64_t* info)
@@ -721,12 +780,17 @@ static void lapack_dsposv_impl(char uplo, int n, int nrhs, double* a, int lda, d
     cudaStream_t s = lapack_stream();
     slt_options o = lapack_opts();
     DevBuf dA, dB, dX, tmp;
-    // phase timers of the host entry point (slt_timer("dsposv::h2d") etc.)
+    // phase timers of the host entry point (slt_timer("dsposv::h2d") etc.):
+    // with streaming, h2d covers the work issued before the solve and the
+    // copies of A overlap the solve's factorisation
     TimerSet tm(s);
     tm.start("dsposv::h2d");
+    StreamedLower sl;
+    const bool stream_a = !up && env_int("SLATE_LAPACK_STREAM", 1) != 0;
     // only the referenced triangle crosses the link
     if (dA.alloc(sizeof(double) * size_t(n) * size_t(n), s) ||
-        tri_copy<double>(!up, n, a, lda, dA.as<double>(), n, cudaMemcpyHostToDevice, s) ||
+        (stream_a ? sl.start(n, a, lda, dA.as<double>(), s, lapack_copy_stream())
+                  : tri_copy<double>(!up, n, a, lda, dA.as<double>(), n, cudaMemcpyHostToDevice, s)) ||
         to_device(b, n, nrhs, ldb, dB, s) ||
         dX.alloc(sizeof(double) * size_t(n) * size_t(std::max(nrhs, 1)), s)) { *info = -100; return; }
     if (lower_view(uplo, n, dA, tmp, s)) { *info = -100; return; }
@@ -734,8 +798,13 @@ static void lapack_dsposv_impl(char uplo, int n, int nrhs, double* a, int lda, d
     int64_t inf = 0;
     int it = 0;
     tm.start("dsposv::solve");
-    int rc = slt_dsposv_device(n, nrhs, dA.as<double>(), n, dB.as<double>(), n, dX.as<double>(), n, &o, s,
+    int rc;
+    {
+        InputArrivalScope scope(stream_a ? &sl.arr : nullptr);
+        rc = slt_dsposv_device(n, nrhs, dA.as<double>(), n, dB.as<double>(), n, dX.as<double>(), n, &o, s,
                                &it, &inf);
+    }
+    if (stream_a && !rc) rc = sl.join(s);
     if (rc) { *info = -1000 + rc; return; }
     tm.stop("dsposv::solve");
     tm.start("dsposv::d2h");

@@ -17,6 +17,7 @@
 #include <mutex>
 #include <string>
 #include <utility>
+#include <functional>
 #include <vector>
 
 namespace slt {
@@ -41,6 +42,11 @@ TimerSet::~TimerSet()
     cudaGetLastError();
     for (auto& kv : acc) t_timers[kv.first] = kv.second;
 }
+
+static thread_local const InputArrival* t_arrival = nullptr;
+const InputArrival* input_arrival() { return t_arrival; }
+InputArrivalScope::InputArrivalScope(const InputArrival* a) { t_arrival = a; }
+InputArrivalScope::~InputArrivalScope() { t_arrival = nullptr; }
 
 double timer_value(const char* name)
 {
@@ -521,6 +527,72 @@ int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc,
     return la.join();
 }
 
+// Left-looking Cholesky by blocks of S columns for the 16-bit tensor-core
+// tiers (FP16, BF16), S a multiple of 64: before block [s0, s1) is factored,
+// its columns (rows s0 .. n) take the whole contribution of columns 0 .. s0
+// in one tensor-core update with k = s0, read from a row-major 16-bit copy of
+// the factor (L16) that every finished block adds its columns to; inside the
+// block, each nb-column panel is brought up to date with the block's earlier
+// panels and factored by the panel kernel.  Same factor as the right-looking
+// order (the same operand roundings, FP32 sums grouped differently), but the
+// trailing matrix is read and written once in all, the operands are packed
+// once instead of at every update, and block s needs only columns s0 .. s1
+// of A -- which lets the caller stream A in while earlier blocks are being
+// factored (prologue(s0, s1) runs first on each block).
+static int potrf_ll_tc(int64_t n, float* A, int64_t lda, const slt_options& o, int64_t S, FactorCtx& fc,
+                       cudaStream_t s, const std::function<int(int64_t, int64_t)>& prologue)
+{
+    const int64_t nb = eff_nb(o);
+    const int tier = o.factor_precision;
+    DevBuf bar, L16;
+    TRY(bar.alloc(slt_chol_panel_ws_bytes(), s));
+    const int64_t kld = (n + 63) / 64 * 64;
+    TRY(L16.alloc(size_t(n) * size_t(kld) * 2, s));
+    slt_options ot = o;
+    if (ot.gemm_engine == 0) ot.gemm_engine = 1;
+    char* L16b = L16.as<char>();
+    for (int64_t s0 = 0; s0 < n; s0 += S) {
+        const int64_t s1 = std::min(n, s0 + S);
+        if (prologue) TRY(prologue(s0, s1));
+        if (s0 > 0) {
+            const char* Lr = L16b + size_t(s0) * size_t(kld) * 2;      // rows s0 .. n
+            TRY(slt_tc_gemm_packed(tier, n - s0, s1 - s0, s0, Lr, kld, Lr, kld, A + s0 + s0 * lda, lda, 1, s));
+        }
+        for (int64_t c = s0; c < s1; c += nb) {
+            const int64_t kb = std::min(nb, s1 - c);
+            if (c > s0)
+                TRY(k_gemm('T', n - c, kb, c - s0, -1.f, A + c + s0 * lda, lda, A + c + s0 * lda, lda, 1.f,
+                           A + c + c * lda, lda, 1, ot, s));
+            TRY(k_chol_panel(n - c, kb, A + c + c * lda, lda, fc.d_info, c, bar.p, fc.d_status, s));
+        }
+        // later blocks read rows s1 .. n of these columns
+        if (s1 < n) TRY(slt_pack_rows16(tier, n, s1, s0, s1, A, lda, L16b, kld, s));
+    }
+    return SLT_OK;
+}
+
+// The left-looking form applies to FP16 / BF16 factors when the size
+// bucket defers its updates (depth > 1) and nb is a multiple of 64;
+// SLT_POTRF_LL=0 turns it off, =1 forces it.  Returns the block width S, or
+// 0 for the right-looking driver.
+static int64_t potrf_ll_width(int64_t n, const slt_options& o)
+{
+    const int p = o.factor_precision;
+    if (p != SLT_PREC_FP16 && p != SLT_PREC_BF16) return 0;
+    const int64_t nb = eff_nb(o);
+    if (nb % 64 != 0) return 0;
+    const DriverTune& t = driver_tune(1, 2, n);
+    int64_t depth = update_depth(t);
+    if (const char* e = std::getenv("SLT_POTRF_LL")) {
+        if (std::atoi(e) == 0) return 0;
+        depth = std::max<int64_t>(depth, 2);
+    }
+    else if (depth <= 1 || t.panel_sms > 0) {
+        return 0;
+    }
+    return depth * nb;
+}
+
 // potrs lower: forward with L, backward with L^T (src/potrs.cc:55-78).
 template <typename T>
 int potrs_dev(int64_t n, int64_t nrhs, const T* L, int64_t lda, int64_t nb, T* B, int64_t ldb,
@@ -587,6 +659,10 @@ struct LoFactor {
     int factor(const double* Ahi, int64_t lda, FactorCtx& fc, int64_t* info, cudaStream_t s) {
         ld = ((n + 31) / 32) * 32;
         TRY(A.alloc(sizeof(float) * size_t(ld) * size_t(n), s));
+        const InputArrival* arr = input_arrival();
+        if (arr) TRY(arr->wait_diag(s));
+        // only the Cholesky factor below streams its columns in
+        if (arr && !(chol && potrf_ll_width(n, o) > 0)) TRY(arr->wait_all(s));
         if (equilibrate_on(o)) {
             TRY(scales.alloc(sizeof(double) * 3 * size_t(n), s));
             double* rr = scales.as<double>();
@@ -614,15 +690,30 @@ struct LoFactor {
         const bool shift = low_tier(o.factor_precision);
         const double u = o.factor_precision == SLT_PREC_BF16 ? 0x1p-8
                        : o.factor_precision == SLT_PREC_FP8  ? 0x1p-4 : 0x1p-11;
+        const int64_t S = potrf_ll_width(n, o);
         for (int attempt = 0;; ++attempt) {
-            // the factor reads and writes the lower triangle only
-            TRY(slt_convert_d2s_scaled_lower(n, Ahi, lda, r, A.as<float>(), ld, s));
-            if (attempt > 0) {
-                sigma = u * double(int64_t(1) << (3 * (attempt - 1)));
-                TRY(slt_sshift_diag(n, float(sigma), A.as<float>(), ld, s));
-                SLT_CUDA_TRY(cudaMemsetAsync(fc.d_info, 0, sizeof(int), s));
+            if (attempt == 0 && S > 0) {
+                // left-looking: each block of columns is cast (lower part) just
+                // before it is needed, after its columns have arrived
+                const double* dr = r;
+                float* Af = A.as<float>();
+                const int64_t ldf = ld;
+                TRY(potrf_ll_tc(n, Af, ld, o, S, fc, s, [&](int64_t s0, int64_t s1) -> int {
+                    if (arr) TRY(arr->wait_cols(s1, s));
+                    return slt_convert_d2s_scaled_lower_cols(n, s0, s1, Ahi, lda, dr, Af, ldf, s);
+                }));
             }
-            TRY(potrf_dev<float>(n, A.as<float>(), ld, o, fc, s));
+            else {
+                // the factor reads and writes the lower triangle only
+                TRY(slt_convert_d2s_scaled_lower(n, Ahi, lda, r, A.as<float>(), ld, s));
+                if (attempt > 0) {
+                    sigma = u * double(int64_t(1) << (3 * (attempt - 1)));
+                    TRY(slt_sshift_diag(n, float(sigma), A.as<float>(), ld, s));
+                    SLT_CUDA_TRY(cudaMemsetAsync(fc.d_info, 0, sizeof(int), s));
+                }
+                if (S > 0) TRY(potrf_ll_tc(n, A.as<float>(), ld, o, S, fc, s, nullptr));
+                else TRY(potrf_dev<float>(n, A.as<float>(), ld, o, fc, s));
+            }
             TRY(finish_factor(fc, info, s));
             if (*info == 0 || !shift || attempt == 3) return SLT_OK;
         }
@@ -1001,17 +1092,20 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
     SLT_CUDA_TRY(cudaMemsetAsync(st.p, 0, 2 * sizeof(int), s));
     FactorCtx fc{st.as<int>(), st.as<int>() + 1};
 
-    double Anorm = 0;
-    TRY(slt_dnorm_inf(n, n, A, lda, chol, scal.as<double>(), nws.p, s));
-    TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
-    const double cte = Anorm * tol;
-
     LoFactor lo{chol, n, nb, o, {}, ipiv};
     if (lo.o.factor_precision == SLT_PREC_FP64) lo.o.factor_precision = SLT_PREC_FP32;
     int64_t linfo = 0;
     tm.start(std::string(pfx) + (chol ? "::potrf_lo" : "::getrf_lo"));
     TRY(lo.factor(A, lda, fc, &linfo, s));
     tm.stop(std::string(pfx) + (chol ? "::potrf_lo" : "::getrf_lo"));
+
+    // ||A||_inf for the stopping test, after the factor (A may still have been
+    // arriving from the host while it ran; the factor waited for all of it)
+    double Anorm = 0;
+    if (const InputArrival* arr = input_arrival()) TRY(arr->wait_all(s));
+    TRY(slt_dnorm_inf(n, n, A, lda, chol, scal.as<double>(), nws.p, s));
+    TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
+    const double cte = Anorm * tol;
     bool conv = false;
     std::vector<double> h(2 * nrhs);
     double* dcx = col.as<double>();
@@ -1245,17 +1339,20 @@ static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, i
     SLT_CUDA_TRY(cudaMemsetAsync(st.p, 0, 2 * sizeof(int), s));
     FactorCtx fc{st.as<int>(), st.as<int>() + 1};
 
-    double Anorm = 0;
-    TRY(slt_dnorm_inf(n, n, A, lda, chol, scal.as<double>(), nws.p, s));
-    TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
-    const double cte = Anorm * tol;
-
     LoFactor lo{chol, n, nb, o, {}, ipiv};
     if (lo.o.factor_precision == SLT_PREC_FP64) lo.o.factor_precision = SLT_PREC_FP32;
     int64_t linfo = 0;
     tm.start(std::string(pfx) + (chol ? "::potrf_lo" : "::getrf_lo"));
     TRY(lo.factor(A, lda, fc, &linfo, s));
     tm.stop(std::string(pfx) + (chol ? "::potrf_lo" : "::getrf_lo"));
+
+    // ||A||_inf for the stopping test, after the factor (A may still have been
+    // arriving from the host while it ran; the factor waited for all of it)
+    double Anorm = 0;
+    if (const InputArrival* arr = input_arrival()) TRY(arr->wait_all(s));
+    TRY(slt_dnorm_inf(n, n, A, lda, chol, scal.as<double>(), nws.p, s));
+    TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
+    const double cte = Anorm * tol;
     *info = linfo;
     bool all_conv = true;
     int worst_iter = 0;

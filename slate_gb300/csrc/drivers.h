@@ -9,6 +9,7 @@
 #include "slate_gb300.h"
 #include "status.h"
 
+#include <algorithm>
 #include <map>
 #include <string>
 #include <vector>
@@ -120,6 +121,34 @@ struct TimerSet {
     ~TimerSet();
 };
 
+
+// Columns of A still arriving from the host while a driver runs (set by the
+// LAPACK entry points around one call, on the calling thread): the driver's
+// stream waits for ev[j / blk] before it reads columns of block j, and for
+// ev_diag before it reads the diagonal.  The events are recorded in column
+// order on one copy stream.
+struct InputArrival {
+    cudaEvent_t ev_diag = nullptr;
+    const cudaEvent_t* ev = nullptr;
+    int64_t nev = 0, blk = 1;
+    int wait_diag(cudaStream_t s) const {
+        return ev_diag ? slt_from_cuda(cudaStreamWaitEvent(s, ev_diag, 0)) : SLT_OK;
+    }
+    // columns [0, j1)
+    int wait_cols(int64_t j1, cudaStream_t s) const {
+        if (!ev || nev <= 0 || j1 <= 0) return SLT_OK;
+        const int64_t b = std::min<int64_t>(nev - 1, (j1 - 1) / blk);
+        return slt_from_cuda(cudaStreamWaitEvent(s, ev[b], 0));
+    }
+    int wait_all(cudaStream_t s) const { return ev && nev > 0 ? wait_cols(nev * blk, s) : SLT_OK; }
+};
+// The calling thread's arrivals (null: A is complete when the driver starts).
+const InputArrival* input_arrival();
+// Sets the calling thread's arrivals for its lifetime.
+struct InputArrivalScope {
+    explicit InputArrivalScope(const InputArrival* a);
+    ~InputArrivalScope();
+};
 
 struct FactorCtx {
     int* d_info = nullptr;      // first failing column (1-based), 0 = ok

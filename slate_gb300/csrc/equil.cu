@@ -196,6 +196,23 @@ extern "C" int slt_convert_d2s_scaled_lower(int64_t n, const double* A, int64_t 
     return slt_from_cuda(cudaGetLastError());
 }
 
+// Columns [j0, j1), rows [j0, n) of the same (the lower part of one block of
+// columns): the streaming form of the cast above.
+extern "C" int slt_convert_d2s_scaled_lower_cols(int64_t n, int64_t j0, int64_t j1, const double* A, int64_t lda,
+                                                 const double* d, float* B, int64_t ldb, cudaStream_t stream)
+{
+    if (j0 >= j1 || j0 >= n) return SLT_OK;
+    const int64_t m = n - j0, nc = j1 - j0;
+    dim3 g(unsigned(ceildiv(m, 1024)), unsigned(std::min<int64_t>(nc, 65535)));
+    const double* dd = d ? d + j0 : nullptr;
+    if (d) convert_scaled_kernel<double, float, true, true><<<g, 256, 0, stream>>>(m, nc, A + j0 + j0 * lda, lda, dd, dd,
+                                                                                B + j0 + j0 * ldb, ldb);
+    else convert_scaled_kernel<double, float, false, true><<<g, 256, 0, stream>>>(m, nc, A + j0 + j0 * lda, lda, dd, dd,
+                                                                                B + j0 + j0 * ldb, ldb);
+    count_launch();
+    return slt_from_cuda(cudaGetLastError());
+}
+
 // X (double) = diag(r) B; r may be null.
 extern "C" int slt_convert_s2d_scaled(int64_t m, int64_t n, const float* B, int64_t ldb, const double* r,
                                       double* X, int64_t ldx, cudaStream_t stream)

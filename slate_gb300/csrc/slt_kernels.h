@@ -193,6 +193,18 @@ int slt_dcgs2(int64_t n, double* V, int64_t R1, const slt_cgs_cols* cols, const 
  * strictly upper part of B untouched: the Cholesky factor's working copy. */
 int slt_convert_d2s_scaled_lower(int64_t n, const double* A, int64_t lda, const double* d, float* B,
                                  int64_t ldb, cudaStream_t stream);
+/* The same for columns [j0, j1) only (rows [j0, n)). */
+int slt_convert_d2s_scaled_lower_cols(int64_t n, int64_t j0, int64_t j1, const double* A, int64_t lda,
+                                      const double* d, float* B, int64_t ldb, cudaStream_t stream);
+/* Tensor-core update on operands already in 16-bit K-major form (tier FP16
+ * or BF16): C (fp32, m x n) -= A B^T, row i of A at A16 + i lda16 elements,
+ * kpad a multiple of 64; lower: only C(i, j), i >= j.  slt_pack_rows16 writes
+ * rows [r0, m) x columns [c0, c1) of a column-major FP32 lower factor into
+ * that form (zero above the diagonal). */
+int slt_tc_gemm_packed(int tier, int64_t m, int64_t n, int64_t kpad, const void* A16, int64_t lda16,
+                       const void* B16, int64_t ldb16, float* C, int64_t ldc, int lower, cudaStream_t stream);
+int slt_pack_rows16(int tier, int64_t m, int64_t r0, int64_t c0, int64_t c1, const float* src, int64_t lds,
+                    void* dst, int64_t ldd, cudaStream_t stream);
 /* Philox matrix generator identical to SLATE's slate::random::generate. */
 int slt_dgenerate(int dist, int64_t seed, int64_t m, int64_t n, int64_t ioff, int64_t joff,
                   double* A, int64_t lda, cudaStream_t stream);

@@ -189,6 +189,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
 // it to C with a TMA tensor reduce (cp.reduce.async.bulk.tensor .add), so the
 // read-modify-write of C is done by the memory system with full overlap.
 constexpr int kPThreads = 192;
+constexpr int64_t kTcGroup = 8;        // column blocks per tile group of the persistent kernel
 
 __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, uint32_t src, int x, int y)
 {
@@ -245,9 +246,21 @@ tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_cons
     tc_fence_after();
     const uint32_t taddr = *tmem_slot;
 
+    // Tile t -> (row block, column block) in groups of kTcGroup column
+    // blocks: consecutive tiles walk the group's columns first, then its
+    // rows, so the CTAs of one wave share a few A row blocks and a few B
+    // column blocks in L2 instead of streaming every A row block again for
+    // each column block.
+    auto tile_rc = [&](int64_t t, int64_t& rb, int64_t& cb) {
+        const int64_t per = kTcGroup * mt;
+        const int64_t g = t / per, w = (nt - g * kTcGroup < kTcGroup) ? nt - g * kTcGroup : kTcGroup, q = t - g * per;
+        cb = g * kTcGroup + q % w;
+        rb = q / w;
+    };
     auto skip = [&](int64_t t) {
-        const int64_t r0 = (t % mt) * BM, c0 = (t / mt) * BN;
-        return a.lower && r0 + BM - 1 < c0;
+        int64_t rb, cb;
+        tile_rc(t, rb, cb);
+        return a.lower && rb * BM + BM - 1 < cb * BN;
     };
 
     if (warp == 0) {
@@ -257,7 +270,9 @@ tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_cons
             bool ok = true;
             for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 if (skip(t)) continue;
-                const int row0 = int((t % mt) * BM), col0 = int((t / mt) * BN);
+                int64_t rb, cb;
+                tile_rc(t, rb, cb);
+                const int row0 = int(rb * BM), col0 = int(cb * BN);
                 for (int kt = 0; kt < KT; ++kt, ++it) {
                     const int s = int(it % S);
                     const uint32_t par = uint32_t((it / S) & 1) ^ 1u;
@@ -337,7 +352,9 @@ tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_cons
                 break;
             }
             tc_fence_after();
-            const int64_t row0 = (t % mt) * BM, col0 = (t / mt) * BN;
+            int64_t rbt, cbt;
+            tile_rc(t, rbt, cbt);
+            const int64_t row0 = rbt * BM, col0 = cbt * BN;
             const int64_t r = row0 + q * 32 + lane;
             const float f = tile_factor(a, row0, col0);
             #pragma unroll 1
@@ -538,6 +555,30 @@ pack3_kernel(int64_t rows, int64_t k, const float* __restrict__ src, int64_t ld,
             const int64_t r = r0 + q, c = c0 + tx;
             if (r < rpad && c < kseg) put(r, c, (r < rows && c < k) ? src[c + r * ld] : 0.f);
         }
+    }
+}
+
+// Rows [r0, m) x columns [c0, c1) of the column-major FP32 factor into the
+// row-major 16-bit copy: dst[r * ldd + c] = round(src[r + c * lds]) for
+// r >= c, zero above the diagonal.  32 x 32 tiles through shared memory
+// (coalesced reads along rows, writes along columns).
+// grid (ceil((c1 - c0) / 32), ceil((m - r0) / 32)), 256 threads.
+template <typename TO>
+__global__ void __launch_bounds__(256)
+pack_rows_kernel(int64_t m, int64_t r0, int64_t c0, int64_t c1, const float* __restrict__ src, int64_t lds,
+                 TO* __restrict__ dst, int64_t ldd)
+{
+    __shared__ float tl[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int64_t rb = r0 + int64_t(blockIdx.y) * 32, cb = c0 + int64_t(blockIdx.x) * 32;
+    for (int q = ty; q < 32; q += 8) {
+        const int64_t row = rb + tx, col = cb + q;
+        tl[q][tx] = (row < m && col < c1 && row >= col) ? src[row + col * lds] : 0.f;
+    }
+    __syncthreads();
+    for (int q = ty; q < 32; q += 8) {
+        const int64_t row = rb + q, col = cb + tx;
+        if (row < m && col < c1) dst[row * ldd + col] = TO(tl[tx][q]);
     }
 }
 
@@ -802,4 +843,69 @@ extern "C" int slt_tc_status(void)
     if (cudaMemcpy(&h, g_tc_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return SLT_ERR_CUDA_BASE;
     if (h) cudaMemset(g_tc_status, 0, sizeof(int));
     return h;
+}
+
+// Rows [r0, m) x columns [c0, c1) of the lower FP32 factor L (column-major,
+// leading dimension lds) into the row-major 16-bit copy L16 (row stride ldd
+// elements; tier FP16 or BF16), zero above the diagonal.
+extern "C" int slt_pack_rows16(int tier, int64_t m, int64_t r0, int64_t c0, int64_t c1, const float* src,
+                               int64_t lds, void* dst, int64_t ldd, cudaStream_t stream)
+{
+    if (r0 >= m || c0 >= c1) return SLT_OK;
+    dim3 grid(unsigned(ceildiv(c1 - c0, 32)), unsigned(ceildiv(m - r0, 32)));
+    if (tier == SLT_PREC_FP16)
+        pack_rows_kernel<__half><<<grid, 256, 0, stream>>>(m, r0, c0, c1, src, lds, static_cast<__half*>(dst), ldd);
+    else if (tier == SLT_PREC_BF16)
+        pack_rows_kernel<__nv_bfloat16><<<grid, 256, 0, stream>>>(m, r0, c0, c1, src, lds,
+                                                                 static_cast<__nv_bfloat16*>(dst), ldd);
+    else
+        return SLT_ERR_ARG;
+    count_launch();
+    return slt_from_cuda(cudaGetLastError());
+}
+
+// C (fp32, m x n) -= A B^T on the tensor cores, A (m x kpad) and B (n x kpad)
+// already in the tier's 16-bit type, K-major (row i of A at A16 + i lda16
+// elements); kpad a multiple of 64, 16-byte aligned rows; C 16-byte aligned
+// with ldc a multiple of 4.  lower: only C(i, j) with i >= j is updated.
+extern "C" int slt_tc_gemm_packed(int tier, int64_t m, int64_t n, int64_t kpad, const void* A16, int64_t lda16,
+                                  const void* B16, int64_t ldb16, float* C, int64_t ldc, int lower,
+                                  cudaStream_t stream)
+{
+    if (tier != SLT_PREC_FP16 && tier != SLT_PREC_BF16) return SLT_ERR_ARG;
+    if (m < 0 || n < 0 || kpad < 0) return SLT_ERR_ARG;
+    if (m == 0 || n == 0 || kpad == 0) return SLT_OK;
+    if (kpad % 64 || (lda16 * 2) % 16 || (ldb16 * 2) % 16 || reinterpret_cast<uintptr_t>(A16) % 16 ||
+        reinterpret_cast<uintptr_t>(B16) % 16 || reinterpret_cast<uintptr_t>(C) % 16 || ldc % 4)
+        return SLT_ERR_ARG;
+    int rc = get_encode();
+    if (rc) return rc;
+    if (!g_tc_status) {
+        SLT_CUDA_TRY(cudaMalloc(&g_tc_status, sizeof(int)));
+        SLT_CUDA_TRY(cudaMemset(g_tc_status, 0, sizeof(int)));
+    }
+    const CUtensorMapDataType dt = tier == SLT_PREC_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                                         : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    CUtensorMap mapA, mapB, mapC;
+    TRY(tma_map_2d(&mapA, const_cast<void*>(A16), dt, kpad, m, lda16 * 2, 64, kTcBM, CU_TENSOR_MAP_SWIZZLE_128B));
+    TRY(tma_map_2d(&mapB, const_cast<void*>(B16), dt, kpad, n, ldb16 * 2, 64, kTcBN, CU_TENSOR_MAP_SWIZZLE_128B));
+    TRY(make_map_c(&mapC, C, m, n, ldc));
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    TcArgs args{m, n, kpad, C, ldc, lower, g_tc_status, nullptr, nullptr};
+    const size_t psm = tcp_smem_bytes();
+    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<0>, psm);
+    if (rc) return rc;
+    const int64_t tiles = ceildiv(m, kTcBM) * ceildiv(n, kTcBN);
+    const unsigned grid = unsigned(std::min<int64_t>(tiles, capped_sms(g_sms)));
+    const int pidx = prof_begin(SLT_PROF_GEMM_TC, stream);
+    tc_update_persistent<0><<<grid, kPThreads, psm, stream>>>(mapA, mapB, mapC, args,
+                                                              make_idesc(tier == SLT_PREC_BF16 ? 1u : 0u, kTcBM, kTcBN));
+    count_launch();
+    const double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);
+    prof_end(pidx, stream, 2.0 * mn * double(kpad), 8.0 * mn + 2.0 * double(kpad) * double(m + n));
+    return slt_from_cuda(cudaGetLastError());
 }

@@ -129,3 +129,28 @@ def test_cholesky_entry_points_read_only_their_triangle(orc, slt, uplo):
     R = F @ F.T if uplo == "L" else F.T @ F              # the factor reproduces S
     assert np.abs(R - S).max() <= 8 * n * EPS * np.abs(S).max()
     assert np.all(np.isnan(a[:n][other])) and np.all(np.isnan(a[n:]))
+
+
+@pytest.mark.parametrize("refine", ["gmres", "ir"])
+@pytest.mark.parametrize("stream", ["1", "0"])
+def test_dsposv_streamed_lower_triangle(orc, slt, monkeypatch, refine, stream):
+    """slate_dsposv with an FP16 factor: the lower triangle of A arrives by
+    512-column blocks on a copy stream while the left-looking factor consumes
+    it (SLATE_LAPACK_STREAM=1, the default) or is copied before the solve
+    (=0); same solution quality, A unchanged, NaN above the diagonal never
+    read; n off the block size, lda above n."""
+    monkeypatch.setenv("SLATE_LAPACK_FACTOR_PRECISION", "fp16")
+    monkeypatch.setenv("SLATE_LAPACK_REFINE", refine)
+    monkeypatch.setenv("SLATE_LAPACK_STREAM", stream)
+    monkeypatch.setenv("SLT_POTRF_LL", "1")
+    n, nrhs, lda = 3000, 4, 3011
+    A = spd(orc, n, 85)
+    B = orc.generate(2, 86, n, nrhs)
+    Ain = A.copy(order="F")
+    Ain[np.triu_indices(n, 1)] = np.nan
+    x = np.zeros((n, nrhs), order="F")
+    info, it, a = _call_chol(slt, "dsposv", "L", Ain, lda, B=B.copy(order="F"), X=x)
+    assert info == 0 and it >= 0, (info, it)
+    assert orc.backward_error(A, x, B) <= 3 * n * EPS
+    keep = ~np.isnan(Ain)
+    assert np.array_equal(a[:n][keep], Ain[keep]) and np.all(np.isnan(a[n:]))
