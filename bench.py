@@ -675,12 +675,19 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     iters = []
     barrier()
+    # BENCH_PROFILE_RANGE=1: only the timed steps inside the profiler range
+    # (ncu --profile-from-start off captures exactly them)
+    prange = os.environ.get("BENCH_PROFILE_RANGE") == "1"
+    if prange:
+        torch.cuda.profiler.start()
     e0.record(stream)
     for _ in range(args.steps):
         info, it, _ = solve(A, B, X, opts)
         iters.append(it)
     e1.record(stream)
     barrier()
+    if prange:
+        torch.cuda.profiler.stop()
     launches = slt.lib().slt_launch_count() - l0
     clocks = clk.stop()
     t_step = e0.elapsed_time(e1) / 1e3 / args.steps

@@ -300,6 +300,34 @@ __global__ void colmax_kernel(int64_t m, const double* __restrict__ A, int64_t l
     if (threadIdx.x == 0) out[j] = red[0];
 }
 
+// Segment [r0, r0 + rps) of column j: max |A(i, j)| combined with an atomic
+// max on the bit pattern (non-negative doubles order like their bits, and a
+// NaN, made positive by fabs, orders above +Inf, so it propagates).  out
+// (as bits) starts at 0.  grid (ceil(m / rps), n).
+__global__ void __launch_bounds__(256)
+colmax_seg_kernel(int64_t m, const double* __restrict__ A, int64_t lda, int64_t rps, unsigned long long* out)
+{
+    __shared__ unsigned long long red[8];
+    const int64_t j = blockIdx.y;
+    const int64_t r0 = int64_t(blockIdx.x) * rps;
+    const int64_t r1 = r0 + rps < m ? r0 + rps : m;
+    unsigned long long mx = 0;
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += 256) {
+        const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(fabs(A[i + j * lda])));
+        mx = b > mx ? b : mx;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = v > mx ? v : mx;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; ++w) mx = red[w] > mx ? red[w] : mx;
+        atomicMax(out + j, mx);
+    }
+}
+
 // ---- Philox generator (same sequence as slate::random::generate)
 __device__ __forceinline__ void philox2x64_dev(uint64_t s0, uint64_t s1, uint64_t key, uint64_t out[2])
 {
@@ -513,7 +541,16 @@ extern "C" int slt_dcolmax(int64_t m, int64_t n, const double* A, int64_t lda, d
                            cudaStream_t stream)
 {
     if (n <= 0) return SLT_OK;
-    colmax_kernel<<<unsigned(n), 256, 0, stream>>>(m, A, lda, out); slt::count_launch();
+    if (m <= 16384) {
+        colmax_kernel<<<unsigned(n), 256, 0, stream>>>(m, A, lda, out); slt::count_launch();
+        return slt_from_cuda(cudaGetLastError());
+    }
+    // long columns: 8192-row segments in parallel
+    const int64_t rps = 8192;
+    SLT_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * size_t(n), stream));
+    colmax_seg_kernel<<<dim3(unsigned(ceildiv(m, rps)), unsigned(n)), 256, 0, stream>>>(
+        m, A, lda, rps, reinterpret_cast<unsigned long long*>(out));
+    slt::count_launch();
     return slt_from_cuda(cudaGetLastError());
 }
 

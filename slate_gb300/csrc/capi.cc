@@ -10,9 +10,12 @@
 #include "lapack_opts.h"
 
 #include <algorithm>
+#include <condition_variable>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace slt {
@@ -140,51 +143,88 @@ cudaStream_t lapack_copy_stream()
 // the device array d (leading dimension n) on the copy stream cs, in the
 // order the left-looking factor reads it: all 512 x 512 diagonal blocks
 // first (the equilibration scales need the diagonal), then the columns
-// below them block by block, one event per block.  cs first waits for
-// `ready` (d allocated on the compute stream).
+// below them block by block, one event each.  The copies are enqueued by a
+// worker thread: cudaMemcpy2DAsync blocks the enqueuing thread once the
+// driver's copy queue is full, which would hold back the enqueue of the
+// solve itself until most of A had arrived.  The driver's stream waits
+// through arr (whose recorded() blocks until the event it is about to wait
+// for has been recorded).  cs first waits for `ready` (d allocated on s).
 struct StreamedLower {
     static constexpr int64_t kB = 512;
     std::vector<cudaEvent_t> ev;
     cudaEvent_t ev_diag = nullptr, ev_ready = nullptr;
     InputArrival arr;
     cudaStream_t s_ = nullptr;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv;
+    int64_t done = -2;          // last recorded event: -2 none, -1 the diagonal's, b block b
+    int err = SLT_OK;
+
     ~StreamedLower() {
         // whatever happened, the compute stream (which frees d) waits for the copies
-        if (s_) join(s_);
+        if (worker.joinable()) worker.join();
+        if (s_ && done >= 0) cudaStreamWaitEvent(s_, ev[size_t(done)], 0);
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
         if (ev_diag) cudaEventDestroy(ev_diag);
         if (ev_ready) cudaEventDestroy(ev_ready);
     }
-    int start(int64_t n, const double* a, int64_t lda, double* d, cudaStream_t s, cudaStream_t cs) {
+    void publish(int64_t k, int rc) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (rc) err = rc;
+        else done = k;
+        cv.notify_all();
+    }
+    int start(int64_t n, const double* a, int64_t lda, double* d, cudaStream_t s, cudaStream_t cs, bool whole) {
         const int64_t nblk = (n + kB - 1) / kB;
+        int dev = 0;
+        SLT_CUDA_TRY(cudaGetDevice(&dev));
         SLT_CUDA_TRY(cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming));
         SLT_CUDA_TRY(cudaEventCreateWithFlags(&ev_diag, cudaEventDisableTiming));
         ev.assign(size_t(nblk), nullptr);
         for (auto& e : ev) SLT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         SLT_CUDA_TRY(cudaEventRecord(ev_ready, s));
-        SLT_CUDA_TRY(cudaStreamWaitEvent(cs, ev_ready, 0));
+        arr.ev_diag = ev_diag;
         arr.ev = ev.data();
         arr.nev = nblk;
         arr.blk = kB;
+        arr.recorded = [this](int64_t k) -> int {
+            std::unique_lock<std::mutex> lk(mu);
+            cv.wait(lk, [&] { return err != SLT_OK || done >= k; });
+            return err;
+        };
         s_ = s;
-        for (int64_t j0 = 0; j0 < n; j0 += kB) {
-            const int64_t w = std::min(kB, n - j0);
-            SLT_CUDA_TRY(cudaMemcpy2DAsync(d + j0 + j0 * n, size_t(n) * 8, a + j0 + j0 * lda, size_t(lda) * 8,
-                                           size_t(w) * 8, size_t(w), cudaMemcpyHostToDevice, cs));
-        }
-        SLT_CUDA_TRY(cudaEventRecord(ev_diag, cs));
-        for (int64_t j0 = 0, b = 0; j0 < n; j0 += kB, ++b) {
-            const int64_t w = std::min(kB, n - j0), r0 = j0 + w;
-            if (r0 < n)
-                SLT_CUDA_TRY(cudaMemcpy2DAsync(d + r0 + j0 * n, size_t(n) * 8, a + r0 + j0 * lda, size_t(lda) * 8,
-                                               size_t(n - r0) * 8, size_t(w), cudaMemcpyHostToDevice, cs));
-            SLT_CUDA_TRY(cudaEventRecord(ev[size_t(b)], cs));
-        }
-        arr.ev_diag = ev_diag;
+        worker = std::thread([=]() {
+            int rc = slt_from_cuda(cudaSetDevice(dev));
+            if (!rc) rc = slt_from_cuda(cudaStreamWaitEvent(cs, ev_ready, 0));
+            for (int64_t j0 = 0; j0 < n && !rc; j0 += kB) {
+                const int64_t w = std::min(kB, n - j0);
+                rc = slt_from_cuda(cudaMemcpy2DAsync(d + j0 + j0 * n, size_t(n) * 8, a + j0 + j0 * lda, size_t(lda) * 8,
+                                                     size_t(w) * 8, size_t(w), cudaMemcpyHostToDevice, cs));
+            }
+            if (!rc) rc = slt_from_cuda(cudaEventRecord(ev_diag, cs));
+            publish(-1, rc);
+            for (int64_t j0 = 0, b = 0; j0 < n && !rc; j0 += kB, ++b) {
+                const int64_t w = std::min(kB, n - j0), r0 = j0 + w;
+                if (whole && lda == n)          // the whole block column: one contiguous copy
+                    rc = slt_from_cuda(cudaMemcpyAsync(d + j0 * n, a + j0 * lda, size_t(n) * size_t(w) * 8,
+                                                       cudaMemcpyHostToDevice, cs));
+                else if (r0 < n)
+                    rc = slt_from_cuda(cudaMemcpy2DAsync(d + r0 + j0 * n, size_t(n) * 8, a + r0 + j0 * lda,
+                                                         size_t(lda) * 8, size_t(n - r0) * 8, size_t(w),
+                                                         cudaMemcpyHostToDevice, cs));
+                if (!rc) rc = slt_from_cuda(cudaEventRecord(ev[size_t(b)], cs));
+                publish(b, rc);
+            }
+        });
         return SLT_OK;
     }
     // the compute stream waits for every copy (before d is freed or reused)
-    int join(cudaStream_t s) const { return arr.wait_all(s); }
+    int join(cudaStream_t s) {
+        if (worker.joinable()) worker.join();
+        if (err) return err;
+        return arr.wait_all(s);
+    }
 };
 
 template <typename T>
@@ -786,13 +826,23 @@ static void lapack_dsposv_impl(char uplo, int n, int nrhs, double* a, int lda, d
     TimerSet tm(s);
     tm.start("dsposv::h2d");
     StreamedLower sl;
-    const bool stream_a = !up && env_int("SLATE_LAPACK_STREAM", 1) != 0;
-    // only the referenced triangle crosses the link
-    if (dA.alloc(sizeof(double) * size_t(n) * size_t(n), s) ||
-        (stream_a ? sl.start(n, a, lda, dA.as<double>(), s, lapack_copy_stream())
-                  : tri_copy<double>(!up, n, a, lda, dA.as<double>(), n, cudaMemcpyHostToDevice, s)) ||
-        to_device(b, n, nrhs, ldb, dB, s) ||
-        dX.alloc(sizeof(double) * size_t(n) * size_t(std::max(nrhs, 1)), s)) { *info = -100; return; }
+    // SLATE_LAPACK_STREAM: 0 copy A first, 1 (default) stream the lower
+    // triangle by 512-column blocks, 2 stream whole block columns (one
+    // contiguous copy each when lda == n: twice the bytes, plain 1-D copies)
+    const char* se = std::getenv("SLATE_LAPACK_STREAM");
+    const int smode = se ? std::atoi(se) : 1;
+    const bool stream_a = !up && smode != 0;
+    // B first: a copy queued on the compute stream behind A's blocks on the
+    // copy engine would hold the solve back until all of A had arrived.
+    // Only the referenced triangle of A crosses the link.
+    if (to_device(b, n, nrhs, ldb, dB, s) ||
+        dX.alloc(sizeof(double) * size_t(n) * size_t(std::max(nrhs, 1)), s) ||
+        dA.alloc(sizeof(double) * size_t(n) * size_t(n), s) ||
+        (stream_a ? sl.start(n, a, lda, dA.as<double>(), s, lapack_copy_stream(), smode == 2)
+                  : tri_copy<double>(!up, n, a, lda, dA.as<double>(), n, cudaMemcpyHostToDevice, s))) {
+        *info = -100;
+        return;
+    }
     if (lower_view(uplo, n, dA, tmp, s)) { *info = -100; return; }
     tm.stop("dsposv::h2d");
     int64_t inf = 0;

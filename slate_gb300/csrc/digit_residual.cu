@@ -165,32 +165,43 @@ __device__ __forceinline__ long long dg_fixed(double v, int e)
 
 // The eight balanced base-128 digits of F (d_0 most significant), each in
 // [-64, 64] and exact in BF16, packed four BF16 per 8 bytes for four
-// consecutive k: F = sum_p d_p 128^(7 - p), taken from the low end.  A key of
+// consecutive k: F = sum_p d_p 128^(7 - p).  With G = F + C7, C7 = 64 in
+// each of the seven low base-128 places, the low digits are d_p = (7-bit
+// field of G) - 64 and d_0 = G >> 49 -- the representation whose low digits
+// lie in [-64, 63], taken with 32-bit shifts of G's two halves.  A digit
+// d = u - 64 becomes a float exactly as (2^23 + u) - (2^23 + 64).  A key of
 // 2047 (Inf / NaN in the row or column) gives zero digits; the reduction
 // writes NaN for it.
+constexpr long long kDgC7 = 0x1020408102040ll;
+
+__device__ __forceinline__ float dg_digit_float(uint32_t u)     // u - 64, u in [0, 2^23)
+{
+    return __int_as_float(int(0x4B000000u | u)) - 8388672.0f;
+}
+
 __device__ __forceinline__ void dg_digits4(const double (&v)[4], int key, uint2 (&out)[kDgPlanes])
 {
     const int e = dg_scale(key);
-    int d[4][kDgPlanes];
+    float f[4][kDgPlanes];
     #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        long long F = key == kDgBadKey ? 0 : dg_fixed(v[u], e);
-        #pragma unroll
-        for (int p = kDgPlanes - 1; p > 0; --p) {
-            int r = int(F & 127);
-            r -= (r >= 64) ? 128 : 0;
-            d[u][p] = r;
-            F = (F - r) >> 7;
-        }
-        d[u][0] = int(F);
+        const long long G = (key == kDgBadKey ? 0 : dg_fixed(v[u], e)) + kDgC7;
+        const uint32_t lo = uint32_t(G), hi = uint32_t(static_cast<unsigned long long>(G) >> 32);
+        f[u][7] = dg_digit_float(lo & 127u);
+        f[u][6] = dg_digit_float((lo >> 7) & 127u);
+        f[u][5] = dg_digit_float((lo >> 14) & 127u);
+        f[u][4] = dg_digit_float((lo >> 21) & 127u);
+        f[u][3] = dg_digit_float(((lo >> 28) | (hi << 4)) & 127u);
+        f[u][2] = dg_digit_float((hi >> 3) & 127u);
+        f[u][1] = dg_digit_float((hi >> 10) & 127u);
+        f[u][0] = float(int(G >> 49));                   // in [-64, 64]
     }
     #pragma unroll
     for (int p = 0; p < kDgPlanes; ++p) {
-        uint32_t h[4];
-        #pragma unroll
-        for (int u = 0; u < 4; ++u) h[u] = __bfloat16_as_ushort(__float2bfloat16_rn(float(d[u][p])));
-        out[p].x = h[0] | (h[1] << 16);
-        out[p].y = h[2] | (h[3] << 16);
+        const __nv_bfloat162 a = __floats2bfloat162_rn(f[0][p], f[1][p]);
+        const __nv_bfloat162 b = __floats2bfloat162_rn(f[2][p], f[3][p]);
+        out[p].x = *reinterpret_cast<const uint32_t*>(&a);
+        out[p].y = *reinterpret_cast<const uint32_t*>(&b);
     }
 }
 

@@ -43,6 +43,15 @@ TimerSet::~TimerSet()
     for (auto& kv : acc) t_timers[kv.first] = kv.second;
 }
 
+bool plain_alloc()
+{
+    static const bool plain = [] {
+        const char* e = std::getenv("SLT_WORKSPACE_POOL");
+        return e && std::atoi(e) == 0;
+    }();
+    return plain;
+}
+
 static thread_local const InputArrival* t_arrival = nullptr;
 const InputArrival* input_arrival() { return t_arrival; }
 InputArrivalScope::InputArrivalScope(const InputArrival* a) { t_arrival = a; }
@@ -540,7 +549,8 @@ int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc,
 // of A -- which lets the caller stream A in while earlier blocks are being
 // factored (prologue(s0, s1) runs first on each block).
 static int potrf_ll_tc(int64_t n, float* A, int64_t lda, const slt_options& o, int64_t S, FactorCtx& fc,
-                       cudaStream_t s, const std::function<int(int64_t, int64_t)>& prologue)
+                       cudaStream_t s, const std::function<int(int64_t, int64_t, cudaStream_t)>& prologue,
+                       int panel_sms)
 {
     const int64_t nb = eff_nb(o);
     const int tier = o.factor_precision;
@@ -551,13 +561,8 @@ static int potrf_ll_tc(int64_t n, float* A, int64_t lda, const slt_options& o, i
     slt_options ot = o;
     if (ot.gemm_engine == 0) ot.gemm_engine = 1;
     char* L16b = L16.as<char>();
-    for (int64_t s0 = 0; s0 < n; s0 += S) {
-        const int64_t s1 = std::min(n, s0 + S);
-        if (prologue) TRY(prologue(s0, s1));
-        if (s0 > 0) {
-            const char* Lr = L16b + size_t(s0) * size_t(kld) * 2;      // rows s0 .. n
-            TRY(slt_tc_gemm_packed(tier, n - s0, s1 - s0, s0, Lr, kld, Lr, kld, A + s0 + s0 * lda, lda, 1, s));
-        }
+    auto rows16 = [&](int64_t r, int64_t k) { return L16b + (size_t(r) * size_t(kld) + size_t(k)) * 2; };
+    auto panels = [&](int64_t s0, int64_t s1) -> int {
         for (int64_t c = s0; c < s1; c += nb) {
             const int64_t kb = std::min(nb, s1 - c);
             if (c > s0)
@@ -566,9 +571,93 @@ static int potrf_ll_tc(int64_t n, float* A, int64_t lda, const slt_options& o, i
             TRY(k_chol_panel(n - c, kb, A + c + c * lda, lda, fc.d_info, c, bar.p, fc.d_status, s));
         }
         // later blocks read rows s1 .. n of these columns
-        if (s1 < n) TRY(slt_pack_rows16(tier, n, s1, s0, s1, A, lda, L16b, kld, s));
+        return s1 < n ? slt_pack_rows16(tier, n, s1, s0, s1, A, lda, L16b, kld, s) : SLT_OK;
+    };
+    int dev = 0, sms = 0;
+    SLT_CUDA_TRY(cudaGetDevice(&dev));
+    SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t nblk = (n + S - 1) / S;
+    if (panel_sms <= 0 || panel_sms >= sms || nblk <= 2) {
+        for (int64_t s0 = 0; s0 < n; s0 += S) {
+            const int64_t s1 = std::min(n, s0 + S);
+            if (prologue) TRY(prologue(s0, s1, s));
+            if (s0 > 0)
+                TRY(slt_tc_gemm_packed(tier, n - s0, s1 - s0, s0, rows16(s0, 0), kld, rows16(s0, 0), kld,
+                                       A + s0 + s0 * lda, lda, 1, s));
+            TRY(panels(s0, s1));
+        }
+        return SLT_OK;
     }
-    return SLT_OK;
+    // Overlap: block b's update splits into the part from blocks 0 .. b-2
+    // (k = (b-1) S, "big") and the part from block b-1 (k = S, "small").
+    // The big part of block b+1 needs nothing of block b, so it runs on a
+    // second, lower-priority stream on sms - panel_sms SMs while block b's
+    // panels run on panel_sms SMs; the small part follows on the caller's
+    // stream once block b-1 is packed.  Events order the two streams:
+    //   cast + big(b+1)      after  pack(b-1)         (ev_issue)
+    //   small(b+1), panels   after  cast + big(b+1)   (ev_big)
+    int lo = 0, hi = 0;
+    SLT_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    struct Res {
+        cudaStream_t su = nullptr;
+        cudaEvent_t ev_issue = nullptr, ev_big = nullptr;
+        ~Res() {
+            if (su) cudaStreamDestroy(su);
+            if (ev_issue) cudaEventDestroy(ev_issue);
+            if (ev_big) cudaEventDestroy(ev_big);
+        }
+    } r;
+    SLT_CUDA_TRY(cudaStreamCreateWithPriority(&r.su, cudaStreamNonBlocking, lo));
+    SLT_CUDA_TRY(cudaEventCreateWithFlags(&r.ev_issue, cudaEventDisableTiming));
+    SLT_CUDA_TRY(cudaEventCreateWithFlags(&r.ev_big, cudaEventDisableTiming));
+    int rc = SLT_OK;
+    bool big_pending = false;
+    if (prologue) rc = prologue(0, std::min(n, S), s);
+    for (int64_t b = 0; b < nblk && !rc; ++b) {
+        const int64_t s0 = b * S, s1 = std::min(n, s0 + S);
+        if (b >= 1) {
+            if ((rc = slt_from_cuda(cudaStreamWaitEvent(s, r.ev_big, 0)))) break;
+            big_pending = false;
+            // small part: block b-1's columns (k from s0 - S to s0)
+            if ((rc = slt_tc_gemm_packed(tier, n - s0, s1 - s0, S, rows16(s0, s0 - S), kld, rows16(s0, s0 - S), kld,
+                                         A + s0 + s0 * lda, lda, 1, s)))
+                break;
+        }
+        const bool side = b + 1 < nblk;
+        if (side) {
+            const int64_t t0 = s1, t1 = std::min(n, t0 + S);
+            if ((rc = slt_from_cuda(cudaEventRecord(r.ev_issue, s)))) break;
+            if ((rc = slt_from_cuda(cudaStreamWaitEvent(r.su, r.ev_issue, 0)))) break;
+            if (prologue && (rc = prologue(t0, t1, r.su))) break;
+            if (b >= 1) {
+                SmCap cap(sms - panel_sms);
+                if ((rc = slt_tc_gemm_packed(tier, n - t0, t1 - t0, s0, rows16(t0, 0), kld, rows16(t0, 0), kld,
+                                             A + t0 + t0 * lda, lda, 1, r.su)))
+                    break;
+            }
+            if ((rc = slt_from_cuda(cudaEventRecord(r.ev_big, r.su)))) break;
+            big_pending = true;
+        }
+        {
+            SmCap cap(side && b >= 1 ? panel_sms : 0);
+            rc = panels(s0, s1);
+        }
+    }
+    // nothing of the side stream may outlive the call
+    if (big_pending) {
+        const int jr = slt_from_cuda(cudaStreamWaitEvent(s, r.ev_big, 0));
+        if (!rc) rc = jr;
+    }
+    return rc;
+}
+
+// SMs of the left-looking factor's panels while the next block's big
+// update runs beside them: SLT_LL_PANEL_SMS when set (0: no overlap).
+static int potrf_ll_panel_sms(int64_t n)
+{
+    (void) n;
+    if (const char* e = std::getenv("SLT_LL_PANEL_SMS")) return std::atoi(e);
+    return 0;
 }
 
 // The left-looking form applies to FP16 / BF16 factors when the size
@@ -698,10 +787,10 @@ struct LoFactor {
                 const double* dr = r;
                 float* Af = A.as<float>();
                 const int64_t ldf = ld;
-                TRY(potrf_ll_tc(n, Af, ld, o, S, fc, s, [&](int64_t s0, int64_t s1) -> int {
-                    if (arr) TRY(arr->wait_cols(s1, s));
-                    return slt_convert_d2s_scaled_lower_cols(n, s0, s1, Ahi, lda, dr, Af, ldf, s);
-                }));
+                TRY(potrf_ll_tc(n, Af, ld, o, S, fc, s, [&](int64_t s0, int64_t s1, cudaStream_t cs) -> int {
+                    if (arr) TRY(arr->wait_cols(s1, cs));
+                    return slt_convert_d2s_scaled_lower_cols(n, s0, s1, Ahi, lda, dr, Af, ldf, cs);
+                }, potrf_ll_panel_sms(n)));
             }
             else {
                 // the factor reads and writes the lower triangle only
@@ -711,7 +800,7 @@ struct LoFactor {
                     TRY(slt_sshift_diag(n, float(sigma), A.as<float>(), ld, s));
                     SLT_CUDA_TRY(cudaMemsetAsync(fc.d_info, 0, sizeof(int), s));
                 }
-                if (S > 0) TRY(potrf_ll_tc(n, A.as<float>(), ld, o, S, fc, s, nullptr));
+                if (S > 0) TRY(potrf_ll_tc(n, A.as<float>(), ld, o, S, fc, s, nullptr, potrf_ll_panel_sms(n)));
                 else TRY(potrf_dev<float>(n, A.as<float>(), ld, o, fc, s));
             }
             TRY(finish_factor(fc, info, s));

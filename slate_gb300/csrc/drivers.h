@@ -10,6 +10,7 @@
 #include "status.h"
 
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -48,6 +49,11 @@ namespace slt {
 // workspace afresh each time; slt_release_workspace() hands it back.
 cudaMemPool_t workspace_pool();
 
+// SLT_WORKSPACE_POOL=0: workspace from cudaMalloc / cudaFree instead of the
+// stream-ordered pool (slower: every free synchronises the device).  For
+// tools that replay kernels and must save and restore the memory they touch.
+bool plain_alloc();
+
 // Device workspace owned by one driver call (stream-ordered, from the
 // library's pool).
 struct DevBuf {
@@ -56,20 +62,29 @@ struct DevBuf {
     DevBuf() = default;
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { if (p) cudaFreeAsync(p, s); }
+    ~DevBuf() { free_now(); }
     int alloc(size_t bytes, cudaStream_t stream) {
         s = stream;
         if (bytes == 0) bytes = 16;
-        cudaMemPool_t pool = workspace_pool();
-        cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, stream) : cudaMallocAsync(&p, bytes, stream);
+        cudaError_t e;
+        if (plain_alloc()) {
+            e = cudaMalloc(&p, bytes);
+        }
+        else {
+            cudaMemPool_t pool = workspace_pool();
+            e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, stream) : cudaMallocAsync(&p, bytes, stream);
+        }
         if (e != cudaSuccess) { p = nullptr; cudaGetLastError(); return SLT_ERR_NOMEM; }
         return SLT_OK;
     }
-    template <typename T> T* as() const { return static_cast<T*>(p); }
-    void reset() {
-        if (p) cudaFreeAsync(p, s);
+    void free_now() {
+        if (!p) return;
+        if (plain_alloc()) cudaFree(p);       // synchronises the device
+        else cudaFreeAsync(p, s);
         p = nullptr;
     }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+    void reset() { free_now(); }
 };
 
 // A of order n split once into the BF16 digit planes of the tensor-core
@@ -127,17 +142,25 @@ struct TimerSet {
 // stream waits for ev[j / blk] before it reads columns of block j, and for
 // ev_diag before it reads the diagonal.  The events are recorded in column
 // order on one copy stream.
+// The events may be recorded by another host thread: recorded(b) (when
+// set) blocks until event b (-1: the diagonal's) has been recorded, so that
+// the stream wait below waits for that recording and is not a no-op, and
+// returns non-zero if the producer failed.
 struct InputArrival {
     cudaEvent_t ev_diag = nullptr;
     const cudaEvent_t* ev = nullptr;
     int64_t nev = 0, blk = 1;
+    std::function<int(int64_t)> recorded;
     int wait_diag(cudaStream_t s) const {
-        return ev_diag ? slt_from_cuda(cudaStreamWaitEvent(s, ev_diag, 0)) : SLT_OK;
+        if (!ev_diag) return SLT_OK;
+        if (recorded) TRY(recorded(-1));
+        return slt_from_cuda(cudaStreamWaitEvent(s, ev_diag, 0));
     }
     // columns [0, j1)
     int wait_cols(int64_t j1, cudaStream_t s) const {
         if (!ev || nev <= 0 || j1 <= 0) return SLT_OK;
         const int64_t b = std::min<int64_t>(nev - 1, (j1 - 1) / blk);
+        if (recorded) TRY(recorded(b));
         return slt_from_cuda(cudaStreamWaitEvent(s, ev[b], 0));
     }
     int wait_all(cudaStream_t s) const { return ev && nev > 0 ? wait_cols(nev * blk, s) : SLT_OK; }

@@ -32,6 +32,7 @@
 #include "prof.h"
 #include "slate_gb300.h"
 #include "tc_ptx.cuh"
+#include "drivers.h"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -190,6 +191,10 @@ tc_update_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
 // read-modify-write of C is done by the memory system with full overlap.
 constexpr int kPThreads = 192;
 constexpr int64_t kTcGroup = 8;        // column blocks per tile group of the persistent kernel
+// The dynamic shared-memory limit set for tc_update_persistent<0> (one value
+// for every launcher: the attribute is per kernel and device): a launch
+// under an SM budget asks for all of it so no other CTA fits on its SMs.
+constexpr size_t kTcExclusiveSmem = 200 * 1024;
 
 __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, uint32_t src, int x, int y)
 {
@@ -708,10 +713,10 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
     const int64_t mtl = mp / kTcBM, ntl = np / kTcBN;
     const size_t scale_bytes = fp8 ? sizeof(float) * 2 * size_t(mtl + ntl) + 256 : 0;
     const size_t need = size_t(mp + np) * size_t(kpad) * esize + 2048 + scale_bytes;
-    void* owned = nullptr;
+    DevBuf owned;          // the library's workspace pool (freed in stream order on return)
     if (!ws || ws_bytes < need) {
-        if (cudaMallocAsync(&owned, need, stream) != cudaSuccess) { cudaGetLastError(); return SLT_ERR_NOMEM; }
-        ws = owned;
+        TRY(owned.alloc(need, stream));
+        ws = owned.p;
     }
     char* pa = static_cast<char*>(ws);
     char* pb = pa + ((size_t(mp) * kpad * esize + 1023) & ~size_t(1023));
@@ -802,7 +807,7 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
                     if (!rc) tc_update_persistent<2><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(0, kTcBM, kTcBN));
                 }
                 else {
-                    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<0>, psm);
+                    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<0>, kTcExclusiveSmem);
                     const uint32_t fmt = tier == SLT_PREC_BF16 ? 1u : 0u;
                     if (!rc) tc_update_persistent<0><<<grid1, kPThreads, psm, stream>>>(mapA, mapB, mapC, args, make_idesc(fmt, kTcBM, kTcBN));
                 }
@@ -830,7 +835,6 @@ extern "C" int slt_tc_gemm_update(int tier, char transb, int64_t m, int64_t n, i
             prof_end(pidx, stream, 2.0 * mn * double(k), 8.0 * mn + double(esize) * double(kpad) * double(m + n));
         }
     }
-    if (owned) cudaFreeAsync(owned, stream);
     return rc;
 }
 
@@ -896,11 +900,15 @@ extern "C" int slt_tc_gemm_packed(int tier, int64_t m, int64_t n, int64_t kpad, 
         cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
     }
     TcArgs args{m, n, kpad, C, ldc, lower, g_tc_status, nullptr, nullptr};
-    const size_t psm = tcp_smem_bytes();
-    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<0>, psm);
+    // Under an SM budget the launch reserves 200 KB of shared memory per CTA
+    // (it uses tcp_smem_bytes()): no other CTA of this library fits beside it,
+    // so the kernels that run concurrently on the remaining SMs keep them.
+    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<0>, kTcExclusiveSmem);
     if (rc) return rc;
+    const int capped = capped_sms(g_sms);
+    const size_t psm = capped < g_sms ? kTcExclusiveSmem : tcp_smem_bytes();
     const int64_t tiles = ceildiv(m, kTcBM) * ceildiv(n, kTcBN);
-    const unsigned grid = unsigned(std::min<int64_t>(tiles, capped_sms(g_sms)));
+    const unsigned grid = unsigned(std::min<int64_t>(tiles, capped));
     const int pidx = prof_begin(SLT_PROF_GEMM_TC, stream);
     tc_update_persistent<0><<<grid, kPThreads, psm, stream>>>(mapA, mapB, mapC, args,
                                                               make_idesc(tier == SLT_PREC_BF16 ? 1u : 0u, kTcBM, kTcBN));

@@ -70,3 +70,34 @@ def test_cgs2_matches_numpy(slt, n):
         assert np.array_equal(V[q, :j + 1], Vh[q, :j + 1])
     for q in set(range(slots)) - {a for a, _ in act}:
         assert np.array_equal(V[q], Vh[q])
+
+
+@pytest.mark.parametrize("m", [1000, 70001])
+def test_colmax_matches_numpy(slt, m):
+    """slt_dcolmax (the residual and solution max-norms of the stopping
+    tests): one block per column for short columns, 8192-row segments
+    combined by an atomic max for long ones; NaN propagates, -Inf counts as
+    Inf, zero columns give 0."""
+    import torch
+    L = slt.lib()
+    f = L.slt_dcolmax
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+    n, lda = 6, m + 5
+    rng = np.random.default_rng(m)
+    A = rng.standard_normal((n, lda))              # column j at A[j, :]
+    A[:, m:] = 1e300                               # beyond m: never read
+    A[1, m // 2] = np.nan
+    A[2, 7] = -np.inf
+    A[3, :m] = 0.0
+    A[4, m - 1] = -123.0
+    dA = torch.from_numpy(A).cuda()
+    out = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert f(m, n, dA.data_ptr(), lda, out.data_ptr(), s) == 0
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    ref = np.abs(A[:, :m]).max(axis=1)
+    assert np.isnan(got[1]) and np.isinf(got[2]) and got[3] == 0.0
+    keep = [0, 4, 5]
+    assert np.array_equal(got[keep], ref[keep])

@@ -132,13 +132,14 @@ def test_cholesky_entry_points_read_only_their_triangle(orc, slt, uplo):
 
 
 @pytest.mark.parametrize("refine", ["gmres", "ir"])
-@pytest.mark.parametrize("stream", ["1", "0"])
+@pytest.mark.parametrize("stream", ["1", "2", "0"])
 def test_dsposv_streamed_lower_triangle(orc, slt, monkeypatch, refine, stream):
     """slate_dsposv with an FP16 factor: the lower triangle of A arrives by
     512-column blocks on a copy stream while the left-looking factor consumes
-    it (SLATE_LAPACK_STREAM=1, the default) or is copied before the solve
-    (=0); same solution quality, A unchanged, NaN above the diagonal never
-    read; n off the block size, lda above n."""
+    it (SLATE_LAPACK_STREAM=1, the default; =2 whole block columns, here 2-D
+    copies since lda > n) or is copied before the solve (=0); same solution
+    quality, A unchanged, NaN above the diagonal never read; n off the block
+    size, lda above n."""
     monkeypatch.setenv("SLATE_LAPACK_FACTOR_PRECISION", "fp16")
     monkeypatch.setenv("SLATE_LAPACK_REFINE", refine)
     monkeypatch.setenv("SLATE_LAPACK_STREAM", stream)

@@ -9,9 +9,11 @@ potrf_ll_tc) and its two kernels.
   (exact rounding, zero above the diagonal, nothing written outside the
   block);
 * the FP16 / BF16 mixed Cholesky solvers with the left-looking factor forced
-  on (SLT_POTRF_LL=1) against the right-looking one (=0): both converge to
-  the tester's bound, iteration counts within one, and a non-SPD matrix ends
-  in the FP64 fallback's info on both paths (no wait runs out).
+  on (SLT_POTRF_LL=1), with and without the next block's update running
+  beside the panels (SLT_LL_PANEL_SMS), against the right-looking one (=0):
+  all converge to the tester's bound, iteration counts within one, and a
+  non-SPD matrix ends in the FP64 fallback's info on every path (no wait
+  runs out).
 """
 import ctypes
 
@@ -97,8 +99,11 @@ def test_mixed_cholesky_left_looking_vs_right_looking(orc, slt, monkeypatch, pre
     A = spd(orc, n, 400 + n)
     B = orc.generate(2, 401 + n, n, nrhs)
     res = {}
-    for ll in ("1", "0"):
-        monkeypatch.setenv("SLT_POTRF_LL", ll)
+    # left-looking without and with the next block's update beside the panels
+    # (SLT_LL_PANEL_SMS: the panels' SM share), then right-looking
+    for ll in ("1", "1:38", "0"):
+        monkeypatch.setenv("SLT_POTRF_LL", ll[0])
+        monkeypatch.setenv("SLT_LL_PANEL_SMS", ll[2:] if ":" in ll else "0")
         for name, fn in (("gmres", slt.posv_mixed_gmres), ("ir", slt.posv_mixed)):
             dX = to_dev(np.zeros((n, nrhs)))
             info, it, _ = fn(to_dev(A), to_dev(B), dX, slt.Options(nb=512, factor_precision=prec))
@@ -108,6 +113,7 @@ def test_mixed_cholesky_left_looking_vs_right_looking(orc, slt, monkeypatch, pre
             res[(ll, name)] = it
     for name in ("gmres", "ir"):
         assert abs(res[("1", name)] - res[("0", name)]) <= 1, res
+        assert abs(res[("1:38", name)] - res[("0", name)]) <= 1, res
 
 
 def test_mixed_cholesky_left_looking_not_spd(orc, slt, monkeypatch):
@@ -116,8 +122,9 @@ def test_mixed_cholesky_left_looking_not_spd(orc, slt, monkeypatch):
     A = spd(orc, n, 9)
     A[bad, bad] = -5.0
     B = orc.generate(2, 10, n, 2)
-    for ll in ("1", "0"):
-        monkeypatch.setenv("SLT_POTRF_LL", ll)
+    for ll in ("1", "1:38", "0"):
+        monkeypatch.setenv("SLT_POTRF_LL", ll[0])
+        monkeypatch.setenv("SLT_LL_PANEL_SMS", ll[2:] if ":" in ll else "0")
         dX = to_dev(np.zeros((n, 2)))
         info, it, _ = slt.posv_mixed(to_dev(A), to_dev(B), dX, slt.Options(nb=512, factor_precision="fp16"))
         torch.cuda.synchronize()
