@@ -95,35 +95,74 @@ __device__ __forceinline__ int dg_scale(int key) { return key == 0 ? 0 : key - 1
 
 // Maximum keys of the rows of A (general: over the whole row; sym, lower
 // storage: over the stored part j <= i and, through the columns, over the
-// part held in column i below the diagonal).  Block: rows I0 .. I0 + 63 and
-// four 64-column tiles from J0.  grid (ceil(n / 256), ceil(n / 64)).
+// part held in column i below the diagonal).  With rsum, also the row sums
+// of |a_ij| over the same full rows (the infinity norm's), added with
+// double atomics (so their last bit depends on the order).  Block: rows
+// I0 .. I0 + 63 and four 64-column tiles from J0.
+// grid (ceil(n / 256), ceil(n / 64)).
 __global__ void __launch_bounds__(256)
-dg_akeys_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym, int* key)
+dg_akeys_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym, int* key, double* rsum)
 {
     __shared__ int K[64][65];
+    __shared__ double V[64][65];
     const int64_t I0 = int64_t(blockIdx.y) * 64;
     const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
     int rmax = 0;
+    double racc = 0.0;
     for (int t = 0; t < 4; ++t) {
         const int64_t J0 = (int64_t(blockIdx.x) * 4 + t) * 64;
         if (J0 >= n || (sym && J0 > I0)) break;
         for (int kk = ty; kk < 64; kk += 4) {
             const int64_t i = I0 + tx, j = J0 + kk;
-            K[tx][kk] = (i < n && j < n && !(sym && j > i)) ? dg_key(A[i + j * lda]) : 0;
+            const double v = (i < n && j < n && !(sym && j > i)) ? A[i + j * lda] : 0.0;
+            K[tx][kk] = dg_key(v);
+            if (rsum) V[tx][kk] = fabs(v);
         }
         __syncthreads();
         if (threadIdx.x < 64) {
             for (int c = 0; c < 64; ++c) rmax = max(rmax, K[threadIdx.x][c]);
+            if (rsum)
+                for (int c = 0; c < 64; ++c) racc += V[threadIdx.x][c];
         }
         else if (sym && threadIdx.x < 128) {
             const int c = threadIdx.x - 64;
             int cm = 0;
-            for (int r = 0; r < 64; ++r) cm = max(cm, K[r][c]);
+            double cs = 0.0;
+            for (int r = 0; r < 64; ++r) {
+                cm = max(cm, K[r][c]);
+                if (rsum && I0 + r > J0 + c) cs += V[r][c];       // strictly below the diagonal
+            }
             if (cm && J0 + c < n) atomicMax(key + J0 + c, cm);
+            if (rsum && cs != 0.0 && J0 + c < n) atomicAdd(rsum + J0 + c, cs);
         }
         __syncthreads();
     }
-    if (threadIdx.x < 64 && rmax && I0 + threadIdx.x < n) atomicMax(key + I0 + threadIdx.x, rmax);
+    if (threadIdx.x < 64 && I0 + threadIdx.x < n) {
+        if (rmax) atomicMax(key + I0 + threadIdx.x, rmax);
+        if (rsum && racc != 0.0) atomicAdd(rsum + I0 + threadIdx.x, racc);
+    }
+}
+
+// *out = max_i v[i], NaN if any v[i] is NaN.  One block of 1024 threads.
+__global__ void __launch_bounds__(1024)
+dg_max_kernel(int64_t n, const double* __restrict__ v, double* out)
+{
+    __shared__ double red[32];
+    double m = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += 1024) {
+        const double x = v[i];
+        m = (x > m || x != x) ? x : m;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_xor_sync(0xffffffffu, m, o);
+        m = (y > m || y != y) ? y : m;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 32; ++w) m = (red[w] > m || red[w] != red[w]) ? red[w] : m;
+        *out = m;
+    }
 }
 
 // Maximum keys of the columns of an m x ncols column-major matrix.
@@ -554,7 +593,7 @@ void DigitMatrix::release()
     ready = false;
 }
 
-int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cudaStream_t s)
+int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cudaStream_t s, double* d_norm)
 {
     release();
     if (n_ <= 0 || lda < n_) return SLT_ERR_ARG;
@@ -578,10 +617,20 @@ int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cuda
     SLT_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(int), s));
     SLT_CUDA_TRY(cudaMemsetAsync(rexp.p, 0, sizeof(int) * size_t(rows_pad), s));
 
-    // row keys: one pass over the stored part of A
+    // row keys (and the row sums of |A| for the infinity norm): one pass over
+    // the stored part of A
+    DevBuf rs;
+    if (d_norm) {
+        TRY(rs.alloc(sizeof(double) * size_t(n), s));
+        SLT_CUDA_TRY(cudaMemsetAsync(rs.p, 0, sizeof(double) * size_t(n), s));
+    }
     dg_akeys_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(ceildiv(n, 64))), 256, 0, s>>>(
-        n, A, lda, sym, rexp.as<int>());
+        n, A, lda, sym, rexp.as<int>(), d_norm ? rs.as<double>() : nullptr);
     count_launch();
+    if (d_norm) {
+        dg_max_kernel<<<1, 1024, 0, s>>>(n, rs.as<double>(), d_norm);
+        count_launch();
+    }
     dg_split_a_kernel<<<dim3(unsigned(ldk / 64), unsigned(rows_pad / 64)), 256, 0, s>>>(
         n, A, lda, sym, rexp.as<int>(), planes.as<__nv_bfloat16>(), ldk, pstride);
     count_launch();

@@ -540,14 +540,15 @@ int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc,
 // tiers (FP16, BF16), S a multiple of 64: before block [s0, s1) is factored,
 // its columns (rows s0 .. n) take the whole contribution of columns 0 .. s0
 // in one tensor-core update with k = s0, read from a row-major 16-bit copy of
-// the factor (L16) that every finished block adds its columns to; inside the
-// block, each nb-column panel is brought up to date with the block's earlier
-// panels and factored by the panel kernel.  Same factor as the right-looking
-// order (the same operand roundings, FP32 sums grouped differently), but the
-// trailing matrix is read and written once in all, the operands are packed
-// once instead of at every update, and block s needs only columns s0 .. s1
-// of A -- which lets the caller stream A in while earlier blocks are being
-// factored (prologue(s0, s1) runs first on each block).
+// the factor (L16); inside the block, each nb-column panel is brought up to
+// date with the block's earlier panels (again from L16), factored by the
+// panel kernel, and its rows below it added to L16.  Same factor as the
+// right-looking order (the same operand roundings, FP32 sums grouped
+// differently), but the trailing matrix is read and written once in all,
+// every column is packed once instead of at every update, and block s needs
+// only columns s0 .. s1 of A -- which lets the caller stream A in while
+// earlier blocks are being factored (prologue(s0, s1, stream) runs first on
+// each block).
 static int potrf_ll_tc(int64_t n, float* A, int64_t lda, const slt_options& o, int64_t S, FactorCtx& fc,
                        cudaStream_t s, const std::function<int(int64_t, int64_t, cudaStream_t)>& prologue,
                        int panel_sms)
@@ -558,20 +559,20 @@ static int potrf_ll_tc(int64_t n, float* A, int64_t lda, const slt_options& o, i
     TRY(bar.alloc(slt_chol_panel_ws_bytes(), s));
     const int64_t kld = (n + 63) / 64 * 64;
     TRY(L16.alloc(size_t(n) * size_t(kld) * 2, s));
-    slt_options ot = o;
-    if (ot.gemm_engine == 0) ot.gemm_engine = 1;
     char* L16b = L16.as<char>();
     auto rows16 = [&](int64_t r, int64_t k) { return L16b + (size_t(r) * size_t(kld) + size_t(k)) * 2; };
+    // the panels of one block, each brought up to date with the block's
+    // earlier panels from L16 and added to L16 (rows below it) once factored
     auto panels = [&](int64_t s0, int64_t s1) -> int {
         for (int64_t c = s0; c < s1; c += nb) {
             const int64_t kb = std::min(nb, s1 - c);
             if (c > s0)
-                TRY(k_gemm('T', n - c, kb, c - s0, -1.f, A + c + s0 * lda, lda, A + c + s0 * lda, lda, 1.f,
-                           A + c + c * lda, lda, 1, ot, s));
+                TRY(slt_tc_gemm_packed(tier, n - c, kb, c - s0, rows16(c, s0), kld, rows16(c, s0), kld,
+                                       A + c + c * lda, lda, 1, s));
             TRY(k_chol_panel(n - c, kb, A + c + c * lda, lda, fc.d_info, c, bar.p, fc.d_status, s));
+            if (c + kb < n) TRY(slt_pack_rows16(tier, n, c + kb, c, c + kb, A, lda, L16b, kld, s));
         }
-        // later blocks read rows s1 .. n of these columns
-        return s1 < n ? slt_pack_rows16(tier, n, s1, s0, s1, A, lda, L16b, kld, s) : SLT_OK;
+        return SLT_OK;
     };
     int dev = 0, sms = 0;
     SLT_CUDA_TRY(cudaGetDevice(&dev));
@@ -873,6 +874,21 @@ struct Residual {
         }
         if (!ws.p) TRY(ws.alloc(slt_residual_ws_bytes(n, 16), s));
         return slt_dresidual(n, nc, A, lda, sym, B, ldb, X, ldx, R, ldr, ws.p, s);
+    }
+
+    // ||A||_inf to d_out: from the digit split's pass over A when the
+    // tensor-core products will run (the planes are prepared here, once), else
+    // the FP64 norm kernel (ws: slt_norm_ws_bytes(n) bytes).  nc: the columns
+    // of the first products.
+    int norm_inf(double* d_out, void* nws, int64_t nc, cudaStream_t s) {
+        if (use_digits(nc) && !dm.ready) {
+            const int rc = dm.prepare(n, A, lda, sym, s, d_out);
+            if (rc == SLT_OK) return SLT_OK;
+            if (rc != SLT_ERR_NOMEM && rc != SLT_ERR_NOT_SUPPORTED) return rc;
+            dm.release();
+            dm_failed = true;
+        }
+        return slt_dnorm_inf(n, n, A, lda, sym, d_out, nws, s);
     }
 
     // the bounded-wait status of the tensor-core products (synchronises)
@@ -1192,7 +1208,9 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
     // arriving from the host while it ran; the factor waited for all of it)
     double Anorm = 0;
     if (const InputArrival* arr = input_arrival()) TRY(arr->wait_all(s));
-    TRY(slt_dnorm_inf(n, n, A, lda, chol, scal.as<double>(), nws.p, s));
+    Residual res(n, A, lda, chol, o.residual_engine);
+    // (no planes when the factor failed: no product will run)
+    TRY(res.norm_inf(scal.as<double>(), nws.p, linfo ? 0 : std::min<int64_t>(nrhs, 16), s));
     TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
     const double cte = Anorm * tol;
     bool conv = false;
@@ -1200,7 +1218,6 @@ static int gesv_mixed_once(int chol, int64_t n, int64_t nrhs, double* A, int64_t
     double* dcx = col.as<double>();
     double* dcr = dcx + nrhs;
     const int64_t rhs_chunks = (nrhs + 15) / 16;
-    Residual res(n, A, lda, chol, o.residual_engine);
     auto residual = [&]() -> int {
         tm.start(std::string(pfx) + (chol ? "::hemm_hi" : "::gemm_hi"));
         for (int64_t c = 0; c < rhs_chunks; ++c) {
@@ -1439,13 +1456,14 @@ static int gesv_mixed_gmres_once(int chol, int64_t n, int64_t nrhs, double* A, i
     // arriving from the host while it ran; the factor waited for all of it)
     double Anorm = 0;
     if (const InputArrival* arr = input_arrival()) TRY(arr->wait_all(s));
-    TRY(slt_dnorm_inf(n, n, A, lda, chol, scal.as<double>(), nws.p, s));
+    Residual res(n, A, lda, chol, o.residual_engine);
+    // (no planes when the factor failed: no product will run)
+    TRY(res.norm_inf(scal.as<double>(), nws.p, linfo ? 0 : std::min<int64_t>(nrhs, 16), s));
     TRY(read_doubles(scal.as<double>(), &Anorm, 1, s));
     const double cte = Anorm * tol;
     *info = linfo;
     bool all_conv = true;
     int worst_iter = 0;
-    Residual res(n, A, lda, chol, o.residual_engine);
     if (linfo != 0) {
         *iter = -3;
         all_conv = false;

@@ -100,7 +100,8 @@ struct DigitMatrix {
     DigitMatrix() = default;
     DigitMatrix(const DigitMatrix&) = delete;
     DigitMatrix& operator=(const DigitMatrix&) = delete;
-    int prepare(int64_t n, const double* A, int64_t lda, int sym_lower, cudaStream_t s);
+    // d_norm (device, optional): also ||A||_inf, from the same pass over A
+    int prepare(int64_t n, const double* A, int64_t lda, int sym_lower, cudaStream_t s, double* d_norm = nullptr);
     int residual(int64_t nrhs, const double* B, int64_t ldb, const double* X, int64_t ldx, double* R,
                  int64_t ldr, cudaStream_t s);
     // SLT_OK, or SLT_ERR_TIMEOUT when a bounded wait of a product ran out
