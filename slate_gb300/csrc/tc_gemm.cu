@@ -206,12 +206,14 @@ __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, uint32
 __device__ __forceinline__ void bulk_wait_read_le1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
-template <int KIND>
+// BN: tile width, 128 or 256 (N of the MMA; two BN-column TMEM accumulators).
+template <int KIND, int BN = kTcBN>
 __global__ void __launch_bounds__(kPThreads, 1)
 tc_update_persistent(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                      const __grid_constant__ CUtensorMap mapC, TcArgs a, uint32_t idesc)
 {
-    constexpr int BM = kTcBM, BN = kTcBN, S = kTcStages;
+    static_assert(BN == 128 || BN == 256, "tile width");
+    constexpr int BM = kTcBM, S = kTcStages;
     constexpr int A_BYTES = BM * 128;
     constexpr int B_BYTES = BN * 128;
     constexpr int STAGE = A_BYTES + B_BYTES;
@@ -650,9 +652,9 @@ static size_t tc_smem_bytes()
     return size_t(kTcStages) * (kTcBM + kTcBN) * 128 + 1024 + 256;
 }
 
-static size_t tcp_smem_bytes()
+static size_t tcp_smem_bytes(int bn = kTcBN)
 {
-    return size_t(kTcStages) * (kTcBM + kTcBN) * 128 + 8 * 32 * 32 * 4 + 1024 + 256;
+    return size_t(kTcStages) * (kTcBM + bn) * 128 + 8 * 32 * 32 * 4 + 1024 + 256;
 }
 
 // fp32 column-major C: inner dim m (rows), outer n, box 32 x 32, no swizzle.
@@ -891,8 +893,11 @@ extern "C" int slt_tc_gemm_packed(int tier, int64_t m, int64_t n, int64_t kpad, 
     const CUtensorMapDataType dt = tier == SLT_PREC_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
                                                          : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
     CUtensorMap mapA, mapB, mapC;
+    // 128 x 256 tiles: 48 KB of operands per 64-k stage for 4.2 MFLOP (128 x 128:
+    // 32 KB for 2.1 MFLOP), so a third less shared-memory fill per flop
+    constexpr int BN = 256;
     TRY(tma_map_2d(&mapA, const_cast<void*>(A16), dt, kpad, m, lda16 * 2, 64, kTcBM, CU_TENSOR_MAP_SWIZZLE_128B));
-    TRY(tma_map_2d(&mapB, const_cast<void*>(B16), dt, kpad, n, ldb16 * 2, 64, kTcBN, CU_TENSOR_MAP_SWIZZLE_128B));
+    TRY(tma_map_2d(&mapB, const_cast<void*>(B16), dt, kpad, n, ldb16 * 2, 64, BN, CU_TENSOR_MAP_SWIZZLE_128B));
     TRY(make_map_c(&mapC, C, m, n, ldc));
     if (!g_sms) {
         int dev = 0;
@@ -900,18 +905,16 @@ extern "C" int slt_tc_gemm_packed(int tier, int64_t m, int64_t n, int64_t kpad, 
         cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
     }
     TcArgs args{m, n, kpad, C, ldc, lower, g_tc_status, nullptr, nullptr};
-    // Under an SM budget the launch reserves 200 KB of shared memory per CTA
-    // (it uses tcp_smem_bytes()): no other CTA of this library fits beside it,
-    // so the kernels that run concurrently on the remaining SMs keep them.
-    SLT_SMEM_ONCE_INTO(rc, tc_update_persistent<0>, kTcExclusiveSmem);
+    // ~225 KB of shared memory per CTA: one CTA per SM, and no other CTA of
+    // this library fits beside it (what a launch under an SM budget needs)
+    const size_t psm = tcp_smem_bytes(BN);
+    SLT_SMEM_ONCE_INTO(rc, (tc_update_persistent<0, BN>), psm);
     if (rc) return rc;
-    const int capped = capped_sms(g_sms);
-    const size_t psm = capped < g_sms ? kTcExclusiveSmem : tcp_smem_bytes();
-    const int64_t tiles = ceildiv(m, kTcBM) * ceildiv(n, kTcBN);
-    const unsigned grid = unsigned(std::min<int64_t>(tiles, capped));
+    const int64_t tiles = ceildiv(m, kTcBM) * ceildiv(n, BN);
+    const unsigned grid = unsigned(std::min<int64_t>(tiles, capped_sms(g_sms)));
     const int pidx = prof_begin(SLT_PROF_GEMM_TC, stream);
-    tc_update_persistent<0><<<grid, kPThreads, psm, stream>>>(mapA, mapB, mapC, args,
-                                                              make_idesc(tier == SLT_PREC_BF16 ? 1u : 0u, kTcBM, kTcBN));
+    tc_update_persistent<0, BN><<<grid, kPThreads, psm, stream>>>(mapA, mapB, mapC, args,
+                                                                  make_idesc(tier == SLT_PREC_BF16 ? 1u : 0u, kTcBM, BN));
     count_launch();
     const double mn = lower ? (double(m) * double(n) - (double(n) * double(n) - double(n)) / 2.0) : double(m) * double(n);
     prof_end(pidx, stream, 2.0 * mn * double(kpad), 8.0 * mn + 2.0 * double(kpad) * double(m + n));
