@@ -20,37 +20,51 @@
 //  * a' x' = sum_w S_w 128^-(w+2) with S_w = sum_k sum_{p+q=w} d_p d_q; the
 //    weight classes w >= 8 lie below 2^-53 of the product scale and are
 //    dropped, so 8 classes remain;
-//  * the tensor cores form the eight class sums for one chunk of 256 k in
-//    FP32: every digit product is an integer of magnitude <= 2^12 and every
-//    partial sum at most 256 * 8 * 2^12 = 2^23, so FP32 accumulation is
+//  * the operands of the tensor cores are the BF16 values d + 192 of the A
+//    digits (d in [-64, 64], so 128 <= d + 192 <= 256) and the digits of X;
+//    they form the class sums of one chunk of 256 k in two FP32 accumulators
+//    (A planes 0-3 and 4-7), each taking at most four digit pairs per class:
+//    every product is an integer of magnitude <= 256 * 64 = 2^14 and every
+//    partial sum at most 256 * 4 * 2^14 = 2^24, so FP32 accumulation is
 //    exact in any order;
 //  * per chunk the epilogue folds the class sums exactly into two int64
 //    words, hi = sum_{w<4} S_w 2^(7(3-w)) and lo = sum_{w>=4} S_w 2^(7(7-w));
-//    split-K segments add in int64 (exact), and the last kernel forms
+//    split-K segments add in int64 (exact); the last kernel removes the
+//    offset, 192 sum_{q<=w} T_q(c) in class w with T_q(c) the sum of digit q
+//    of column c of X over all k (exact integers), and forms
 //    r = (b - hi 2^(e-35)) - lo 2^(e-63), e = ea_i + ex_c.
 //
 // The computed A x differs from the exact one by at most about
 // 2^-50 n max_k |a_ik| max_k |x_kc| (the dropped digits and classes), and
 // typically by 2^-56 sqrt(n) of that scale: as accurate as an FP64 product.
 //
-// Layout in HBM.  The digit planes of A are BF16, K-major (row i of plane p
-// contiguous over k), zero-padded to rows_pad = 128-multiple rows and
-// ldk = 64-multiple columns: 16 n^2 bytes, twice the FP64 matrix, written
-// once per solve.  The digits of X (per call) are 128 rows (plane q, column c
-// at row 16 q + c) of ldk BF16.
+// Layout in HBM.  The digit planes of A are bytes u = d + 64 in [0, 128],
+// zero-padded (u = 64) to rows_pad = 128-multiple rows and ldk = 64-multiple
+// columns: 8 n^2 bytes, the size of the FP64 matrix, written once per solve.
+// They are stored as tiles of 128 rows x 64 k, the eight planes of one tile
+// adjacent (64 KB), tiles of one row block in k order: a CTA streams its K
+// segment as one contiguous run.  Within a plane tile row r holds its 64
+// bytes at r * 64 with the 16-byte chunk j at position j ^ ((r >> 1) & 3)
+// (the 64-byte swizzle, so that 32 threads reading 32 rows hit distinct
+// banks).  The digits of X (per call) are 128 rows (plane q, column c at row
+// 16 q + c) of ldk BF16.
 //
-// The MMA.  A CTA takes a 128-row block of A and a K segment.  Per 64 k it
-// loads the X digit tile (128 x 64) into the upper half of a 32 KB stage
-// whose lower half is zero, and the eight A digit tiles (128 x 64 each).  For
-// A plane p the B descriptor starts 16 p rows before the X tile, so MMA row
-// j = 16 w + c of B is X plane w - p (zero for w < p): one
-// tcgen05.mma M128 N128 K16 accumulates plane p into all eight class
-// accumulators D[:, 16 w + c] at once.  32 MMAs per 64 k; D is double
-// buffered in TMEM (2 x 128 columns) so the epilogue of one chunk overlaps
-// the next chunk's MMAs.  Warp 0 issues TMA loads, warp 1 the MMAs, warps
-// 2-5 fold the accumulators (one TMEM lane quarter each).  Every mbarrier
-// wait is bounded; on timeout the CTA records SLT_ERR_TIMEOUT, drains its
-// own copies and MMAs, frees its TMEM and returns.
+// The MMA.  A CTA takes a 128-row block of A and a K segment.  Per 64 k, warp
+// 0 loads the 64 KB byte tile of A with one bulk copy (three stages) and warp
+// 10 the X digit tile (128 x 64 BF16, 128-byte swizzle) with TMA (two
+// stages), each running ahead on its own ring.  Warps 6-9 (one
+// TMEM lane quarter each; thread = row) turn the bytes into the BF16 operand
+// in tensor memory: BF16 0x4300 | u is exactly 128 + u = d + 192 for every
+// u in [0, 128] (u = 128 carries into the exponent: 0x4380 = 256), so one
+// byte permute makes two operands, stored with tcgen05.st.  Warp 1 issues,
+// per 16 k and plane p, tcgen05.mma M128 N(128 - 16 p) K16 with A from
+// tensor memory and B = X planes 0 .. 7 - p, accumulating class w = p + q
+// into column 16 w + c of D_L (planes 0-3) or 16 (w - 4) + c of D_H (planes
+// 4-7): the 36 digit products of weight <= 7 and no others, in two
+// independent accumulator chains issued alternately.  The epilogue (warps
+// 2-5) empties D once per 256 k; the A operand has three 16-k stages.  Every
+// mbarrier wait is bounded; on timeout the CTA records SLT_ERR_TIMEOUT,
+// drains its own copies and MMAs, frees its TMEM and returns.
 
 #include "common.cuh"
 #include "drivers.h"
@@ -67,15 +81,29 @@ namespace slt {
 
 constexpr int kDgPlanes = 8;          // digits per operand
 constexpr int kDgBM = 128;            // rows of A per CTA (MMA M)
-constexpr int kDgBK = 64;             // k per stage: 128 bytes of BF16
+constexpr int kDgBK = 64;             // k per stage
 constexpr int kDgChunk = 4;           // k-blocks per accumulator flush (256 k)
-constexpr int kDgAStages = 8;
+constexpr int kDgUStages = 3;
 constexpr int kDgXStages = 2;
-constexpr int kDgThreads = 192;
+constexpr int kDgThreads = 352;
 constexpr int kDgCols = 16;           // right-hand sides per call
-constexpr uint32_t kDgATile = kDgBM * 128;          // 16 KB
-constexpr uint32_t kDgXHalf = 128 * 128;            // 128 rows x 128 bytes
-constexpr uint32_t kDgXStage = 2 * kDgXHalf;        // zero half + digit half
+constexpr int kDgOffset = 192;        // the A operand of digit d is d + 192
+constexpr uint32_t kDgUPlane = kDgBM * kDgBK;          // 8 KB: one byte plane, 128 rows x 64 k
+constexpr uint32_t kDgUStage = kDgPlanes * kDgUPlane;  // 64 KB
+constexpr uint32_t kDgXStage = 128 * 128;              // 128 digit rows x 64 k BF16
+// TMEM columns.  The accumulators are D_L (planes 0-3, classes 0-7: 128
+// columns, two buffers at 0 and 128) and D_H (planes 4-7, classes 4-7: 64
+// columns at 256): two independent accumulation chains, since consecutive
+// MMAs into one accumulator run at one per ~130 clocks whatever N <= 128 is.
+// The epilogue empties D_H first, so the next chunk's MMAs wait only for that
+// third of the drain.  The A operand stages (16 k of 8 planes: 64 columns
+// each) fill the other 192 columns.
+constexpr uint32_t kDgTmemL = 128;                     // D_L buffer stride
+constexpr uint32_t kDgTmemH = 256;
+constexpr uint32_t kDgTmemA = 320;
+constexpr uint32_t kDgTmemAStage = 64;
+constexpr int kDgAStagesT = 3;
+constexpr int kDgASub = kDgBK / 16;                    // A operand stages per 64 k
 // Exponent keys.  key(v) = 0 for v = 0, 2047 for Inf / NaN, else
 // max(biased exponent of v, 1); keys are monotone in |v|, and for the largest
 // key K of a row, |v| < 2^(K - 1022) for every v of the row, so the scale
@@ -202,55 +230,45 @@ __device__ __forceinline__ long long dg_fixed(double v, int e)
     return (b >> 63) ? -F : F;
 }
 
-// The eight balanced base-128 digits of F (d_0 most significant), each in
-// [-64, 64] and exact in BF16, packed four BF16 per 8 bytes for four
-// consecutive k: F = sum_p d_p 128^(7 - p).  With G = F + C7, C7 = 64 in
-// each of the seven low base-128 places, the low digits are d_p = (7-bit
-// field of G) - 64 and d_0 = G >> 49 -- the representation whose low digits
-// lie in [-64, 63], taken with 32-bit shifts of G's two halves.  A digit
-// d = u - 64 becomes a float exactly as (2^23 + u) - (2^23 + 64).  A key of
-// 2047 (Inf / NaN in the row or column) gives zero digits; the reduction
-// writes NaN for it.
+// The eight balanced base-128 digits of F (d_0 most significant) as bytes
+// u_p = d_p + 64: F = sum_p d_p 128^(7 - p), d_p in [-64, 63] for p >= 1 and
+// d_0 in [-64, 64], so u_p in [0, 128].  With G = F + C7, C7 = 64 in each of
+// the seven low base-128 places, u_p (p >= 1) is the 7-bit field of G and
+// d_0 = G >> 49 -- taken with 32-bit shifts of G's two halves.  A key of 2047
+// (Inf / NaN in the row or column) gives zero digits (u = 64); the
+// reduction writes NaN for it.
 constexpr long long kDgC7 = 0x1020408102040ll;
 
-__device__ __forceinline__ float dg_digit_float(uint32_t u)     // u - 64, u in [0, 2^23)
+__device__ __forceinline__ void dg_digit_bytes(double v, int key, uint32_t (&u)[kDgPlanes])
 {
-    return __int_as_float(int(0x4B000000u | u)) - 8388672.0f;
+    const long long G = (key == kDgBadKey ? 0 : dg_fixed(v, dg_scale(key))) + kDgC7;
+    const uint32_t lo = uint32_t(G), hi = uint32_t(static_cast<unsigned long long>(G) >> 32);
+    u[7] = lo & 127u;
+    u[6] = (lo >> 7) & 127u;
+    u[5] = (lo >> 14) & 127u;
+    u[4] = (lo >> 21) & 127u;
+    u[3] = ((lo >> 28) | (hi << 4)) & 127u;
+    u[2] = (hi >> 3) & 127u;
+    u[1] = (hi >> 10) & 127u;
+    u[0] = uint32_t((int(hi) >> 17) + 64);
 }
 
-__device__ __forceinline__ void dg_digits4(const double (&v)[4], int key, uint2 (&out)[kDgPlanes])
+// Byte offset of (plane p, row i, k) in the tiled byte planes.
+__device__ __forceinline__ int64_t dg_byte_at(int64_t i, int64_t k, int p, int64_t kbt)
 {
-    const int e = dg_scale(key);
-    float f[4][kDgPlanes];
-    #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const long long G = (key == kDgBadKey ? 0 : dg_fixed(v[u], e)) + kDgC7;
-        const uint32_t lo = uint32_t(G), hi = uint32_t(static_cast<unsigned long long>(G) >> 32);
-        f[u][7] = dg_digit_float(lo & 127u);
-        f[u][6] = dg_digit_float((lo >> 7) & 127u);
-        f[u][5] = dg_digit_float((lo >> 14) & 127u);
-        f[u][4] = dg_digit_float((lo >> 21) & 127u);
-        f[u][3] = dg_digit_float(((lo >> 28) | (hi << 4)) & 127u);
-        f[u][2] = dg_digit_float((hi >> 3) & 127u);
-        f[u][1] = dg_digit_float((hi >> 10) & 127u);
-        f[u][0] = float(int(G >> 49));                   // in [-64, 64]
-    }
-    #pragma unroll
-    for (int p = 0; p < kDgPlanes; ++p) {
-        const __nv_bfloat162 a = __floats2bfloat162_rn(f[0][p], f[1][p]);
-        const __nv_bfloat162 b = __floats2bfloat162_rn(f[2][p], f[3][p]);
-        out[p].x = *reinterpret_cast<const uint32_t*>(&a);
-        out[p].y = *reinterpret_cast<const uint32_t*>(&b);
-    }
+    const int64_t tile = ((i >> 7) * kbt + (k >> 6)) * kDgPlanes + p;
+    const int r = int(i & 127), j = int(k & 63);
+    return tile * kDgUPlane + r * kDgBK + ((((j >> 4) ^ (r >> 1)) & 3) << 4) + (j & 15);
 }
 
-// Digit planes of A: the 64 x 64 tile (rows I0.., k K0..) of plane p at
-// planes + p pstride + i ldk + k.  A column-major; with sym only its lower
+// Byte digit planes of A, the 64 x 64 block (rows I0.., k K0..); A
+// column-major; with sym only its lower
 // triangle is read (element (i, k), k > i, is A(k, i)).  Rows >= n and
-// k >= n are written as zeros.  grid (ldk / 64, rows_pad / 64), 256 threads.
+// k >= n get the zero digit (u = 64).  grid (ldk / 64, rows_pad / 64), 256
+// threads.
 __global__ void __launch_bounds__(256)
 dg_split_a_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym, const int* __restrict__ rexp,
-                  __nv_bfloat16* planes, int64_t ldk, int64_t pstride)
+                  uint8_t* planes, int64_t kbt)
 {
     __shared__ double T[64][65];
     const int64_t I0 = int64_t(blockIdx.y) * 64, K0 = int64_t(blockIdx.x) * 64;
@@ -278,37 +296,59 @@ dg_split_a_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym,
     for (int r = threadIdx.x >> 4; r < 64; r += 16) {
         const int64_t i = I0 + r;
         const int key = i < n ? rexp[i] : 0;
-        double v[4] = {T[r][kq], T[r][kq + 1], T[r][kq + 2], T[r][kq + 3]};
-        uint2 d[kDgPlanes];
-        dg_digits4(v, key, d);
-        __nv_bfloat16* dst = planes + i * ldk + K0 + kq;
+        uint32_t w[kDgPlanes] = {0, 0, 0, 0, 0, 0, 0, 0};
+        #pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            uint32_t u[kDgPlanes];
+            dg_digit_bytes(T[r][kq + t], key, u);
+            #pragma unroll
+            for (int p = 0; p < kDgPlanes; ++p) w[p] |= u[p] << (8 * t);
+        }
         #pragma unroll
         for (int p = 0; p < kDgPlanes; ++p)
-            *reinterpret_cast<uint2*>(dst + int64_t(p) * pstride) = d[p];
+            *reinterpret_cast<uint32_t*>(planes + dg_byte_at(i, K0 + kq, p, kbt)) = w[p];
     }
 }
 
-// Digits of X (n x nrhs, column-major): plane q of column c at row 16 q + c of
-// xd (128 rows of ldk), zeros for k >= n and c >= nrhs.  grid (ldk / 1024, 16).
+// Digits of X (n x nrhs, column-major) in BF16: plane q of column c at row
+// 16 q + c of xd (128 rows of ldk), zeros for k >= n and c >= nrhs; and the
+// digit sums T_q(c) over k, added into xsum[16 q + c] (zeroed by the caller;
+// int64 atomics, exact).  grid (ldk / 1024, 16), 256 threads.
 __global__ void __launch_bounds__(256)
 dg_split_x_kernel(int64_t n, int nrhs, const double* __restrict__ X, int64_t ldx, const int* __restrict__ cexp,
-                  __nv_bfloat16* xd, int64_t ldk)
+                  __nv_bfloat16* xd, int64_t ldk, unsigned long long* xsum)
 {
     const int c = blockIdx.y;
     const int64_t k = (int64_t(blockIdx.x) * 256 + threadIdx.x) * 4;
-    if (k >= ldk) return;
     const int key = c < nrhs ? cexp[c] : 0;
-    double v[4];
+    int d[4][kDgPlanes];
     #pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = (c < nrhs && k + u < n) ? X[k + u + int64_t(c) * ldx] : 0.0;
-    uint2 d[kDgPlanes];
-    dg_digits4(v, key, d);
+    for (int t = 0; t < 4; ++t) {
+        const double v = (c < nrhs && k + t < n) ? X[k + t + int64_t(c) * ldx] : 0.0;
+        uint32_t u[kDgPlanes];
+        dg_digit_bytes(v, key, u);
+        #pragma unroll
+        for (int q = 0; q < kDgPlanes; ++q) d[t][q] = int(u[q]) - 64;
+    }
     #pragma unroll
-    for (int q = 0; q < kDgPlanes; ++q)
-        *reinterpret_cast<uint2*>(xd + int64_t(q * kDgCols + c) * ldk + k) = d[q];
+    for (int q = 0; q < kDgPlanes; ++q) {
+        if (k < ldk) {
+            const __nv_bfloat162 a = __floats2bfloat162_rn(float(d[0][q]), float(d[1][q]));
+            const __nv_bfloat162 b = __floats2bfloat162_rn(float(d[2][q]), float(d[3][q]));
+            uint2 o;
+            o.x = *reinterpret_cast<const uint32_t*>(&a);
+            o.y = *reinterpret_cast<const uint32_t*>(&b);
+            *reinterpret_cast<uint2*>(xd + int64_t(q * kDgCols + c) * ldk + k) = o;
+        }
+        int sum = d[0][q] + d[1][q] + d[2][q] + d[3][q];
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if ((threadIdx.x & 31) == 0 && sum != 0)
+            atomicAdd(xsum + q * kDgCols + c, static_cast<unsigned long long>(static_cast<long long>(sum)));
+    }
 }
 
 struct DgArgs {
+    const uint8_t* planes;  // tiled byte planes
     int64_t rows_pad;       // rows of one A plane
     int rb;                 // 128-row blocks
     int kb_total;           // 64-k blocks
@@ -324,148 +364,208 @@ __device__ __forceinline__ void dg_fail(int* status, volatile int* abort_flag)
     *abort_flag = 1;
 }
 
-__global__ void __launch_bounds__(kDgThreads, 1)
-dg_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapX, DgArgs a,
-               uint32_t idesc)
+// Two BF16 operands 128 + u from bytes 2j, 2j + 1 of w (j = 0, 1).
+__device__ __forceinline__ void dg_expand(uint32_t w, uint32_t& o0, uint32_t& o1)
 {
-    constexpr int S = kDgAStages, XS = kDgXStages;
+    o0 = __byte_perm(w, 0x43434343u, 0x4140);
+    o1 = __byte_perm(w, 0x43434343u, 0x4342);
+}
+
+__global__ void __launch_bounds__(kDgThreads, 1)
+dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
+{
+    constexpr int US = kDgUStages, XS = kDgXStages;
     extern __shared__ __align__(1024) unsigned char dg_smem_raw[];
     const uint32_t raw = smem_u32(dg_smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     unsigned char* gbase = dg_smem_raw + (base - raw);
-    const uint32_t a0 = base, x0 = base + S * kDgATile;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + S * kDgATile + XS * kDgXStage);
-    // afull[S] aempty[S] xfull[XS] xempty[XS] tfull[2] tempty[2] fin
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 2 * XS + 5);
+    const uint32_t u0 = base, x0 = base + US * kDgUStage;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + US * kDgUStage + XS * kDgXStage);
+    constexpr int AS = kDgAStagesT;
+    // ufull[US] uempty[US] xfull[XS] xempty[XS] afull[AS] aempty[AS] tfull[2] templ[2] temph fin
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * US + 2 * XS + 2 * AS + 6);
     __shared__ int s_abort;
     volatile int* abort_flag = &s_abort;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t afull0 = smem_u32(bars), aempty0 = afull0 + 8 * S;
-    const uint32_t xfull0 = aempty0 + 8 * S, xempty0 = xfull0 + 8 * XS;
-    const uint32_t tfull0 = xempty0 + 8 * XS, tempty0 = tfull0 + 16, fin = tempty0 + 16;
+    const uint32_t ufull0 = smem_u32(bars), uempty0 = ufull0 + 8 * US;
+    const uint32_t xfull0 = uempty0 + 8 * US, xempty0 = xfull0 + 8 * XS;
+    const uint32_t afull0 = xempty0 + 8 * XS, aempty0 = afull0 + 8 * AS;
+    const uint32_t tfull0 = aempty0 + 8 * AS, templ0 = tfull0 + 16, temph = templ0 + 16, fin = temph + 8;
     const int64_t items = int64_t(a.rb) * a.segs;
 
-    // zero halves of the X stages (read by the MMAs of planes p >= 1)
-    for (uint32_t off = threadIdx.x * 16; off < kDgXHalf; off += kDgThreads * 16)
-        for (int xs = 0; xs < XS; ++xs)
-            *reinterpret_cast<uint4*>(gbase + S * kDgATile + xs * kDgXStage + off) = make_uint4(0, 0, 0, 0);
     if (threadIdx.x == 0) {
         s_abort = 0;
-        for (int s = 0; s < S; ++s) { mbar_init(afull0 + 8 * s, 1); mbar_init(aempty0 + 8 * s, 1); }
+        for (int s = 0; s < US; ++s) { mbar_init(ufull0 + 8 * s, 1); mbar_init(uempty0 + 8 * s, 4); }
         for (int s = 0; s < XS; ++s) { mbar_init(xfull0 + 8 * s, 1); mbar_init(xempty0 + 8 * s, 1); }
-        for (int b = 0; b < 2; ++b) { mbar_init(tfull0 + 8 * b, 1); mbar_init(tempty0 + 8 * b, 4); }
+        for (int b = 0; b < AS; ++b) {
+            mbar_init(afull0 + 8 * b, 4);
+            mbar_init(aempty0 + 8 * b, 1);
+        }
+        for (int b = 0; b < 2; ++b) { mbar_init(tfull0 + 8 * b, 1); mbar_init(templ0 + 8 * b, 4); }
+        mbar_init(temph, 4);
         mbar_init(fin, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    if (warp == 1) tmem_alloc(smem_u32(tmem_slot), 256);
+    if (warp == 1) tmem_alloc(smem_u32(tmem_slot), 512);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t taddr = *tmem_slot;
 
-    if (warp == 0) {
+    if (warp == 0 || warp == 10) {
         if (lane == 0) {
-            // ---- TMA producer
-            long long ia = 0, ix = 0;
+            // ---- producers: warp 0 streams the byte tiles of A (bulk copies),
+            // warp 10 the X digit tiles (TMA), each as far ahead as its ring
+            // allows
+            const bool isx = warp == 10;
+            const int NS = isx ? XS : US;
+            const uint32_t full0 = isx ? xfull0 : ufull0, empty0 = isx ? xempty0 : uempty0;
+            int st = 0;
+            uint32_t ph = 0;
+            long long issued = 0;
             bool ok = true;
             for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x) {
                 const int row0 = int(t % a.rb) * kDgBM;
                 const int seg = int(t / a.rb);
                 const int kb0 = seg * a.kb_per_seg, kb1 = min(a.kb_total, kb0 + a.kb_per_seg);
-                for (int kb = kb0; kb < kb1 && ok; ++kb) {
-                    const int xs = int(ix % XS);
-                    if (!mbar_wait(xempty0 + 8 * xs, uint32_t((ix / XS) & 1) ^ 1u) || *abort_flag) {
+                for (int kb = kb0; kb < kb1; ++kb) {
+                    if (!mbar_wait(empty0 + 8 * st, ph ^ 1u) || *abort_flag) {
                         dg_fail(a.status, abort_flag);
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(xfull0 + 8 * xs, kDgXHalf);
-                    tma_load_2d(x0 + xs * kDgXStage + kDgXHalf, &mapX, xfull0 + 8 * xs, kb * kDgBK, 0);
-                    ++ix;
-                    for (int p = 0; p < kDgPlanes; ++p) {
-                        const int s = int(ia % S);
-                        if (!mbar_wait(aempty0 + 8 * s, uint32_t((ia / S) & 1) ^ 1u) || *abort_flag) {
-                            dg_fail(a.status, abort_flag);
-                            ok = false;
-                            break;
-                        }
-                        mbar_expect_tx(afull0 + 8 * s, kDgATile);
-                        tma_load_2d(a0 + s * kDgATile, &mapA, afull0 + 8 * s, kb * kDgBK,
-                                    int(int64_t(p) * a.rows_pad) + row0);
-                        ++ia;
+                    if (isx) {
+                        mbar_expect_tx(full0 + 8 * st, kDgXStage);
+                        tma_load_2d(x0 + st * kDgXStage, &mapX, full0 + 8 * st, kb * kDgBK, 0);
                     }
+                    else {
+                        mbar_expect_tx(full0 + 8 * st, kDgUStage);
+                        bulk_load(u0 + st * kDgUStage,
+                                  a.planes + (int64_t(row0 / kDgBM) * a.kb_total + kb) * int64_t(kDgUStage),
+                                  kDgUStage, full0 + 8 * st);
+                    }
+                    ++issued;
+                    if (++st == NS) { st = 0; ph ^= 1u; }
                 }
             }
             // drain: the last armed phase of every stage lands before exit
-            for (int s = 0; s < S && s < ia; ++s) {
-                const long long last = s + ((ia - 1 - s) / S) * S;
-                mbar_wait(afull0 + 8 * s, uint32_t((last / S) & 1));
-            }
-            for (int s = 0; s < XS && s < ix; ++s) {
-                const long long last = s + ((ix - 1 - s) / XS) * XS;
-                mbar_wait(xfull0 + 8 * s, uint32_t((last / XS) & 1));
+            for (int s = 0; s < NS && s < issued; ++s) {
+                const long long last = s + ((issued - 1 - s) / NS) * NS;
+                mbar_wait(full0 + 8 * s, uint32_t((last / NS) & 1));
             }
         }
     }
     else if (warp == 1) {
-        if (lane == 0) {
-            // ---- MMA issuer
-            long long ia = 0, ix = 0, lt = 0;
-            bool ok = true;
-            for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x) {
-                const int seg = int(t / a.rb);
-                const int kb0 = seg * a.kb_per_seg, kb1 = min(a.kb_total, kb0 + a.kb_per_seg);
-                for (int kc = kb0; kc < kb1 && ok; kc += kDgChunk, ++lt) {
-                    const int buf = int(lt & 1);
-                    if (!mbar_wait(tempty0 + 8 * buf, uint32_t((lt >> 1) & 1) ^ 1u) || *abort_flag) {
-                        dg_fail(a.status, abort_flag);
+        // ---- MMA issuer: the whole warp runs the loop (operands stay in
+        // uniform registers), lane 0 issues the tcgen05 instructions
+        const uint32_t lead = lane == 0 ? 1u : 0u;
+        int as = 0, xs = 0;
+        uint32_t aph = 0, xph = 0;
+        long long lt = 0;
+        bool ok = true;
+        for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x) {
+            const int seg = int(t / a.rb);
+            const int kb0 = seg * a.kb_per_seg, kb1 = min(a.kb_total, kb0 + a.kb_per_seg);
+            for (int kc = kb0; kc < kb1 && ok; kc += kDgChunk, ++lt) {
+                const int buf = int(lt & 1);
+                ok = __all_sync(0xffffffffu, mbar_wait(templ0 + 8 * buf, uint32_t((lt >> 1) & 1) ^ 1u) &&
+                                                 mbar_wait(temph, uint32_t(lt & 1) ^ 1u) && !*abort_flag);
+                if (!ok) break;
+                tc_fence_after();
+                const uint32_t tl = taddr + uint32_t(buf) * kDgTmemL;
+                const int kend = min(kb1, kc + kDgChunk);
+                for (int kb = kc; kb < kend && ok; ++kb) {
+                    ok = __all_sync(0xffffffffu, mbar_wait(xfull0 + 8 * xs, xph) && !*abort_flag);
+                    if (!ok) break;
+                    tc_fence_after();
+                    const uint64_t dx = sw128_desc(x0 + uint32_t(xs) * kDgXStage);
+                    for (int h = 0; h < kDgASub; ++h) {
+                        ok = __all_sync(0xffffffffu, mbar_wait(afull0 + 8 * as, aph) && !*abort_flag);
+                        if (!ok) break;
+                        tc_fence_after();
+                        const uint32_t ta = taddr + kDgTmemA + uint32_t(as) * kDgTmemAStage;
+                        const uint32_t first = (kb == kc && h == 0) ? 0u : 1u;
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            // plane j into D_L from column 16 j, plane j + 4 into D_H
+                            // from column 16 j; B = X planes 0 .. 7 - p
+                            umma_ta_w(tl + uint32_t(16 * j), ta + uint32_t(8 * j), dx + uint64_t(2 * h),
+                                      make_idesc(1u, kDgBM, 128 - 16 * j), j == 0 ? first : 1u, lead);
+                            umma_ta_w(taddr + kDgTmemH + uint32_t(16 * j), ta + uint32_t(8 * (j + 4)),
+                                      dx + uint64_t(2 * h), make_idesc(1u, kDgBM, 64 - 16 * j),
+                                      j == 0 ? first : 1u, lead);
+                        }
+                        umma_commit_w(aempty0 + 8 * as, lead);
+                        if (++as == AS) { as = 0; aph ^= 1u; }
+                    }
+                    if (!ok) break;
+                    umma_commit_w(xempty0 + 8 * xs, lead);
+                    if (++xs == XS) { xs = 0; xph ^= 1u; }
+                }
+                if (!ok) break;
+                umma_commit_w(tfull0 + 8 * buf, lead);
+            }
+        }
+        if (!ok && lane == 0) dg_fail(a.status, abort_flag);
+        // every MMA issued above has completed before TMEM is freed
+        umma_commit_w(fin, lead);
+        if (lane == 0 && !mbar_wait(fin, 0u)) atomicCAS(a.status, 0, SLT_ERR_TIMEOUT);
+        __syncwarp();
+    }
+    else if (warp >= 6) {
+        // ---- operand warps 6..9: TMEM lanes 32 q .. 32 q + 31, q = warp % 4;
+        // thread = row of the 128-row block
+        const int q = warp & 3;
+        const int row = q * 32 + lane;
+        const uint32_t sw = uint32_t((row >> 1) & 3);          // 64-byte swizzle of the byte tiles
+        const uint32_t tlane = taddr + (uint32_t(q * 32) << 16) + kDgTmemA;
+        int us = 0, as = 0;
+        uint32_t uph = 0, aph = 0;
+        bool ok = true;
+        for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x) {
+            const int seg = int(t / a.rb);
+            const int kb0 = seg * a.kb_per_seg, kb1 = min(a.kb_total, kb0 + a.kb_per_seg);
+            for (int kb = kb0; kb < kb1 && ok; ++kb) {
+                bool ready = mbar_wait(ufull0 + 8 * us, uph);
+                ready = __all_sync(0xffffffffu, ready && !*abort_flag);
+                if (!ready) {
+                    if (lane == 0) dg_fail(a.status, abort_flag);
+                    ok = false;
+                    break;
+                }
+                const unsigned char* urow = gbase + us * kDgUStage + row * kDgBK;
+                for (int h = 0; h < kDgASub; ++h) {
+                    bool free_ = mbar_wait(aempty0 + 8 * as, aph ^ 1u);
+                    free_ = __all_sync(0xffffffffu, free_ && !*abort_flag);
+                    if (!free_) {
+                        if (lane == 0) dg_fail(a.status, abort_flag);
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t tacc = taddr + uint32_t(buf * 128);
-                    const int kend = min(kb1, kc + kDgChunk);
-                    for (int kb = kc; kb < kend && ok; ++kb) {
-                        const int xs = int(ix % XS);
-                        if (!mbar_wait(xfull0 + 8 * xs, uint32_t((ix / XS) & 1)) || *abort_flag) {
-                            dg_fail(a.status, abort_flag);
-                            ok = false;
-                            break;
-                        }
-                        tc_fence_after();
-                        const uint32_t xrows = x0 + xs * kDgXStage + kDgXHalf;
-                        for (int p = 0; p < kDgPlanes; ++p) {
-                            const int s = int(ia % S);
-                            if (!mbar_wait(afull0 + 8 * s, uint32_t((ia / S) & 1)) || *abort_flag) {
-                                dg_fail(a.status, abort_flag);
-                                ok = false;
-                                break;
-                            }
-                            tc_fence_after();
-                            const uint64_t da = sw128_desc(a0 + s * kDgATile);
-                            // 16 p rows (2048 p bytes) before the X digits: rows of
-                            // classes w < p fall in the zero half
-                            const uint64_t db = sw128_desc(xrows - uint32_t(p) * 2048u);
-                            #pragma unroll
-                            for (int k = 0; k < 4; ++k)
-                                umma<0>(tacc, da + uint64_t(2 * k), db + uint64_t(2 * k), idesc,
-                                        (kb == kc && p == 0 && k == 0) ? 0u : 1u);
-                            umma_commit(aempty0 + 8 * s);
-                            ++ia;
-                        }
-                        if (!ok) break;
-                        umma_commit(xempty0 + 8 * xs);
-                        ++ix;
+                    #pragma unroll 4
+                    for (int p = 0; p < kDgPlanes; ++p) {
+                        const uint4 w = *reinterpret_cast<const uint4*>(urow + p * kDgUPlane +
+                                                                        ((uint32_t(h) ^ sw) << 4));
+                        uint32_t o[8];
+                        dg_expand(w.x, o[0], o[1]);
+                        dg_expand(w.y, o[2], o[3]);
+                        dg_expand(w.z, o[4], o[5]);
+                        dg_expand(w.w, o[6], o[7]);
+                        tmem_st8(tlane + uint32_t(as) * kDgTmemAStage + uint32_t(8 * p), o);
                     }
-                    if (!ok) break;
-                    umma_commit(tfull0 + 8 * buf);
+                    tmem_st_wait();
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(afull0 + 8 * as);
+                    if (++as == AS) { as = 0; aph ^= 1u; }
                 }
+                if (!ok) break;
+                __syncwarp();
+                if (lane == 0) mbar_arrive(uempty0 + 8 * us);
+                if (++us == US) { us = 0; uph ^= 1u; }
             }
-            // every MMA issued above has completed before TMEM is freed
-            umma_commit(fin);
-            if (!mbar_wait(fin, 0u)) atomicCAS(a.status, 0, SLT_ERR_TIMEOUT);
         }
     }
     else {
@@ -490,24 +590,34 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
                     break;
                 }
                 tc_fence_after();
-                const uint32_t tl = taddr + (uint32_t(q * 32) << 16) + uint32_t(buf * 128);
+                const uint32_t tq = taddr + (uint32_t(q * 32) << 16);
                 #pragma unroll 1
-                for (int h = 0; h < 4; ++h) {     // classes 2h and 2h + 1
+                for (int g = 0; g < 6; ++g) {     // D_H classes 4 .. 7 (g < 2), then D_L classes 2h, 2h + 1
+                    const int h = g < 2 ? g + 2 : g - 2;
+                    if (g == 2) {
+                        // D_H is read: the next chunk's MMAs may start
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(temph);
+                    }
                     float v[32];
-                    tmem_ld32(tl + uint32_t(h * 32), v);
+                    tmem_ld32(tq + (g < 2 ? kDgTmemH + uint32_t(g * 32) : uint32_t(buf) * kDgTmemL + uint32_t(h * 32)),
+                              v);
                     // class w weighs 2^(7(3-w)) in hi (w < 4), 2^(7(7-w)) in lo
                     const long long m0 = (h & 1) ? (1ll << 7) : (1ll << 21);
                     const long long m1 = (h & 1) ? 1ll : (1ll << 14);
                     #pragma unroll
                     for (int c = 0; c < kDgCols; ++c) {
-                        const long long f = __float2ll_rn(v[c]) * m0 + __float2ll_rn(v[16 + c]) * m1;
+                        // |v| <= 2^24: exact in int32
+                        const long long f = (long long) __float2int_rn(v[c]) * m0 +
+                                            (long long) __float2int_rn(v[16 + c]) * m1;
                         if (h < 2) hi[c] += f;
                         else lo[c] += f;
                     }
                 }
                 tc_fence_before();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(tempty0 + 8 * buf);
+                if (lane == 0) mbar_arrive(templ0 + 8 * buf);
             }
             if (!ok) break;
             const int64_t r = int64_t(row0) + q * 32 + lane;
@@ -522,25 +632,38 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 1) tmem_dealloc(taddr, 256);
+    if (warp == 1) tmem_dealloc(taddr, 512);
 }
 
 // R(i, c) = B(i, c) - sum over segments of (hi 2^(e-35) + lo 2^(e-63)),
-// e = ea_i + ex_c; NaN where row i of A or column c of X holds Inf / NaN.
-// grid (ceil(n / 256), nrhs).
+// e = ea_i + ex_c, after removing the operand offset of the A digits:
+// 192 sum_{q<=w} T_q(c) from class w, folded like the class sums.  NaN where
+// row i of A or column c of X holds Inf / NaN.  grid (ceil(n / 256), nrhs).
 __global__ void __launch_bounds__(256)
 dg_reduce_kernel(int64_t n, int64_t rows_pad, int segs, const long long* __restrict__ part,
-                 const int* __restrict__ rexp, const int* __restrict__ cexp, const double* __restrict__ B,
-                 int64_t ldb, double* R, int64_t ldr)
+                 const int* __restrict__ rexp, const int* __restrict__ cexp,
+                 const unsigned long long* __restrict__ xsum, const double* __restrict__ B, int64_t ldb,
+                 double* R, int64_t ldr)
 {
     const int64_t i = int64_t(blockIdx.x) * 256 + threadIdx.x;
     const int c = blockIdx.y;
     if (i >= n) return;
-    long long hi = 0, lo = 0;
+    // sums in unsigned (two's complement) arithmetic: the offset-carrying
+    // partial words and the offset itself are exact modulo 2^64, and the
+    // difference is the true, representable value
+    unsigned long long hi = 0, lo = 0;
     for (int s = 0; s < segs; ++s) {
         const long long* p = part + (int64_t(s) * 2 * kDgCols + c) * rows_pad + i;
-        hi += p[0];
-        lo += p[int64_t(kDgCols) * rows_pad];
+        hi += static_cast<unsigned long long>(p[0]);
+        lo += static_cast<unsigned long long>(p[int64_t(kDgCols) * rows_pad]);
+    }
+    unsigned long long pre = 0;
+    #pragma unroll
+    for (int w = 0; w < kDgPlanes; ++w) {
+        pre += xsum[w * kDgCols + c];
+        const unsigned long long off = pre * unsigned(kDgOffset);
+        if (w < 4) hi -= off << (7 * (3 - w));
+        else lo -= off << (7 * (7 - w));
     }
     double r;
     if (rexp[i] == kDgBadKey || cexp[c] == kDgBadKey) {
@@ -548,17 +671,19 @@ dg_reduce_kernel(int64_t n, int64_t rows_pad, int segs, const long long* __restr
     }
     else {
         const int e = dg_scale(rexp[i]) + dg_scale(cexp[c]);
-        const double yh = double(hi);
-        // hi - yh is exact in int64 whenever |yh| < 2^62; fold it into lo
-        if (fabs(yh) < 4.611686018427387904e18) lo += (hi - (long long) yh) * (1ll << 28);
-        r = (B[i + c * ldb] - ldexp(yh, e - 35)) - ldexp(double(lo), e - 63);
+        const long long hs = static_cast<long long>(hi);
+        long long ls = static_cast<long long>(lo);
+        const double yh = double(hs);
+        // hs - yh is exact in int64 whenever |yh| < 2^62; fold it into lo
+        if (fabs(yh) < 4.611686018427387904e18) ls += (hs - (long long) yh) * (1ll << 28);
+        r = (B[i + c * ldb] - ldexp(yh, e - 35)) - ldexp(double(ls), e - 63);
     }
     R[i + c * ldr] = r;
 }
 
 static size_t dg_smem_bytes()
 {
-    return 1024 + size_t(kDgAStages) * kDgATile + size_t(kDgXStages) * kDgXStage + 256;
+    return 1024 + size_t(kDgUStages) * kDgUStage + size_t(kDgXStages) * kDgXStage + 256;
 }
 
 // Split-K segments: the count that minimises waves x (k-blocks per item + 2).
@@ -579,7 +704,7 @@ static void dg_plan(int64_t rb, int64_t kb_total, int sms, int* segs, int* kps)
 size_t DigitMatrix::bytes_for(int64_t n)
 {
     const int64_t ldk = ceildiv(n, kDgBK) * kDgBK, rp = ceildiv(n, kDgBM) * kDgBM;
-    return size_t(kDgPlanes) * size_t(rp) * size_t(ldk) * 2;
+    return size_t(kDgPlanes) * size_t(rp) * size_t(ldk);
 }
 
 void DigitMatrix::release()
@@ -588,6 +713,7 @@ void DigitMatrix::release()
     rexp.reset();
     cexp.reset();
     xplanes.reset();
+    xsum.reset();
     part.reset();
     status.reset();
     ready = false;
@@ -602,7 +728,6 @@ int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cuda
     n = n_;
     ldk = ceildiv(n, kDgBK) * kDgBK;
     rows_pad = ceildiv(n, kDgBM) * kDgBM;
-    pstride = rows_pad * ldk;
     int dev = 0, nsm = 0;
     SLT_CUDA_TRY(cudaGetDevice(&dev));
     SLT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -612,6 +737,7 @@ int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cuda
     TRY(rexp.alloc(sizeof(int) * size_t(rows_pad), s));
     TRY(cexp.alloc(sizeof(int) * kDgCols, s));
     TRY(xplanes.alloc(size_t(kDgPlanes) * kDgCols * size_t(ldk) * 2, s));
+    TRY(xsum.alloc(sizeof(unsigned long long) * kDgPlanes * kDgCols, s));
     TRY(part.alloc(size_t(segs) * 2 * kDgCols * size_t(rows_pad) * sizeof(long long), s));
     TRY(status.alloc(sizeof(int), s));
     SLT_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(int), s));
@@ -632,12 +758,10 @@ int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cuda
         count_launch();
     }
     dg_split_a_kernel<<<dim3(unsigned(ldk / 64), unsigned(rows_pad / 64)), 256, 0, s>>>(
-        n, A, lda, sym, rexp.as<int>(), planes.as<__nv_bfloat16>(), ldk, pstride);
+        n, A, lda, sym, rexp.as<int>(), planes.as<uint8_t>(), ldk / kDgBK);
     count_launch();
     SLT_CUDA_TRY(cudaGetLastError());
 
-    TRY(tma_map_2d(&mapA, planes.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, ldk, int64_t(kDgPlanes) * rows_pad,
-                   ldk * 2, kDgBK, kDgBM, CU_TENSOR_MAP_SWIZZLE_128B));
     TRY(tma_map_2d(&mapX, xplanes.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, ldk, int64_t(kDgPlanes) * kDgCols,
                    ldk * 2, kDgBK, kDgPlanes * kDgCols, CU_TENSOR_MAP_SWIZZLE_128B));
     ready = true;
@@ -656,27 +780,28 @@ int DigitMatrix::residual(int64_t nrhs, const double* B, int64_t ldb, const doub
                                                   int(dg_smem_bytes())));
     }));
     SLT_CUDA_TRY(cudaMemsetAsync(cexp.p, 0, sizeof(int) * kDgCols, s));
+    SLT_CUDA_TRY(cudaMemsetAsync(xsum.p, 0, sizeof(unsigned long long) * kDgPlanes * kDgCols, s));
     const int64_t rps = 16384;
     dg_colkeys_kernel<<<dim3(unsigned(nrhs), unsigned(ceildiv(n, rps))), 256, 0, s>>>(n, X, ldx, rps,
                                                                                     cexp.as<int>());
     count_launch();
     dg_split_x_kernel<<<dim3(unsigned(ceildiv(ldk, 1024)), kDgCols), 256, 0, s>>>(
-        n, int(nrhs), X, ldx, cexp.as<int>(), xplanes.as<__nv_bfloat16>(), ldk);
+        n, int(nrhs), X, ldx, cexp.as<int>(), xplanes.as<__nv_bfloat16>(), ldk, xsum.as<unsigned long long>());
     count_launch();
 
-    DgArgs args{rows_pad, int(rows_pad / kDgBM), int(ldk / kDgBK), kb_per_seg, segs, part.as<long long>(),
+    DgArgs args{planes.as<uint8_t>(), rows_pad, int(rows_pad / kDgBM), int(ldk / kDgBK), kb_per_seg, segs, part.as<long long>(),
                 status.as<int>()};
     const int64_t items = int64_t(args.rb) * segs;
     const unsigned grid = unsigned(std::min<int64_t>(items, sms));
-    const uint32_t idesc = make_idesc(1u, kDgBM, 128);       // BF16 x BF16 -> FP32, M 128, N 128
     const int pidx = prof_begin(SLT_PROF_DIGIT, s);
-    dg_gemm_kernel<<<grid, kDgThreads, dg_smem_bytes(), s>>>(mapA, mapX, args, idesc);
+    dg_gemm_kernel<<<grid, kDgThreads, dg_smem_bytes(), s>>>(mapX, args);
     count_launch();
     // algorithmic: 2 n^2 nrhs flops of the FP64 product; bytes: the digit planes of A
     prof_end(pidx, s, 2.0 * double(n) * double(n) * double(nrhs), double(bytes_for(n)));
     SLT_CUDA_TRY(cudaGetLastError());
     dg_reduce_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(nrhs)), 256, 0, s>>>(
-        n, rows_pad, segs, part.as<long long>(), rexp.as<int>(), cexp.as<int>(), B, ldb, R, ldr);
+        n, rows_pad, segs, part.as<long long>(), rexp.as<int>(), cexp.as<int>(), xsum.as<unsigned long long>(), B,
+        ldb, R, ldr);
     count_launch();
     return slt_from_cuda(cudaGetLastError());
 }

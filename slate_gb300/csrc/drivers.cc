@@ -549,11 +549,27 @@ int potrf_dev(int64_t n, T* A, int64_t lda, const slt_options& o, FactorCtx& fc,
 // only columns s0 .. s1 of A -- which lets the caller stream A in while
 // earlier blocks are being factored (prologue(s0, s1, stream) runs first on
 // each block).
+// Width of the left-looking factor's SIMT panels: SLT_LL_PANEL_WIDTH when
+// set (a multiple of 64 dividing nb), else 256 when it divides nb, else nb.
+// The block's earlier panels reach each panel through the tensor-core
+// update, so a narrower panel moves the intra-block update work from the
+// SIMT panel to tcgen05 (n = 65536, nb = 512: 138.5 ms factor at width 512,
+// 130.3 ms at 256, 136.7 ms at 128).
+static int64_t potrf_ll_panel_width(const slt_options& o)
+{
+    const int64_t nb = eff_nb(o);
+    if (const char* e = std::getenv("SLT_LL_PANEL_WIDTH")) {
+        const int64_t w = std::atoll(e);
+        if (w >= 64 && w % 64 == 0 && nb % w == 0) return w;
+    }
+    return nb % 256 == 0 ? 256 : nb;
+}
+
 static int potrf_ll_tc(int64_t n, float* A, int64_t lda, const slt_options& o, int64_t S, FactorCtx& fc,
                        cudaStream_t s, const std::function<int(int64_t, int64_t, cudaStream_t)>& prologue,
                        int panel_sms)
 {
-    const int64_t nb = eff_nb(o);
+    const int64_t nb = potrf_ll_panel_width(o);
     const int tier = o.factor_precision;
     DevBuf bar, L16;
     TRY(bar.alloc(slt_chol_panel_ws_bytes(), s));

@@ -87,16 +87,16 @@ struct DevBuf {
     void reset() { free_now(); }
 };
 
-// A of order n split once into the BF16 digit planes of the tensor-core
+// A of order n split once into the byte digit planes of the tensor-core
 // residual (digit_residual.cu); residual() then forms R = B - A X for up to
-// 16 right-hand sides per call with FP64 accuracy.  The planes take 16 n^2
+// 16 right-hand sides per call with FP64 accuracy.  The planes take 8 n^2
 // bytes (bytes_for); A must not change while they are in use.
 struct DigitMatrix {
-    int64_t n = 0, ldk = 0, rows_pad = 0, pstride = 0;
+    int64_t n = 0, ldk = 0, rows_pad = 0;
     int segs = 1, kb_per_seg = 0, sms = 0;
     bool ready = false;
-    DevBuf planes, rexp, cexp, xplanes, part, status;
-    CUtensorMap mapA, mapX;
+    DevBuf planes, rexp, cexp, xplanes, xsum, part, status;
+    CUtensorMap mapX;
     DigitMatrix() = default;
     DigitMatrix(const DigitMatrix&) = delete;
     DigitMatrix& operator=(const DigitMatrix&) = delete;

@@ -64,6 +64,14 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
                  : "memory");
 }
 
+// Contiguous global -> shared copy (cp.async.bulk): both addresses 16-byte
+// aligned, bytes a multiple of 16; completes on the mbarrier's tx count.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar) : "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -119,6 +127,60 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
     #pragma unroll
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
+
+// tcgen05.mma with A in tensor memory ([atmem]: row m of A in lane m, 16-bit
+// elements packed two per 32-bit column, the lower k in the low half) and B
+// in shared memory (descriptor), kind::f16.
+__device__ __forceinline__ void umma_ta(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
+                 :: "r"(dtmem), "r"(atmem), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
+}
+
+// Warp-converged forms: every lane of the warp executes the call with the
+// same operands and only the lane with lead != 0 issues it.  Keeping the
+// issuing warp converged lets the compiler hold the operands in uniform
+// registers; a loop run by one lane alone recomputes and moves them for every
+// instruction, about 150 clocks per MMA.
+__device__ __forceinline__ void umma_ta_w(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t acc, uint32_t lead)
+{
+    asm volatile("{\n\t.reg .pred p, e;\n\tsetp.ne.b32 p, %4, 0;\n\tsetp.ne.b32 e, %5, 0;\n\t"
+                 "@e tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}"
+                 :: "r"(dtmem), "r"(atmem), "l"(bdesc), "r"(idesc), "r"(acc), "r"(lead) : "memory");
+}
+
+__device__ __forceinline__ void umma_commit_w(uint32_t bar, uint32_t lead)
+{
+    asm volatile("{\n\t.reg .pred e;\n\tsetp.ne.b32 e, %1, 0;\n\t"
+                 "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}"
+                 :: "r"(bar), "r"(lead) : "memory");
+}
+
+// 32 lanes x 16 consecutive 32-bit columns of TMEM from registers (lane l of
+// the warp writes TMEM lane (taddr >> 16) + l); tmem_st_wait() completes them.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+                 "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};"
+                 :: "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+                    "r"(r[7]), "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+                    "r"(r[15])
+                 : "memory");
+}
+
+// 32 lanes x 8 consecutive 32-bit columns of TMEM from registers.
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&r)[8])
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+                 :: "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+                    "r"(r[7])
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
 // 1024 bytes apart (SBO), start address in 16-byte units.

@@ -1,23 +1,30 @@
 """Host model of the tensor-core FP64 residual's arithmetic (digit_residual.cu).
 
-The kernel forms A x from eight balanced base-128 digits of each operand,
-sums the digit products of weight classes w = p + q <= 7 in FP32 over chunks
-of 256 k, folds the class sums into two int64 words and scales the result.
-These tests check, with numpy on the host, the facts the kernel relies on:
+The kernel forms A x from eight balanced base-128 digits of each operand.  The
+digits of A are stored as bytes u = d + 64 and reach the tensor cores as the
+BF16 values d + 192; the kernel sums the digit products of weight classes
+w = p + q <= 7 in FP32 over chunks of 128 k, folds the class sums into two
+int64 words, removes the offset 192 sum_{q<=w} T_q exactly and scales the
+result.  These tests check, with numpy on the host, the facts the kernel
+relies on:
 
 * the split is exact up to its stated remainder: F = round(a' 2^56) taken
   from the bits of the double, a' = sum_p d_p 128^-(p+1) + r, |r| <= 2^-57,
-  |d_p| <= 64 (so every digit is exact in BF16);
-* FP32 class sums over 256 k are exact whatever the order of accumulation
-  (every partial sum is an integer of magnitude <= 2^23);
-* the int64 fold and the final scaling reproduce A x within the bound
-  2^-50 n max_k|a_ik| max_k|x_k| stated in the kernel's header, and in
-  practice within a small multiple of FP64's own rounding.
+  |d_p| <= 64, and the byte fields of F + C7 are the digits plus 64;
+* BF16 0x4300 | u is 128 + u for every byte u in [0, 128], and the byte
+  permute of the kernel makes the two operands of bytes 2j, 2j + 1;
+* FP32 class sums over 128 k of offset operands are exact whatever the order
+  of accumulation (every partial sum is an integer of magnitude <= 2^24);
+* the int64 fold, the offset removal and the final scaling reproduce A x
+  within the bound 2^-50 n max_k|a_ik| max_k|x_k| stated in the kernel's
+  header, and in practice within a small multiple of FP64's own rounding.
 """
 import numpy as np
 import pytest
 
 PLANES = 8
+OFFSET = 192          # BF16 operand of A digit d: d + 192
+C7 = 0x1020408102040  # 64 in each of the seven low base-128 places
 
 
 def _keys(M):
@@ -59,7 +66,7 @@ def _split(M, e):
 
 
 def _digit_product(A, x):
-    """A x (x one column) the way the kernel forms it."""
+    """A x (x one column) the way the kernel forms it: A operands d + 192."""
     n = A.shape[0]
     ea = _keys(A)
     ex = _keys(x.reshape(1, -1))[0]
@@ -67,14 +74,14 @@ def _digit_product(A, x):
     dx, _ = _split(x.reshape(1, -1), np.array([ex]))
     hi = np.zeros(n, dtype=np.int64)
     lo = np.zeros(n, dtype=np.int64)
-    for k0 in range(0, n, 256):
-        sl = slice(k0, min(n, k0 + 256))
+    for k0 in range(0, n, 128):
+        sl = slice(k0, min(n, k0 + 128))
         for w in range(PLANES):
             acc = np.zeros(n, dtype=np.float32)
             for p in range(w + 1):
                 q = w - p
                 # the products are exact in FP32; accumulate term by term
-                prod = (da[p][:, sl] * dx[q][0, sl]).astype(np.float32)
+                prod = ((da[p][:, sl] + OFFSET) * dx[q][0, sl]).astype(np.float32)
                 for j in range(prod.shape[1]):
                     acc = acc + prod[:, j]
             S = acc.astype(np.int64)
@@ -82,10 +89,61 @@ def _digit_product(A, x):
                 hi += S * (1 << (7 * (3 - w)))
             else:
                 lo += S * (1 << (7 * (7 - w)))
+    # offset removal: class w carries 192 sum_{q<=w} T_q, T_q = sum_k dx_q
+    T = [int(dx[q].astype(np.int64).sum()) for q in range(PLANES)]
+    pre = 0
+    for w in range(PLANES):
+        pre += T[w]
+        if w < 4:
+            hi -= OFFSET * pre * (1 << (7 * (3 - w)))
+        else:
+            lo -= OFFSET * pre * (1 << (7 * (7 - w)))
     e = ea + ex
     yh = hi.astype(np.float64)
     lo = lo + (hi - yh.astype(np.int64)) * (1 << 28)
     return np.ldexp(yh, e - 35) + np.ldexp(lo.astype(np.float64), e - 63)
+
+
+def _bf16(bits):
+    """BF16 bit patterns (uint16) as float64."""
+    return (np.asarray(bits, dtype=np.uint32) << np.uint32(16)).view(np.float32).astype(np.float64)
+
+
+def _byte_perm(x, y, sel):
+    """CUDA's __byte_perm(x, y, sel) (default mode) on uint32 arrays."""
+    b = [(np.uint64(x) >> np.uint64(8 * i)) & np.uint64(0xFF) for i in range(4)] + \
+        [(np.uint64(y) >> np.uint64(8 * i)) & np.uint64(0xFF) for i in range(4)]
+    out = np.uint64(0)
+    for i in range(4):
+        out |= b[(sel >> (4 * i)) & 7] << np.uint64(8 * i)
+    return int(out)
+
+
+def test_bf16_operand_of_a_byte():
+    u = np.arange(129, dtype=np.uint32)
+    assert np.array_equal(_bf16(0x4300 | u), 128.0 + u)
+    rng = np.random.default_rng(3)
+    for w in rng.integers(0, 129, size=(50, 4)):
+        word = int(w[0] | (w[1] << 8) | (w[2] << 16) | (w[3] << 24))
+        o0 = _byte_perm(word, 0x43434343, 0x4140)
+        o1 = _byte_perm(word, 0x43434343, 0x4342)
+        vals = _bf16([o0 & 0xFFFF, o0 >> 16, o1 & 0xFFFF, o1 >> 16])
+        assert np.array_equal(vals, 128.0 + w)          # lower k in the low half
+
+
+def test_digit_bytes_are_the_fields_of_f_plus_c7():
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((16, 200)) * np.ldexp(1.0, rng.integers(-30, 30, size=(16, 1)))
+    A[2, 3] = 0.5 - 2.0 ** -54
+    e = _keys(A)
+    d, F = _split(A, e)
+    G = F + C7
+    for p in range(1, PLANES):
+        assert np.array_equal((G >> (7 * (PLANES - 1 - p))) & 127, d[p].astype(np.int64) + 64)
+    assert np.array_equal((G >> 49) + 64, d[0].astype(np.int64) + 64)
+    for p in range(PLANES):
+        u = d[p] + 64
+        assert u.min() >= 0 and u.max() <= 128
 
 
 def test_split_is_exact_up_to_remainder():
@@ -109,15 +167,15 @@ def test_split_is_exact_up_to_remainder():
 
 
 def test_fp32_class_sums_are_exact_at_the_limit():
-    # every digit at its extreme: 256 k x 8 pairs x 64 x 64 = 2^23
-    prod = np.full(256 * 8, 64.0 * 64.0, dtype=np.float32)
+    # every operand at its extreme: 128 k x 8 pairs x 256 x 64 = 2^24
+    prod = np.full(128 * 8, 256.0 * 64.0, dtype=np.float32)
     acc = np.float32(0)
     for v in prod:
         acc = np.float32(acc + v)
-    assert int(acc) == 256 * 8 * 4096 == 2 ** 23
-    # alternating signs and magnitudes: every order gives the integer sum
+    assert int(acc) == 128 * 8 * 256 * 64 == 2 ** 24
+    # mixed signs and magnitudes: every order gives the integer sum
     rng = np.random.default_rng(2)
-    vals = (rng.integers(-64, 65, 2048) * rng.integers(-64, 65, 2048)).astype(np.float32)
+    vals = (rng.integers(128, 257, 1024) * rng.integers(-64, 65, 1024)).astype(np.float32)
     for _ in range(3):
         rng.shuffle(vals)
         a = np.float32(0)
