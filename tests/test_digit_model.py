@@ -3,9 +3,9 @@
 The kernel forms A x from eight balanced base-128 digits of each operand.  The
 digits of A are stored as bytes u = d + 64 and reach the tensor cores as the
 BF16 values d + 192; the kernel sums the digit products of weight classes
-w = p + q <= 7 in FP32 over chunks of 128 k, folds the class sums into two
-int64 words, removes the offset 192 sum_{q<=w} T_q exactly and scales the
-result.  These tests check, with numpy on the host, the facts the kernel
+w = p + q <= 7 in two FP32 accumulators (A planes 0-3 and 4-7) over chunks
+of 256 k, folds the class sums into two int64 words, removes the offset
+192 sum_{q<=w} T_q exactly and scales the result.  These tests check, with numpy on the host, the facts the kernel
 relies on:
 
 * the split is exact up to its stated remainder: F = round(a' 2^56) taken
@@ -13,8 +13,9 @@ relies on:
   |d_p| <= 64, and the byte fields of F + C7 are the digits plus 64;
 * BF16 0x4300 | u is 128 + u for every byte u in [0, 128], and the byte
   permute of the kernel makes the two operands of bytes 2j, 2j + 1;
-* FP32 class sums over 128 k of offset operands are exact whatever the order
-  of accumulation (every partial sum is an integer of magnitude <= 2^24);
+* FP32 class sums over 256 k of offset operands, at most four digit pairs
+  per class and accumulator, are exact whatever the order of accumulation
+  (every partial sum is an integer of magnitude <= 2^24);
 * the int64 fold, the offset removal and the final scaling reproduce A x
   within the bound 2^-50 n max_k|a_ik| max_k|x_k| stated in the kernel's
   header, and in practice within a small multiple of FP64's own rounding.
@@ -74,17 +75,21 @@ def _digit_product(A, x):
     dx, _ = _split(x.reshape(1, -1), np.array([ex]))
     hi = np.zeros(n, dtype=np.int64)
     lo = np.zeros(n, dtype=np.int64)
-    for k0 in range(0, n, 128):
-        sl = slice(k0, min(n, k0 + 128))
+    for k0 in range(0, n, 256):
+        sl = slice(k0, min(n, k0 + 256))
         for w in range(PLANES):
-            acc = np.zeros(n, dtype=np.float32)
-            for p in range(w + 1):
-                q = w - p
-                # the products are exact in FP32; accumulate term by term
-                prod = ((da[p][:, sl] + OFFSET) * dx[q][0, sl]).astype(np.float32)
-                for j in range(prod.shape[1]):
-                    acc = acc + prod[:, j]
-            S = acc.astype(np.int64)
+            S = np.zeros(n, dtype=np.int64)
+            for planes in (range(0, 4), range(4, 8)):         # the two accumulators
+                acc = np.zeros(n, dtype=np.float32)
+                for p in planes:
+                    if p > w:
+                        continue
+                    q = w - p
+                    # the products are exact in FP32; accumulate term by term
+                    prod = ((da[p][:, sl] + OFFSET) * dx[q][0, sl]).astype(np.float32)
+                    for j in range(prod.shape[1]):
+                        acc = acc + prod[:, j]
+                S += acc.astype(np.int64)
             if w < 4:
                 hi += S * (1 << (7 * (3 - w)))
             else:
@@ -167,12 +172,12 @@ def test_split_is_exact_up_to_remainder():
 
 
 def test_fp32_class_sums_are_exact_at_the_limit():
-    # every operand at its extreme: 128 k x 8 pairs x 256 x 64 = 2^24
-    prod = np.full(128 * 8, 256.0 * 64.0, dtype=np.float32)
+    # every operand at its extreme: 256 k x 4 pairs x 256 x 64 = 2^24
+    prod = np.full(256 * 4, 256.0 * 64.0, dtype=np.float32)
     acc = np.float32(0)
     for v in prod:
         acc = np.float32(acc + v)
-    assert int(acc) == 128 * 8 * 256 * 64 == 2 ** 24
+    assert int(acc) == 256 * 4 * 256 * 64 == 2 ** 24
     # mixed signs and magnitudes: every order gives the integer sum
     rng = np.random.default_rng(2)
     vals = (rng.integers(128, 257, 1024) * rng.integers(-64, 65, 1024)).astype(np.float32)
