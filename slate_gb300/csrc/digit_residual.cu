@@ -20,18 +20,14 @@
 //  * a' x' = sum_w S_w 128^-(w+2) with S_w = sum_k sum_{p+q=w} d_p d_q; the
 //    weight classes w >= 8 lie below 2^-53 of the product scale and are
 //    dropped, so 8 classes remain;
-//  * the operands of the tensor cores are the BF16 values d + 192 of the A
-//    digits (d in [-64, 64], so 128 <= d + 192 <= 256) and the digits of X;
-//    they form the class sums of one chunk of 256 k in two FP32 accumulators
-//    (A planes 0-3 and 4-7), each taking at most four digit pairs per class:
-//    every product is an integer of magnitude <= 256 * 64 = 2^14 and every
-//    partial sum at most 256 * 4 * 2^14 = 2^24, so FP32 accumulation is
-//    exact in any order;
+//  * the tensor cores form the class sums of one chunk of 1024 k in two FP32
+//    accumulators (A planes 0-3 and 4-7), each taking at most four digit
+//    pairs per class: every product is an integer of magnitude <= 2^12 and
+//    every partial sum at most 1024 * 4 * 2^12 = 2^24, so FP32 accumulation
+//    is exact in any order;
 //  * per chunk the epilogue folds the class sums exactly into two int64
 //    words, hi = sum_{w<4} S_w 2^(7(3-w)) and lo = sum_{w>=4} S_w 2^(7(7-w));
-//    split-K segments add in int64 (exact); the last kernel removes the
-//    offset, 192 sum_{q<=w} T_q(c) in class w with T_q(c) the sum of digit q
-//    of column c of X over all k (exact integers), and forms
+//    split-K segments add in int64 (exact), and the last kernel forms
 //    r = (b - hi 2^(e-35)) - lo 2^(e-63), e = ea_i + ex_c.
 //
 // The computed A x differs from the exact one by at most about
@@ -52,17 +48,18 @@
 // The MMA.  A CTA takes a 128-row block of A and a K segment.  Per 64 k, warp
 // 0 loads the 64 KB byte tile of A with one bulk copy (three stages) and warp
 // 10 the X digit tile (128 x 64 BF16, 128-byte swizzle) with TMA (two
-// stages), each running ahead on its own ring.  Warps 6-9 (one
-// TMEM lane quarter each; thread = row) turn the bytes into the BF16 operand
-// in tensor memory: BF16 0x4300 | u is exactly 128 + u = d + 192 for every
-// u in [0, 128] (u = 128 carries into the exponent: 0x4380 = 256), so one
-// byte permute makes two operands, stored with tcgen05.st.  Warp 1 issues,
+// stages), each running ahead on its own ring.  Warps 6-9 (one TMEM lane
+// quarter each; thread = row) turn the bytes into the BF16 digits
+// in tensor memory: BF16 0x4300 | u is exactly 128 + u for every u in
+// [0, 128] (u = 128 carries into the exponent: 0x4380 = 256), so one byte
+// permute and one exact BF16x2 subtraction of 192 make two digits, stored
+// with tcgen05.st.  Warp 1 issues,
 // per 16 k and plane p, tcgen05.mma M128 N(128 - 16 p) K16 with A from
 // tensor memory and B = X planes 0 .. 7 - p, accumulating class w = p + q
 // into column 16 w + c of D_L (planes 0-3) or 16 (w - 4) + c of D_H (planes
 // 4-7): the 36 digit products of weight <= 7 and no others, in two
 // independent accumulator chains issued alternately.  The epilogue (warps
-// 2-5) empties D once per 256 k; the A operand has three 16-k stages.  Every
+// 2-5) empties D once per 1024 k; the A operand has five 16-k stages.  Every
 // mbarrier wait is bounded; on timeout the CTA records SLT_ERR_TIMEOUT,
 // drains its own copies and MMAs, frees its TMEM and returns.
 
@@ -82,27 +79,24 @@ namespace slt {
 constexpr int kDgPlanes = 8;          // digits per operand
 constexpr int kDgBM = 128;            // rows of A per CTA (MMA M)
 constexpr int kDgBK = 64;             // k per stage
-constexpr int kDgChunk = 4;           // k-blocks per accumulator flush (256 k)
+constexpr int kDgChunk = 16;          // k-blocks per accumulator flush (1024 k)
 constexpr int kDgUStages = 3;
 constexpr int kDgXStages = 2;
 constexpr int kDgThreads = 352;
 constexpr int kDgCols = 16;           // right-hand sides per call
-constexpr int kDgOffset = 192;        // the A operand of digit d is d + 192
 constexpr uint32_t kDgUPlane = kDgBM * kDgBK;          // 8 KB: one byte plane, 128 rows x 64 k
 constexpr uint32_t kDgUStage = kDgPlanes * kDgUPlane;  // 64 KB
 constexpr uint32_t kDgXStage = 128 * 128;              // 128 digit rows x 64 k BF16
 // TMEM columns.  The accumulators are D_L (planes 0-3, classes 0-7: 128
-// columns, two buffers at 0 and 128) and D_H (planes 4-7, classes 4-7: 64
-// columns at 256): two independent accumulation chains, since consecutive
-// MMAs into one accumulator run at one per ~130 clocks whatever N <= 128 is.
-// The epilogue empties D_H first, so the next chunk's MMAs wait only for that
-// third of the drain.  The A operand stages (16 k of 8 planes: 64 columns
-// each) fill the other 192 columns.
-constexpr uint32_t kDgTmemL = 128;                     // D_L buffer stride
-constexpr uint32_t kDgTmemH = 256;
-constexpr uint32_t kDgTmemA = 320;
+// columns at 0) and D_H (planes 4-7, classes 4-7: 64 columns at 128): two
+// independent accumulation chains, since consecutive MMAs into one
+// accumulator run at one per ~130 clocks whatever N <= 128 is.  The A
+// operand stages (16 k of 8 planes: 64 columns each) fill the other 320
+// columns, so the operand warps run up to five stages ahead of the MMAs.
+constexpr uint32_t kDgTmemH = 128;
+constexpr uint32_t kDgTmemA = 192;
 constexpr uint32_t kDgTmemAStage = 64;
-constexpr int kDgAStagesT = 3;
+constexpr int kDgAStagesT = 5;
 constexpr int kDgASub = kDgBK / 16;                    // A operand stages per 64 k
 // Exponent keys.  key(v) = 0 for v = 0, 2047 for Inf / NaN, else
 // max(biased exponent of v, 1); keys are monotone in |v|, and for the largest
@@ -311,15 +305,15 @@ dg_split_a_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym,
 }
 
 // Digits of X (n x nrhs, column-major) in BF16: plane q of column c at row
-// 16 q + c of xd (128 rows of ldk), zeros for k >= n and c >= nrhs; and the
-// digit sums T_q(c) over k, added into xsum[16 q + c] (zeroed by the caller;
-// int64 atomics, exact).  grid (ldk / 1024, 16), 256 threads.
+// 16 q + c of xd (128 rows of ldk), zeros for k >= n and c >= nrhs.
+// grid (ldk / 1024, 16), 256 threads.
 __global__ void __launch_bounds__(256)
 dg_split_x_kernel(int64_t n, int nrhs, const double* __restrict__ X, int64_t ldx, const int* __restrict__ cexp,
-                  __nv_bfloat16* xd, int64_t ldk, unsigned long long* xsum)
+                  __nv_bfloat16* xd, int64_t ldk)
 {
     const int c = blockIdx.y;
     const int64_t k = (int64_t(blockIdx.x) * 256 + threadIdx.x) * 4;
+    if (k >= ldk) return;
     const int key = c < nrhs ? cexp[c] : 0;
     int d[4][kDgPlanes];
     #pragma unroll
@@ -332,18 +326,12 @@ dg_split_x_kernel(int64_t n, int nrhs, const double* __restrict__ X, int64_t ldx
     }
     #pragma unroll
     for (int q = 0; q < kDgPlanes; ++q) {
-        if (k < ldk) {
-            const __nv_bfloat162 a = __floats2bfloat162_rn(float(d[0][q]), float(d[1][q]));
-            const __nv_bfloat162 b = __floats2bfloat162_rn(float(d[2][q]), float(d[3][q]));
-            uint2 o;
-            o.x = *reinterpret_cast<const uint32_t*>(&a);
-            o.y = *reinterpret_cast<const uint32_t*>(&b);
-            *reinterpret_cast<uint2*>(xd + int64_t(q * kDgCols + c) * ldk + k) = o;
-        }
-        int sum = d[0][q] + d[1][q] + d[2][q] + d[3][q];
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        if ((threadIdx.x & 31) == 0 && sum != 0)
-            atomicAdd(xsum + q * kDgCols + c, static_cast<unsigned long long>(static_cast<long long>(sum)));
+        const __nv_bfloat162 a = __floats2bfloat162_rn(float(d[0][q]), float(d[1][q]));
+        const __nv_bfloat162 b = __floats2bfloat162_rn(float(d[2][q]), float(d[3][q]));
+        uint2 o;
+        o.x = *reinterpret_cast<const uint32_t*>(&a);
+        o.y = *reinterpret_cast<const uint32_t*>(&b);
+        *reinterpret_cast<uint2*>(xd + int64_t(q * kDgCols + c) * ldk + k) = o;
     }
 }
 
@@ -364,11 +352,20 @@ __device__ __forceinline__ void dg_fail(int* status, volatile int* abort_flag)
     *abort_flag = 1;
 }
 
-// Two BF16 operands 128 + u from bytes 2j, 2j + 1 of w (j = 0, 1).
+// The BF16 digits u - 64 of bytes 2j, 2j + 1 of w (j = 0, 1): the byte
+// permute forms 128 + u, the subtraction of 192 (0x4340) is exact.
+__device__ __forceinline__ uint32_t dg_bf16x2_sub192(uint32_t x)
+{
+    __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162*>(&x);
+    const uint32_t c = 0x43404340u;
+    v = __hsub2(v, *reinterpret_cast<const __nv_bfloat162*>(&c));
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
 __device__ __forceinline__ void dg_expand(uint32_t w, uint32_t& o0, uint32_t& o1)
 {
-    o0 = __byte_perm(w, 0x43434343u, 0x4140);
-    o1 = __byte_perm(w, 0x43434343u, 0x4342);
+    o0 = dg_bf16x2_sub192(__byte_perm(w, 0x43434343u, 0x4140));
+    o1 = dg_bf16x2_sub192(__byte_perm(w, 0x43434343u, 0x4342));
 }
 
 __global__ void __launch_bounds__(kDgThreads, 1)
@@ -382,8 +379,8 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
     const uint32_t u0 = base, x0 = base + US * kDgUStage;
     uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + US * kDgUStage + XS * kDgXStage);
     constexpr int AS = kDgAStagesT;
-    // ufull[US] uempty[US] xfull[XS] xempty[XS] afull[AS] aempty[AS] tfull[2] templ[2] temph fin
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * US + 2 * XS + 2 * AS + 6);
+    // ufull[US] uempty[US] xfull[XS] xempty[XS] afull[AS] aempty[AS] tfull tempty fin
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * US + 2 * XS + 2 * AS + 3);
     __shared__ int s_abort;
     volatile int* abort_flag = &s_abort;
 
@@ -391,7 +388,7 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
     const uint32_t ufull0 = smem_u32(bars), uempty0 = ufull0 + 8 * US;
     const uint32_t xfull0 = uempty0 + 8 * US, xempty0 = xfull0 + 8 * XS;
     const uint32_t afull0 = xempty0 + 8 * XS, aempty0 = afull0 + 8 * AS;
-    const uint32_t tfull0 = aempty0 + 8 * AS, templ0 = tfull0 + 16, temph = templ0 + 16, fin = temph + 8;
+    const uint32_t tfull = aempty0 + 8 * AS, tempty = tfull + 8, fin = tempty + 8;
     const int64_t items = int64_t(a.rb) * a.segs;
 
     if (threadIdx.x == 0) {
@@ -402,8 +399,8 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
             mbar_init(afull0 + 8 * b, 4);
             mbar_init(aempty0 + 8 * b, 1);
         }
-        for (int b = 0; b < 2; ++b) { mbar_init(tfull0 + 8 * b, 1); mbar_init(templ0 + 8 * b, 4); }
-        mbar_init(temph, 4);
+        mbar_init(tfull, 1);
+        mbar_init(tempty, 4);
         mbar_init(fin, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -468,12 +465,10 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
             const int seg = int(t / a.rb);
             const int kb0 = seg * a.kb_per_seg, kb1 = min(a.kb_total, kb0 + a.kb_per_seg);
             for (int kc = kb0; kc < kb1 && ok; kc += kDgChunk, ++lt) {
-                const int buf = int(lt & 1);
-                ok = __all_sync(0xffffffffu, mbar_wait(templ0 + 8 * buf, uint32_t((lt >> 1) & 1) ^ 1u) &&
-                                                 mbar_wait(temph, uint32_t(lt & 1) ^ 1u) && !*abort_flag);
+                ok = __all_sync(0xffffffffu, mbar_wait(tempty, uint32_t(lt & 1) ^ 1u) && !*abort_flag);
                 if (!ok) break;
                 tc_fence_after();
-                const uint32_t tl = taddr + uint32_t(buf) * kDgTmemL;
+                const uint32_t tl = taddr;
                 const int kend = min(kb1, kc + kDgChunk);
                 for (int kb = kc; kb < kend && ok; ++kb) {
                     ok = __all_sync(0xffffffffu, mbar_wait(xfull0 + 8 * xs, xph) && !*abort_flag);
@@ -504,7 +499,7 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
                     if (++xs == XS) { xs = 0; xph ^= 1u; }
                 }
                 if (!ok) break;
-                umma_commit_w(tfull0 + 8 * buf, lead);
+                umma_commit_w(tfull, lead);
             }
         }
         if (!ok && lane == 0) dg_fail(a.status, abort_flag);
@@ -581,8 +576,7 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
             #pragma unroll
             for (int c = 0; c < kDgCols; ++c) { hi[c] = 0; lo[c] = 0; }
             for (int kc = kb0; kc < kb1; kc += kDgChunk, ++lt) {
-                const int buf = int(lt & 1);
-                bool ready = mbar_wait(tfull0 + 8 * buf, uint32_t((lt >> 1) & 1));
+                bool ready = mbar_wait(tfull, uint32_t(lt & 1));
                 ready = __all_sync(0xffffffffu, ready && !*abort_flag);
                 if (!ready) {
                     if (lane == 0) dg_fail(a.status, abort_flag);
@@ -592,17 +586,10 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
                 tc_fence_after();
                 const uint32_t tq = taddr + (uint32_t(q * 32) << 16);
                 #pragma unroll 1
-                for (int g = 0; g < 6; ++g) {     // D_H classes 4 .. 7 (g < 2), then D_L classes 2h, 2h + 1
-                    const int h = g < 2 ? g + 2 : g - 2;
-                    if (g == 2) {
-                        // D_H is read: the next chunk's MMAs may start
-                        tc_fence_before();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(temph);
-                    }
+                for (int g = 0; g < 6; ++g) {     // D_L classes 2h, 2h + 1 (g = h < 4), then D_H classes 4 .. 7
+                    const int h = g < 4 ? g : g - 2;
                     float v[32];
-                    tmem_ld32(tq + (g < 2 ? kDgTmemH + uint32_t(g * 32) : uint32_t(buf) * kDgTmemL + uint32_t(h * 32)),
-                              v);
+                    tmem_ld32(tq + (g < 4 ? uint32_t(h * 32) : kDgTmemH + uint32_t((g - 4) * 32)), v);
                     // class w weighs 2^(7(3-w)) in hi (w < 4), 2^(7(7-w)) in lo
                     const long long m0 = (h & 1) ? (1ll << 7) : (1ll << 21);
                     const long long m1 = (h & 1) ? 1ll : (1ll << 14);
@@ -617,7 +604,7 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
                 }
                 tc_fence_before();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(templ0 + 8 * buf);
+                if (lane == 0) mbar_arrive(tempty);
             }
             if (!ok) break;
             const int64_t r = int64_t(row0) + q * 32 + lane;
@@ -636,34 +623,21 @@ dg_gemm_kernel(const __grid_constant__ CUtensorMap mapX, DgArgs a)
 }
 
 // R(i, c) = B(i, c) - sum over segments of (hi 2^(e-35) + lo 2^(e-63)),
-// e = ea_i + ex_c, after removing the operand offset of the A digits:
-// 192 sum_{q<=w} T_q(c) from class w, folded like the class sums.  NaN where
-// row i of A or column c of X holds Inf / NaN.  grid (ceil(n / 256), nrhs).
+// e = ea_i + ex_c; NaN where row i of A or column c of X holds Inf / NaN.
+// grid (ceil(n / 256), nrhs).
 __global__ void __launch_bounds__(256)
 dg_reduce_kernel(int64_t n, int64_t rows_pad, int segs, const long long* __restrict__ part,
-                 const int* __restrict__ rexp, const int* __restrict__ cexp,
-                 const unsigned long long* __restrict__ xsum, const double* __restrict__ B, int64_t ldb,
-                 double* R, int64_t ldr)
+                 const int* __restrict__ rexp, const int* __restrict__ cexp, const double* __restrict__ B,
+                 int64_t ldb, double* R, int64_t ldr)
 {
     const int64_t i = int64_t(blockIdx.x) * 256 + threadIdx.x;
     const int c = blockIdx.y;
     if (i >= n) return;
-    // sums in unsigned (two's complement) arithmetic: the offset-carrying
-    // partial words and the offset itself are exact modulo 2^64, and the
-    // difference is the true, representable value
-    unsigned long long hi = 0, lo = 0;
+    long long hi = 0, lo = 0;
     for (int s = 0; s < segs; ++s) {
         const long long* p = part + (int64_t(s) * 2 * kDgCols + c) * rows_pad + i;
-        hi += static_cast<unsigned long long>(p[0]);
-        lo += static_cast<unsigned long long>(p[int64_t(kDgCols) * rows_pad]);
-    }
-    unsigned long long pre = 0;
-    #pragma unroll
-    for (int w = 0; w < kDgPlanes; ++w) {
-        pre += xsum[w * kDgCols + c];
-        const unsigned long long off = pre * unsigned(kDgOffset);
-        if (w < 4) hi -= off << (7 * (3 - w));
-        else lo -= off << (7 * (7 - w));
+        hi += p[0];
+        lo += p[int64_t(kDgCols) * rows_pad];
     }
     double r;
     if (rexp[i] == kDgBadKey || cexp[c] == kDgBadKey) {
@@ -671,12 +645,10 @@ dg_reduce_kernel(int64_t n, int64_t rows_pad, int segs, const long long* __restr
     }
     else {
         const int e = dg_scale(rexp[i]) + dg_scale(cexp[c]);
-        const long long hs = static_cast<long long>(hi);
-        long long ls = static_cast<long long>(lo);
-        const double yh = double(hs);
-        // hs - yh is exact in int64 whenever |yh| < 2^62; fold it into lo
-        if (fabs(yh) < 4.611686018427387904e18) ls += (hs - (long long) yh) * (1ll << 28);
-        r = (B[i + c * ldb] - ldexp(yh, e - 35)) - ldexp(double(ls), e - 63);
+        const double yh = double(hi);
+        // hi - yh is exact in int64 whenever |yh| < 2^62; fold it into lo
+        if (fabs(yh) < 4.611686018427387904e18) lo += (hi - (long long) yh) * (1ll << 28);
+        r = (B[i + c * ldb] - ldexp(yh, e - 35)) - ldexp(double(lo), e - 63);
     }
     R[i + c * ldr] = r;
 }
@@ -713,7 +685,6 @@ void DigitMatrix::release()
     rexp.reset();
     cexp.reset();
     xplanes.reset();
-    xsum.reset();
     part.reset();
     status.reset();
     ready = false;
@@ -737,7 +708,6 @@ int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cuda
     TRY(rexp.alloc(sizeof(int) * size_t(rows_pad), s));
     TRY(cexp.alloc(sizeof(int) * kDgCols, s));
     TRY(xplanes.alloc(size_t(kDgPlanes) * kDgCols * size_t(ldk) * 2, s));
-    TRY(xsum.alloc(sizeof(unsigned long long) * kDgPlanes * kDgCols, s));
     TRY(part.alloc(size_t(segs) * 2 * kDgCols * size_t(rows_pad) * sizeof(long long), s));
     TRY(status.alloc(sizeof(int), s));
     SLT_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(int), s));
@@ -780,13 +750,12 @@ int DigitMatrix::residual(int64_t nrhs, const double* B, int64_t ldb, const doub
                                                   int(dg_smem_bytes())));
     }));
     SLT_CUDA_TRY(cudaMemsetAsync(cexp.p, 0, sizeof(int) * kDgCols, s));
-    SLT_CUDA_TRY(cudaMemsetAsync(xsum.p, 0, sizeof(unsigned long long) * kDgPlanes * kDgCols, s));
     const int64_t rps = 16384;
     dg_colkeys_kernel<<<dim3(unsigned(nrhs), unsigned(ceildiv(n, rps))), 256, 0, s>>>(n, X, ldx, rps,
                                                                                     cexp.as<int>());
     count_launch();
     dg_split_x_kernel<<<dim3(unsigned(ceildiv(ldk, 1024)), kDgCols), 256, 0, s>>>(
-        n, int(nrhs), X, ldx, cexp.as<int>(), xplanes.as<__nv_bfloat16>(), ldk, xsum.as<unsigned long long>());
+        n, int(nrhs), X, ldx, cexp.as<int>(), xplanes.as<__nv_bfloat16>(), ldk);
     count_launch();
 
     DgArgs args{planes.as<uint8_t>(), rows_pad, int(rows_pad / kDgBM), int(ldk / kDgBK), kb_per_seg, segs, part.as<long long>(),
@@ -800,8 +769,7 @@ int DigitMatrix::residual(int64_t nrhs, const double* B, int64_t ldb, const doub
     prof_end(pidx, s, 2.0 * double(n) * double(n) * double(nrhs), double(bytes_for(n)));
     SLT_CUDA_TRY(cudaGetLastError());
     dg_reduce_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(nrhs)), 256, 0, s>>>(
-        n, rows_pad, segs, part.as<long long>(), rexp.as<int>(), cexp.as<int>(), xsum.as<unsigned long long>(), B,
-        ldb, R, ldr);
+        n, rows_pad, segs, part.as<long long>(), rexp.as<int>(), cexp.as<int>(), B, ldb, R, ldr);
     count_launch();
     return slt_from_cuda(cudaGetLastError());
 }

@@ -95,7 +95,7 @@ struct DigitMatrix {
     int64_t n = 0, ldk = 0, rows_pad = 0;
     int segs = 1, kb_per_seg = 0, sms = 0;
     bool ready = false;
-    DevBuf planes, rexp, cexp, xplanes, xsum, part, status;
+    DevBuf planes, rexp, cexp, xplanes, part, status;
     CUtensorMap mapX;
     DigitMatrix() = default;
     DigitMatrix(const DigitMatrix&) = delete;

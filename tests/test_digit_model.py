@@ -1,22 +1,23 @@
 """Host model of the tensor-core FP64 residual's arithmetic (digit_residual.cu).
 
 The kernel forms A x from eight balanced base-128 digits of each operand.  The
-digits of A are stored as bytes u = d + 64 and reach the tensor cores as the
-BF16 values d + 192; the kernel sums the digit products of weight classes
-w = p + q <= 7 in two FP32 accumulators (A planes 0-3 and 4-7) over chunks
-of 256 k, folds the class sums into two int64 words, removes the offset
-192 sum_{q<=w} T_q exactly and scales the result.  These tests check, with numpy on the host, the facts the kernel
+digits of A are stored as bytes u = d + 64 and turned back into BF16 digits
+in the kernel (a byte permute to 128 + u, then an exact subtraction of 192);
+the kernel sums the digit products of weight classes w = p + q <= 7 in two
+FP32 accumulators (A planes 0-3 and 4-7) over chunks of 1024 k, folds the
+class sums into two int64 words and scales the result.  These tests check, with numpy on the host, the facts the kernel
 relies on:
 
 * the split is exact up to its stated remainder: F = round(a' 2^56) taken
   from the bits of the double, a' = sum_p d_p 128^-(p+1) + r, |r| <= 2^-57,
   |d_p| <= 64, and the byte fields of F + C7 are the digits plus 64;
-* BF16 0x4300 | u is 128 + u for every byte u in [0, 128], and the byte
-  permute of the kernel makes the two operands of bytes 2j, 2j + 1;
-* FP32 class sums over 256 k of offset operands, at most four digit pairs
-  per class and accumulator, are exact whatever the order of accumulation
-  (every partial sum is an integer of magnitude <= 2^24);
-* the int64 fold, the offset removal and the final scaling reproduce A x
+* BF16 0x4300 | u is 128 + u for every byte u in [0, 128], the byte permute
+  of the kernel makes the two values of bytes 2j, 2j + 1, and subtracting
+  192 gives the digits exactly;
+* FP32 class sums over 1024 k, at most four digit pairs per class and
+  accumulator, are exact whatever the order of accumulation (every partial
+  sum is an integer of magnitude <= 2^24);
+* the int64 fold and the final scaling reproduce A x
   within the bound 2^-50 n max_k|a_ik| max_k|x_k| stated in the kernel's
   header, and in practice within a small multiple of FP64's own rounding.
 """
@@ -24,7 +25,6 @@ import numpy as np
 import pytest
 
 PLANES = 8
-OFFSET = 192          # BF16 operand of A digit d: d + 192
 C7 = 0x1020408102040  # 64 in each of the seven low base-128 places
 
 
@@ -67,7 +67,7 @@ def _split(M, e):
 
 
 def _digit_product(A, x):
-    """A x (x one column) the way the kernel forms it: A operands d + 192."""
+    """A x (x one column) the way the kernel forms it."""
     n = A.shape[0]
     ea = _keys(A)
     ex = _keys(x.reshape(1, -1))[0]
@@ -75,8 +75,8 @@ def _digit_product(A, x):
     dx, _ = _split(x.reshape(1, -1), np.array([ex]))
     hi = np.zeros(n, dtype=np.int64)
     lo = np.zeros(n, dtype=np.int64)
-    for k0 in range(0, n, 256):
-        sl = slice(k0, min(n, k0 + 256))
+    for k0 in range(0, n, 1024):
+        sl = slice(k0, min(n, k0 + 1024))
         for w in range(PLANES):
             S = np.zeros(n, dtype=np.int64)
             for planes in (range(0, 4), range(4, 8)):         # the two accumulators
@@ -86,7 +86,7 @@ def _digit_product(A, x):
                         continue
                     q = w - p
                     # the products are exact in FP32; accumulate term by term
-                    prod = ((da[p][:, sl] + OFFSET) * dx[q][0, sl]).astype(np.float32)
+                    prod = (da[p][:, sl] * dx[q][0, sl]).astype(np.float32)
                     for j in range(prod.shape[1]):
                         acc = acc + prod[:, j]
                 S += acc.astype(np.int64)
@@ -94,19 +94,17 @@ def _digit_product(A, x):
                 hi += S * (1 << (7 * (3 - w)))
             else:
                 lo += S * (1 << (7 * (7 - w)))
-    # offset removal: class w carries 192 sum_{q<=w} T_q, T_q = sum_k dx_q
-    T = [int(dx[q].astype(np.int64).sum()) for q in range(PLANES)]
-    pre = 0
-    for w in range(PLANES):
-        pre += T[w]
-        if w < 4:
-            hi -= OFFSET * pre * (1 << (7 * (3 - w)))
-        else:
-            lo -= OFFSET * pre * (1 << (7 * (7 - w)))
     e = ea + ex
     yh = hi.astype(np.float64)
     lo = lo + (hi - yh.astype(np.int64)) * (1 << 28)
     return np.ldexp(yh, e - 35) + np.ldexp(lo.astype(np.float64), e - 63)
+
+
+def _to_bf16_bits(v):
+    """BF16 bit patterns of float64 values that BF16 holds exactly."""
+    b = np.asarray(v, dtype=np.float32).view(np.uint32)
+    assert np.all(b & 0xFFFF == 0)
+    return b >> np.uint32(16)
 
 
 def _bf16(bits):
@@ -134,6 +132,11 @@ def test_bf16_operand_of_a_byte():
         o1 = _byte_perm(word, 0x43434343, 0x4342)
         vals = _bf16([o0 & 0xFFFF, o0 >> 16, o1 & 0xFFFF, o1 >> 16])
         assert np.array_equal(vals, 128.0 + w)          # lower k in the low half
+        # minus 192 (BF16 0x4340): the digit u - 64, exact in BF16
+        assert _bf16(0x4340) == 192.0
+        d = vals - 192.0
+        assert np.array_equal(d, w.astype(np.float64) - 64)
+        assert np.array_equal(_bf16(_to_bf16_bits(d)), d)
 
 
 def test_digit_bytes_are_the_fields_of_f_plus_c7():
@@ -172,15 +175,15 @@ def test_split_is_exact_up_to_remainder():
 
 
 def test_fp32_class_sums_are_exact_at_the_limit():
-    # every operand at its extreme: 256 k x 4 pairs x 256 x 64 = 2^24
-    prod = np.full(256 * 4, 256.0 * 64.0, dtype=np.float32)
+    # every digit at its extreme: 1024 k x 4 pairs x 64 x 64 = 2^24
+    prod = np.full(1024 * 4, 64.0 * 64.0, dtype=np.float32)
     acc = np.float32(0)
     for v in prod:
         acc = np.float32(acc + v)
-    assert int(acc) == 256 * 4 * 256 * 64 == 2 ** 24
+    assert int(acc) == 1024 * 4 * 64 * 64 == 2 ** 24
     # mixed signs and magnitudes: every order gives the integer sum
     rng = np.random.default_rng(2)
-    vals = (rng.integers(128, 257, 1024) * rng.integers(-64, 65, 1024)).astype(np.float32)
+    vals = (rng.integers(-64, 65, 4096) * rng.integers(-64, 65, 4096)).astype(np.float32)
     for _ in range(3):
         rng.shuffle(vals)
         a = np.float32(0)
