@@ -30,6 +30,8 @@
 // for more, each group owns 4 right-hand sides.
 
 #include "common.cuh"
+
+#include <cstdlib>
 #include "prof.h"
 
 #include <type_traits>
@@ -402,9 +404,13 @@ sweep_kernel(int64_t n, int nrhs, const T* __restrict__ M, int64_t ldm, const T*
 // FP32 sweep for 5 to 16 right-hand sides (the preconditioner of the block
 // FGMRES).  Same ticket order, mailbox and chain step as sweep_kernel; the
 // products with the blocks solved two or more steps earlier differ:
-//  * the tiles stream through a ring of kS16 shared-memory stages filled with
-//    cp.async (zero-filled outside the matrix), so kS16 - 1 tiles are in
-//    flight while one is multiplied;
+//  * every solved block also goes to a row-major copy xr (64 rows x 16
+//    right-hand sides, 4 KB) followed by a release of its done flag; a block
+//    acquires the flag of a solved block and copies its 4 KB with cp.async;
+//  * the tiles and those solved blocks stream through a ring of kS16
+//    shared-memory stages filled with cp.async (tiles zero-filled outside the
+//    matrix), so kS16 - 1 tiles are in flight while one is multiplied, with
+//    one barrier per tile; the mailbox serves only the chain step;
 //  * thread t owns a 4 x 4 register tile -- 4 rows by 4 right-hand sides --
 //    over one quarter (16 columns) of every tile: two 16-byte shared loads per
 //    16 FMAs; the four quarters are added once per block row.
@@ -421,7 +427,73 @@ struct Sweep16Smem {
     float Ws[kSwBS][kSwBS + 1];        // W_i, [row][col]
     float xs[kS16][kSwBS][kSwRhs];     // solved blocks x_k, [row][rhs]
     float xi[kSwBS][kSwRhs];           // this block's right-hand side
+    float xin[kSwBS][kSwRhs];          // x_{i-1} of the chain step
 };
+
+// Thread-block cluster helpers (sm_90+): rank and size, a full cluster
+// barrier, shared-memory addresses of another CTA of the cluster (mapa),
+// stores to them, and remote / cluster-scope mbarrier operations.
+__device__ __forceinline__ uint32_t cluster_ctarank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_nctarank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void st_cluster_u32(uint32_t addr, int v)
+{
+    asm volatile("st.shared::cluster.u32 [%0], %1;" :: "r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster_f4(uint32_t addr, float4 v)
+{
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};"
+                 :: "r"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w) : "memory");
+}
+__device__ __forceinline__ void mbar_init_cta(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t bar_cluster_addr)
+{
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" :: "r"(bar_cluster_addr) : "memory");
+}
+// Bounded wait (two seconds, or a failure recorded in status) for the phase
+// with the given parity of a local mbarrier that CTAs of the cluster arrive on.
+__device__ __forceinline__ bool mbar_wait_cluster(uint32_t bar, uint32_t parity, const int* status)
+{
+    auto try_once = [&]() -> bool {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred P1;\n\t"
+                     "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 P1, [%1], %2;\n\t"
+                     "selp.b32 %0, 1, 0, P1;\n\t}"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        return ok != 0;
+    };
+    if (try_once()) return true;
+    const uint64_t t0 = sw_globaltimer();
+    for (unsigned it = 1; !try_once(); ++it) {
+        if ((it & 63u) == 0 && (ld_volatile_i32(status) != 0 || sw_globaltimer() - t0 > 2000000000ull)) {
+            atomicCAS(const_cast<int*>(status), 0, SLT_ERR_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
 
 __device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, bool valid)
 {
@@ -433,18 +505,30 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ int ld_acquire_i32(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_i32(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" :: "n"(N) : "memory"); }
 
 template <bool FORWARD, bool UNIT, bool TRANS>
 __global__ void __launch_bounds__(256)
 sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, const float* __restrict__ Dinv,
-               float* X, int64_t ldx, int* ticket, unsigned long long* mb, int* status, int vec)
+               float* X, int64_t ldx, int* ticket, unsigned long long* mb, float* xr, int* done, int* status,
+               int vec)
 {
     using MB = Mailbox<float>;
     extern __shared__ __align__(16) unsigned char sw_smem_raw[];
     Sweep16Smem& sm = *reinterpret_cast<Sweep16Smem*>(sw_smem_raw);
-    __shared__ int s_p;
+    __shared__ int s_p, s_dead;
+    __shared__ __align__(8) unsigned long long xin_bar;
     constexpr int XPER = kSwBS * kSwRhs / 256;
     const int t = threadIdx.x;
     const int nblk = int(ceildiv(n, kSwBS));
@@ -467,11 +551,19 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
         return true;
     };
 
-    for (;;) {
-        if (t == 0) s_p = atomicAdd(ticket, 1);
-        __syncthreads();
-        const int p = s_p;
-        if (p >= nblk) break;
+    // cluster: rank crank of csize CTAs; the cluster takes csize consecutive
+    // blocks per ticket, rank r the r-th, and hands x of each block to the
+    // next rank through its shared memory (xin, xin_bar)
+    const uint32_t crank = cluster_ctarank(), csize = cluster_nctarank();
+    const uint32_t bar_local = static_cast<uint32_t>(__cvta_generic_to_shared(&xin_bar));
+    const uint32_t xin_local = static_cast<uint32_t>(__cvta_generic_to_shared(&sm.xin[r][qb]));
+    if (t == 0) {
+        mbar_init_cta(bar_local, 256);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    uint32_t xph = 0;
+
+    auto process = [&](const int p) -> bool {
         const int bi = FORWARD ? p : nblk - 1 - p;
         const int64_t i0 = int64_t(bi) * kSwBS;
         const int ni = int(min64(kSwBS, n - i0));
@@ -546,6 +638,44 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
                 sm.xs[st][e % kSwBS][e / kSwBS] = xv[u];
             }
         };
+        const int K = p > 0 ? p - 1 : 0;      // solved blocks streamed before the chain step
+        // the k-th solved block into ring stage st: its tile of op(M) and, once
+        // its done flag is seen, its 64 x 16 values from xr (thread t: row t / 4,
+        // right-hand sides 4 (t % 4) ..).  Done flags are read 256 blocks at a
+        // time (thread t the (k + t)-th): while all are set, no block waits on a
+        // flag; at the solve front the block waits for the one flag it needs.
+        // Called by every thread with the same k; returns the same value to all.
+        int known = 0;                          // blocks 0 .. known - 1 seen done
+        auto issue = [&](int k, int st) -> bool {
+            issue_tile(k, st);
+            const int bj = FORWARD ? k : nblk - 1 - k;
+            if (k >= known) {
+                const int kk = min(k + t, K - 1);
+                const int v = ld_acquire_i32(done + (FORWARD ? kk : nblk - 1 - kk));
+                if (__syncthreads_and(v != 0)) {
+                    known = min(K, k + 256);
+                }
+                else {
+                    bool okw = true;
+                    if (ld_acquire_i32(done + bj) == 0) {
+                        const uint64_t t0 = sw_globaltimer();
+                        for (unsigned it = 1; ld_acquire_i32(done + bj) == 0; ++it) {
+                            if ((it & 255u) == 0 &&
+                                (ld_volatile_i32(status) != 0 || sw_globaltimer() - t0 > 2000000000ull)) {
+                                atomicCAS(status, 0, SLT_ERR_TIMEOUT);
+                                okw = false;
+                                break;
+                            }
+                        }
+                    }
+                    if (!__syncthreads_and(okw)) return false;
+                    known = k + 1;
+                }
+            }
+            cp_async16(static_cast<uint32_t>(__cvta_generic_to_shared(&sm.xs[st][t >> 2][4 * (t & 3)])),
+                       xr + (int64_t(bj) * kSwBS + (t >> 2)) * kSwRhs + 4 * (t & 3));
+            return true;
+        };
 
         // acc = sum over the blocks solved two or more steps earlier
         float acc[4][4];
@@ -553,26 +683,18 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
         for (int i = 0; i < 4; ++i)
             #pragma unroll
             for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-        const int K = p > 0 ? p - 1 : 0;
-        if (K > 0) {
-            #pragma unroll
-            for (int st = 0; st < kS16 - 1; ++st) {
-                if (st < K) issue_tile(st, st);
-                cp_async_commit();
-            }
-            try_x(0);
-            const bool ok = finish_x(0);
-            put_x(0);
-            if (__syncthreads_or(!ok)) { cp_async_wait<0>(); return; }
+        bool ok = true;
+        #pragma unroll
+        for (int st = 0; st < kS16 - 1; ++st) {
+            if (st < K && ok) ok = issue(st, st);
+            cp_async_commit();
         }
         for (int k = 0; k < K; ++k) {
             const int st = k % kS16;
-            if (k + kS16 - 1 < K) issue_tile(k + kS16 - 1, (k + kS16 - 1) % kS16);
+            cp_async_wait<kS16 - 2>();          // this thread's copies of block k
+            if (__syncthreads_or(!ok)) { cp_async_wait<0>(); return false; }   // everyone's; stage (k - 1) free
+            if (k + kS16 - 1 < K) ok = issue(k + kS16 - 1, (k + kS16 - 1) % kS16);
             cp_async_commit();
-            const bool more = k + 1 < K;
-            if (more) try_x(k + 1);
-            cp_async_wait<kS16 - 1>();          // this thread's copies of tile k
-            __syncthreads();                    // everyone's
             const float* Tt = &sm.Ts[st][0][0];
             if (!TRANS) {
                 #pragma unroll 4
@@ -608,15 +730,11 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
                             for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i][u], xw[u][j], acc[i][j]);
                 }
             }
-            bool ok = true;
-            if (more) {
-                ok = finish_x(k + 1);
-                put_x((k + 1) % kS16);
-            }
-            if (__syncthreads_or(!ok)) { cp_async_wait<0>(); return; }
         }
+        if (__syncthreads_or(!ok)) { cp_async_wait<0>(); return false; }
         cp_async_wait<0>();
-        if (p > 0) try_x(p - 1);       // in flight while y_i is formed
+        const bool from_mailbox = crank == 0;   // else x_{p-1} comes from rank crank - 1
+        if (p > 0 && from_mailbox) try_x(p - 1);       // in flight while y_i is formed
 
         // the four column quarters' partial sums, then z = b_i - acc (in xi)
         float (*red)[kSwBS][kSwRhs] = reinterpret_cast<float (*)[kSwBS][kSwRhs]>(&sm.Ts[0][0][0]);
@@ -639,25 +757,80 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
 
         // chain step: x_i = y_i - W_i x_{i-1}
         if (p > 0) {
-            const bool ok = finish_x(p - 1);
-            put_x(0);
-            if (__syncthreads_or(!ok)) return;
+            bool okc = true;
+            if (from_mailbox) {
+                okc = finish_x(p - 1);
+                #pragma unroll
+                for (int u = 0; u < XPER; ++u) {
+                    const int e = t + 256 * u;
+                    sm.xin[e % kSwBS][e / kSwBS] = xv[u];
+                }
+            }
+            else {
+                okc = mbar_wait_cluster(bar_local, xph, status);
+                xph ^= 1u;
+            }
+            if (__syncthreads_or(!okc)) return false;
             float v[4] = {0.f, 0.f, 0.f, 0.f};
             #pragma unroll 4
-            for (int c = 0; c < kSwBS; ++c) axpy4(sm.Ws[r][c], &sm.xs[0][c][qb], v);
+            for (int c = 0; c < kSwBS; ++c) axpy4(sm.Ws[r][c], &sm.xin[c][qb], v);
             #pragma unroll
             for (int u = 0; u < 4; ++u) y[u] -= v[u];
+        }
+        // x_i: to the next rank's shared memory (its chain step), else to the
+        // mailbox (the next cluster's rank 0); to X; to the row-major copy
+        // (zeros past n), then this block's done flag
+        const float4 yv = r < ni ? make_float4(y[0], y[1], y[2], y[3]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool to_next = crank + 1 < csize;
+        if (to_next && p + 1 < nblk) {
+            st_cluster_f4(mapa_shared(xin_local, crank + 1), yv);
+            mbar_arrive_remote(mapa_shared(bar_local, crank + 1));
         }
         if (r < ni) {
             #pragma unroll
             for (int u = 0; u < 4; ++u)
                 if (qb + u < nrhs) {
-                    MB::put(mbox(i0 + r, qb + u), y[u]);
+                    if (!to_next) MB::put(mbox(i0 + r, qb + u), y[u]);
                     X[i0 + r + (qb + u) * ldx] = y[u];
                 }
         }
+        *reinterpret_cast<float4*>(xr + (int64_t(bi) * kSwBS + r) * kSwRhs + qb) = yv;
+        __threadfence();
         __syncthreads();
+        if (t == 0) st_release_i32(done + bi, 1);
+        return true;
+    };
+
+    for (;;) {
+        // one ticket per cluster, taken by rank 0 and written to every rank
+        cluster_sync_all();
+        if (crank == 0 && t == 0) {
+            const int cp = atomicAdd(ticket, 1);
+            const int dead = ld_volatile_i32(status) != 0;
+            for (uint32_t q = 0; q < csize; ++q) {
+                st_cluster_u32(mapa_shared(static_cast<uint32_t>(__cvta_generic_to_shared(&s_p)), q), cp);
+                st_cluster_u32(mapa_shared(static_cast<uint32_t>(__cvta_generic_to_shared(&s_dead)), q), dead);
+            }
+        }
+        cluster_sync_all();
+        const int p0 = s_p * int(csize);
+        if (p0 >= nblk) break;
+        const int p = p0 + int(crank);
+        if (p < nblk && !s_dead) process(p);
     }
+    // no shared-memory traffic of the cluster may target an exited CTA
+    cluster_sync_all();
+}
+
+// CTAs per cluster of the FP32 16-right-hand-side sweep: SLT_SWEEP_CLUSTER
+// (1, 2, 4 or 8) when set, else 4.
+static int sweep_cluster_size()
+{
+    if (const char* e = std::getenv("SLT_SWEEP_CLUSTER")) {
+        const int v = std::atoi(e);
+        if (v == 1 || v == 2 || v == 4 || v == 8) return v;
+    }
+    return 4;
 }
 
 template <typename T, bool FORWARD, bool UNIT, bool TRANS>
@@ -670,8 +843,13 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     const int64_t npad = nblk * kSwBS;
     // scratch layout: [ticket, pad to 256 B][mailbox: kSwRhs x npad x 2 words]
     // [Dinv: nblk x 64 x 64][W: nblk x 64 x 64] (sized for double)
+    // [xr: npad x kSwRhs floats][done: nblk ints]
     unsigned long long* mb = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(flags) + 256);
     T* Dinv = reinterpret_cast<T*>(reinterpret_cast<char*>(flags) + 256 + size_t(kSwRhs) * npad * 2 * 8);
+    char* tail = reinterpret_cast<char*>(flags) + 256 + size_t(kSwRhs) * npad * 2 * 8 +
+                 2 * size_t(nblk) * kSwBS * kSwBS * sizeof(double);
+    float* xr = reinterpret_cast<float*>(tail);
+    int* done = reinterpret_cast<int*>(tail + size_t(npad) * kSwRhs * sizeof(float));
     const size_t ti_smem = size_t(2) * kSwBS * (kSwBS + 1) * sizeof(T);
     SLT_SMEM_ONCE((trinv_kernel<T, FORWARD, UNIT, TRANS>), ti_smem);
     trinv_kernel<T, FORWARD, UNIT, TRANS><<<unsigned(nblk), 256, ti_smem, s>>>(n, M, ldm, Dinv);
@@ -681,19 +859,37 @@ static int launch_sweep(int64_t n, int64_t nrhs, const T* M, int64_t ldm, T* X, 
     SLT_CUDA_TRY(cudaMemsetAsync(flags, 0, 256 + size_t(nrhs) * size_t(npad) * Mailbox<T>::kWords * 8, s));
     if (std::is_same<T, float>::value && nrhs > 4) {
         // 5 to 16 right-hand sides in FP32: the cp.async / register-tile variant
+        // clusters of sweep_cluster_size() CTAs (consecutive blocks per cluster)
         auto fn16 = sweep16_kernel<FORWARD, UNIT, TRANS>;
         const size_t smem16 = sizeof(Sweep16Smem);
         SLT_SMEM_ONCE(fn16, smem16);
-        int dev = 0, sms = 0, per = 0;
-        SLT_CUDA_TRY(cudaGetDevice(&dev));
-        SLT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        SLT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn16, 256, smem16));
-        const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(nblk, int64_t(sms) * std::max(per, 1)));
         const int vec = (reinterpret_cast<uintptr_t>(M) % 16 == 0) && ((ldm * int64_t(sizeof(T))) % 16 == 0);
+        SLT_CUDA_TRY(cudaMemsetAsync(done, 0, size_t(nblk) * sizeof(int), s));
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = smem16;
+        cfg.stream = s;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        int csize = sweep_cluster_size();
+        int nclusters = 0;
+        for (;; csize /= 2) {
+            attr[0].val.clusterDim.x = unsigned(csize);
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3(unsigned(csize));
+            SLT_CUDA_TRY(cudaOccupancyMaxActiveClusters(&nclusters, fn16, &cfg));
+            if (nclusters > 0 || csize == 1) break;
+        }
+        if (nclusters <= 0) return SLT_ERR_NOT_SUPPORTED;
+        const int64_t grid = std::min<int64_t>(ceildiv(nblk, int64_t(csize)), nclusters) * csize;
+        cfg.gridDim = dim3(unsigned(grid));
         const int pidx = prof_begin(SLT_PROF_SWEEP, s);
-        fn16<<<unsigned(grid), 256, smem16, s>>>(n, int(nrhs), reinterpret_cast<const float*>(M), ldm,
-                                                 reinterpret_cast<const float*>(Dinv), reinterpret_cast<float*>(X),
-                                                 ldx, flags, mb, status, vec);
+        SLT_CUDA_TRY(cudaLaunchKernelEx(&cfg, fn16, n, int(nrhs), reinterpret_cast<const float*>(M), ldm,
+                                        reinterpret_cast<const float*>(Dinv), reinterpret_cast<float*>(X), ldx,
+                                        flags, mb, xr, done, status, vec));
         count_launch();
         prof_end(pidx, s, double(n) * double(n) * double(nrhs), sizeof(T) * (double(n) * double(n) / 2 + 2.0 * n * nrhs));
         return slt_from_cuda(cudaGetLastError());
@@ -754,5 +950,7 @@ extern "C" int slt_ssweep(int kind, int64_t n, int64_t nrhs, const float* M, int
 extern "C" size_t slt_sweep_flags_bytes(int64_t n)
 {
     const int64_t nblk = ceildiv(n, kSwBS);
-    return 256 + size_t(kSwRhs) * size_t(nblk) * kSwBS * 2 * 8 + 2 * size_t(nblk) * kSwBS * kSwBS * sizeof(double);
+    return 256 + size_t(kSwRhs) * size_t(nblk) * kSwBS * 2 * 8 + 2 * size_t(nblk) * kSwBS * kSwBS * sizeof(double) +
+           size_t(nblk) * kSwBS * kSwRhs * sizeof(float) + size_t(nblk) * sizeof(int);
 }
+

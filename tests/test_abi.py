@@ -89,7 +89,8 @@ def test_device_scratch_sizes(slt):
     panel launch (host-only size functions).  Sweep: 256 bytes of ticket,
     a mailbox of 16 right-hand sides x npad rows x two 8-byte words, then
     the 64 x 64 diagonal inverses and chain-step blocks W of every 64-row
-    block, sized for double.  Panel: 512 bytes of counters, then one 64 x 64
+    block, sized for double, then the row-major FP32 copy of the solution
+    (npad x 16) and one done flag per block.  Panel: 512 bytes of counters, then one 64 x 64
     inverse per 64-column step (at most 16), sized for double."""
     L = slt.lib()
     L.slt_sweep_flags_bytes.restype = ctypes.c_size_t
@@ -97,7 +98,8 @@ def test_device_scratch_sizes(slt):
     for n in (1, 63, 64, 65, 16384, 65537):
         nblk = -(-n // 64)
         npad = nblk * 64
-        assert L.slt_sweep_flags_bytes(n) == 256 + 16 * npad * 2 * 8 + 2 * nblk * 64 * 64 * 8
+        assert L.slt_sweep_flags_bytes(n) == (256 + 16 * npad * 2 * 8 + 2 * nblk * 64 * 64 * 8 +
+                                              npad * 16 * 4 + nblk * 4)
     L.slt_chol_panel_ws_bytes.restype = ctypes.c_size_t
     L.slt_chol_panel_ws_bytes.argtypes = []
     assert L.slt_chol_panel_ws_bytes() == 512 + 16 * 64 * 64 * 8
