@@ -117,63 +117,55 @@ __device__ __forceinline__ int dg_scale(int key) { return key == 0 ? 0 : key - 1
 
 // Maximum keys of the rows of A (general: over the whole row; sym, lower
 // storage: over the stored part j <= i and, through the columns, over the
-// part held in column i below the diagonal).  With rsum, also the row sums
-// of |a_ij| over the same full rows (the infinity norm's), added with
-// double atomics (so their last bit depends on the order).  Block: rows
-// I0 .. I0 + 63 and four 64-column tiles from J0.
+// part held in column i below the diagonal), kept with atomicMax on zeroed
+// words.  Block: rows I0 .. I0 + 63 and four 64-column tiles from J0.
 // grid (ceil(n / 256), ceil(n / 64)).
 __global__ void __launch_bounds__(256)
-dg_akeys_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym, int* key, double* rsum)
+dg_akeys_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym, int* key)
 {
     __shared__ int K[64][65];
-    __shared__ double V[64][65];
     const int64_t I0 = int64_t(blockIdx.y) * 64;
     const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
     int rmax = 0;
-    double racc = 0.0;
     for (int t = 0; t < 4; ++t) {
         const int64_t J0 = (int64_t(blockIdx.x) * 4 + t) * 64;
         if (J0 >= n || (sym && J0 > I0)) break;
         for (int kk = ty; kk < 64; kk += 4) {
             const int64_t i = I0 + tx, j = J0 + kk;
-            const double v = (i < n && j < n && !(sym && j > i)) ? A[i + j * lda] : 0.0;
-            K[tx][kk] = dg_key(v);
-            if (rsum) V[tx][kk] = fabs(v);
+            K[tx][kk] = dg_key((i < n && j < n && !(sym && j > i)) ? A[i + j * lda] : 0.0);
         }
         __syncthreads();
         if (threadIdx.x < 64) {
             for (int c = 0; c < 64; ++c) rmax = max(rmax, K[threadIdx.x][c]);
-            if (rsum)
-                for (int c = 0; c < 64; ++c) racc += V[threadIdx.x][c];
         }
         else if (sym && threadIdx.x < 128) {
             const int c = threadIdx.x - 64;
             int cm = 0;
-            double cs = 0.0;
-            for (int r = 0; r < 64; ++r) {
-                cm = max(cm, K[r][c]);
-                if (rsum && I0 + r > J0 + c) cs += V[r][c];       // strictly below the diagonal
-            }
+            for (int r = 0; r < 64; ++r) cm = max(cm, K[r][c]);
             if (cm && J0 + c < n) atomicMax(key + J0 + c, cm);
-            if (rsum && cs != 0.0 && J0 + c < n) atomicAdd(rsum + J0 + c, cs);
         }
         __syncthreads();
     }
-    if (threadIdx.x < 64 && I0 + threadIdx.x < n) {
-        if (rmax) atomicMax(key + I0 + threadIdx.x, rmax);
-        if (rsum && racc != 0.0) atomicAdd(rsum + I0 + threadIdx.x, racc);
-    }
+    if (threadIdx.x < 64 && I0 + threadIdx.x < n && rmax) atomicMax(key + I0 + threadIdx.x, rmax);
 }
 
-// *out = max_i v[i], NaN if any v[i] is NaN.  One block of 1024 threads.
+// ||A||_inf from the split's exact row sums of |F| (F = round(a' 2^56), the
+// fixed-point value of a' = a 2^-e of row i, e = dg_scale(key_i)), kept as
+// two int64 words: sum |F| = h 2^28 + l.  Row sum = h 2^(e - 28) + l 2^(e - 56)
+// (|a| and |F| 2^(e - 56) differ by at most 2^(e - 57)); NaN for a row holding
+// Inf / NaN.  One block of 1024 threads.
 __global__ void __launch_bounds__(1024)
-dg_max_kernel(int64_t n, const double* __restrict__ v, double* out)
+dg_norm_kernel(int64_t n, const int* __restrict__ key, const unsigned long long* __restrict__ sh,
+               const unsigned long long* __restrict__ sl, double* out)
 {
     __shared__ double red[32];
     double m = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += 1024) {
-        const double x = v[i];
-        m = (x > m || x != x) ? x : m;
+        const int k = key[i];
+        double v = 0.0;
+        if (k == kDgBadKey) v = __longlong_as_double(0x7ff8000000000000ll);
+        else if (k) v = ldexp(double(sh[i]), dg_scale(k) - 28) + ldexp(double(sl[i]), dg_scale(k) - 56);
+        m = (v > m || v != v) ? v : m;
     }
     for (int o = 16; o > 0; o >>= 1) {
         const double y = __shfl_xor_sync(0xffffffffu, m, o);
@@ -233,9 +225,10 @@ __device__ __forceinline__ long long dg_fixed(double v, int e)
 // reduction writes NaN for it.
 constexpr long long kDgC7 = 0x1020408102040ll;
 
-__device__ __forceinline__ void dg_digit_bytes(double v, int key, uint32_t (&u)[kDgPlanes])
+__device__ __forceinline__ long long dg_digit_bytes(double v, int key, uint32_t (&u)[kDgPlanes])
 {
-    const long long G = (key == kDgBadKey ? 0 : dg_fixed(v, dg_scale(key))) + kDgC7;
+    const long long F = key == kDgBadKey ? 0 : dg_fixed(v, dg_scale(key));
+    const long long G = F + kDgC7;
     const uint32_t lo = uint32_t(G), hi = uint32_t(static_cast<unsigned long long>(G) >> 32);
     u[7] = lo & 127u;
     u[6] = (lo >> 7) & 127u;
@@ -245,6 +238,7 @@ __device__ __forceinline__ void dg_digit_bytes(double v, int key, uint32_t (&u)[
     u[2] = (hi >> 3) & 127u;
     u[1] = (hi >> 10) & 127u;
     u[0] = uint32_t((int(hi) >> 17) + 64);
+    return F;
 }
 
 // Byte offset of (plane p, row i, k) in the tiled byte planes.
@@ -255,52 +249,81 @@ __device__ __forceinline__ int64_t dg_byte_at(int64_t i, int64_t k, int p, int64
     return tile * kDgUPlane + r * kDgBK + ((((j >> 4) ^ (r >> 1)) & 3) << 4) + (j & 15);
 }
 
-// Byte digit planes of A, the 64 x 64 block (rows I0.., k K0..); A
-// column-major; with sym only its lower
-// triangle is read (element (i, k), k > i, is A(k, i)).  Rows >= n and
-// k >= n get the zero digit (u = 64).  grid (ldk / 64, rows_pad / 64), 256
-// threads.
+// Byte digit planes of A, kDgSplitTiles 64 x 64 blocks along k per CTA (rows
+// I0.., k K0..); A column-major; with sym only its lower triangle is read
+// (element (i, k), k > i, is A(k, i)).  Rows >= n and k >= n get the zero
+// digit (u = 64).  With rsh / rsl (zeroed), also the exact row sums of |F|
+// over k, as sum = rsh 2^28 + rsl (int64 atomics, order-free).
+// grid (ceil(ldk / (64 kDgSplitTiles)), rows_pad / 64), 256 threads.
+constexpr int kDgSplitTiles = 4;
+
 __global__ void __launch_bounds__(256)
 dg_split_a_kernel(int64_t n, const double* __restrict__ A, int64_t lda, int sym, const int* __restrict__ rexp,
-                  uint8_t* planes, int64_t kbt)
+                  uint8_t* planes, int64_t kbt, int64_t ldk, unsigned long long* rsh, unsigned long long* rsl)
 {
     __shared__ double T[64][65];
-    const int64_t I0 = int64_t(blockIdx.y) * 64, K0 = int64_t(blockIdx.x) * 64;
+    const int64_t I0 = int64_t(blockIdx.y) * 64;
     const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;
-    if (sym && K0 > I0) {
-        // strictly above the diagonal: element (i, k) = A(k, i), contiguous in k
-        for (int ii = ty; ii < 64; ii += 4) {
-            const int64_t i = I0 + ii, k = K0 + tx;
-            T[ii][tx] = (i < n && k < n) ? A[k + i * lda] : 0.0;
-        }
-    }
-    else {
-        for (int kk = ty; kk < 64; kk += 4) {
-            const int64_t i = I0 + tx, k = K0 + kk;
-            T[tx][kk] = (i < n && k < n && !(sym && k > i)) ? A[i + k * lda] : 0.0;
-        }
-        if (sym && K0 == I0) {
-            __syncthreads();
-            for (int kk = ty; kk < 64; kk += 4)
-                if (kk > tx) T[tx][kk] = T[kk][tx];
-        }
-    }
-    __syncthreads();
     const int kq = (threadIdx.x & 15) * 4;
-    for (int r = threadIdx.x >> 4; r < 64; r += 16) {
-        const int64_t i = I0 + r;
-        const int key = i < n ? rexp[i] : 0;
-        uint32_t w[kDgPlanes] = {0, 0, 0, 0, 0, 0, 0, 0};
-        #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            uint32_t u[kDgPlanes];
-            dg_digit_bytes(T[r][kq + t], key, u);
-            #pragma unroll
-            for (int p = 0; p < kDgPlanes; ++p) w[p] |= u[p] << (8 * t);
+    unsigned long long sh[4] = {0, 0, 0, 0}, sl[4] = {0, 0, 0, 0};   // rows r0 + 16 m
+    for (int tile = 0; tile < kDgSplitTiles; ++tile) {
+        const int64_t K0 = (int64_t(blockIdx.x) * kDgSplitTiles + tile) * 64;
+        if (K0 >= ldk) break;
+        if (tile) __syncthreads();                 // the previous block's reads of T
+        if (sym && K0 > I0) {
+            // strictly above the diagonal: element (i, k) = A(k, i), contiguous in k
+            for (int ii = ty; ii < 64; ii += 4) {
+                const int64_t i = I0 + ii, k = K0 + tx;
+                T[ii][tx] = (i < n && k < n) ? A[k + i * lda] : 0.0;
+            }
         }
+        else {
+            for (int kk = ty; kk < 64; kk += 4) {
+                const int64_t i = I0 + tx, k = K0 + kk;
+                T[tx][kk] = (i < n && k < n && !(sym && k > i)) ? A[i + k * lda] : 0.0;
+            }
+            if (sym && K0 == I0) {
+                __syncthreads();
+                for (int kk = ty; kk < 64; kk += 4)
+                    if (kk > tx) T[tx][kk] = T[kk][tx];
+            }
+        }
+        __syncthreads();
         #pragma unroll
-        for (int p = 0; p < kDgPlanes; ++p)
-            *reinterpret_cast<uint32_t*>(planes + dg_byte_at(i, K0 + kq, p, kbt)) = w[p];
+        for (int m = 0; m < 4; ++m) {
+            const int r = (threadIdx.x >> 4) + 16 * m;
+            const int64_t i = I0 + r;
+            const int key = i < n ? rexp[i] : 0;
+            uint32_t w[kDgPlanes] = {0, 0, 0, 0, 0, 0, 0, 0};
+            #pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                uint32_t u[kDgPlanes];
+                const long long F = dg_digit_bytes(T[r][kq + t], key, u);
+                const unsigned long long a = static_cast<unsigned long long>(F < 0 ? -F : F);
+                sh[m] += a >> 28;
+                sl[m] += a & ((1ull << 28) - 1);
+                #pragma unroll
+                for (int p = 0; p < kDgPlanes; ++p) w[p] |= u[p] << (8 * t);
+            }
+            #pragma unroll
+            for (int p = 0; p < kDgPlanes; ++p)
+                *reinterpret_cast<uint32_t*>(planes + dg_byte_at(i, K0 + kq, p, kbt)) = w[p];
+        }
+    }
+    if (rsh) {
+        // the 16 threads of a row are 16 consecutive lanes
+        #pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            for (int o = 8; o > 0; o >>= 1) {
+                sh[m] += __shfl_xor_sync(0xffffffffu, sh[m], o);
+                sl[m] += __shfl_xor_sync(0xffffffffu, sl[m], o);
+            }
+            const int64_t i = I0 + (threadIdx.x >> 4) + 16 * m;
+            if ((threadIdx.x & 15) == 0 && i < n && (sh[m] | sl[m])) {
+                atomicAdd(rsh + i, sh[m]);
+                atomicAdd(rsl + i, sl[m]);
+            }
+        }
     }
 }
 
@@ -713,23 +736,27 @@ int DigitMatrix::prepare(int64_t n_, const double* A, int64_t lda, int sym, cuda
     SLT_CUDA_TRY(cudaMemsetAsync(status.p, 0, sizeof(int), s));
     SLT_CUDA_TRY(cudaMemsetAsync(rexp.p, 0, sizeof(int) * size_t(rows_pad), s));
 
-    // row keys (and the row sums of |A| for the infinity norm): one pass over
-    // the stored part of A
-    DevBuf rs;
+    // row keys: one pass over the stored part of A (integer work only)
+    dg_akeys_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(ceildiv(n, 64))), 256, 0, s>>>(n, A, lda, sym,
+                                                                                          rexp.as<int>());
+    count_launch();
+    // the split also sums |F| per row, for the infinity norm
+    DevBuf rsh, rsl;
     if (d_norm) {
-        TRY(rs.alloc(sizeof(double) * size_t(n), s));
-        SLT_CUDA_TRY(cudaMemsetAsync(rs.p, 0, sizeof(double) * size_t(n), s));
+        TRY(rsh.alloc(sizeof(unsigned long long) * size_t(n), s));
+        TRY(rsl.alloc(sizeof(unsigned long long) * size_t(n), s));
+        SLT_CUDA_TRY(cudaMemsetAsync(rsh.p, 0, sizeof(unsigned long long) * size_t(n), s));
+        SLT_CUDA_TRY(cudaMemsetAsync(rsl.p, 0, sizeof(unsigned long long) * size_t(n), s));
     }
-    dg_akeys_kernel<<<dim3(unsigned(ceildiv(n, 256)), unsigned(ceildiv(n, 64))), 256, 0, s>>>(
-        n, A, lda, sym, rexp.as<int>(), d_norm ? rs.as<double>() : nullptr);
+    dg_split_a_kernel<<<dim3(unsigned(ceildiv(ldk, int64_t(64 * kDgSplitTiles))), unsigned(rows_pad / 64)), 256, 0, s>>>(
+        n, A, lda, sym, rexp.as<int>(), planes.as<uint8_t>(), ldk / kDgBK, ldk,
+        d_norm ? rsh.as<unsigned long long>() : nullptr, d_norm ? rsl.as<unsigned long long>() : nullptr);
     count_launch();
     if (d_norm) {
-        dg_max_kernel<<<1, 1024, 0, s>>>(n, rs.as<double>(), d_norm);
+        dg_norm_kernel<<<1, 1024, 0, s>>>(n, rexp.as<int>(), rsh.as<unsigned long long>(),
+                                           rsl.as<unsigned long long>(), d_norm);
         count_launch();
     }
-    dg_split_a_kernel<<<dim3(unsigned(ldk / 64), unsigned(rows_pad / 64)), 256, 0, s>>>(
-        n, A, lda, sym, rexp.as<int>(), planes.as<uint8_t>(), ldk / kDgBK);
-    count_launch();
     SLT_CUDA_TRY(cudaGetLastError());
 
     TRY(tma_map_2d(&mapX, xplanes.p, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, ldk, int64_t(kDgPlanes) * kDgCols,
