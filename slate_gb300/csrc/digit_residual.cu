@@ -815,16 +815,26 @@ int DigitMatrix::check_status(cudaStream_t s)
 using namespace slt;
 
 // One-shot digit residual (prepare, one product, status): R = B - A X for
-// nrhs <= 16, A of order n (sym_lower: symmetric, lower storage).  The
-// drivers keep the digit planes for a whole solve instead.
+// nrhs <= 16, A of order n (sym_lower: symmetric, lower storage); with
+// d_norm (device, optional), also ||A||_inf from the split's exact integer
+// row sums -- the norm the mixed solvers' stopping test uses.  The drivers
+// keep the digit planes for a whole solve instead.
+extern "C" int slt_dresidual_digits_norm(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower,
+                                         const double* B, int64_t ldb, const double* X, int64_t ldx, double* R,
+                                         int64_t ldr, double* d_norm, cudaStream_t stream)
+{
+    if (n < 0 || nrhs < 0 || nrhs > kDgCols) return SLT_ERR_ARG;
+    if (n == 0) return d_norm ? slt_from_cuda(cudaMemsetAsync(d_norm, 0, sizeof(double), stream)) : SLT_OK;
+    if (nrhs == 0 && !d_norm) return SLT_OK;
+    DigitMatrix dm;
+    TRY(dm.prepare(n, A, lda, sym_lower, stream, d_norm));
+    if (nrhs) TRY(dm.residual(nrhs, B, ldb, X, ldx, R, ldr, stream));
+    return dm.check_status(stream);
+}
+
 extern "C" int slt_dresidual_digits(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower,
                                     const double* B, int64_t ldb, const double* X, int64_t ldx, double* R,
                                     int64_t ldr, cudaStream_t stream)
 {
-    if (n < 0 || nrhs < 0 || nrhs > kDgCols) return SLT_ERR_ARG;
-    if (n == 0 || nrhs == 0) return SLT_OK;
-    DigitMatrix dm;
-    TRY(dm.prepare(n, A, lda, sym_lower, stream));
-    TRY(dm.residual(nrhs, B, ldb, X, ldx, R, ldr, stream));
-    return dm.check_status(stream);
+    return slt_dresidual_digits_norm(n, nrhs, A, lda, sym_lower, B, ldb, X, ldx, R, ldr, nullptr, stream);
 }

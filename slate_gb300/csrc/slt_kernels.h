@@ -168,10 +168,15 @@ int slt_dresidual(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym
                   double* R, int64_t ldr, void* ws, cudaStream_t stream);
 /* R = B - A X with FP64 accuracy on the BF16 tensor cores (digit splitting,
  * digit_residual.cu), nrhs <= 16, one call with its own workspace: the
- * drivers keep the digit planes of A for a whole solve instead. */
+ * drivers keep the digit planes of A for a whole solve instead.  The _norm
+ * form also writes ||A||_inf (d_norm, device) from the split's exact integer
+ * row sums. */
 int slt_dresidual_digits(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower,
                          const double* B, int64_t ldb, const double* X, int64_t ldx,
                          double* R, int64_t ldr, cudaStream_t stream);
+int slt_dresidual_digits_norm(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower,
+                              const double* B, int64_t ldb, const double* X, int64_t ldx,
+                              double* R, int64_t ldr, double* d_norm, cudaStream_t stream);
 /* Classical Gram-Schmidt applied twice (CGS2) for the columns of one block
  * FGMRES step (arnoldi.cu).  Column i of the step uses basis slot q[i] of V
  * (slot q: n x R1 doubles at V + q n R1) and its step j[i]: the new vector

@@ -1,7 +1,8 @@
 """The tensor-core FP64 residual (digit_residual.cu) against the exact residual.
 
-slt_dresidual_digits forms R = B - A X from BF16 digit planes of A and X on
-the tcgen05 tensor cores.  Checked here through the C ABI:
+slt_dresidual_digits forms R = B - A X from the digit planes of A (bytes,
+rebuilt into BF16 digits in tensor memory) and the BF16 digits of X on the
+tcgen05 tensor cores.  Checked here through the C ABI:
 
 * accuracy against B - A X in extended precision (np.longdouble) on the
   host: |R - R_exact| <= 2^-50 n max_k|a_ik| max_k|x_kc| + 2^-51 (|b| +
@@ -13,7 +14,9 @@ the tcgen05 tensor cores.  Checked here through the C ABI:
   above n, 1 to 16 right-hand sides, rows spread over 2^+-300, zero rows and
   columns, and a non-finite column of X (NaN in that column of R only);
 * the mixed solvers with residual_engine 2 (tensor cores) against 1 (FP64):
-  both converge to the tester's bound with iteration counts within one.
+  both converge to the tester's bound with iteration counts within one;
+* ||A||_inf from the split's exact integer row sums
+  (slt_dresidual_digits_norm), NaN for a non-finite entry.
 """
 import ctypes
 
@@ -151,3 +154,45 @@ def test_solvers_digit_vs_fp64_residual(orc, slt, chol):
         assert info == 0 and it2 >= 0, (eng, info, it2)
         assert berr(orc, A, to_host(dX), B, sym=bool(chol)) <= 3 * n * EPS, eng
     assert abs(out[1] - out[2]) <= 1, out
+
+
+@pytest.mark.parametrize("n,sym,ld_pad", [(1000, 0, 0), (2100, 1, 3), (4097, 1, 0), (777, 0, 1), (64, 1, 0)])
+def test_digit_split_infinity_norm(slt, n, sym, ld_pad):
+    """||A||_inf from the split's exact integer row sums of the fixed-point
+    digits (slt_dresidual_digits_norm): rows spread over 2^+-300, a zero
+    row, general and symmetric lower storage (the upper triangle holds NaN and
+    must not be read); against the row sums of |A| in extended precision,
+    within the rounding of the fixed-point digits; then a NaN entry makes the
+    norm NaN."""
+    import torch
+    L = slt.lib()
+    f = L.slt_dresidual_digits_norm
+    f.argtypes = [i64, i64, vp, i64, cint, vp, i64, vp, i64, vp, i64, vp, vp]
+    f.restype = cint
+    rng = np.random.default_rng(n + sym)
+    A = rng.standard_normal((n, n)) * np.ldexp(1.0, rng.integers(-300, 300, size=(n, 1)))
+    if sym:
+        A = np.tril(A) + np.tril(A, -1).T        # symmetric: row scales from both triangles
+    A[n // 3, :] = 0.0
+    A[:, n // 3] = 0.0
+    Af = A.copy()
+    if sym:
+        A = np.where(np.tril(np.ones((n, n), dtype=bool)), A, np.nan)
+    ref = float(np.max(np.abs(Af).astype(np.longdouble).sum(axis=1)))
+    lda = n + ld_pad
+    dA = _padded(A, lda)
+    dN = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    s = vp(torch.cuda.current_stream().cuda_stream)
+    assert f(n, 0, dA.data_ptr(), lda, sym, None, n, None, n, None, n, dN.data_ptr(), s) == 0
+    torch.cuda.synchronize()
+    got = float(dN.item())
+    # every |a| enters as |F| 2^(e - 56), |F| = round(|a| 2^(56 - e)): at most
+    # 2^(e - 57) off, and the row's largest entry is >= 2^(e - 2)
+    assert abs(got - ref) <= (n * 2.0 ** -55 + 2.0 ** -50) * ref, (got, ref)
+    # a NaN in the stored part
+    A2 = A.copy()
+    A2[n - 1, n // 2] = np.nan
+    dA2 = _padded(A2, lda)
+    assert f(n, 0, dA2.data_ptr(), lda, sym, None, n, None, n, None, n, dN.data_ptr(), s) == 0
+    torch.cuda.synchronize()
+    assert np.isnan(float(dN.item()))

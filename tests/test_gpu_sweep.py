@@ -7,8 +7,9 @@ diagonally dominant (off-diagonal entries U(-1, 1) / n), so the solution is
 well conditioned and the sweep must match to a few units of its working
 precision: relative error <= 2e-5 (float) / 1e-12 (double).  Sizes cover a
 single row, exact and ragged multiples of the 64-row block, right-hand-side
-counts on both sides of the 4-column split, padded leading dimensions and
-back-to-back launches on one scratch buffer.
+counts on both sides of the 4-column split, padded leading dimensions,
+back-to-back launches on one scratch buffer and every cluster size of the
+FP32 16-right-hand-side sweep.
 """
 import ctypes
 
@@ -103,3 +104,23 @@ def test_sweep_scratch_reuse(slt, dtype):
     assert np.abs(X - Xr).max() / np.abs(Xr).max() <= 4 * TOL[dtype]
     X1r = _reference(2, M, B[:, :2])
     assert np.abs(X1 - X1r).max() / np.abs(X1r).max() <= TOL[dtype]
+
+
+@pytest.mark.parametrize("csize", ["1", "2", "4", "8"])
+@pytest.mark.parametrize("kind", [2, 3, 0, 1])
+@pytest.mark.parametrize("n,nrhs", [(4100, 16), (777, 9), (130, 8), (64, 5)])
+def test_sweep16_cluster_sizes(slt, monkeypatch, csize, kind, n, nrhs):
+    """The FP32 5-16 right-hand-side sweep for every cluster size
+    (SLT_SWEEP_CLUSTER): consecutive blocks inside a cluster pass the chain
+    input through distributed shared memory, across clusters through the
+    mailbox; block counts that are not a multiple of the cluster size leave
+    the last cluster's ranks partly idle."""
+    import torch
+    monkeypatch.setenv("SLT_SWEEP_CLUSTER", csize)
+    uplo, _, _ = KINDS[kind]
+    M = _triangle(n, uplo == "L", 31 * kind + n, np.float32)
+    B = np.random.default_rng(n + kind).uniform(-1, 1, (n, nrhs)).astype(np.float32).astype(np.float64)
+    X, _ = _sweep(slt, torch, kind, M, B, np.float32, ldm_pad=1 if n % 2 else 0)
+    Xr = _reference(kind, M, B)
+    err = np.abs(X - Xr).max() / np.abs(Xr).max()
+    assert err <= TOL[np.float32], (csize, kind, n, nrhs, err)
