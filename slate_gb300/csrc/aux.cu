@@ -647,11 +647,26 @@ extern "C" int slt_dtranspose(int64_t m, int64_t n, const double* A, int64_t lda
 }
 
 // ---------------------------------------------------------------------------
+namespace slt {
+// Column segments of an n x n residual product with nc right-hand sides whose
+// partial sums (nseg x n x nc doubles) must fit in ws_doubles: the usual plan,
+// with the segment count lowered (more 64-column tiles per segment) when it
+// does not fit.  Requires n x nc <= ws_doubles.
+static void plan_segments_fit(int64_t n, int64_t nc, size_t ws_doubles, int64_t* nseg, int64_t* tps)
+{
+    plan_segments(n, n, nseg, tps);
+    const int64_t ktiles = ceildiv(n, 64);
+    const int64_t fit = int64_t(ws_doubles / (size_t(n) * size_t(nc)));
+    if (*nseg > fit) {
+        *tps = ceildiv(ktiles, fit);
+        *nseg = ceildiv(ktiles, *tps);
+    }
+}
+
 // Residual into caller-provided partial-sum scratch (ws_doubles doubles): the
 // column-segment count is lowered until the partial sums fit.  Used by the
 // allocation-free entry point; returns SLT_ERR_LIMIT when a single segment
 // (n x min(nrhs, 16) doubles) does not fit.
-namespace slt {
 int dresidual_into(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sym_lower, const double* B,
                    int64_t ldb, const double* X, int64_t ldx, double* R, int64_t ldr, double* ws,
                    size_t ws_doubles, cudaStream_t stream)
@@ -669,13 +684,7 @@ int dresidual_into(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sy
     for (int64_t c0 = 0; c0 < nrhs; c0 += kMaxRhs) {
         const int64_t nc = std::min<int64_t>(kMaxRhs, nrhs - c0);
         int64_t nseg, tps;
-        plan_segments(n, n, &nseg, &tps);
-        const int64_t ktiles = ceildiv(n, 64);
-        const int64_t fit = int64_t(ws_doubles / (size_t(n) * size_t(nc)));
-        if (nseg > fit) {
-            tps = ceildiv(ktiles, fit);
-            nseg = ceildiv(ktiles, tps);
-        }
+        plan_segments_fit(n, nc, ws_doubles, &nseg, &tps);
         dim3 grid(unsigned(ceildiv(n, 64)), unsigned(nseg));
         int rc = sym_lower ? launch_rowop<0, true>(grid, stream, n, n, int(nc), A, lda, X + c0 * ldx, ldx, tps, ws)
                            : launch_rowop<0, false>(grid, stream, n, n, int(nc), A, lda, X + c0 * ldx, ldx, tps, ws);
@@ -688,3 +697,15 @@ int dresidual_into(int64_t n, int64_t nrhs, const double* A, int64_t lda, int sy
     return SLT_OK;
 }
 } // namespace slt
+
+// The segment plan of the allocation-free residual (host only, for tests):
+// segment count and 64-column tiles per segment for order n, nc <= 16
+// right-hand sides and ws_doubles doubles of scratch.  SLT_ERR_LIMIT when one
+// segment does not fit.
+extern "C" int slt_noalloc_segment_plan(int64_t n, int64_t nc, uint64_t ws_doubles, int64_t* nseg, int64_t* tps)
+{
+    if (n <= 0 || nc <= 0 || nc > 16 || !nseg || !tps) return SLT_ERR_ARG;
+    if (uint64_t(n) * uint64_t(nc) > ws_doubles) return SLT_ERR_LIMIT;
+    slt::plan_segments_fit(n, nc, size_t(ws_doubles), nseg, tps);
+    return SLT_OK;
+}

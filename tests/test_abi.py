@@ -103,3 +103,32 @@ def test_device_scratch_sizes(slt):
     L.slt_chol_panel_ws_bytes.restype = ctypes.c_size_t
     L.slt_chol_panel_ws_bytes.argtypes = []
     assert L.slt_chol_panel_ws_bytes() == 512 + 16 * 64 * 64 * 8
+
+
+def test_noalloc_segment_plan_fits_the_scratch(slt):
+    """The allocation-free residual's column-segment plan (host only): for
+    orders near the 2,097,152-double scratch with 16 right-hand sides the
+    plan lowers the segment count until nseg * n * nc fits, the segments
+    cover every 64-column tile, and one segment too large is refused."""
+    L = slt.lib()
+    f = L.slt_noalloc_segment_plan
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int64),
+                  ctypes.POINTER(ctypes.c_int64)]
+    ws = 2097152
+    lowered = 0
+    for n in (1, 64, 3000, 40000, 60000, 65600, 70000, 100000, 131072):
+        for nc in (1, 4, 16):
+            nseg, tps = ctypes.c_int64(), ctypes.c_int64()
+            rc = f(n, nc, ws, ctypes.byref(nseg), ctypes.byref(tps))
+            if n * nc > ws:
+                assert rc != 0, (n, nc)
+                continue
+            assert rc == 0, (n, nc, rc)
+            ktiles = -(-n // 64)
+            assert nseg.value >= 1 and tps.value >= 1
+            assert nseg.value * n * nc <= ws, (n, nc, nseg.value)
+            assert (nseg.value - 1) * tps.value < ktiles <= nseg.value * tps.value, (n, nc, nseg.value, tps.value)
+            unconstrained = min(ktiles, -(-152 * 8 // -(-n // 64)))
+            lowered += nseg.value < unconstrained
+    assert lowered > 0                        # the lowering branch ran
