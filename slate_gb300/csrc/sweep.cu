@@ -428,6 +428,7 @@ struct Sweep16Smem {
     float xs[kS16][kSwBS][kSwRhs];     // solved blocks x_k, [row][rhs]
     float xi[kSwBS][kSwRhs];           // this block's right-hand side
     float xin[kSwBS][kSwRhs];          // x_{i-1} of the chain step
+    float xin2[kSwBS][kSwRhs];         // x_{i-2}, the last streamed block (from rank r - 2)
 };
 
 // Thread-block cluster helpers (sm_90+): rank and size, a full cluster
@@ -519,7 +520,7 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" :: "n"(N) : "memory"); }
 
 template <bool FORWARD, bool UNIT, bool TRANS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, const float* __restrict__ Dinv,
                float* X, int64_t ldx, int* ticket, unsigned long long* mb, float* xr, int* done, int* status,
                int vec)
@@ -528,7 +529,7 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
     extern __shared__ __align__(16) unsigned char sw_smem_raw[];
     Sweep16Smem& sm = *reinterpret_cast<Sweep16Smem*>(sw_smem_raw);
     __shared__ int s_p, s_dead;
-    __shared__ __align__(8) unsigned long long xin_bar;
+    __shared__ __align__(8) unsigned long long xin_bar[2];
     constexpr int XPER = kSwBS * kSwRhs / 256;
     const int t = threadIdx.x;
     const int nblk = int(ceildiv(n, kSwBS));
@@ -553,15 +554,20 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
 
     // cluster: rank crank of csize CTAs; the cluster takes csize consecutive
     // blocks per ticket, rank r the r-th, and hands x of each block to the
-    // next rank through its shared memory (xin, xin_bar)
+    // next rank through its shared memory (xin, xin_bar[0]) and to the rank
+    // after it (xin2, xin_bar[1]: its last streamed block); the last two
+    // ranks also write the mailbox, for the next cluster's ranks 0 and 1
     const uint32_t crank = cluster_ctarank(), csize = cluster_nctarank();
-    const uint32_t bar_local = static_cast<uint32_t>(__cvta_generic_to_shared(&xin_bar));
+    const uint32_t bar_local = static_cast<uint32_t>(__cvta_generic_to_shared(&xin_bar[0]));
+    const uint32_t bar2_local = static_cast<uint32_t>(__cvta_generic_to_shared(&xin_bar[1]));
     const uint32_t xin_local = static_cast<uint32_t>(__cvta_generic_to_shared(&sm.xin[r][qb]));
+    const uint32_t xin2_local = static_cast<uint32_t>(__cvta_generic_to_shared(&sm.xin2[r][qb]));
     if (t == 0) {
         mbar_init_cta(bar_local, 256);
+        mbar_init_cta(bar2_local, 256);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    uint32_t xph = 0;
+    uint32_t xph = 0, xph2 = 0;
 
     auto process = [&](const int p) -> bool {
         const int bi = FORWARD ? p : nblk - 1 - p;
@@ -644,13 +650,16 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
         // right-hand sides 4 (t % 4) ..).  Done flags are read 256 blocks at a
         // time (thread t the (k + t)-th): while all are set, no block waits on a
         // flag; at the solve front the block waits for the one flag it needs.
-        // Called by every thread with the same k; returns the same value to all.
+        // The last streamed block (k = K - 1, solved two steps before) gets
+        // its values later, from rank r - 2 or the mailbox.  Called by every
+        // thread with the same k; returns the same value to all.
         int known = 0;                          // blocks 0 .. known - 1 seen done
         auto issue = [&](int k, int st) -> bool {
             issue_tile(k, st);
+            if (k == K - 1) return true;
             const int bj = FORWARD ? k : nblk - 1 - k;
             if (k >= known) {
-                const int kk = min(k + t, K - 1);
+                const int kk = min(k + t, K - 2);
                 const int v = ld_acquire_i32(done + (FORWARD ? kk : nblk - 1 - kk));
                 if (__syncthreads_and(v != 0)) {
                     known = min(K, k + 256);
@@ -689,12 +698,32 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
             if (st < K && ok) ok = issue(st, st);
             cp_async_commit();
         }
+        const bool x2_mailbox = crank <= 1;    // x of the last streamed block: mailbox, else rank r - 2
         for (int k = 0; k < K; ++k) {
             const int st = k % kS16;
+            if (k == K - 1 && x2_mailbox) try_x(k);
             cp_async_wait<kS16 - 2>();          // this thread's copies of block k
             if (__syncthreads_or(!ok)) { cp_async_wait<0>(); return false; }   // everyone's; stage (k - 1) free
             if (k + kS16 - 1 < K) ok = issue(k + kS16 - 1, (k + kS16 - 1) % kS16);
             cp_async_commit();
+            if (k == K - 1) {
+                bool okx;
+                if (x2_mailbox) {
+                    okx = finish_x(k);
+                    #pragma unroll
+                    for (int u = 0; u < XPER; ++u) {
+                        const int e = t + 256 * u;
+                        sm.xs[st][e % kSwBS][e / kSwBS] = xv[u];
+                    }
+                }
+                else {
+                    okx = mbar_wait_cluster(bar2_local, xph2, status);
+                    xph2 ^= 1u;
+                    *reinterpret_cast<float4*>(&sm.xs[st][t >> 2][4 * (t & 3)]) =
+                        *reinterpret_cast<const float4*>(&sm.xin2[t >> 2][4 * (t & 3)]);
+                }
+                if (__syncthreads_or(!okx)) { cp_async_wait<0>(); return false; }
+            }
             const float* Tt = &sm.Ts[st][0][0];
             if (!TRANS) {
                 #pragma unroll 4
@@ -786,11 +815,16 @@ sweep16_kernel(int64_t n, int nrhs, const float* __restrict__ M, int64_t ldm, co
             st_cluster_f4(mapa_shared(xin_local, crank + 1), yv);
             mbar_arrive_remote(mapa_shared(bar_local, crank + 1));
         }
+        if (crank + 2 < csize && p + 2 < nblk) {
+            st_cluster_f4(mapa_shared(xin2_local, crank + 2), yv);
+            mbar_arrive_remote(mapa_shared(bar2_local, crank + 2));
+        }
+        const bool to_mailbox = crank + 2 >= csize;
         if (r < ni) {
             #pragma unroll
             for (int u = 0; u < 4; ++u)
                 if (qb + u < nrhs) {
-                    if (!to_next) MB::put(mbox(i0 + r, qb + u), y[u]);
+                    if (to_mailbox) MB::put(mbox(i0 + r, qb + u), y[u]);
                     X[i0 + r + (qb + u) * ldx] = y[u];
                 }
         }
