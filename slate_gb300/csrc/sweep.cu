@@ -28,6 +28,15 @@
 // up to 4 right-hand sides the four thread groups of a block split the 64
 // columns of every product and add their partial sums in shared memory;
 // for more, each group owns 4 right-hand sides.
+//
+// The FP32 kernel for 5 to 16 right-hand sides (sweep16_kernel, the block
+// FGMRES preconditioner) runs in thread-block clusters (4 CTAs by default):
+// a cluster takes consecutive blocks per ticket, and the chain input x_{i-1}
+// and the last streamed block x_{i-2} reach a block through distributed
+// shared memory from ranks r - 1 and r - 2 of its cluster (about 0.5 us
+// against about 2 us through L2), through the mailbox across clusters.  The
+// older solved blocks stream through the same cp.async ring as the matrix
+// tiles, from a row-major copy released by per-block done flags.
 
 #include "common.cuh"
 
