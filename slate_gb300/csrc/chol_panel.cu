@@ -519,6 +519,75 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 int i = e % kCpIB, l = e / kCpIB;
                 if (i < kb && l < kb && i >= l) P[c0 + i + (c0 + l) * ld] = D[i * (kCpIB + 1) + l];
             }
+        const bool owns_next = !failed && cbeg < a.nbk && cbeg >= rb && cbeg < re;
+        // ---- 4. lookahead: the owner of the next diagonal block forms it as
+        //      D - X X^T from its own solved rows X (the old block D fetched at
+        //      the start of the step on the fast path, read from P here
+        //      otherwise), factors and publishes it now, before its update of
+        //      the other rows (section 3, which leaves that block's rows alone), while the
+        //      other blocks are still updating.
+        if (owns_next) {
+            const int kbn = int(min64(kCpIB, a.nbk - cbeg));
+            __syncthreads();
+            if (!fast) {
+                // the old block and the solved rows of the block's row tile
+                staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                    const int i = e % kCpIB, l = e / kCpIB;
+                    return (i < kbn && l < kbn && i >= l) ? __ldcg(&P[cbeg + i + (cbeg + l) * ld]) : T(0);
+                }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
+                staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
+                    const int i = e % kCpIB, l = e / kCpIB;
+                    return (i < kbn && l < kb) ? __ldcg(&P[cbeg + i + (c0 + l) * ld]) : T(0);
+                }, [&](int e, T v) { Xs[(e / kCpIB) * 68 + e % kCpIB] = v; });
+                __syncthreads();
+            }
+            {
+                // D -= X X^T on the lower triangle, X = the solved rows in Xs
+                // ([l][row], stride 68); the same FMA order as the update of
+                // section 3, so the block is the one that update would make
+                const int tr = t & 15, tc = t >> 4;      // rows 4 tr + i, columns 4 tc + j
+                if (tc <= tr) {
+                    T acc[4][4];
+                    #pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+                    #pragma unroll 4
+                    for (int l = 0; l < kb; ++l) {
+                        T xr[4], xc[4];
+                        lds4(Xs + l * 68 + 4 * tr, xr);
+                        lds4(Xs + l * 68 + 4 * tc, xc);
+                        #pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            #pragma unroll
+                            for (int j = 0; j < 4; ++j) acc[i][j] = fma(xr[i], xc[j], acc[i][j]);
+                    }
+                    #pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int row = 4 * tr + i, col = 4 * tc + j;
+                            if (row < kbn && col <= row) D[row * (kCpIB + 1) + col] -= acc[i][j];
+                        }
+                }
+            }
+            __syncthreads();
+            const int f = factor_diag_block(D, Dinv, kbn);
+            if (f == 0) build_linv_t(D, Dinv, Us, Xs, kbn);
+            for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
+                int i = e % kCpIB, l = e / kCpIB;
+                if (i < kbn && l < kbn && i >= l) P[cbeg + i + (cbeg + l) * ld] = D[i * (kCpIB + 1) + l];
+            }
+            for (int e = t; e < kCpLinv; e += kCpThreads)
+                a.dinv_ws[size_t(k + 1) * kCpLinv + e] = Us[(e / kCpIB) * 68 + e % kCpIB];
+            if (t == 0 && f) {
+                atomicCAS(a.info, 0, int(a.info_offset + cbeg + f));
+                *reinterpret_cast<volatile int*>(a.next_fail) = k + 2;     // 1 + step k + 1
+            }
+            __threadfence();
+            __syncthreads();
+            if (t == 0) st_release_u32(a.diag_ready, unsigned(k + 1));
+        }
         // ---- 3. rank-kb update of the owned rows in panel columns [c0+kb, nbk):
         //      per 64-row tile of the block (its solved rows staged once,
         //      [l][row], row stride 68) and per 64-column tile at or left of
@@ -535,8 +604,9 @@ chol_panel_kernel(CholPanelArgs<T> a)
             for (int64_t rr = r0; rr < re; rr += kCpIB) {
                 const int nr = int(min64(kCpIB, re - rr));
                 __syncthreads();
-                // one row tile per block: the solve left exactly these rows in Xs
-                if (a.rows_per_block != kCpIB)
+                // one row tile per block: the solve left exactly these rows in Xs,
+                // unless section 4 used Xs since
+                if (a.rows_per_block != kCpIB || owns_next)
                     staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
                         const int i = e % kCpIB, l = e / kCpIB;
                         return (i < nr && l < kb) ? __ldcg(&P[rr + i + (c0 + l) * ld]) : T(0);
@@ -544,6 +614,8 @@ chol_panel_kernel(CholPanelArgs<T> a)
                 // a column tile starting past the row tile's last row has no
                 // lower-triangular entries here, nor have the tiles after it
                 for (int64_t cb = cbeg; cb < a.nbk && cb < rr + nr; cb += kCpIB) {
+                    // rows of the next diagonal block (factored in section 4) keep L11
+                    const int keep = (owns_next && rr == cbeg && cb == cbeg) ? int(min64(kCpIB, a.nbk - cbeg)) : 0;
                     const int nc = int(min64(kCpIB, a.nbk - cb));
                     __syncthreads();
                     staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
@@ -597,72 +669,11 @@ chol_panel_kernel(CholPanelArgs<T> a)
                             #pragma unroll
                             for (int i = 0; i < 4; ++i) {
                                 const int c = 4 * tc + j, ii = 4 * tr + i;
-                                if (c < nc && ii < nr && rr + ii >= cb + c) Pt[i + j * ld] = old[j][i] - acc[i][j];
+                                if (c < nc && ii < nr && ii >= keep && rr + ii >= cb + c) Pt[i + j * ld] = old[j][i] - acc[i][j];
                             }
                     }
                 }
             }
-        }
-        // ---- 4. lookahead: the owner of the next diagonal block (its rows
-        //      updated just above, and it has no other work in lower-
-        //      triangular column tiles) factors it now, while the other
-        //      blocks are still updating.
-        if (!failed && cbeg < a.nbk && cbeg >= rb && cbeg < re) {
-            const int kbn = int(min64(kCpIB, a.nbk - cbeg));
-            __syncthreads();
-            if (fast) {
-                // D (the old block, fetched at the start of the step) -= X X^T
-                // on the lower triangle, X = the solved rows in Xs ([l][row],
-                // stride 68); the same FMA order as the update above, so the
-                // factor matches the general path bit for bit
-                const int tr = t & 15, tc = t >> 4;      // rows 4 tr + i, columns 4 tc + j
-                if (tc <= tr) {
-                    T acc[4][4];
-                    #pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        #pragma unroll
-                        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
-                    #pragma unroll 4
-                    for (int l = 0; l < kb; ++l) {
-                        T xr[4], xc[4];
-                        lds4(Xs + l * 68 + 4 * tr, xr);
-                        lds4(Xs + l * 68 + 4 * tc, xc);
-                        #pragma unroll
-                        for (int i = 0; i < 4; ++i)
-                            #pragma unroll
-                            for (int j = 0; j < 4; ++j) acc[i][j] = fma(xr[i], xc[j], acc[i][j]);
-                    }
-                    #pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        #pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            const int row = 4 * tr + i, col = 4 * tc + j;
-                            if (row < kbn && col <= row) D[row * (kCpIB + 1) + col] -= acc[i][j];
-                        }
-                }
-            }
-            else {
-                staged_copy<kStage, kCpThreads>(kCpIB * kCpIB, [&](int e) {
-                    const int i = e % kCpIB, l = e / kCpIB;
-                    return (i < kbn && l < kbn && i >= l) ? __ldcg(&P[cbeg + i + (cbeg + l) * ld]) : T(0);
-                }, [&](int e, T v) { D[(e % kCpIB) * (kCpIB + 1) + e / kCpIB] = v; });
-            }
-            __syncthreads();
-            const int f = factor_diag_block(D, Dinv, kbn);
-            if (f == 0) build_linv_t(D, Dinv, Us, Xs, kbn);
-            for (int e = t; e < kCpIB * kCpIB; e += kCpThreads) {
-                int i = e % kCpIB, l = e / kCpIB;
-                if (i < kbn && l < kbn && i >= l) P[cbeg + i + (cbeg + l) * ld] = D[i * (kCpIB + 1) + l];
-            }
-            for (int e = t; e < kCpLinv; e += kCpThreads)
-                a.dinv_ws[size_t(k + 1) * kCpLinv + e] = Us[(e / kCpIB) * 68 + e % kCpIB];
-            if (t == 0 && f) {
-                atomicCAS(a.info, 0, int(a.info_offset + cbeg + f));
-                *reinterpret_cast<volatile int*>(a.next_fail) = k + 2;     // 1 + step k + 1
-            }
-            __threadfence();
-            __syncthreads();
-            if (t == 0) st_release_u32(a.diag_ready, unsigned(k + 1));
         }
         if (failed) return;       // every block saw the same failing diagonal block
     }
