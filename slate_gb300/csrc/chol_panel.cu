@@ -176,7 +176,6 @@ __device__ __forceinline__ void lds4(const double* p, double* v)
     v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
 }
 
-constexpr int kCpDinv = (kCpIB / kCpSub) * kCpSub * (kCpSub + 1);   // sub-block inverses of one diagonal block
 constexpr int kCpLinv = kCpIB * kCpIB;                                 // transposed inverse of one diagonal block
 
 // Bounded acquire spin of thread 0 until *p >= target; false on timeout or
