@@ -98,6 +98,12 @@ constexpr uint32_t kDgTmemA = 192;
 constexpr uint32_t kDgTmemAStage = 64;
 constexpr int kDgAStagesT = 5;
 constexpr int kDgASub = kDgBK / 16;                    // A operand stages per 64 k
+static_assert(kDgTmemH + 64 <= kDgTmemA && kDgTmemA + kDgAStagesT * kDgTmemAStage <= 512,
+              "D_L, D_H and the A operand stages fit the 512 TMEM columns");
+static_assert(kDgAStagesT * kDgTmemAStage >= 2 * kDgTmemAStage, "at least two A operand stages");
+static_assert(1024 + kDgUStages * kDgUStage + kDgXStages * kDgXStage + 256 + 1024 <= 232448,
+              "stages, barriers and the static shared memory fit one CTA");
+static_assert(kDgChunk * kDgBK * 4 * 64 * 64 <= (1 << 24), "FP32 class sums stay exact per chunk");
 // Exponent keys.  key(v) = 0 for v = 0, 2047 for Inf / NaN, else
 // max(biased exponent of v, 1); keys are monotone in |v|, and for the largest
 // key K of a row, |v| < 2^(K - 1022) for every v of the row, so the scale
