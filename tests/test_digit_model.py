@@ -17,6 +17,8 @@ relies on:
 * FP32 class sums over 1024 k, at most four digit pairs per class and
   accumulator, are exact whatever the order of accumulation (every partial
   sum is an integer of magnitude <= 2^24);
+* the infinity norm from exact integer row sums of |F| (two words per row)
+  matches the row sums of |A| within the rounding of the fixed-point values;
 * the int64 fold and the final scaling reproduce A x
   within the bound 2^-50 n max_k|a_ik| max_k|x_k| stated in the kernel's
   header, and in practice within a small multiple of FP64's own rounding.
@@ -209,3 +211,28 @@ def test_digit_product_accuracy(n, spread):
     fp64 = np.abs(A @ x - exact)
     scale = np.abs(A) @ np.abs(x)
     assert err.max() <= max(4 * fp64.max(), 2.0 ** -52 * scale.max())
+
+
+@pytest.mark.parametrize("n,spread", [(300, 0), (700, 200)])
+def test_norm_from_fixed_point_row_sums(n, spread):
+    """The infinity norm the split forms from its fixed-point values: per row,
+    sum |F| kept exactly as h 2^28 + l (h = sum |F| >> 28, l = sum of the
+    low 28 bits), then h 2^(e - 28) + l 2^(e - 56); within n 2^-55 (the
+    rounding of each F) plus a few FP64 roundings of the exact row sums."""
+    rng = np.random.default_rng(n + spread)
+    A = rng.standard_normal((n, n))
+    if spread:
+        A *= np.ldexp(1.0, rng.integers(-spread, spread, size=(n, 1)))
+    A[n // 4] = 0.0
+    e = _keys(A)
+    F = _fixed(A, e)
+    a = np.abs(F).astype(np.uint64)
+    h = (a >> np.uint64(28)).sum(axis=1, dtype=np.uint64)
+    lo = (a & np.uint64((1 << 28) - 1)).sum(axis=1, dtype=np.uint64)
+    rows = np.ldexp(h.astype(np.float64), e - 28) + np.ldexp(lo.astype(np.float64), e - 56)
+    assert rows[n // 4] == 0.0
+    exact = np.abs(A).astype(np.longdouble).sum(axis=1)
+    assert np.all(np.abs(rows - exact) <= (n * 2.0 ** -55 + 2.0 ** -50) * exact + 1e-300)
+    norm = rows.max()
+    ref = float(exact.max())
+    assert abs(norm - ref) <= (n * 2.0 ** -55 + 2.0 ** -50) * ref
