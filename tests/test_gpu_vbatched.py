@@ -1,4 +1,6 @@
-"""Variable-size batched solves on the GPU against the oracle, per system.
+"""Variable-size batched solves on the GPU against the oracle, per system,
+for sizes from 1 to 1024 (config 5's range, across the tuning table's
+switch of panel width).
 
 Bar: every system's pivots equal the oracle's (SLATE's getrf restated) on
 rows whose pivot margin exceeds rounding; FP64 backward error <= 3 eps64
@@ -168,3 +170,24 @@ def test_vbatched_mixed_tiers(orc, slt, monkeypatch, tier, pb):
         bar = 3 * EPS if tier == "fp64" else 3 * n * EPS
         assert berr(orc, A, to_host(x), B, sym=(k == 1)) <= bar, (t, n, k)
         assert np.array_equal(to_host(dA), A) and np.array_equal(to_host(dB), B)
+
+
+def test_vbatched_large_sizes_match_oracle(orc, slt):
+    """Sizes across the tuning table's switch to 32-wide panels and up to
+    config 5's largest (1024): every system's backward error and, for LU,
+    its pivots on rows with a clear margin, against the oracle."""
+    import torch
+    systems = _systems(orc, [511, 512, 513, 640, 777, 1000, 1024], 11, nrhs_max=4, kinds=[0, 1, 0, 1, 0, 0, 1])
+    dsys = _to_dev_systems(slt, systems)
+    vb = slt.VBatch(dsys)
+    info = slt.solve_vbatched(vb)
+    torch.cuda.synchronize()
+    assert (info == 0).all()
+    for t, ((k, A, B), (_, dA, dB)) in enumerate(zip(systems, dsys)):
+        n = A.shape[0]
+        assert berr(orc, A, to_host(dB), B, sym=(k == 1)) <= 3 * EPS, (t, n, k)
+        if k == 0:
+            oinfo, pt, po, oipiv, mg = orc.getrf(A.copy(order="F"), 32, 32, margins=True)
+            gip = vb.ipiv_t[t][:n].cpu().numpy().astype(np.int64)
+            robust = mg > 1 + 1e3 * n * EPS
+            assert np.array_equal(gip[robust], oipiv[robust]), (t, n)
